@@ -1,0 +1,213 @@
+/*
+ * shark_gpu.h -- C ABI of the GB300 (sm_103a) per-step Godunov update for gas + N dust species.
+ *
+ * The reference (SHARK, Fortran 90) runs one time step as the argument-less subroutine
+ * `solve(verbose,outputing)` (src/solver/solve.f90:10-181), called once per step from
+ * `time_loop` (src/shark.f90:102).  `solve` talks to the rest of the code only through module
+ * arrays: the conserved state `u_prim(1:ncells,1:nvar)` (src/commons/allocate_init.f90:82),
+ * its primitive copy `q`, the sound speed `cs`, the stopping times `tstop` and the forces.
+ * This header replaces that whole call with a device-resident context:
+ *
+ *   shark_gpu_init      <- allocate_init + gridinit + the per-setup parameter reads
+ *   shark_gpu_upload    <- the state produced by `setup` (or by a restart)
+ *   shark_gpu_step      <- solve(verbose,outputing)            src/solver/solve.f90:10-181
+ *   shark_gpu_download  <- the host copy that `output`/`check_output` read
+ *   shark_gpu_ctoprim   <- ctoprim                             src/solver/solve.f90:195-253
+ *   shark_gpu_totals    <- the mass/momentum sums of check_output (e.g. src/setups/SI/setup.f90:271-285)
+ *
+ * Every function returns an int32 status (SHARK_OK == 0).  No function throws, aborts or
+ * traps; device-side failures are reported through the step status word.
+ *
+ * Layout contract (identical to the reference): u_prim is variable-major with stride ncells
+ * (Fortran u_prim(1:ncells,1:nvar), column-major), cells are x-fastest with ghost cells,
+ * icell = ix + iy*nx_max (0-based), nx_max = nx + 2*nghost, ny_max = ny + 2*nghost (1 in 1D).
+ * Variable order: rho, rho*vx, rho*vy, rho*vz, E, then rho_d(1..N), rho_d*vdx(1..N),
+ * rho_d*vdy(1..N), rho_d*vdz(1..N)   (src/commons/allocate_init.f90:225-262).
+ * nvar = 5 + 4*N (no MHD, no dust passive scalars: src/commons/parameters.f90:43).
+ */
+#ifndef SHARK_GPU_H
+#define SHARK_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SHARK_GPU_ABI_VERSION 1
+#define SHARK_MAX_DUST 64
+
+/* ---- return codes ------------------------------------------------------------------------ */
+#define SHARK_OK                   0
+#define SHARK_ERR_INVALID_ARG     -1   /* bad pointer, size or config field                   */
+#define SHARK_ERR_UNSUPPORTED     -2   /* valid reference option not built on the GPU path    */
+#define SHARK_ERR_CUDA            -3   /* a CUDA runtime call failed (message: shark_gpu_last_error) */
+#define SHARK_ERR_NO_DEVICE       -4   /* no sm_103 device visible                            */
+#define SHARK_ERR_STATE           -5   /* call order violated (e.g. step before upload)       */
+#define SHARK_ERR_NUMERICS        -6   /* the step status word reports a numerical failure    */
+
+/* ---- step status word (bit mask written by the kernels, read back with the dt) ----------- */
+#define SHARK_STATUS_NAN          0x1  /* a non-finite conserved value was produced            */
+#define SHARK_STATUS_NEG_DENSITY  0x2  /* gas density <= 0 after the update                    */
+#define SHARK_STATUS_DT_UNDERFLOW 0x4  /* CFL dt not positive/finite                           */
+#define SHARK_STATUS_NEWTON       0x8  /* a charging Newton solve hit its iteration cap        */
+#define SHARK_STATUS_GROWTH       0x10 /* growth sub-cycling hit its cap                        */
+
+/* ---- setups whose per-step hooks exist on the device (src/setups/<NAME>/) ----------------- */
+#define SHARK_SETUP_SOD         1   /* fixed left/right ghost states   SOD/boundaries.f90:49-77 */
+#define SHARK_SETUP_DUSTYWAVE   2   /* periodic; tstop = rho_d/K        DUSTYWAVE/setup.f90:212-221 */
+#define SHARK_SETUP_SI          3   /* shearing box                     SI/setup.f90, SI/boundaries.f90 */
+#define SHARK_SETUP_DISK_POLAR  4   /* polar disk (FARGO)               disk_polar/                 */
+#define SHARK_SETUP_DUSTYTURB   5   /* periodic driven turbulence       dustyTurb/                  */
+
+/* ---- run-time switches (the reference's namelist logicals) -------------------------------- */
+#define SHARK_FLAG_DRAG           0x1   /* drag               src/dust/dust_commons.f90:5        */
+#define SHARK_FLAG_BACK_REACTION  0x2   /* dust_back_reaction src/dust/dust_commons.f90:15       */
+#define SHARK_FLAG_FORCE_KICK     0x4   /* force_kick         src/commons/parameters.f90:49      */
+#define SHARK_FLAG_FARGO          0x8   /* fargo              src/commons/parameters.f90:51      */
+#define SHARK_FLAG_GROWTH         0x10  /* growth             src/dust/dust_commons.f90:6        */
+#define SHARK_FLAG_CHARGING       0x20  /* charging           src/chemistry/ionisation_commons.f90 */
+#define SHARK_FLAG_VISCOSITY      0x40  /* viscosity          src/commons/parameters.f90:50      */
+#define SHARK_FLAG_STATIC         0x80  /* static             src/commons/parameters.f90:48      */
+
+/* ---- precision of the device state and of the flux/update stage -------------------------- */
+#define SHARK_PREC_FP64   0   /* everything FP64 (the FP64 GPU oracle run)                      */
+#define SHARK_PREC_MIXED  1   /* FP32 state + FP32 flux/update; FP64 drag, FARGO split, totals  */
+
+/*
+ * Run configuration.  Plain old data: the Fortran shim fills it from the module parameters
+ * (src/commons/parameters.f90, src/hydro/hydro_commons.f90, src/dust/dust_commons.f90) and
+ * the setup_parameters module of the chosen setup.  Compile-time -D flags of the reference
+ * (bin/Makefile:36) are run-time fields here.
+ */
+typedef struct shark_gpu_config {
+    int32_t abi_version;      /* must be SHARK_GPU_ABI_VERSION                                  */
+    int32_t nx, ny;           /* active cells (-DNX, -DNY); ny == 1 selects the 1D code path     */
+    int32_t nghost;           /* must be 2 (-DNGHOST, bin/Makefile:8)                           */
+    int32_t ndust;            /* -DNDUST, 0..SHARK_MAX_DUST                                      */
+    int32_t geom;             /* -DGEOM: 0 Cartesian, 2 polar face-on                            */
+    int32_t gridspace;        /* -DGRIDSPACE: 0 linear, 1 log-spaced radius (geom 2)             */
+    int32_t solver;           /* -DSOLVER: 0 LLF, 1 HLL, 2 HLLC                                  */
+    int32_t solverdust;       /* -DSOLVERDUST: 0 Huang & Bai, 1 LLF, 2 HLL                       */
+    int32_t slope_type;       /* 1 minmod, 2 van Leer (harmonic), 3 MC(1.5)                      */
+    int32_t iso_cs;           /* 1: isothermal (P = rho cs^2 with cs fixed by the setup)         */
+    int32_t precision;        /* SHARK_PREC_*                                                    */
+    int32_t setup;            /* SHARK_SETUP_*                                                   */
+    int32_t flags;            /* SHARK_FLAG_*                                                    */
+    int32_t device;           /* CUDA device ordinal                                             */
+    int32_t pad0;
+
+    double gamma, cfl;                 /* hydro_commons.f90:16, parameters.f90:55              */
+    double smallr, smallc, smallp;     /* floors after allocate_init.f90:277-279 scaling       */
+    double box_l, box_l_y;             /* domain extents handed to gridinit                    */
+    double inner_r;                    /* inner radius for geom 2 (gridinit_disk_log inner_r)  */
+    double cs0;                        /* isothermal sound speed scale (setup-defined profile) */
+    double dust_ratio_min;             /* dust_commons.f90:29                                   */
+    double rhograin;                   /* grain intrinsic density (code units)                  */
+
+    /* per-species constants */
+    double dust_size[SHARK_MAX_DUST];  /* sdust: grain radius (code units)                      */
+    double dust_K[SHARK_MAX_DUST];     /* DUSTYWAVE drag constant K(idust)                      */
+    double dust_tstop[SHARK_MAX_DUST]; /* SI: constant stopping time per species                */
+    double dust_eps[SHARK_MAX_DUST];   /* initial dust-to-gas ratio per species (ICs only)      */
+    double dust_stokes[SHARK_MAX_DUST];/* SI Stokes number per species (ICs only)               */
+
+    /* SOD (src/setups/SOD/setup_commons.f90) */
+    double sod_rho_l, sod_rho_r, sod_P_l, sod_P_r;
+    int32_t sod_direction;             /* 0: shock along x, 1: along y                          */
+    int32_t pad1;
+    /* DUSTYWAVE (src/setups/DUSTYWAVE/setup_commons.f90; ICs only) */
+    double dw_rho_0, dw_delta_rho, dw_vx_0, dw_kx_wave;
+    /* SI shearing box (src/setups/SI/setup_commons.f90) */
+    double si_q_shear, si_omega, si_eta_stream, si_rad0, si_rho_init, si_hoverr;
+    /* polar disk / turbulence / charging / growth parameters (unused by the setups above) */
+    double disk_mstar, disk_hoverr, disk_sigma0, disk_r0, disk_rout;
+    double reserved[48];
+
+    /* Optional grid metrics from the caller (Fortran dx(ncells,ndim), surf(ncells,ndim),
+     * vol(ncells), radii_c(ncells), position(ncells,ndim), cs(ncells)).  NULL: the library
+     * builds them with the formulas of src/grid/grid.f90:104-173 (gridinit) and
+     * gridinit_disk_log.  When given they must depend on ix only (true for every reference
+     * grid); the library checks this and returns SHARK_ERR_UNSUPPORTED otherwise. */
+    const double* dx;
+    const double* surf;
+    const double* vol;
+    const double* radii_c;
+    const double* position;
+    const double* cs;
+} shark_gpu_config;
+
+typedef struct shark_gpu_ctx shark_gpu_ctx;
+
+/* Library/ABI identification; never fails. */
+int32_t shark_gpu_abi_version(void);
+
+/* Fill *cfg with the reference defaults (hydro_commons.f90, dust_commons.f90, parameters.f90):
+ * gamma 1.66667, CFL 0.5, smallr=smallc=1e-27, smallp=smallr*smallc^2, slope_type 1, HLLC,
+ * Huang & Bai, nghost 2, drag + back reaction on, FP64. */
+int32_t shark_gpu_config_defaults(shark_gpu_config* cfg);
+
+/* Validate cfg, select the device, build the grid and allocate the device state.
+ * Replaces allocate_init/gridinit (src/commons/allocate_init.f90:3-282, src/grid/grid.f90). */
+int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** ctx_out);
+
+/* Copy the conserved state (ncells*nvar doubles, Fortran order) to the device.
+ * ncells and nvar must match the context.  Also computes the first CFL dt. */
+int32_t shark_gpu_upload(shark_gpu_ctx* ctx, const double* u_prim, int64_t ncells, int32_t nvar);
+
+/* One full `solve` on the device (src/solver/solve.f90:10-181): boundaries, ctoprim, forces,
+ * stopping times, CFL dt, kick, MUSCL-Hancock predictor + Riemann fluxes + update, source
+ * terms, FARGO, drag, setup_inloop.  *dt_out receives the dt used by this step (the value
+ * `courant` sets, src/solver/courant.f90:11-124); *status_out the status word of the step
+ * before this one (the kernels run asynchronously; the final word is returned by
+ * shark_gpu_sync).  Either pointer may be NULL. */
+int32_t shark_gpu_step(shark_gpu_ctx* ctx, double* dt_out, int32_t* status_out);
+
+/* Run up to nsteps steps, stopping once time >= tend (src/shark.f90:71-110; dt is not clipped
+ * to tend, exactly like the reference).  *time_io is advanced by the dts; *steps_done and
+ * *status_out receive the count and the OR of all status words.  Pointers may be NULL except
+ * time_io. */
+int32_t shark_gpu_run(shark_gpu_ctx* ctx, int64_t nsteps, double tend, double* time_io,
+                      int64_t* steps_done, int32_t* status_out);
+
+/* Wait for all queued work; *status_out = OR of the status words so far (may be NULL). */
+int32_t shark_gpu_sync(shark_gpu_ctx* ctx, int32_t* status_out);
+
+/* Copy the conserved state back (ncells*nvar doubles, Fortran order), ghost cells included as
+ * the last step left them.  q (nullable) receives the primitive variables of ctoprim. */
+int32_t shark_gpu_download(shark_gpu_ctx* ctx, double* u_prim, double* q);
+
+/* ctoprim on the device state (src/solver/solve.f90:195-253) into host q (ncells*nvar) and
+ * cs (ncells, nullable). */
+int32_t shark_gpu_ctoprim(shark_gpu_ctx* ctx, double* q, double* cs);
+
+/* Compensated (Kahan) FP64 totals over the active cells, for each species s = 0..N (gas
+ * first): out[4*s+0] = sum rho, out[4*s+1..3] = sum of the three momenta.  out has 4*(N+1)
+ * doubles.  Deterministic: fixed reduction tree. */
+int32_t shark_gpu_totals(shark_gpu_ctx* ctx, double* out);
+
+/* Device time of the last `step` in milliseconds: ms_out[0] boundaries, ms_out[1] flux/update
+ * kernel, ms_out[2] drag + dt kernel (CUDA events on the context's stream; waits for the step). */
+int32_t shark_gpu_last_step_ms(shark_gpu_ctx* ctx, float* ms_out);
+
+/* Benchmark helper: synchronize, record a CUDA event on the context's stream, run nsteps steps
+ * exactly as shark_gpu_run does (per-step dt readback included), record a second event,
+ * synchronize.  *ms_out = device time between the events; *time_io is advanced by the dts. */
+int32_t shark_gpu_timed_run(shark_gpu_ctx* ctx, int64_t nsteps, double* time_io, float* ms_out);
+
+/* Benchmark helper: run nsteps steps with CUDA events around every kernel on the context's
+ * stream and return the mean device time per launch in milliseconds: avg_ms[0] boundaries,
+ * avg_ms[1] flux/update (K1), avg_ms[2] drag + dt (K2), avg_ms[3] whole step. */
+int32_t shark_gpu_kernel_times(shark_gpu_ctx* ctx, int64_t nsteps, float* avg_ms);
+
+/* Human-readable message of the last error on this thread (static storage). */
+const char* shark_gpu_last_error(void);
+
+/* Release the device state and the context. */
+int32_t shark_gpu_free(shark_gpu_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHARK_GPU_H */

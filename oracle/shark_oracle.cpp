@@ -1,0 +1,1276 @@
+// shark_oracle.cpp -- TEST INFRASTRUCTURE ONLY (see shark_oracle.h).
+//
+// Line-faithful FP64 restatement of SHARK's per-step update.  Each routine cites the Fortran it
+// follows; operation order inside expressions follows Fortran's left-to-right evaluation so the
+// FP64 GPU path (same order, no FMA contraction) can be compared at round-off level.  Built with
+// -O2 -ffp-contract=off (gfortran -O3 on x86-64/aarch64 without -ffast-math keeps IEEE order).
+//
+// Array layout mirrors the Fortran module arrays: u(i,ivar) -> u[ivar*ncells + i] (0-based),
+// qm/qp/flux(i,ivar,idim) -> [(idim*nvar + ivar)*ncells + i], force(i,1:3) -> [c*ncells + i],
+// force_dust(i,1:3,idust) -> [(idust*3 + c)*ncells + i], tstop(i,idust) -> [idust*ncells + i].
+#include "shark_oracle.h"
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+constexpr double half = 0.5;
+constexpr double pi = 3.141592653589793238462643383279;   // src/commons/phys_const.f90:14
+
+// gfortran evaluates x**n (integer n) with __builtin_powi; x**2 / x**2.0 fold to x*x.
+inline double sq(double x) { return x * x; }
+inline double powi(double x, int n) { return __builtin_powi(x, n); }
+// Fortran SIGN(1.0d0, x): +1 for +0 and positive, -1 for -0 and negative.
+inline double fsign1(double x) { return std::signbit(x) ? -1.0 : 1.0; }
+inline double fmax2(double a, double b) { return a > b ? a : b; }   // gfortran MAX for non-NaN
+inline double fmin2(double a, double b) { return a < b ? a : b; }
+
+}  // namespace
+
+struct oracle_state {
+    shark_gpu_config cfg;
+    int nx, ny, nghost, ndust, nvar, ndim;
+    int nx_max, ny_max;
+    int64_t ncells;
+    int first_active, last_active, first_active_y, last_active_y;  // 0-based inclusive
+    // variable indices (src/commons/allocate_init.f90:225-262), 0-based
+    int irho = 0, ivx = 1, ivy = 2, ivz = 3, iP = 4;
+    std::vector<int> irhod, ivdx, ivdy, ivdz;
+    int index_vn[2], index_vt[2];
+    std::vector<int> index_vdn, index_vdt;   // [idust*2 + idim]
+
+    std::vector<double> u, q, qm, qp, flux, cs;
+    std::vector<double> dx, surf, vol, position, radii_c;
+    std::vector<uint8_t> active, active_pred;
+    std::vector<double> force, force_dust, tstop, sdust, epsilondust;
+    double dt = 0.0, time = 0.0;
+
+    // setup-derived scalars
+    double box_l = 1.0, box_l_y = 1.0;
+
+    double& U(int64_t i, int v) { return u[(int64_t)v * ncells + i]; }
+    double& Q(int64_t i, int v) { return q[(int64_t)v * ncells + i]; }
+    double& QM(int64_t i, int v, int d) { return qm[((int64_t)d * nvar + v) * ncells + i]; }
+    double& QP(int64_t i, int v, int d) { return qp[((int64_t)d * nvar + v) * ncells + i]; }
+    double& FLX(int64_t i, int v, int d) { return flux[((int64_t)d * nvar + v) * ncells + i]; }
+    double& DX(int64_t i, int d) { return dx[(int64_t)d * ncells + i]; }
+    double& SURF(int64_t i, int d) { return surf[(int64_t)d * ncells + i]; }
+    double& POS(int64_t i, int d) { return position[(int64_t)d * ncells + i]; }
+    double& FORCE(int64_t i, int c) { return force[(int64_t)c * ncells + i]; }
+    double& FDUST(int64_t i, int c, int k) { return force_dust[((int64_t)k * 3 + c) * ncells + i]; }
+    double& TSTOP(int64_t i, int k) { return tstop[(int64_t)k * ncells + i]; }
+    double& SDUST(int64_t i, int k) { return sdust[(int64_t)k * ncells + i]; }
+    double& EPSD(int64_t i, int k) { return epsilondust[(int64_t)k * ncells + i]; }
+
+    int64_t icell(int ix, int iy) const { return (ny == 1) ? ix : (int64_t)ix + (int64_t)iy * nx_max; }
+    int ixx(int64_t i) const { return (ny == 1) ? (int)i : (int)(i % nx_max); }
+    int iyy(int64_t i) const { return (ny == 1) ? 0 : (int)(i / nx_max); }
+
+    bool flag(int f) const { return (cfg.flags & f) != 0; }
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// slope_limit  (src/solver/slope_limiters.f90:5-37)
+// ---------------------------------------------------------------------------------------------
+inline double slope_limit(int slope_type, double slope_lft, double slope_rgt) {
+    double r;
+    if (slope_type == 1) {
+        r = slope_lft;
+        if (std::fabs(slope_rgt) < std::fabs(slope_lft)) r = slope_rgt;
+        if (slope_rgt * slope_lft < 0.0) r = 0.0;
+    } else if (slope_type == 2) {
+        r = 2.0 * slope_lft * slope_rgt / (slope_lft + slope_rgt);
+        if (slope_rgt * slope_lft <= 0.0) r = 0.0;
+    } else {  // 3: MC with factor 1.5 (other values rejected at create time)
+        double dcen = half * (slope_lft + slope_rgt);
+        double dsgn = fsign1(dcen);
+        double slop = fmin2(1.5 * std::fabs(slope_lft), 1.5 * std::fabs(slope_rgt));
+        double dlim = slop;
+        if ((slope_lft * slope_rgt) <= 0.0) dlim = 0.0;
+        r = dsgn * fmin2(dlim, std::fabs(dcen));
+    }
+    return r;
+}
+
+// ---------------------------------------------------------------------------------------------
+// get_active_cells (src/grid/grid.f90:57-99)
+// ---------------------------------------------------------------------------------------------
+void get_active_cells(oracle_state& s) {
+    s.active.assign(s.ncells, 0);
+    s.active_pred.assign(s.ncells, 0);
+    if (s.ndim == 1) {
+        for (int ix = 0; ix < s.nx_max; ++ix) {
+            if (ix >= s.first_active && ix <= s.last_active) s.active[ix] = 1;
+            if (ix >= 1 && ix <= s.nx_max - 2) s.active_pred[ix] = 1;
+        }
+    } else {
+        for (int ix = 0; ix < s.nx_max; ++ix)
+            for (int iy = 0; iy < s.ny_max; ++iy) {
+                int64_t ii = s.icell(ix, iy);
+                if (ix >= s.first_active && ix <= s.last_active && iy >= s.first_active_y &&
+                    iy <= s.last_active_y)
+                    s.active[ii] = 1;
+                if (ix >= 1 && ix <= s.nx_max - 2 && iy >= 1 && iy <= s.ny_max - 2) s.active_pred[ii] = 1;
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// gridinit (src/grid/grid.f90:104-173) and gridinit_disk_log (src/grid/grid.f90:180-240)
+// float(n) is default REAL in gfortran: exact for the integers involved.
+// ---------------------------------------------------------------------------------------------
+void gridinit(oracle_state& s) {
+    const double rmax_x = s.box_l, rmax_y = s.box_l_y;
+    const int nx = s.nx, ny = s.ny;
+    std::fill(s.radii_c.begin(), s.radii_c.end(), 1.0);   // allocate_init.f90:27-30
+    if (s.cfg.geom == 0) {
+        if (s.ndim == 1) {
+            for (int ix = 0; ix < s.ncells; ++ix) {
+                s.DX(ix, 0) = rmax_x / (double)(float)nx;
+                s.vol[ix] = s.DX(ix, 0);
+                s.SURF(ix, 0) = 1.0;
+                // 1D positions are right cell edges, accumulated (grid.f90:131)
+                if (s.active[ix]) s.POS(ix, 0) = s.POS(ix - 1, 0) + s.DX(ix, 0);
+            }
+        } else {
+            for (int ix = 0; ix < s.nx_max; ++ix)
+                for (int iy = 0; iy < s.ny_max; ++iy) {
+                    int64_t c = s.icell(ix, iy);
+                    s.DX(c, 0) = rmax_x / (double)(float)nx;
+                    s.DX(c, 1) = rmax_y / (double)(float)ny;
+                    s.SURF(c, 0) = s.DX(c, 0);
+                    s.SURF(c, 1) = s.DX(c, 1);
+                    s.vol[c] = s.DX(c, 0) * s.DX(c, 1);
+                    s.POS(c, 0) = ((double)(float)(ix - s.first_active) + half) * rmax_x / (double)(float)nx;
+                    s.POS(c, 1) = ((double)(float)(iy - s.first_active_y) + half) * rmax_y / (double)(float)ny;
+                }
+        }
+    } else {  // geom 2, polar face-on, 2D only (validated at create)
+        const double inner_r = s.cfg.inner_r;
+        if (s.cfg.gridspace == 0) {
+            for (int ix = 0; ix < s.nx_max; ++ix)
+                for (int iy = 0; iy < s.ny_max; ++iy) {
+                    int64_t c = s.icell(ix, iy);
+                    s.DX(c, 0) = rmax_x / (double)(float)nx;
+                    s.DX(c, 1) = 2.0 * pi / (double)(float)ny;
+                    s.radii_c[c] = inner_r + ((double)(float)(ix - s.first_active) + half) * rmax_x / (double)(float)nx;
+                    double phi = ((double)(float)(iy - s.first_active_y) + half) * 2.0 * pi / (double)(float)ny;
+                    s.POS(c, 0) = s.radii_c[c] * std::cos(phi);
+                    s.POS(c, 1) = s.radii_c[c] * std::sin(phi);
+                    s.SURF(c, 0) = (s.radii_c[c] - half * s.DX(c, 0)) * (s.DX(c, 1));
+                    s.SURF(c, 1) = s.DX(c, 0);
+                    s.vol[c] = s.radii_c[c] * s.DX(c, 0) * s.DX(c, 1);
+                }
+        } else {
+            const double zeta_r = std::pow(rmax_x / inner_r, 1.0 / (double)(nx - 1));
+            for (int iy = 0; iy < s.ny_max; ++iy) {
+                for (int ix = 0; ix < s.nx_max; ++ix) {
+                    int64_t c = s.icell(ix, iy);
+                    int k = ix - s.first_active;
+                    s.radii_c[c] = inner_r * half * (powi(zeta_r, k) + powi(zeta_r, k + 1));
+                    s.DX(c, 0) = inner_r * (powi(zeta_r, k + 1) - powi(zeta_r, k));
+                    s.DX(c, 1) = 2.0 * pi / (double)(float)ny;
+                    double phi = ((double)(float)(iy - s.first_active_y) + half) * 2.0 * pi / (double)(float)ny;
+                    s.POS(c, 0) = s.radii_c[c] * std::cos(phi);
+                    s.POS(c, 1) = s.radii_c[c] * std::sin(phi);
+                    s.SURF(c, 0) = inner_r * (powi(zeta_r, k)) * (s.DX(c, 1));
+                    s.SURF(c, 1) = s.DX(c, 0);
+                    s.vol[c] = s.radii_c[c] * s.DX(c, 0) * s.DX(c, 1);
+                }
+                for (int g = 0; g < s.nghost; ++g) {
+                    int64_t cl = s.icell(g, iy), cr = s.icell(s.nx_max - 1 - g, iy);
+                    s.radii_c[cl] = inner_r * 0.5;
+                    s.radii_c[cr] = rmax_x + 0.5 * s.DX(s.icell(s.last_active, iy), 0);
+                    s.DX(cl, 0) = s.DX(s.icell(s.first_active, iy), 0);
+                    s.DX(cr, 0) = s.DX(s.icell(s.last_active, iy), 0);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// ctoprim (src/solver/solve.f90:195-253); non_standard_eos is not used by the in-scope setups.
+// ---------------------------------------------------------------------------------------------
+void ctoprim(oracle_state& s) {
+    const double gamma = s.cfg.gamma, smallr = s.cfg.smallr, smallp = s.cfg.smallp;
+    const int N = s.ndust;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        double rho = s.U(i, s.irho);
+        s.Q(i, s.irho) = fmax2(rho, smallr);
+        s.Q(i, s.ivx) = s.U(i, s.ivx) / rho;
+        s.Q(i, s.ivy) = s.U(i, s.ivy) / rho;
+        s.Q(i, s.ivz) = s.U(i, s.ivz) / rho;
+        double ekin = half * rho * sq(s.U(i, s.ivx) / rho) + half * rho * sq(s.U(i, s.ivy) / rho) +
+                      half * rho * sq(s.U(i, s.ivz) / rho);
+        double emag = 0.0;
+        s.Q(i, s.iP) = fmax2((gamma - 1.0) * (s.U(i, s.iP) - ekin - emag), smallp);
+        if (s.cfg.iso_cs < 1) s.cs[i] = std::sqrt(gamma * s.Q(i, s.iP) / s.Q(i, s.irho));
+        if (s.cfg.iso_cs == 1) s.Q(i, s.iP) = s.U(i, s.irho) * sq(s.cs[i]);
+        for (int k = 0; k < N; ++k) {
+            double rd = s.U(i, s.irhod[k]);
+            s.Q(i, s.irhod[k]) = rd;
+            s.Q(i, s.ivdx[k]) = s.U(i, s.ivdx[k]) / rd;
+            s.Q(i, s.ivdy[k]) = s.U(i, s.ivdy[k]) / rd;
+            s.Q(i, s.ivdz[k]) = s.U(i, s.ivdz[k]) / rd;
+        }
+    }
+}
+
+// primtoc (src/solver/solve.f90:265-302)
+void primtoc(oracle_state& s) {
+    const double gamma = s.cfg.gamma;
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        double r = s.Q(i, s.irho);
+        s.U(i, s.irho) = r;
+        s.U(i, s.ivx) = r * s.Q(i, s.ivx);
+        s.U(i, s.ivy) = r * s.Q(i, s.ivy);
+        s.U(i, s.ivz) = r * s.Q(i, s.ivz);
+        s.U(i, s.iP) = s.Q(i, s.iP) / (gamma - 1.0) + half * r * sq(s.Q(i, s.ivx)) +
+                       half * r * sq(s.Q(i, s.ivy)) + half * r * sq(s.Q(i, s.ivz));
+        for (int k = 0; k < s.ndust; ++k) {
+            double rd = s.Q(i, s.irhod[k]);
+            s.U(i, s.irhod[k]) = rd;
+            s.U(i, s.ivdx[k]) = rd * s.Q(i, s.ivdx[k]);
+            s.U(i, s.ivdy[k]) = rd * s.Q(i, s.ivdy[k]);
+            s.U(i, s.ivdz[k]) = rd * s.Q(i, s.ivdz[k]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Boundaries
+// ---------------------------------------------------------------------------------------------
+// periodic_boundaries (src/grid/boundary_types.f90:149-186): y rows first (active x only),
+// then x columns over all y (which fills the corners).
+void periodic_boundaries(oracle_state& s) {
+    const int ng = s.nghost;
+    if (s.ndim == 2) {
+        for (int ix = s.first_active; ix <= s.last_active; ++ix)
+            for (int g = 0; g < ng; ++g) {
+                int64_t bl = s.icell(ix, g), br = s.icell(ix, s.ny_max - 1 - g);
+                int64_t al = s.icell(ix, s.last_active_y - ng + 1 + g), ar = s.icell(ix, s.first_active_y + ng - 1 - g);
+                for (int v = 0; v < s.nvar; ++v) {
+                    s.U(bl, v) = s.U(al, v);
+                    s.U(br, v) = s.U(ar, v);
+                }
+            }
+    }
+    for (int g = 0; g < ng; ++g)
+        for (int iy = 0; iy < s.ny_max; ++iy) {
+            int64_t bl = s.icell(g, iy), br = s.icell(s.nx_max - 1 - g, iy);
+            int64_t al = s.icell(s.last_active - ng + 1 + g, iy), ar = s.icell(s.first_active + ng - 1 - g, iy);
+            for (int v = 0; v < s.nvar; ++v) {
+                s.U(bl, v) = s.U(al, v);
+                s.U(br, v) = s.U(ar, v);
+            }
+        }
+}
+
+// SOD apply_boundaries (src/setups/SOD/boundaries.f90:49-77): fixed left/right states along the
+// shock direction, periodic along the other one.
+void sod_boundaries(oracle_state& s) {
+    const int ng = s.nghost;
+    const double g1 = s.cfg.gamma - 1.0;
+    auto fix = [&](int64_t bl, int64_t br) {
+        s.U(bl, s.irho) = s.cfg.sod_rho_l;
+        s.U(br, s.irho) = s.cfg.sod_rho_r;
+        s.U(bl, s.iP) = s.cfg.sod_P_l / g1;
+        s.U(br, s.iP) = s.cfg.sod_P_r / g1;
+        s.U(bl, s.ivx) = 0.0; s.U(br, s.ivx) = 0.0;
+        s.U(bl, s.ivy) = 0.0; s.U(br, s.ivy) = 0.0;
+        s.U(bl, s.ivz) = 0.0; s.U(br, s.ivz) = 0.0;
+    };
+    if (s.ndim == 2) {
+        for (int ix = s.first_active; ix <= s.last_active; ++ix)
+            for (int g = 0; g < ng; ++g) {
+                int64_t bl = s.icell(ix, g), br = s.icell(ix, s.ny_max - 1 - g);
+                int64_t al = s.icell(ix, s.last_active_y - ng + 1 + g), ar = s.icell(ix, s.first_active_y + ng - 1 - g);
+                if (s.cfg.sod_direction == 1) fix(bl, br);
+                else for (int v = 0; v < s.nvar; ++v) { s.U(bl, v) = s.U(al, v); s.U(br, v) = s.U(ar, v); }
+            }
+    }
+    for (int g = 0; g < ng; ++g)
+        for (int iy = 0; iy < s.ny_max; ++iy) {
+            int64_t bl = s.icell(g, iy), br = s.icell(s.nx_max - 1 - g, iy);
+            int64_t al = s.icell(s.last_active - ng + 1 + g, iy), ar = s.icell(s.first_active + ng - 1 - g, iy);
+            if (s.cfg.sod_direction == 0) fix(bl, br);
+            else for (int v = 0; v < s.nvar; ++v) { s.U(bl, v) = s.U(al, v); s.U(br, v) = s.U(ar, v); }
+        }
+}
+
+// SI apply_boundaries (src/setups/SI/boundaries.f90:1-81): periodic along y; shear-periodic along
+// x with the azimuthal (vz) momentum shifted by -/+ rho q Omega L.  The first loop's `mom_new`
+// lines have no effect in the reference (values computed and discarded) and are omitted.
+void si_boundaries(oracle_state& s) {
+    const int ng = s.nghost;
+    const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, L = s.box_l;
+    for (int ix = s.first_active; ix <= s.last_active; ++ix)
+        for (int g = 0; g < ng; ++g) {
+            int64_t bl = s.icell(ix, g), br = s.icell(ix, s.ny_max - 1 - g);
+            int64_t al = s.icell(ix, s.last_active_y - ng + 1 + g), ar = s.icell(ix, s.first_active_y + ng - 1 - g);
+            for (int v = 0; v < s.nvar; ++v) { s.U(bl, v) = s.U(al, v); s.U(br, v) = s.U(ar, v); }
+        }
+    for (int g = 0; g < ng; ++g)
+        for (int iy = 0; iy < s.ny_max; ++iy) {
+            int64_t bl = s.icell(g, iy), br = s.icell(s.nx_max - 1 - g, iy);
+            int64_t al = s.icell(s.last_active - ng + 1 + g, iy), ar = s.icell(s.first_active + ng - 1 - g, iy);
+            for (int v = 0; v < s.nvar; ++v) { s.U(bl, v) = s.U(al, v); s.U(br, v) = s.U(ar, v); }
+            s.U(bl, s.ivz) = s.U(al, s.ivz) - s.U(al, s.irho) * qs * om * L;
+            s.U(br, s.ivz) = s.U(ar, s.ivz) + s.U(ar, s.irho) * qs * om * L;
+            for (int k = 0; k < s.ndust; ++k) {
+                s.U(bl, s.ivdz[k]) = s.U(al, s.ivdz[k]) - s.U(al, s.irhod[k]) * qs * om * L;
+                s.U(br, s.ivdz[k]) = s.U(ar, s.ivdz[k]) + s.U(ar, s.irhod[k]) * qs * om * L;
+            }
+        }
+}
+
+void apply_boundaries(oracle_state& s) {
+    switch (s.cfg.setup) {
+        case SHARK_SETUP_SOD: sod_boundaries(s); break;
+        case SHARK_SETUP_SI: si_boundaries(s); break;
+        default: periodic_boundaries(s); break;   // DUSTYWAVE (DUSTYWAVE/boundaries.f90), dustyTurb
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// compute_tstop per setup
+// ---------------------------------------------------------------------------------------------
+void compute_tstop(oracle_state& s) {
+    const int N = s.ndust;
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        for (int k = 0; k < N; ++k) {
+            double ts;
+            switch (s.cfg.setup) {
+                case SHARK_SETUP_DUSTYWAVE:   // DUSTYWAVE/setup.f90:212-221
+                    ts = s.Q(i, s.irhod[k]) * s.Q(i, s.irho) / s.cfg.dust_K[k] / (s.Q(i, s.irho));
+                    break;
+                case SHARK_SETUP_SI:          // SI/setup.f90:389-397 (constant, precomputed on host)
+                    ts = s.cfg.dust_tstop[k];
+                    break;
+                default:                      // SOD/setup.f90:179-185, Epstein
+                    ts = std::sqrt(pi * s.cfg.gamma / 8.0) * (s.cfg.rhograin) * s.SDUST(i, k) /
+                         (s.Q(i, s.irho) * s.cs[i]);
+                    break;
+            }
+            s.TSTOP(i, k) = ts;
+        }
+    }
+}
+
+// update_force_setup (SI/setup.f90:335-368); the other in-scope setups leave force at zero.
+void update_force_setup(oracle_state& s) {
+    if (s.cfg.setup != SHARK_SETUP_SI) return;
+    const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, r0 = s.cfg.si_rad0, eta = s.cfg.si_eta_stream;
+    const bool drag = s.flag(SHARK_FLAG_DRAG);
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        double xc = s.POS(i, 0) - half * s.box_l;
+        s.FORCE(i, 0) = 2.0 * qs * sq(om) * xc - 2.0 * om * s.Q(i, s.ivz) - 2.0 * r0 * om * eta;
+        s.FORCE(i, 1) = 0.0;
+        s.FORCE(i, 2) = 2.0 * om * s.Q(i, s.ivx);
+        for (int k = 0; k < s.ndust; ++k) {
+            s.FDUST(i, 0, k) = 2.0 * qs * sq(om) * xc - 2.0 * om * s.Q(i, s.ivdz[k]);
+            s.FDUST(i, 1, k) = 0.0;
+            s.FDUST(i, 2, k) = 2.0 * om * s.Q(i, s.ivdx[k]);
+            if (!drag) {
+                double ts = s.TSTOP(i, k), rr = s.Q(i, s.irhod[k]) / s.Q(i, s.irho);
+                s.FORCE(i, 0) = s.FORCE(i, 0) - rr * (s.Q(i, s.ivx) - s.Q(i, s.ivdx[k])) / ts;
+                s.FORCE(i, 1) = s.FORCE(i, 1) - rr * (s.Q(i, s.ivy) - s.Q(i, s.ivdy[k])) / ts;
+                s.FORCE(i, 2) = s.FORCE(i, 2) - rr * (s.Q(i, s.ivz) - s.Q(i, s.ivdz[k])) / ts;
+                s.FDUST(i, 0, k) = s.FDUST(i, 0, k) + (s.Q(i, s.ivx) - s.Q(i, s.ivdx[k])) / ts;
+                s.FDUST(i, 1, k) = s.FDUST(i, 1, k) + (s.Q(i, s.ivy) - s.Q(i, s.ivdy[k])) / ts;
+                s.FDUST(i, 2, k) = s.FDUST(i, 2, k) + (s.Q(i, s.ivz) - s.Q(i, s.ivdz[k])) / ts;
+            }
+        }
+    }
+}
+
+// setup_inloop (SI/setup.f90:299-332): Crank-Nicolson rotation, only without force_kick.
+void setup_inloop(oracle_state& s) {
+    if (s.cfg.setup != SHARK_SETUP_SI) return;
+    if (s.flag(SHARK_FLAG_FORCE_KICK)) return;
+    const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, r0 = s.cfg.si_rad0, eta = s.cfg.si_eta_stream;
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        double u = s.U(i, s.ivz) / s.U(i, s.irho);
+        double v = s.U(i, s.ivx) / s.U(i, s.irho);
+        double d = s.U(i, s.irho);
+        double Ohmdt = om * s.dt;
+        double AA = 2.0 * qs * om * (s.POS(i, 0) - half * s.box_l) - 2.0 * r0 * eta;
+        s.U(i, s.ivz) = d * (u * (1. - sq(Ohmdt)) + 2. * v * Ohmdt + AA * sq(Ohmdt)) / (1. + sq(Ohmdt));
+        s.U(i, s.ivx) = d * (v * (1. - sq(Ohmdt)) - 2. * u * Ohmdt + AA * Ohmdt) / (1. + sq(Ohmdt));
+        AA = 2.0 * qs * om * (s.POS(i, 0) - half * s.box_l);
+        for (int k = 0; k < s.ndust; ++k) {
+            u = s.U(i, s.ivdz[k]) / s.U(i, s.irhod[k]);
+            v = s.U(i, s.ivdx[k]) / s.U(i, s.irhod[k]);
+            d = s.U(i, s.irhod[k]);
+            s.U(i, s.ivdz[k]) = d * (u * (1. - sq(Ohmdt)) + 2. * v * Ohmdt + AA * sq(Ohmdt)) / (1. + sq(Ohmdt));
+            s.U(i, s.ivdx[k]) = d * (v * (1. - sq(Ohmdt)) - 2. * u * Ohmdt + AA * Ohmdt) / (1. + sq(Ohmdt));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// courant (src/solver/courant.f90:11-124), non-MHD, no gravity.  Serial like the reference.
+// Note `vv` in the force limiter is the LAST species' velocity sum (overwritten in the dust loop).
+// ---------------------------------------------------------------------------------------------
+void courant(oracle_state& s) {
+    const double CFL = s.cfg.cfl;
+    const bool fk = s.flag(SHARK_FLAG_FORCE_KICK);
+    double dt = 2e44;
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        double dxx;
+        if (s.ndim == 1) dxx = s.DX(i, 0);
+        else if (s.cfg.geom == 2) dxx = fmin2(s.DX(i, 0), s.radii_c[i] * s.DX(i, 1));
+        else dxx = fmin2(s.DX(i, 0), s.DX(i, 1));
+        double vv = std::fabs(s.Q(i, s.ivx)) + std::fabs(s.Q(i, s.ivy)) + std::fabs(s.Q(i, s.ivz));
+        double vmax = s.cs[i] + vv;
+        double ca = 0.0;
+        for (int k = 0; k < s.ndust; ++k) {
+            vv = std::fabs(s.Q(i, s.ivdx[k])) + std::fabs(s.Q(i, s.ivdy[k])) + std::fabs(s.Q(i, s.ivdz[k]));
+            vmax = fmax2(vmax, ca + vv);
+        }
+        dt = fmin2(dt, CFL * dxx / std::fabs(vmax));
+        if (fk) {
+            double force_max = std::sqrt(sq(s.FORCE(i, 0)) + sq(s.FORCE(i, 1)) + sq(s.FORCE(i, 2)));
+            for (int k = 0; k < s.ndust; ++k)
+                force_max = fmax2(force_max, std::sqrt(sq(s.FDUST(i, 0, k)) + sq(s.FDUST(i, 1, k)) + sq(s.FDUST(i, 2, k))));
+            if (vv != 0.0) {
+                double fratio = fmax2(force_max * dxx / sq(vv), 1e-3);
+                dt = fmin2(dt, CFL * dxx / vv * (std::sqrt(1.0 + 2.0 * CFL * fratio) - 1.0) / fratio);
+            }
+        }
+    }
+    s.dt = dt;
+}
+
+// kick (src/solver/force_kicks.f90:2-41); the energy fix-up condition is always true in practice
+// (iso_cs.ne.1 .or. non_standard_eos.ne.1 with non_standard_eos = -1).
+void kick(oracle_state& s, double coeffdt) {
+    const double dt = s.dt;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        double rho = s.U(i, s.irho);
+        double energy_old = half * sq(s.U(i, s.ivx)) / rho + half * sq(s.U(i, s.ivy)) / rho + half * sq(s.U(i, s.ivz)) / rho;
+        s.U(i, s.ivx) = s.U(i, s.ivx) + rho * coeffdt * dt * s.FORCE(i, 0);
+        s.U(i, s.ivy) = s.U(i, s.ivy) + rho * coeffdt * dt * s.FORCE(i, 1);
+        s.U(i, s.ivz) = s.U(i, s.ivz) + rho * coeffdt * dt * s.FORCE(i, 2);
+        double energy_new = half * sq(s.U(i, s.ivx)) / rho + half * sq(s.U(i, s.ivy)) / rho + half * sq(s.U(i, s.ivz)) / rho;
+        s.U(i, s.iP) = s.U(i, s.iP) + (energy_new - energy_old);
+        for (int k = 0; k < s.ndust; ++k) {
+            double rd = s.U(i, s.irhod[k]);
+            s.U(i, s.ivdx[k]) = s.U(i, s.ivdx[k]) + rd * coeffdt * dt * s.FDUST(i, 0, k);
+            s.U(i, s.ivdy[k]) = s.U(i, s.ivdy[k]) + rd * coeffdt * dt * s.FDUST(i, 1, k);
+            s.U(i, s.ivdz[k]) = s.U(i, s.ivdz[k]) + rd * coeffdt * dt * s.FDUST(i, 2, k);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// predictor (src/solver/godunov.f90:7-629), non-MHD, no gravity, no dust passive scalars.
+// In the reference, drx..dwy are OMP-private and zeroed once per thread; in 1D the y-slopes are
+// never assigned so they stay 0 for gas and dust alike.  The Cartesian source block
+// (`#if GE0M==0`, a typo that is always true) is evaluated first and, for GEOM==2, overwritten.
+// ---------------------------------------------------------------------------------------------
+void predictor(oracle_state& s) {
+    const double gamma = s.cfg.gamma, smallP = s.cfg.smallp, dt = s.dt;
+    const int N = s.ndust, nvar = s.nvar, st = s.cfg.slope_type;
+    const bool fk = s.flag(SHARK_FLAG_FORCE_KICK), polar = (s.cfg.geom == 2), two_d = (s.ndim == 2);
+    std::fill(s.qm.begin(), s.qm.end(), 0.0);
+    std::fill(s.qp.begin(), s.qp.end(), 0.0);
+#pragma omp parallel
+    {
+        std::vector<double> dq((size_t)nvar * 2, 0.0);  // dq(i,:,:) of the current cell
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            if (!s.active_pred[i]) continue;
+            const int ix = s.ixx(i), iy = s.iyy(i);
+            const double radius_polar = polar ? s.radii_c[i] : 1.0;
+            std::fill(dq.begin(), dq.end(), 0.0);
+            if (st > 0) {
+                for (int v = 0; v < nvar; ++v) {
+                    int64_t il = s.icell(ix - 1, iy), ir = s.icell(ix + 1, iy);
+                    dq[v] = slope_limit(st, 2.0 * (s.Q(i, v) - s.Q(il, v)) / (s.DX(i, 0) + s.DX(il, 0)),
+                                        2.0 * (s.Q(ir, v) - s.Q(i, v)) / (s.DX(ir, 0) + s.DX(i, 0)));
+                    if (two_d) {
+                        il = s.icell(ix, iy - 1);
+                        ir = s.icell(ix, iy + 1);
+                        dq[nvar + v] = slope_limit(st, 2.0 * (s.Q(i, v) - s.Q(il, v)) / (s.DX(i, 1) + s.DX(il, 1)),
+                                                   2.0 * (s.Q(ir, v) - s.Q(i, v)) / (s.DX(ir, 1) + s.DX(i, 1))) /
+                                       radius_polar;
+                    }
+                }
+            }
+            double drx, dry = 0, dpx, dpy = 0, dux, duy = 0, dvx, dvy = 0, dwx, dwy = 0;
+            double r_rho = s.Q(i, s.irho);
+            double u = s.Q(i, s.ivx);
+            dux = dq[s.ivx];
+            drx = dq[s.irho];
+            double w = s.Q(i, s.ivz);
+            dwx = dq[s.ivz];
+            double v = s.Q(i, s.ivy);
+            dvx = dq[s.ivy];
+            double p = s.Q(i, s.iP);
+            dpx = dq[s.iP];
+            const double csi = s.cs[i];
+            if (s.cfg.iso_cs == 1) {
+                p = s.Q(i, s.irho) * sq(csi);
+                dpx = dq[s.irho] * sq(csi);
+            }
+            if (two_d) {
+                duy = dq[nvar + s.ivx];
+                dry = dq[nvar + s.irho];
+                dvy = dq[nvar + s.ivy];
+                dpy = dq[nvar + s.iP];
+                dwy = dq[nvar + s.ivz];
+                if (s.cfg.iso_cs == 1) dpy = dq[nvar + s.irho] * sq(csi);
+            }
+            if (fk) {
+                u = u + s.FORCE(i, 0) * half * dt;
+                v = v + s.FORCE(i, 1) * half * dt;
+                w = w + s.FORCE(i, 2) * half * dt;
+            }
+            double sr0 = -u * drx - v * dry - (dux + dvy) * r_rho;
+            double sp0 = -u * dpx - v * dpy - (dux + dvy) * gamma * p;
+            double su0 = -u * dux - v * duy - (dpx) / r_rho;
+            double sv0 = -u * dvx - v * dvy - (dpy) / r_rho;
+            double sw0 = -u * dwx - v * dwy;
+            if (polar) {
+                sr0 = -u * drx - v * dry - (dux + dvy) * r_rho - r_rho * u / radius_polar;
+                sp0 = -u * dpx - v * dpy - (dux + dvy) * gamma * p - gamma * p * u / radius_polar;
+                su0 = -u * dux - v * duy - (dpx) / r_rho + (sq(v)) / radius_polar;
+                sv0 = -u * dvx - v * dvy - (dpy) / r_rho - u * v / radius_polar;
+                sw0 = -u * dwx - v * dwy;
+            }
+            double dx_loc = s.DX(i, 0);
+            s.QM(i, s.irho, 0) = r_rho + half * dt * sr0 + half * drx * dx_loc;
+            s.QM(i, s.ivx, 0) = u + half * dt * su0 + half * dux * dx_loc;
+            s.QM(i, s.iP, 0) = fmax2(p + half * dt * sp0 + half * dpx * dx_loc, smallP);
+            s.QM(i, s.ivy, 0) = v + half * dt * sv0 + half * dvx * dx_loc;
+            s.QM(i, s.ivz, 0) = w + half * dt * sw0 + half * dwx * dx_loc;
+            s.QP(i, s.irho, 0) = r_rho + half * dt * sr0 - half * drx * dx_loc;
+            s.QP(i, s.ivx, 0) = u + half * dt * su0 - half * dux * dx_loc;
+            s.QP(i, s.iP, 0) = fmax2(p + half * dt * sp0 - half * dpx * dx_loc, smallP);
+            s.QP(i, s.ivy, 0) = v + half * dt * sv0 - half * dvx * dx_loc;
+            s.QP(i, s.ivz, 0) = w + half * dt * sw0 - half * dwx * dx_loc;
+            if (two_d) {
+                dx_loc = radius_polar * s.DX(i, 1);
+                s.QM(i, s.irho, 1) = r_rho + half * dt * sr0 + half * dry * dx_loc;
+                s.QM(i, s.ivx, 1) = u + half * dt * su0 + half * duy * dx_loc;
+                s.QM(i, s.iP, 1) = fmax2(p + half * dt * sp0 + half * dpy * dx_loc, smallP);
+                s.QM(i, s.ivy, 1) = v + half * dt * sv0 + half * dvy * dx_loc;
+                s.QM(i, s.ivz, 1) = w + half * dt * sw0 + half * dwy * dx_loc;
+                s.QP(i, s.irho, 1) = r_rho + half * dt * sr0 - half * dry * dx_loc;
+                s.QP(i, s.ivx, 1) = u + half * dt * su0 - half * duy * dx_loc;
+                s.QP(i, s.iP, 1) = fmax2(p + half * dt * sp0 - half * dpy * dx_loc, smallP);
+                s.QP(i, s.ivy, 1) = v + half * dt * sv0 - half * dvy * dx_loc;
+                s.QP(i, s.ivz, 1) = w + half * dt * sw0 - half * dwy * dx_loc;
+            }
+            // dust (godunov.f90:359-510)
+            for (int k = 0; k < N; ++k) {
+                const int irs = s.irhod[k], ivxs = s.ivdx[k], ivys = s.ivdy[k], ivzs = s.ivdz[k];
+                r_rho = s.Q(i, irs);
+                u = s.Q(i, ivxs);
+                dux = dq[ivxs];
+                drx = dq[irs];
+                v = s.Q(i, ivys);
+                dvx = dq[ivys];
+                w = s.Q(i, ivzs);
+                dwx = dq[ivzs];
+                if (two_d) {
+                    dry = dq[nvar + irs];
+                    duy = dq[nvar + ivxs];
+                    dvy = dq[nvar + ivys];
+                    dwy = dq[nvar + ivzs];
+                }
+                if (fk) {
+                    u = u + s.FDUST(i, 0, k) * half * dt;
+                    v = v + s.FDUST(i, 1, k) * half * dt;
+                    w = w + s.FDUST(i, 2, k) * half * dt;
+                }
+                sr0 = -u * drx - v * dry - (dux + dvy) * r_rho;
+                su0 = -u * dux - v * duy;
+                sv0 = -u * dvx - v * dvy;
+                sw0 = -u * dwx - v * dwy;
+                if (polar) {
+                    sr0 = sr0 - r_rho * u / radius_polar;
+                    su0 = su0 + sq(v) / radius_polar;
+                    sv0 = sv0 - u * v / radius_polar;
+                }
+                dx_loc = s.DX(i, 0);
+                s.QM(i, irs, 0) = r_rho + half * dt * sr0 + half * drx * dx_loc;
+                s.QM(i, ivxs, 0) = u + half * dt * su0 + half * dux * dx_loc;
+                s.QM(i, ivys, 0) = v + half * dt * sv0 + half * dvx * dx_loc;
+                s.QM(i, ivzs, 0) = w + half * dt * sw0 + half * dwx * dx_loc;
+                s.QP(i, irs, 0) = r_rho + half * dt * sr0 - half * drx * dx_loc;
+                s.QP(i, ivxs, 0) = u + half * dt * su0 - half * dux * dx_loc;
+                s.QP(i, ivys, 0) = v + half * dt * sv0 - half * dvx * dx_loc;
+                s.QP(i, ivzs, 0) = w + half * dt * sw0 - half * dwx * dx_loc;
+                if (two_d) {
+                    dx_loc = radius_polar * s.DX(i, 1);
+                    s.QM(i, irs, 1) = r_rho + half * dt * sr0 + half * dry * dx_loc;
+                    s.QM(i, ivxs, 1) = u + half * dt * su0 + half * duy * dx_loc;
+                    s.QM(i, ivys, 1) = v + half * dt * sv0 + half * dvy * dx_loc;
+                    s.QM(i, ivzs, 1) = w + half * dt * sw0 + half * dwy * dx_loc;
+                    s.QP(i, irs, 1) = r_rho + half * dt * sr0 - half * dry * dx_loc;
+                    s.QP(i, ivxs, 1) = u + half * dt * su0 - half * duy * dx_loc;
+                    s.QP(i, ivys, 1) = v + half * dt * sv0 - half * dvy * dx_loc;
+                    s.QP(i, ivzs, 1) = w + half * dt * sw0 - half * dwy * dx_loc;
+                }
+            }
+            // isothermal pressure on the faces (godunov.f90:606-611)
+            if (s.cfg.iso_cs == 1) {
+                for (int d = 0; d < s.ndim; ++d) {
+                    s.QP(i, s.iP, d) = sq(csi) * s.QP(i, s.irho, d);
+                    s.QM(i, s.iP, d) = sq(csi) * s.QM(i, s.irho, d);
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Riemann solvers (src/solver/solvers.f90), non-MHD branches.
+// ---------------------------------------------------------------------------------------------
+struct GasFace {  // the five gas fluxes in (rho, normal mom, transverse mom, z mom, energy) order
+    double rho, mn, mt, mz, e;
+};
+
+// solver_llf (solvers.f90:4-155)
+GasFace solver_llf(double gamma, double rho_lft, double u_lft, double v_lft, double w_lft, double P_lft,
+                   double rho_rgt, double u_rgt, double v_rgt, double w_rgt, double P_rgt, double csl, double csr) {
+    double mom_u_rgt = rho_rgt * u_rgt, mom_u_lft = rho_lft * u_lft;
+    double E_rgt = P_rgt / (gamma - 1.0) + half * rho_rgt * sq(u_rgt);
+    double E_lft = P_lft / (gamma - 1.0) + half * rho_lft * sq(u_lft);
+    double mom_v_rgt = rho_rgt * v_rgt, mom_v_lft = rho_lft * v_lft;
+    E_rgt = E_rgt + half * rho_rgt * sq(v_rgt);
+    E_lft = E_lft + half * rho_lft * sq(v_lft);
+    double mom_w_rgt = rho_rgt * w_rgt, mom_w_lft = rho_lft * w_lft;
+    E_rgt = E_rgt + half * rho_rgt * sq(w_rgt);
+    E_lft = E_lft + half * rho_lft * sq(w_lft);
+    double flx_rho_rgt = rho_rgt * u_rgt, flx_rho_lft = rho_lft * u_lft;
+    double flx_mom_u_rgt = (rho_rgt * sq(u_rgt) + P_rgt), flx_mom_u_lft = (rho_lft * sq(u_lft) + P_lft);
+    double flx_mom_v_rgt = rho_rgt * u_rgt * v_rgt, flx_mom_v_lft = rho_lft * u_lft * v_lft;
+    double flx_mom_w_rgt = rho_rgt * u_rgt * w_rgt, flx_mom_w_lft = rho_lft * u_lft * w_lft;
+    double flx_P_rgt = (E_rgt + P_rgt) * u_rgt, flx_P_lft = (E_lft + P_lft) * u_lft;
+    double lam = fmax2(std::fabs(u_lft) + csl, std::fabs(u_rgt) + csr);
+    GasFace f;
+    f.rho = half * (flx_rho_lft + flx_rho_rgt) - half * lam * (rho_rgt - rho_lft);
+    f.mn = half * (flx_mom_u_lft + flx_mom_u_rgt) - half * lam * (mom_u_rgt - mom_u_lft);
+    f.mt = half * (flx_mom_v_lft + flx_mom_v_rgt) - half * lam * (mom_v_rgt - mom_v_lft);
+    f.mz = half * (flx_mom_w_lft + flx_mom_w_rgt) - half * lam * (mom_w_rgt - mom_w_lft);
+    f.e = half * (flx_P_lft + flx_P_rgt) - half * lam * (E_rgt - E_lft);
+    return f;
+}
+
+// solver_hll (solvers.f90:157-306)
+GasFace solver_hll(double gamma, double rho_lft, double u_lft, double v_lft, double w_lft, double P_lft,
+                   double rho_rgt, double u_rgt, double v_rgt, double w_rgt, double P_rgt, double csl, double csr) {
+    double mom_u_rgt = rho_rgt * u_rgt, mom_u_lft = rho_lft * u_lft;
+    double E_rgt = P_rgt / (gamma - 1.0) + half * rho_rgt * sq(u_rgt);
+    double E_lft = P_lft / (gamma - 1.0) + half * rho_lft * sq(u_lft);
+    double mom_v_rgt = rho_rgt * v_rgt, mom_v_lft = rho_lft * v_lft;
+    E_rgt = E_rgt + half * rho_rgt * sq(v_rgt);
+    E_lft = E_lft + half * rho_lft * sq(v_lft);
+    double mom_w_rgt = rho_rgt * w_rgt, mom_w_lft = rho_lft * w_lft;
+    E_rgt = E_rgt + half * rho_rgt * sq(w_rgt);
+    E_lft = E_lft + half * rho_lft * sq(w_lft);
+    double flx_rho_rgt = rho_rgt * u_rgt, flx_rho_lft = rho_lft * u_lft;
+    double flx_mom_u_rgt = (rho_rgt * sq(u_rgt) + P_rgt), flx_mom_u_lft = (rho_lft * sq(u_lft) + P_lft);
+    double flx_mom_v_rgt = rho_rgt * u_rgt * v_rgt, flx_mom_v_lft = rho_lft * u_lft * v_lft;
+    double flx_mom_w_rgt = rho_rgt * u_rgt * w_rgt, flx_mom_w_lft = rho_lft * u_lft * w_lft;
+    double flx_P_rgt = (E_rgt + P_rgt) * u_rgt, flx_P_lft = (E_lft + P_lft) * u_lft;
+    double S_lft = fmin2(fmin2(u_lft, u_rgt) - fmax2(csl, csr), 0.0);
+    double S_rgt = fmax2(fmax2(u_lft, u_rgt) + fmax2(csl, csr), 0.0);
+    GasFace f;
+    f.rho = (S_rgt * flx_rho_lft - S_lft * flx_rho_rgt + S_rgt * S_lft * (rho_rgt - rho_lft)) / (S_rgt - S_lft);
+    f.mn = (S_rgt * flx_mom_u_lft - S_lft * flx_mom_u_rgt + S_rgt * S_lft * (mom_u_rgt - mom_u_lft)) / (S_rgt - S_lft);
+    f.mt = (S_rgt * flx_mom_v_lft - S_lft * flx_mom_v_rgt + S_rgt * S_lft * (mom_v_rgt - mom_v_lft)) / (S_rgt - S_lft);
+    f.mz = (S_rgt * flx_mom_w_lft - S_lft * flx_mom_w_rgt + S_rgt * S_lft * (mom_w_rgt - mom_w_lft)) / (S_rgt - S_lft);
+    f.e = (S_rgt * flx_P_lft - S_lft * flx_P_rgt + S_rgt * S_lft * (E_rgt - E_lft)) / (S_rgt - S_lft);
+    return f;
+}
+
+// solver_hllc (solvers.f90:308-500)
+GasFace solver_hllc(double gamma, double rho_lft, double u_lft, double v_lft, double w_lft, double P_lft,
+                    double rho_rgt, double u_rgt, double v_rgt, double w_rgt, double P_rgt, double csl, double csr) {
+    double E_rgt = P_rgt / (gamma - 1.0) + half * rho_rgt * sq(u_rgt) + half * rho_rgt * sq(v_rgt) + half * rho_rgt * sq(w_rgt);
+    double E_lft = P_lft / (gamma - 1.0) + half * rho_lft * sq(u_lft) + half * rho_lft * sq(v_lft) + half * rho_lft * sq(w_lft);
+    double S_lft = fmin2(fmin2(u_lft, u_rgt) - fmax2(csl, csr), 0.0);
+    double S_rgt = fmax2(fmax2(u_lft, u_rgt) + fmax2(csl, csr), 0.0);
+    double hllc_l = rho_lft * (u_lft - S_lft);
+    double hllc_r = rho_rgt * (S_rgt - u_rgt);
+    double ustar = (hllc_r * u_rgt + hllc_l * u_lft + (P_lft - P_rgt)) / (hllc_r + hllc_l);
+    double Pstar = (hllc_r * P_lft + hllc_l * P_rgt + hllc_l * hllc_r * (u_lft - u_rgt)) / (hllc_r + hllc_l);
+    double rhostarleft = rho_lft * (S_lft - u_lft) / (S_lft - ustar);
+    double estarleft = ((S_lft - u_lft) * E_lft - P_lft * u_lft + Pstar * ustar) / (S_lft - ustar);
+    double rhostarright = rho_rgt * (S_rgt - u_rgt) / (S_rgt - ustar);
+    double estarright = ((S_rgt - u_rgt) * E_rgt - P_rgt * u_rgt + Pstar * ustar) / (S_rgt - ustar);
+    double r_o, u_o, P_o, e_o;
+    if (S_lft > 0.0) { r_o = rho_lft; u_o = u_lft; P_o = P_lft; e_o = E_lft; }
+    else if (ustar > 0.0) { r_o = rhostarleft; u_o = ustar; P_o = Pstar; e_o = estarleft; }
+    else if (S_rgt > 0.0) { r_o = rhostarright; u_o = ustar; P_o = Pstar; e_o = estarright; }
+    else { r_o = rho_rgt; u_o = u_rgt; P_o = P_rgt; e_o = E_rgt; }
+    GasFace f;
+    f.rho = r_o * u_o;
+    f.mn = r_o * u_o * u_o + P_o;
+    f.e = (e_o + P_o) * u_o;
+    if (ustar > 0.0) { f.mt = r_o * u_o * v_lft; f.mz = r_o * u_o * w_lft; }
+    else { f.mt = r_o * u_o * v_rgt; f.mz = r_o * u_o * w_rgt; }
+    return f;
+}
+
+struct DustFace { double rho, mn, mt, mz; };
+
+// solver_dust_Huang_Bai (solvers.f90:506-698), one species.
+DustFace solver_dust_hb(double rho_lft, double u_lft, double v_lft, double w_lft,
+                        double rho_rgt, double u_rgt, double v_rgt, double w_rgt) {
+    double flx_rho_rgt = rho_rgt * u_rgt, flx_rho_lft = rho_lft * u_lft;
+    double flx_mom_u_rgt = rho_rgt * sq(u_rgt), flx_mom_u_lft = rho_lft * sq(u_lft);
+    double flx_mom_v_rgt = rho_rgt * u_rgt * v_rgt, flx_mom_v_lft = rho_lft * u_lft * v_lft;
+    double flx_mom_w_rgt = rho_rgt * u_rgt * w_rgt, flx_mom_w_lft = rho_lft * u_lft * w_lft;
+    DustFace f{0.0, 0.0, 0.0, 0.0};
+    if (u_rgt > 0.0 && u_lft > 0.0) {
+        f = {flx_rho_lft, flx_mom_u_lft, flx_mom_v_lft, flx_mom_w_lft};
+    } else if (u_lft < 0.0 && u_rgt < 0.0) {
+        f = {flx_rho_rgt, flx_mom_u_rgt, flx_mom_v_rgt, flx_mom_w_rgt};
+    } else if (u_lft < 0.0 && u_rgt > 0.0) {
+        f = {0.0, 0.0, 0.0, 0.0};
+    } else if (u_lft > 0.0 && u_rgt < 0.0) {
+        f = {flx_rho_lft + flx_rho_rgt, flx_mom_u_lft + flx_mom_u_rgt, flx_mom_v_lft + flx_mom_v_rgt,
+             flx_mom_w_lft + flx_mom_w_rgt};
+    }
+    return f;
+}
+
+// solver_dust_llf (solvers.f90:840-1001), non-MHD, one species.
+DustFace solver_dust_llf(double rho_lft, double u_lft, double v_lft, double w_lft,
+                         double rho_rgt, double u_rgt, double v_rgt, double w_rgt) {
+    double mom_u_rgt = rho_rgt * u_rgt, mom_u_lft = rho_lft * u_lft;
+    double mom_v_rgt = rho_rgt * v_rgt, mom_v_lft = rho_lft * v_lft;
+    double mom_w_rgt = rho_rgt * w_rgt, mom_w_lft = rho_lft * w_lft;
+    double flx_rho_rgt = rho_rgt * u_rgt, flx_rho_lft = rho_lft * u_lft;
+    double flx_mom_u_rgt = rho_rgt * sq(u_rgt), flx_mom_u_lft = rho_lft * sq(u_lft);
+    double flx_mom_v_rgt = rho_rgt * u_rgt * v_rgt, flx_mom_v_lft = rho_lft * u_lft * v_lft;
+    double flx_mom_w_rgt = rho_rgt * u_rgt * w_rgt, flx_mom_w_lft = rho_lft * u_lft * w_lft;
+    double lam = fmax2(std::fabs(u_lft), std::fabs(u_rgt));
+    DustFace f;
+    f.rho = half * (flx_rho_lft + flx_rho_rgt) - half * lam * (rho_rgt - rho_lft);
+    f.mn = half * (flx_mom_u_lft + flx_mom_u_rgt) - half * lam * (mom_u_rgt - mom_u_lft);
+    f.mt = half * (flx_mom_v_lft + flx_mom_v_rgt) - half * lam * (mom_v_rgt - mom_v_lft);
+    f.mz = half * (flx_mom_w_lft + flx_mom_w_rgt) - half * lam * (mom_w_rgt - mom_w_lft);
+    return f;
+}
+
+// solver_dust_hll (solvers.f90:1010-1194), non-MHD, one species.
+DustFace solver_dust_hll(double rho_lft, double u_lft, double v_lft, double w_lft,
+                         double rho_rgt, double u_rgt, double v_rgt, double w_rgt) {
+    double mom_u_rgt = rho_rgt * u_rgt, mom_u_lft = rho_lft * u_lft;
+    double mom_v_rgt = rho_rgt * v_rgt, mom_v_lft = rho_lft * v_lft;
+    double mom_w_rgt = rho_rgt * w_rgt, mom_w_lft = rho_lft * w_lft;
+    double flx_rho_rgt = rho_rgt * u_rgt, flx_rho_lft = rho_lft * u_lft;
+    double flx_mom_u_rgt = rho_rgt * sq(u_rgt), flx_mom_u_lft = rho_lft * sq(u_lft);
+    double flx_mom_v_rgt = rho_rgt * u_rgt * v_rgt, flx_mom_v_lft = rho_lft * u_lft * v_lft;
+    double flx_mom_w_rgt = rho_rgt * u_rgt * w_rgt, flx_mom_w_lft = rho_lft * u_lft * w_lft;
+    double S_lft = fmin2(fmin2(u_lft, u_rgt), 0.0);
+    double S_rgt = fmax2(fmax2(u_lft, u_rgt), 0.0);
+    DustFace f{0.0, 0.0, 0.0, 0.0};
+    if (S_rgt - S_lft != 0.0) {
+        f.rho = (S_rgt * flx_rho_lft - S_lft * flx_rho_rgt + S_rgt * S_lft * (rho_rgt - rho_lft)) / (S_rgt - S_lft);
+        f.mn = (S_rgt * flx_mom_u_lft - S_lft * flx_mom_u_rgt + S_rgt * S_lft * (mom_u_rgt - mom_u_lft)) / (S_rgt - S_lft);
+        f.mt = (S_rgt * flx_mom_v_lft - S_lft * flx_mom_v_rgt + S_rgt * S_lft * (mom_v_rgt - mom_v_lft)) / (S_rgt - S_lft);
+        f.mz = (S_rgt * flx_mom_w_lft - S_lft * flx_mom_w_rgt + S_rgt * S_lft * (mom_w_rgt - mom_w_lft)) / (S_rgt - S_lft);
+    }
+    return f;
+}
+
+// solve_wrapper (godunov.f90:768-833): gas solver then each dust species, flx in nvar order.
+void solve_wrapper(const oracle_state& s, const double* ql, const double* qr, double* flx, double csl,
+                   double csr, int idim) {
+    const int ivn = s.index_vn[idim], ivt = s.index_vt[idim];
+    GasFace g;
+    const double gamma = s.cfg.gamma;
+    if (s.cfg.solver == 0)
+        g = solver_llf(gamma, ql[0], ql[ivn], ql[ivt], ql[3], ql[4], qr[0], qr[ivn], qr[ivt], qr[3], qr[4], csl, csr);
+    else if (s.cfg.solver == 1)
+        g = solver_hll(gamma, ql[0], ql[ivn], ql[ivt], ql[3], ql[4], qr[0], qr[ivn], qr[ivt], qr[3], qr[4], csl, csr);
+    else
+        g = solver_hllc(gamma, ql[0], ql[ivn], ql[ivt], ql[3], ql[4], qr[0], qr[ivn], qr[ivt], qr[3], qr[4], csl, csr);
+    flx[0] = g.rho;
+    flx[ivn] = g.mn;
+    flx[ivt] = g.mt;
+    flx[3] = g.mz;
+    flx[4] = g.e;
+    for (int k = 0; k < s.ndust; ++k) {
+        const int ir = s.irhod[k], iu = s.index_vdn[k * 2 + idim], iv = s.index_vdt[k * 2 + idim], iw = s.ivdz[k];
+        DustFace d;
+        if (s.cfg.solverdust == 0) d = solver_dust_hb(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw]);
+        else if (s.cfg.solverdust == 1) d = solver_dust_llf(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw]);
+        else d = solver_dust_hll(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw]);
+        flx[ir] = d.rho;
+        flx[iu] = d.mn;
+        flx[iv] = d.mt;
+        flx[iw] = d.mz;
+    }
+}
+
+// add_delta_u (godunov.f90:633-760)
+void add_delta_u(oracle_state& s) {
+    const int nvar = s.nvar;
+    const double gamma = s.cfg.gamma, dt = s.dt;
+    const bool iso = (s.cfg.iso_cs == 1), two_d = (s.ndim == 2);
+    std::fill(s.flux.begin(), s.flux.end(), 0.0);
+#pragma omp parallel
+    {
+        std::vector<double> ql(nvar), qr(nvar), flx(nvar);
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            if (!s.active_pred[i]) continue;
+            const int ix = s.ixx(i), iy = s.iyy(i);
+            for (int d = 0; d < (two_d ? 2 : 1); ++d) {
+                int64_t il = (d == 0) ? s.icell(ix - 1, iy) : s.icell(ix, iy - 1);
+                for (int v = 0; v < nvar; ++v) {
+                    ql[v] = s.QM(il, v, d);
+                    qr[v] = s.QP(i, v, d);
+                    flx[v] = 0.0;
+                }
+                double csl, csr;
+                if (iso) {
+                    csl = s.cs[il];
+                    csr = s.cs[i];
+                } else {
+                    csl = std::sqrt(gamma * ql[s.iP] / ql[s.irho]);
+                    csr = std::sqrt(gamma * qr[s.iP] / qr[s.irho]);
+                }
+                solve_wrapper(s, ql.data(), qr.data(), flx.data(), csl, csr, d);
+                for (int v = 0; v < nvar; ++v) s.FLX(i, v, d) = flx[v];
+            }
+        }
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            if (!s.active[i]) continue;
+            const int ix = s.ixx(i), iy = s.iyy(i);
+            int64_t il = s.icell(ix + 1, iy);
+            if (!two_d) {
+                for (int v = 0; v < nvar; ++v)
+                    s.U(i, v) = s.U(i, v) + (s.FLX(i, v, 0) * s.SURF(i, 0) - s.FLX(il, v, 0) * s.SURF(il, 0)) / s.vol[i] * dt;
+            } else {
+                int64_t ily = s.icell(ix, iy + 1);
+                for (int v = 0; v < nvar; ++v)
+                    s.U(i, v) = s.U(i, v) + (s.FLX(i, v, 0) * s.SURF(i, 0) - s.FLX(il, v, 0) * s.SURF(il, 0)) / s.vol[i] * dt +
+                                (s.FLX(i, v, 1) * s.SURF(i, 1) - s.FLX(ily, v, 1) * s.SURF(ily, 1)) / s.vol[i] * dt;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Source_terms (src/solver/source_terms.f90:1-118,221), non-MHD, no gravity.
+// ---------------------------------------------------------------------------------------------
+void source_terms(oracle_state& s) {
+    const double dt = s.dt;
+    const bool polar = (s.cfg.geom == 2), br = s.flag(SHARK_FLAG_BACK_REACTION), visc = s.flag(SHARK_FLAG_VISCOSITY);
+    if (!polar && !(br && s.cfg.iso_cs < 1 && s.ndust > 0) && !visc) return;   // S_U == 0
+    std::vector<double> S((size_t)s.ncells * s.nvar, 0.0);
+    auto SU = [&](int64_t i, int v) -> double& { return S[(size_t)v * s.ncells + i]; };
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        if (polar) {
+            double rc = s.radii_c[i];
+            SU(i, s.ivx) = SU(i, s.ivx) + dt * (s.Q(i, s.irho) * sq(s.Q(i, s.ivy)) + s.Q(i, s.iP)) / rc;
+            SU(i, s.ivy) = SU(i, s.ivy) - dt * (s.Q(i, s.irho) * s.Q(i, s.ivy) * s.Q(i, s.ivx) / rc);
+            for (int k = 0; k < s.ndust; ++k) {
+                SU(i, s.ivdx[k]) = SU(i, s.ivdx[k]) + dt * (s.Q(i, s.irhod[k]) * sq(s.Q(i, s.ivdy[k])) / rc);
+                SU(i, s.ivdy[k]) = SU(i, s.ivdy[k]) - dt * (s.Q(i, s.irhod[k]) * s.Q(i, s.ivdy[k]) * s.Q(i, s.ivdx[k]) / rc);
+            }
+        }
+        if (s.ndust > 0 && br && s.cfg.iso_cs < 1) {
+            for (int k = 0; k < s.ndust; ++k) {
+                double ts = s.TSTOP(i, k);
+                SU(i, s.iP) = SU(i, s.iP) + dt * (s.Q(i, s.ivx) * (s.Q(i, s.ivx) - s.Q(i, s.ivdx[k]))) / ts +
+                              dt * (s.Q(i, s.ivy) * (s.Q(i, s.ivy) - s.Q(i, s.ivdy[k]))) / ts +
+                              dt * (s.Q(i, s.ivz) * (s.Q(i, s.ivz) - s.Q(i, s.ivdz[k]))) / ts;
+            }
+        }
+        // viscosity (source_terms.f90:99-118) is rejected at create time (not used by any config).
+    }
+    for (size_t j = 0; j < S.size(); ++j) s.u[j] = s.u[j] + S[j];
+}
+
+// ---------------------------------------------------------------------------------------------
+// dust_drag (src/dust/dust_drag.f90:2-75): Krapp et al. implicit multi-species drag + floor.
+// ---------------------------------------------------------------------------------------------
+void dust_drag(oracle_state& s, double coeffdt) {
+    const int N = s.ndust;
+    const double dt = s.dt, dmin = s.cfg.dust_ratio_min;
+    const bool br = s.flag(SHARK_FLAG_BACK_REACTION);
+#pragma omp parallel
+    {
+        std::vector<double> alphak(N);
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            if (!s.active[i]) continue;
+            double rhon = s.U(i, s.irho), pnx = s.U(i, s.ivx), pny = s.U(i, s.ivy), pnz = s.U(i, s.ivz);
+            for (int k = 0; k < N; ++k) {
+                alphak[k] = coeffdt * dt / s.TSTOP(i, k);
+                pnx = pnx + alphak[k] / (1.0 + alphak[k]) * s.U(i, s.ivdx[k]);
+                pny = pny + alphak[k] / (1.0 + alphak[k]) * s.U(i, s.ivdy[k]);
+                pnz = pnz + alphak[k] / (1.0 + alphak[k]) * s.U(i, s.ivdz[k]);
+                rhon = rhon + alphak[k] / (1.0 + alphak[k]) * s.U(i, s.irhod[k]);
+            }
+            for (int k = 0; k < N; ++k) {
+                double a = alphak[k];
+                s.U(i, s.ivdx[k]) = s.U(i, s.ivdx[k]) / (1.0 + a) + (a / (1.0 + a)) * pnx / rhon * s.U(i, s.irhod[k]);
+                s.U(i, s.ivdy[k]) = s.U(i, s.ivdy[k]) / (1.0 + a) + (a / (1.0 + a)) * pny / rhon * s.U(i, s.irhod[k]);
+                s.U(i, s.ivdz[k]) = s.U(i, s.ivdz[k]) / (1.0 + a) + (a / (1.0 + a)) * pnz / rhon * s.U(i, s.irhod[k]);
+            }
+            if (br) {
+                s.U(i, s.ivx) = pnx / rhon * s.U(i, s.irho);
+                s.U(i, s.ivy) = pny / rhon * s.U(i, s.irho);
+                s.U(i, s.ivz) = pnz / rhon * s.U(i, s.irho);
+            }
+        }
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            if (!s.active[i]) continue;
+            for (int k = 0; k < N; ++k)
+                s.U(i, s.irhod[k]) = fmax2(s.U(i, s.irho) * dmin, s.U(i, s.irhod[k]));
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// solve (src/solver/solve.f90:10-181) for the in-scope configurations.
+// ---------------------------------------------------------------------------------------------
+void solve(oracle_state& s) {
+    const bool fk = s.flag(SHARK_FLAG_FORCE_KICK);
+    apply_boundaries(s);
+    ctoprim(s);
+    if (fk) update_force_setup(s);
+    if (s.ndust > 0) {
+        // distribution_dust(.false.): epsilondust = rho_d/rho over all cells (dust_init.f90:76-82)
+        for (int k = 0; k < s.ndust; ++k)
+            for (int64_t i = 0; i < s.ncells; ++i) s.EPSD(i, k) = s.Q(i, s.irhod[k]) / s.Q(i, s.irho);
+        compute_tstop(s);
+    }
+    courant(s);
+    if (fk) kick(s, 1.0);
+    predictor(s);
+    add_delta_u(s);
+    source_terms(s);
+    if (s.ndust > 0 && s.flag(SHARK_FLAG_DRAG)) dust_drag(s, 1.0);
+    setup_inloop(s);
+}
+
+// Counter-based uniform deviate in [0,1): splitmix64 of (seed, counter).
+inline double hash_uniform(uint64_t seed, uint64_t counter) {
+    uint64_t z = seed * 0x9E3779B97F4A7C15ull + counter + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Initial conditions
+// ---------------------------------------------------------------------------------------------
+// SOD setup (src/setups/SOD/setup.f90:1-46)
+void setup_sod(oracle_state& s) {
+    std::fill(s.q.begin(), s.q.end(), 0.0);
+    for (int iy = 0; iy < s.ny_max; ++iy)
+        for (int ix = 0; ix < s.nx_max; ++ix) {
+            int64_t c = s.icell(ix, iy);
+            s.Q(c, s.irho) = s.cfg.sod_rho_l;
+            s.Q(c, s.ivx) = 0.0;
+            s.Q(c, s.iP) = s.cfg.sod_P_l;
+            double pos = (s.cfg.sod_direction == 0) ? s.POS(c, 0) : s.POS(c, (s.ndim == 2) ? 1 : 0);
+            if (pos > half) {
+                s.Q(c, s.irho) = s.cfg.sod_rho_r;
+                s.Q(c, s.ivx) = 0.0;
+                s.Q(c, s.iP) = s.cfg.sod_P_r;
+            }
+        }
+    apply_boundaries(s);
+    primtoc(s);
+    if (s.cfg.iso_cs < 1) {  // cs is set by ctoprim for adiabatic runs
+        ctoprim(s);
+    }
+}
+
+// DUSTYWAVE setup (src/setups/DUSTYWAVE/setup.f90:12-79); dust2gas_ratio(idust) = dust_eps[k].
+void setup_dustywave(oracle_state& s) {
+    const double delta_rho = s.cfg.dw_delta_rho, vx_0 = s.cfg.dw_vx_0, kx = s.cfg.dw_kx_wave;
+    const double rho_0 = s.cfg.dw_rho_0, L = s.box_l;
+    std::fill(s.q.begin(), s.q.end(), 0.0);
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        double ph = std::sin(2.0 * pi * s.POS(i, 0) / L * kx);
+        s.Q(i, s.irho) = rho_0 * (1 + delta_rho * ph);
+        s.Q(i, s.ivx) = vx_0 * ph;
+        s.cs[i] = s.cfg.cs0;
+        s.Q(i, s.iP) = sq(s.cs[i]) * s.Q(i, s.irho);
+        for (int k = 0; k < s.ndust; ++k) {
+            s.EPSD(i, k) = s.cfg.dust_eps[k];
+            s.Q(i, s.irhod[k]) = s.EPSD(i, k) * s.Q(i, s.irho);
+            s.Q(i, s.ivdx[k]) = vx_0 * ph;
+        }
+    }
+    apply_boundaries(s);
+    primtoc(s);
+}
+
+// SI setup (src/setups/SI/setup.f90:1-117): dust2gas_species = dust_eps[k], Stokes_species =
+// dust_stokes[k] (the host computes both, e.g. from the MRN bins of distribution_dust).  Noise:
+// uniform in [-noise_amp, noise_amp] on the three dust velocity components from a counter-based
+// hash of (seed, component, cell) instead of the reference's ranf stream on all velocities.
+void setup_si(oracle_state& s, double noise_amp, uint64_t seed) {
+    const int N = s.ndust;
+    const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, eta = s.cfg.si_eta_stream, r0 = s.cfg.si_rad0;
+    const double rho_init = s.cfg.si_rho_init;
+    const double vkep = r0 * om, cs0 = s.cfg.cs0;
+    double A_nak = 0.0, B_nak = 1.0;
+    for (int k = 0; k < N; ++k) {
+        double e = s.cfg.dust_eps[k], St = s.cfg.dust_stokes[k];
+        A_nak = A_nak + e * St / (1.0 + sq(St));
+        B_nak = B_nak + e / (1.0 + sq(St));
+    }
+    double vx_nak = 2.0 * eta * vkep * A_nak / (A_nak + B_nak);
+    double vy_nak = -eta * vkep * B_nak / (A_nak + B_nak);
+    std::vector<double> ux(N), uy(N);
+    for (int k = 0; k < N; ++k) {
+        double St = s.cfg.dust_stokes[k];
+        ux[k] = (vx_nak + 2.0 * St * vy_nak) / (1.0 + sq(St));
+        uy[k] = (vy_nak - half * St * vx_nak) / (1.0 + sq(St));
+    }
+    std::fill(s.q.begin(), s.q.end(), 0.0);
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        double xx = s.POS(i, 0) - half * s.box_l;
+        s.Q(i, s.irho) = rho_init;
+        s.Q(i, s.ivx) = vx_nak;
+        s.Q(i, s.ivy) = 0.0;
+        s.Q(i, s.ivz) = qs * om * xx + vy_nak;
+        s.Q(i, s.iP) = s.Q(i, s.irho) * sq(cs0);
+        for (int k = 0; k < N; ++k) {
+            s.Q(i, s.irhod[k]) = s.cfg.dust_eps[k] * rho_init;
+            s.EPSD(i, k) = s.cfg.dust_eps[k];
+            double nx_ = 0, ny_ = 0, nz_ = 0;
+            if (noise_amp > 0) {
+                uint64_t base = ((uint64_t)k * 3) * (uint64_t)s.ncells + (uint64_t)i;
+                nx_ = (2.0 * hash_uniform(seed, base) - 1.0) * noise_amp;
+                ny_ = (2.0 * hash_uniform(seed, base + (uint64_t)s.ncells) - 1.0) * noise_amp;
+                nz_ = (2.0 * hash_uniform(seed, base + 2 * (uint64_t)s.ncells) - 1.0) * noise_amp;
+            }
+            s.Q(i, s.ivdx[k]) = nx_ + ux[k];
+            s.Q(i, s.ivdy[k]) = ny_;
+            s.Q(i, s.ivdz[k]) = nz_ + qs * om * xx + uy[k];
+        }
+        s.cs[i] = cs0;
+    }
+    primtoc(s);
+    apply_boundaries(s);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// C API
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+oracle_state* oracle_create(const shark_gpu_config* cfg) {
+    if (!cfg || cfg->abi_version != SHARK_GPU_ABI_VERSION) return nullptr;
+    if (cfg->nghost != 2 || cfg->nx < 4 || cfg->ny < 1 || cfg->ndust < 0 || cfg->ndust > SHARK_MAX_DUST) return nullptr;
+    if (cfg->slope_type < 0 || cfg->slope_type > 3) return nullptr;
+    if (cfg->geom != 0 && cfg->geom != 2) return nullptr;
+    if (cfg->geom == 2 && cfg->ny == 1) return nullptr;
+    if (cfg->flags & SHARK_FLAG_VISCOSITY) return nullptr;
+    oracle_state* s = new oracle_state();
+    s->cfg = *cfg;
+    s->nx = cfg->nx; s->ny = cfg->ny; s->nghost = cfg->nghost; s->ndust = cfg->ndust;
+    s->nvar = 5 + 4 * s->ndust;
+    s->ndim = (s->ny == 1) ? 1 : 2;
+    s->nx_max = s->nx + 2 * s->nghost;
+    s->ny_max = (s->ny == 1) ? 1 : s->ny + 2 * s->nghost;
+    s->ncells = (int64_t)s->nx_max * s->ny_max;
+    s->first_active = s->nghost;
+    s->last_active = s->nx + s->nghost - 1;
+    s->first_active_y = (s->ny == 1) ? 0 : s->nghost;
+    s->last_active_y = (s->ny == 1) ? 0 : s->ny + s->nghost - 1;
+    const int N = s->ndust;
+    s->irhod.resize(N); s->ivdx.resize(N); s->ivdy.resize(N); s->ivdz.resize(N);
+    s->index_vdn.resize(2 * N); s->index_vdt.resize(2 * N);
+    for (int k = 0; k < N; ++k) {
+        s->irhod[k] = 5 + k; s->ivdx[k] = 5 + N + k; s->ivdy[k] = 5 + 2 * N + k; s->ivdz[k] = 5 + 3 * N + k;
+        s->index_vdn[k * 2 + 0] = s->ivdx[k]; s->index_vdt[k * 2 + 0] = s->ivdy[k];
+        s->index_vdn[k * 2 + 1] = s->ivdy[k]; s->index_vdt[k * 2 + 1] = s->ivdx[k];
+    }
+    s->index_vn[0] = s->ivx; s->index_vt[0] = s->ivy;
+    s->index_vn[1] = s->ivy; s->index_vt[1] = s->ivx;
+    const size_t nc = (size_t)s->ncells;
+    s->u.assign(nc * s->nvar, 0.0);
+    s->q.assign(nc * s->nvar, 0.0);
+    s->qm.assign(nc * s->nvar * s->ndim, 0.0);
+    s->qp.assign(nc * s->nvar * s->ndim, 0.0);
+    s->flux.assign(nc * s->nvar * s->ndim, 0.0);
+    s->cs.assign(nc, 0.0);
+    s->dx.assign(nc * s->ndim, 0.0);
+    s->surf.assign(nc * s->ndim, 0.0);
+    s->vol.assign(nc, 0.0);
+    s->position.assign(nc * s->ndim, 0.0);
+    s->radii_c.assign(nc, 1.0);
+    s->force.assign(nc * 3, 0.0);
+    s->force_dust.assign(nc * 3 * (size_t)N, 0.0);
+    s->tstop.assign(nc * (size_t)N, 0.0);
+    s->sdust.assign(nc * (size_t)N, 0.0);
+    s->epsilondust.assign(nc * (size_t)N, 0.0);
+    for (int k = 0; k < N; ++k)
+        for (size_t i = 0; i < nc; ++i) s->sdust[(size_t)k * nc + i] = cfg->dust_size[k];
+    s->box_l = cfg->box_l;
+    s->box_l_y = cfg->box_l_y;
+    get_active_cells(*s);
+    gridinit(*s);
+    // isothermal sound speed: uniform cs0 unless the caller overrides it with oracle_set_cs
+    if (cfg->iso_cs == 1)
+        for (size_t i = 0; i < nc; ++i) s->cs[i] = cfg->cs0;
+    return s;
+}
+
+void oracle_destroy(oracle_state* s) { delete s; }
+int64_t oracle_ncells(const oracle_state* s) { return s ? s->ncells : -1; }
+int32_t oracle_nvar(const oracle_state* s) { return s ? s->nvar : -1; }
+
+int32_t oracle_setup_ic(oracle_state* s, double noise_amp, uint64_t seed) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    switch (s->cfg.setup) {
+        case SHARK_SETUP_SOD: setup_sod(*s); break;
+        case SHARK_SETUP_DUSTYWAVE: setup_dustywave(*s); break;
+        case SHARK_SETUP_SI: setup_si(*s, noise_amp, seed); break;
+        default: return SHARK_ERR_UNSUPPORTED;
+    }
+    s->time = 0.0;
+    return SHARK_OK;
+}
+
+int32_t oracle_get_u(const oracle_state* s, double* u) {
+    if (!s || !u) return SHARK_ERR_INVALID_ARG;
+    std::memcpy(u, s->u.data(), s->u.size() * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_set_u(oracle_state* s, const double* u) {
+    if (!s || !u) return SHARK_ERR_INVALID_ARG;
+    std::memcpy(s->u.data(), u, s->u.size() * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_get_q(oracle_state* s, double* q, double* cs) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    ctoprim(*s);
+    if (q) std::memcpy(q, s->q.data(), s->q.size() * sizeof(double));
+    if (cs) std::memcpy(cs, s->cs.data(), s->cs.size() * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_get_cs(const oracle_state* s, double* cs) {
+    if (!s || !cs) return SHARK_ERR_INVALID_ARG;
+    std::memcpy(cs, s->cs.data(), s->cs.size() * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_set_cs(oracle_state* s, const double* cs) {
+    if (!s || !cs) return SHARK_ERR_INVALID_ARG;
+    std::memcpy(s->cs.data(), cs, s->cs.size() * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_get_grid(const oracle_state* s, double* dx, double* surf, double* vol, double* position,
+                        double* radii_c) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    if (dx) std::memcpy(dx, s->dx.data(), s->dx.size() * sizeof(double));
+    if (surf) std::memcpy(surf, s->surf.data(), s->surf.size() * sizeof(double));
+    if (vol) std::memcpy(vol, s->vol.data(), s->vol.size() * sizeof(double));
+    if (position) std::memcpy(position, s->position.data(), s->position.size() * sizeof(double));
+    if (radii_c) std::memcpy(radii_c, s->radii_c.data(), s->radii_c.size() * sizeof(double));
+    return SHARK_OK;
+}
+
+int32_t oracle_solve(oracle_state* s, double* dt_out) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    if (!(s->cfg.flags & SHARK_FLAG_STATIC)) solve(*s);
+    if (dt_out) *dt_out = s->dt;
+    return SHARK_OK;
+}
+
+int32_t oracle_run(oracle_state* s, int64_t nsteps, double tend, double* time_io, int64_t* steps_done) {
+    if (!s || !time_io) return SHARK_ERR_INVALID_ARG;
+    double time = *time_io;
+    int64_t n = 0;
+    while (n < nsteps && !(time >= tend)) {
+        solve(*s);
+        time = time + s->dt;
+        ++n;
+    }
+    *time_io = time;
+    s->time = time;
+    if (steps_done) *steps_done = n;
+    return SHARK_OK;
+}
+
+int32_t oracle_totals(const oracle_state* s, double* out) {
+    if (!s || !out) return SHARK_ERR_INVALID_ARG;
+    oracle_state& S = const_cast<oracle_state&>(*s);
+    for (int sp = 0; sp <= s->ndust; ++sp) {
+        int vr = sp == 0 ? S.irho : S.irhod[sp - 1];
+        int vx = sp == 0 ? S.ivx : S.ivdx[sp - 1];
+        int vy = sp == 0 ? S.ivy : S.ivdy[sp - 1];
+        int vz = sp == 0 ? S.ivz : S.ivdz[sp - 1];
+        int vars[4] = {vr, vx, vy, vz};
+        for (int c = 0; c < 4; ++c) {
+            double sum = 0.0, comp = 0.0;
+            for (int64_t i = 0; i < s->ncells; ++i) {
+                if (!s->active[i]) continue;
+                double y = S.U(i, vars[c]) - comp;
+                double t = sum + y;
+                comp = (t - sum) - y;
+                sum = t;
+            }
+            out[4 * sp + c] = sum;
+        }
+    }
+    return SHARK_OK;
+}
+
+int32_t oracle_apply_boundaries(oracle_state* s) { if (!s) return SHARK_ERR_INVALID_ARG; apply_boundaries(*s); return SHARK_OK; }
+int32_t oracle_ctoprim(oracle_state* s) { if (!s) return SHARK_ERR_INVALID_ARG; ctoprim(*s); return SHARK_OK; }
+int32_t oracle_courant(oracle_state* s, double* dt_out) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    ctoprim(*s);
+    if (s->flag(SHARK_FLAG_FORCE_KICK)) update_force_setup(*s);
+    courant(*s);
+    if (dt_out) *dt_out = s->dt;
+    return SHARK_OK;
+}
+int32_t oracle_set_dt(oracle_state* s, double dt) { if (!s) return SHARK_ERR_INVALID_ARG; s->dt = dt; return SHARK_OK; }
+int32_t oracle_dust_drag(oracle_state* s, double coeffdt) { if (!s) return SHARK_ERR_INVALID_ARG; dust_drag(*s, coeffdt); return SHARK_OK; }
+int32_t oracle_compute_tstop(oracle_state* s) { if (!s) return SHARK_ERR_INVALID_ARG; ctoprim(*s); compute_tstop(*s); return SHARK_OK; }
+int32_t oracle_get_tstop(const oracle_state* s, double* tstop) {
+    if (!s || !tstop) return SHARK_ERR_INVALID_ARG;
+    std::memcpy(tstop, s->tstop.data(), s->tstop.size() * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_set_threads(int32_t n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#endif
+    return SHARK_OK;
+}
+
+}  // extern "C"

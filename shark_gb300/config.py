@@ -1,0 +1,118 @@
+"""ctypes mirror of ``shark_gpu_config`` (include/shark_gpu.h) and the constants of the C ABI.
+
+The field order and types must match the C struct exactly; ``tests/test_capi_cpu.py`` checks the
+size and the offsets of the default-filled fields against the compiled library.
+"""
+import ctypes as C
+
+ABI_VERSION = 1
+MAX_DUST = 64
+
+OK = 0
+ERR_INVALID_ARG = -1
+ERR_UNSUPPORTED = -2
+ERR_CUDA = -3
+ERR_NO_DEVICE = -4
+ERR_STATE = -5
+ERR_NUMERICS = -6
+
+STATUS_NAN = 0x1
+STATUS_NEG_DENSITY = 0x2
+STATUS_DT_UNDERFLOW = 0x4
+STATUS_NEWTON = 0x8
+STATUS_GROWTH = 0x10
+
+SETUP_SOD = 1
+SETUP_DUSTYWAVE = 2
+SETUP_SI = 3
+SETUP_DISK_POLAR = 4
+SETUP_DUSTYTURB = 5
+
+FLAG_DRAG = 0x1
+FLAG_BACK_REACTION = 0x2
+FLAG_FORCE_KICK = 0x4
+FLAG_FARGO = 0x8
+FLAG_GROWTH = 0x10
+FLAG_CHARGING = 0x20
+FLAG_VISCOSITY = 0x40
+FLAG_STATIC = 0x80
+
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+_D = C.c_double
+_I = C.c_int32
+_P = C.POINTER(C.c_double)
+
+
+class SharkConfig(C.Structure):
+    _fields_ = [
+        ("abi_version", _I), ("nx", _I), ("ny", _I), ("nghost", _I), ("ndust", _I),
+        ("geom", _I), ("gridspace", _I), ("solver", _I), ("solverdust", _I),
+        ("slope_type", _I), ("iso_cs", _I), ("precision", _I), ("setup", _I),
+        ("flags", _I), ("device", _I), ("pad0", _I),
+        ("gamma", _D), ("cfl", _D), ("smallr", _D), ("smallc", _D), ("smallp", _D),
+        ("box_l", _D), ("box_l_y", _D), ("inner_r", _D), ("cs0", _D),
+        ("dust_ratio_min", _D), ("rhograin", _D),
+        ("dust_size", _D * MAX_DUST), ("dust_K", _D * MAX_DUST), ("dust_tstop", _D * MAX_DUST),
+        ("dust_eps", _D * MAX_DUST), ("dust_stokes", _D * MAX_DUST),
+        ("sod_rho_l", _D), ("sod_rho_r", _D), ("sod_P_l", _D), ("sod_P_r", _D),
+        ("sod_direction", _I), ("pad1", _I),
+        ("dw_rho_0", _D), ("dw_delta_rho", _D), ("dw_vx_0", _D), ("dw_kx_wave", _D),
+        ("si_q_shear", _D), ("si_omega", _D), ("si_eta_stream", _D), ("si_rad0", _D),
+        ("si_rho_init", _D), ("si_hoverr", _D),
+        ("disk_mstar", _D), ("disk_hoverr", _D), ("disk_sigma0", _D), ("disk_r0", _D),
+        ("disk_rout", _D),
+        ("reserved", _D * 48),
+        ("dx", _P), ("surf", _P), ("vol", _P), ("radii_c", _P), ("position", _P), ("cs", _P),
+    ]
+
+    # convenience ------------------------------------------------------------------------
+    @property
+    def nvar(self):
+        return 5 + 4 * self.ndust
+
+    @property
+    def ndim(self):
+        return 1 if self.ny == 1 else 2
+
+    @property
+    def nx_max(self):
+        return self.nx + 2 * self.nghost
+
+    @property
+    def ny_max(self):
+        return 1 if self.ny == 1 else self.ny + 2 * self.nghost
+
+    @property
+    def ncells(self):
+        return self.nx_max * self.ny_max
+
+    def copy(self):
+        c = SharkConfig()
+        C.memmove(C.byref(c), C.byref(self), C.sizeof(SharkConfig))
+        return c
+
+
+def default_config():
+    """Reference defaults (hydro_commons.f90:16-24, parameters.f90:55, dust_commons.f90:5-29)."""
+    c = SharkConfig()
+    c.abi_version = ABI_VERSION
+    c.nghost = 2
+    c.ny = 1
+    c.solver = 2
+    c.solverdust = 0
+    c.slope_type = 1
+    c.iso_cs = -1
+    c.precision = PREC_FP64
+    c.flags = FLAG_DRAG | FLAG_BACK_REACTION
+    c.gamma = 1.66667
+    c.cfl = 0.5
+    c.smallr = 1e-27
+    c.smallc = 1e-27
+    c.smallp = c.smallr * c.smallc ** 2      # allocate_init.f90:279
+    c.box_l = 1.0
+    c.box_l_y = 1.0
+    c.dust_ratio_min = 1e-11
+    c.rhograin = 2.7
+    return c

@@ -1,0 +1,146 @@
+// kernels_impl.cuh -- launch wrappers, instantiated once per state precision by
+// kernels_f64.cu and kernels_f32.cu.
+#pragma once
+
+#include "launch.h"
+#include "step_kernels.cuh"
+
+namespace shark {
+
+template <typename R>
+static KParams<R> make_params(const DeviceView& v) {
+    const shark_gpu_config& c = *v.cfg;
+    KParams<R> p;
+    p.nx = v.nx; p.ny = v.ny; p.ng = v.ng; p.nx_max = v.nx_max; p.ny_max = v.ny_max; p.pitch = v.pitch;
+    p.plane = v.plane;
+    p.ndust = v.ndust; p.nvar = v.nvar; p.ndim = v.ndim; p.geom = c.geom; p.solver = c.solver;
+    p.solverdust = c.solverdust; p.slope_type = c.slope_type; p.iso = c.iso_cs; p.setup = c.setup;
+    p.flags = c.flags; p.sod_dir = c.sod_direction;
+    p.gamma = c.gamma; p.cfl = c.cfl; p.smallr = c.smallr; p.smallp = c.smallp;
+    p.dust_ratio_min = c.dust_ratio_min; p.box_l = c.box_l; p.rhograin = c.rhograin;
+    p.si_q = c.si_q_shear; p.si_om = c.si_omega; p.si_eta = c.si_eta_stream; p.si_r0 = c.si_rad0;
+    p.sod_rho_l = c.sod_rho_l; p.sod_rho_r = c.sod_rho_r; p.sod_P_l = c.sod_P_l; p.sod_P_r = c.sod_P_r;
+    p.dx1 = (const R*)v.m[0]; p.dx2 = (const R*)v.m[1]; p.surf1 = (const R*)v.m[2]; p.surf2 = (const R*)v.m[3];
+    p.vol = (const R*)v.m[4]; p.radc = (const R*)v.m[5]; p.xpos = (const R*)v.m[6]; p.cs = (const R*)v.m[7];
+    p.dx1d = v.md[0]; p.dx2d = v.md[1]; p.radcd = v.md[2]; p.xposd = v.md[3]; p.csd = v.md[4];
+    p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize;
+    p.dt = nullptr; p.dt_next = nullptr; p.status = v.status;
+    p.u_cur = (const R*)v.u[v.cur];
+    p.u_next = (R*)v.u[1 - v.cur];
+    return p;
+}
+
+template <typename R, int NS, int MODE>
+static void finalize_launch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
+    k_finalize<R, NS, MODE><<<grid, 256, 0, st>>>(p);
+}
+
+template <typename R, int MODE>
+static void finalize_dispatch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
+    switch (p.ndust) {
+        case 0: finalize_launch<R, 0, MODE>(p, grid, st); break;
+        case 1: finalize_launch<R, 1, MODE>(p, grid, st); break;
+        case 2: finalize_launch<R, 2, MODE>(p, grid, st); break;
+        case 4: finalize_launch<R, 4, MODE>(p, grid, st); break;
+        case 8: finalize_launch<R, 8, MODE>(p, grid, st); break;
+        case 16: finalize_launch<R, 16, MODE>(p, grid, st); break;
+        default: finalize_launch<R, -1, MODE>(p, grid, st); break;
+    }
+}
+
+template <typename R>
+cudaError_t launch_boundaries(const DeviceView& v) {
+    KParams<R> p = make_params<R>(v);
+    const long long n = (v.ndim == 2 ? 2LL * v.ng * v.nx_max : 0) + 2LL * v.ng * (v.ndim == 2 ? v.ny : 1);
+    k_boundaries<R><<<(unsigned)((n + 255) / 256), 256, 0, v.stream>>>(p, (R*)v.u[v.cur]);
+    return cudaGetLastError();
+}
+
+template <typename R, int NDIM>
+static cudaError_t flux_launch(const KParams<R>& p, cudaStream_t st) {
+    using T = Tile<NDIM>;
+    const size_t smem = TileSmem<R, NDIM>::bytes;
+    cudaError_t e = cudaFuncSetAttribute(k_flux<R, NDIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((p.nx + T::TX - 1) / T::TX, NDIM == 2 ? (p.ny + T::TY - 1) / T::TY : 1, p.ndust + 1);
+    k_flux<R, NDIM><<<grid, T::NT, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_step(const DeviceView& v, int slot) {
+    KParams<R> p = make_params<R>(v);
+    p.dt = v.dt_slots + slot;
+    p.dt_next = reinterpret_cast<unsigned long long*>(v.dt_slots + (1 - slot));
+    cudaError_t e;
+    if (v.time_kernels) cudaEventRecord(v.ev[0], v.stream);
+    if ((e = launch_boundaries<R>(v)) != cudaSuccess) return e;
+    k_reset_dt<<<1, 1, 0, v.stream>>>(p.dt_next);
+    if (v.time_kernels) cudaEventRecord(v.ev[1], v.stream);
+    e = (v.ndim == 2) ? flux_launch<R, 2>(p, v.stream) : flux_launch<R, 1>(p, v.stream);
+    if (e != cudaSuccess) return e;
+    if (v.time_kernels) cudaEventRecord(v.ev[2], v.stream);
+    dim3 g2((v.nx + 255) / 256, v.ndim == 2 ? v.ny : 1, 1);
+    finalize_dispatch<R, 0>(p, g2, v.stream);
+    if (v.time_kernels) cudaEventRecord(v.ev[3], v.stream);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_courant(const DeviceView& v, int slot) {
+    KParams<R> p = make_params<R>(v);
+    // dt-only mode reads the current state through u_next
+    p.u_next = (R*)v.u[v.cur];
+    p.u_cur = (const R*)v.u[v.cur];
+    p.dt = v.dt_slots + slot;   // unused in MODE 1 except by the drag (disabled)
+    p.dt_next = reinterpret_cast<unsigned long long*>(v.dt_slots + slot);
+    k_reset_dt<<<1, 1, 0, v.stream>>>(p.dt_next);
+    dim3 g2((v.nx + 255) / 256, v.ndim == 2 ? v.ny : 1, 1);
+    finalize_dispatch<R, 1>(p, g2, v.stream);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_from_fortran(const DeviceView& v, const double* src_dev, void* dst) {
+    const long long n = (long long)v.nx_max * v.ny_max * v.nvar;
+    k_from_fortran<R><<<(unsigned)((n + 255) / 256), 256, 0, v.stream>>>(src_dev, (R*)dst, v.nx_max, v.ny_max,
+                                                                          v.pitch, v.plane, v.nvar);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_to_fortran(const DeviceView& v, const void* src, double* dst_dev) {
+    const long long n = (long long)v.nx_max * v.ny_max * v.nvar;
+    k_to_fortran<R><<<(unsigned)((n + 255) / 256), 256, 0, v.stream>>>((const R*)src, dst_dev, v.nx_max, v.ny_max,
+                                                                        v.pitch, v.plane, v.nvar);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_ctoprim(const DeviceView& v, double* q_dev, double* cs_dev) {
+    KParams<R> p = make_params<R>(v);
+    const long long n = (long long)v.nx_max * v.ny_max;
+    k_ctoprim<R><<<(unsigned)((n + 255) / 256), 256, 0, v.stream>>>(p, (const R*)v.u[v.cur], q_dev, cs_dev);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_totals(const DeviceView& v, double* part_dev, int nblocks, double* out_dev) {
+    KParams<R> p = make_params<R>(v);
+    const long long nact = (long long)v.nx * (v.ndim == 2 ? v.ny : 1);
+    const long long per = (nact + nblocks - 1) / nblocks;
+    k_totals_stage1<R><<<nblocks, 128, 0, v.stream>>>(p, (const R*)v.u[v.cur], part_dev, per);
+    k_totals_stage2<<<1, 128, 0, v.stream>>>(part_dev, nblocks, 4 * (v.ndust + 1), out_dev);
+    return cudaGetLastError();
+}
+
+#define SHARK_INSTANTIATE(R)                                                                       \
+    template cudaError_t launch_step<R>(const DeviceView&, int);                                   \
+    template cudaError_t launch_courant<R>(const DeviceView&, int);                                \
+    template cudaError_t launch_boundaries<R>(const DeviceView&);                                  \
+    template cudaError_t launch_from_fortran<R>(const DeviceView&, const double*, void*);          \
+    template cudaError_t launch_to_fortran<R>(const DeviceView&, const void*, double*);            \
+    template cudaError_t launch_ctoprim<R>(const DeviceView&, double*, double*);                   \
+    template cudaError_t launch_totals<R>(const DeviceView&, double*, int, double*);
+
+}  // namespace shark

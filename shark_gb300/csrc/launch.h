@@ -1,0 +1,42 @@
+// launch.h -- interface between the C-ABI host code (shark_gpu.cu) and the per-precision kernel
+// translation units (kernels_f64.cu compiled without FMA contraction, kernels_f32.cu with it).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../include/shark_gpu.h"
+
+namespace shark {
+
+// Device-side view of a context, shared by both precisions.  Metric arrays come in two copies:
+// `m` in the state precision (flux/update) and `md` in FP64 (drag, courant).
+struct DeviceView {
+    int nx, ny, ng, nx_max, ny_max, pitch, ndim, nvar, ndust;
+    long long plane;            // elements per variable plane
+    const shark_gpu_config* cfg;
+    void* u[2];                 // state ping-pong buffers (float or double)
+    int cur;                    // index of the current state
+    const void* m[8];           // dx1, dx2, surf1, surf2, vol, radc, xpos, cs  (state precision)
+    const double* md[5];        // dx1, dx2, radc, xpos, cs (FP64)
+    const double* dK;           // per-species constants (device)
+    const double* dtstop;
+    const double* dsize;
+    double* dt_slots;           // [2] dt of step n lives in slot n % 2
+    unsigned int* status;       // OR of SHARK_STATUS_* bits
+    cudaStream_t stream;
+    cudaEvent_t ev[4];          // timing: before boundaries, before flux, before finalize, end
+    bool time_kernels;
+};
+
+// one full step on view.u[view.cur] -> view.u[1-cur]; dt read from slot `slot`, next dt written
+// to slot 1-slot.  Returns a cudaError_t.
+template <typename R> cudaError_t launch_step(const DeviceView& v, int slot);
+// courant only on the current state into dt slot `slot`
+template <typename R> cudaError_t launch_courant(const DeviceView& v, int slot);
+template <typename R> cudaError_t launch_boundaries(const DeviceView& v);
+template <typename R> cudaError_t launch_from_fortran(const DeviceView& v, const double* src_dev, void* dst);
+template <typename R> cudaError_t launch_to_fortran(const DeviceView& v, const void* src, double* dst_dev);
+template <typename R> cudaError_t launch_ctoprim(const DeviceView& v, double* q_dev, double* cs_dev);
+template <typename R> cudaError_t launch_totals(const DeviceView& v, double* part_dev, int nblocks, double* out_dev);
+
+}  // namespace shark

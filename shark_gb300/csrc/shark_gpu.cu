@@ -1,0 +1,615 @@
+// shark_gpu.cu -- host side of the C ABI declared in include/shark_gpu.h.
+//
+// Owns the device-resident state of one run and sequences the kernels of one `solve`
+// (src/solver/solve.f90:10-181).  The conserved state never leaves the GPU between steps; the
+// only per-step device->host traffic is the 8-byte dt (plus the 4-byte status word) that the
+// Fortran driver needs for `time = time + dt` (src/shark.f90:107).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/shark_gpu.h"
+#include "launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int32_t fail(int32_t code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+int32_t fail(int32_t code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return fail(SHARK_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                                \
+    } while (0)
+
+constexpr double kPi = 3.141592653589793238462643383279;   // src/commons/phys_const.f90:14
+
+// x**n for integer n, square-and-multiply (the evaluation gfortran uses for integer powers)
+double powi(double x, int n) {
+    double r = 1.0, a = x;
+    unsigned b = n < 0 ? -n : n;
+    for (;;) {
+        if (b & 1u) r *= a;
+        b >>= 1;
+        if (!b) break;
+        a *= a;
+    }
+    return n < 0 ? 1.0 / r : r;
+}
+
+}  // namespace
+
+struct shark_gpu_ctx {
+    shark_gpu_config cfg;
+    shark::DeviceView v;
+    size_t elem = 8;                 // bytes per state element
+    size_t state_bytes = 0;          // one buffer
+    void* ubuf[2] = {nullptr, nullptr};
+    void* metrics = nullptr;         // 8 arrays x nx_max in state precision
+    double* metrics_d = nullptr;     // 5 arrays x nx_max FP64
+    double* species = nullptr;       // dK | dtstop | dsize (3 x SHARK_MAX_DUST)
+    double* dt_slots = nullptr;      // [2]
+    unsigned int* status = nullptr;
+    double* staging = nullptr;       // ncells*nvar FP64 (Fortran order) for uploads/downloads
+    double* part = nullptr;          // totals partials
+    double* tot_out = nullptr;
+    double* host_ring = nullptr;     // pinned: [2] dt + [2] status (as doubles)
+    cudaEvent_t ev_read[2] = {nullptr, nullptr};
+    cudaEvent_t ev_time[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaStream_t stream = nullptr;
+    long long nstep = 0;             // steps launched since upload
+    bool uploaded = false;
+    bool pending_read[2] = {false, false};
+    int totals_blocks = 0;
+    unsigned int status_seen = 0;
+};
+
+namespace {
+
+// ---- per-column grid metrics (src/grid/grid.f90:104-240) -----------------------------------
+struct Columns {
+    std::vector<double> dx1, dx2, surf1, surf2, vol, radc, xpos, cs;
+};
+
+int32_t build_columns(const shark_gpu_config& c, int nx_max, int ny_max, Columns& col) {
+    const int ng = c.nghost, nx = c.nx, ny = c.ny;
+    const bool one_d = (ny == 1);
+    col.dx1.assign(nx_max, 0.0); col.dx2.assign(nx_max, 1.0);
+    col.surf1.assign(nx_max, 0.0); col.surf2.assign(nx_max, 0.0);
+    col.vol.assign(nx_max, 0.0); col.radc.assign(nx_max, 1.0);
+    col.xpos.assign(nx_max, 0.0); col.cs.assign(nx_max, c.cs0);
+    const long long ncells = (long long)nx_max * ny_max;
+    if (c.dx || c.surf || c.vol || c.radii_c || c.position) {
+        if (!(c.dx && c.surf && c.vol && c.position))
+            return fail(SHARK_ERR_INVALID_ARG, "grid metric pointers must be given together (dx, surf, vol, position)");
+        const int ndim = one_d ? 1 : 2;
+        const int row0 = one_d ? 0 : ng;
+        for (int ix = 0; ix < nx_max; ++ix) {
+            const long long i0 = (long long)row0 * nx_max + ix;
+            col.dx1[ix] = c.dx[i0];
+            if (ndim == 2) col.dx2[ix] = c.dx[ncells + i0];
+            col.surf1[ix] = c.surf[i0];
+            if (ndim == 2) col.surf2[ix] = c.surf[ncells + i0];
+            col.vol[ix] = c.vol[i0];
+            col.xpos[ix] = c.position[i0];
+            if (c.radii_c) col.radc[ix] = c.radii_c[i0];
+            // every row must agree (the reference grids depend on ix only)
+            for (int iy = 0; iy < ny_max; ++iy) {
+                const long long i = (long long)iy * nx_max + ix;
+                bool same = c.dx[i] == col.dx1[ix] && c.surf[i] == col.surf1[ix] && c.vol[i] == col.vol[ix];
+                if (ndim == 2) same = same && c.dx[ncells + i] == col.dx2[ix] && c.surf[ncells + i] == col.surf2[ix];
+                if (c.radii_c) same = same && c.radii_c[i] == col.radc[ix];
+                if (c.geom == 0 && ndim == 2) same = same && c.position[i] == col.xpos[ix];
+                if (!same) return fail(SHARK_ERR_UNSUPPORTED, "grid metrics vary along y at ix=%d iy=%d", ix, iy);
+            }
+        }
+    } else if (c.geom == 0) {
+        const double dx = c.box_l / (double)(float)nx;
+        if (one_d) {
+            double acc = 0.0;
+            for (int ix = 0; ix < nx_max; ++ix) {
+                col.dx1[ix] = dx;
+                col.vol[ix] = dx;
+                col.surf1[ix] = 1.0;
+                if (ix >= ng && ix < ng + nx) { acc = acc + dx; col.xpos[ix] = acc; }   // right edges
+            }
+        } else {
+            const double dy = c.box_l_y / (double)(float)ny;
+            for (int ix = 0; ix < nx_max; ++ix) {
+                col.dx1[ix] = dx;
+                col.dx2[ix] = dy;
+                col.surf1[ix] = dx;   // the reference sets surf(:,1) = dx(:,1) (grid.f90:140)
+                col.surf2[ix] = dy;
+                col.vol[ix] = dx * dy;
+                col.xpos[ix] = ((double)(float)(ix - ng) + 0.5) * c.box_l / (double)(float)nx;
+            }
+        }
+    } else {   // polar face-on
+        const double inner_r = c.inner_r;
+        if (c.gridspace == 0) {
+            for (int ix = 0; ix < nx_max; ++ix) {
+                col.dx1[ix] = c.box_l / (double)(float)nx;
+                col.dx2[ix] = 2.0 * kPi / (double)(float)ny;
+                col.radc[ix] = inner_r + ((double)(float)(ix - ng) + 0.5) * c.box_l / (double)(float)nx;
+                col.surf1[ix] = (col.radc[ix] - 0.5 * col.dx1[ix]) * (col.dx2[ix]);
+                col.surf2[ix] = col.dx1[ix];
+                col.vol[ix] = col.radc[ix] * col.dx1[ix] * col.dx2[ix];
+                col.xpos[ix] = col.radc[ix];
+            }
+        } else {
+            const double zeta = std::pow(c.box_l / inner_r, 1.0 / (double)(nx - 1));
+            for (int ix = 0; ix < nx_max; ++ix) {
+                const int k = ix - ng;
+                col.radc[ix] = inner_r * 0.5 * (powi(zeta, k) + powi(zeta, k + 1));
+                col.dx1[ix] = inner_r * (powi(zeta, k + 1) - powi(zeta, k));
+                col.dx2[ix] = 2.0 * kPi / (double)(float)ny;
+                col.surf1[ix] = inner_r * (powi(zeta, k)) * (col.dx2[ix]);
+                col.surf2[ix] = col.dx1[ix];
+                col.vol[ix] = col.radc[ix] * col.dx1[ix] * col.dx2[ix];
+            }
+            for (int g = 0; g < ng; ++g) {
+                col.radc[g] = inner_r * 0.5;
+                col.radc[nx_max - 1 - g] = c.box_l + 0.5 * col.dx1[ng + nx - 1];
+                col.dx1[g] = col.dx1[ng];
+                col.dx1[nx_max - 1 - g] = col.dx1[ng + nx - 1];
+            }
+            for (int ix = 0; ix < nx_max; ++ix) col.xpos[ix] = col.radc[ix];
+        }
+    }
+    if (c.iso_cs == 1 && c.cs) {
+        for (int ix = 0; ix < nx_max; ++ix) col.cs[ix] = c.cs[(one_d ? 0 : (long long)ng * nx_max) + ix];
+        for (long long i = 0; i < ncells; ++i)
+            if (c.cs[i] != col.cs[i % nx_max]) return fail(SHARK_ERR_UNSUPPORTED, "cs varies along y");
+    }
+    return SHARK_OK;
+}
+
+int32_t validate(const shark_gpu_config* c) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "config is NULL");
+    if (c->abi_version != SHARK_GPU_ABI_VERSION)
+        return fail(SHARK_ERR_INVALID_ARG, "abi_version %d != %d", c->abi_version, SHARK_GPU_ABI_VERSION);
+    if (c->nghost != 2) return fail(SHARK_ERR_UNSUPPORTED, "nghost must be 2");
+    if (c->nx < 4 || c->ny < 1) return fail(SHARK_ERR_INVALID_ARG, "nx >= 4 and ny >= 1 required");
+    if (c->ny > 1 && c->ny < 4) return fail(SHARK_ERR_INVALID_ARG, "2D runs need ny >= 4");
+    if (c->ndust < 0 || c->ndust > SHARK_MAX_DUST) return fail(SHARK_ERR_INVALID_ARG, "ndust out of range");
+    if (c->geom != 0 && c->geom != 2) return fail(SHARK_ERR_UNSUPPORTED, "geom %d not built (0, 2 only)", c->geom);
+    if (c->geom == 2 && c->ny == 1) return fail(SHARK_ERR_UNSUPPORTED, "geom 2 needs ny > 1");
+    if (c->solver < 0 || c->solver > 2) return fail(SHARK_ERR_INVALID_ARG, "solver must be 0..2");
+    if (c->solverdust < 0 || c->solverdust > 2)
+        return fail(SHARK_ERR_UNSUPPORTED, "solverdust %d not built (0 HB, 1 LLF, 2 HLL)", c->solverdust);
+    if (c->slope_type < 0 || c->slope_type > 3) return fail(SHARK_ERR_INVALID_ARG, "unknown slope limiter");
+    if (c->precision != SHARK_PREC_FP64 && c->precision != SHARK_PREC_MIXED)
+        return fail(SHARK_ERR_INVALID_ARG, "precision must be FP64 or MIXED");
+    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_SI)
+        return fail(SHARK_ERR_UNSUPPORTED, "setup %d has no device hooks in this build", c->setup);
+    const int f = c->flags;
+    if (f & SHARK_FLAG_VISCOSITY) return fail(SHARK_ERR_UNSUPPORTED, "viscosity is not built");
+    if (f & (SHARK_FLAG_GROWTH | SHARK_FLAG_CHARGING | SHARK_FLAG_FARGO))
+        return fail(SHARK_ERR_UNSUPPORTED, "growth/charging/fargo are not enabled in this build");
+    if (c->ndust > 0 && (f & SHARK_FLAG_BACK_REACTION) && c->iso_cs < 1)
+        return fail(SHARK_ERR_UNSUPPORTED, "adiabatic drag heating (source_terms.f90:88-97) is not built");
+    if (c->setup == SHARK_SETUP_SI && c->ndust > 0 && !(f & SHARK_FLAG_DRAG) && (f & SHARK_FLAG_FORCE_KICK))
+        return fail(SHARK_ERR_UNSUPPORTED, "SI explicit drag forces (drag=.false.) are not built");
+    if (c->setup == SHARK_SETUP_SOD && c->ndust > 0 && c->iso_cs != 1 && (f & SHARK_FLAG_DRAG))
+        return fail(SHARK_ERR_UNSUPPORTED, "Epstein drag needs an isothermal sound speed in this build");
+    if (!(c->gamma > 1.0) || !(c->cfl > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "gamma > 1 and cfl > 0 required");
+    for (int k = 0; k < c->ndust; ++k) {
+        if (c->setup == SHARK_SETUP_SI && (f & SHARK_FLAG_DRAG) && !(c->dust_tstop[k] > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "dust_tstop[%d] must be > 0", k);
+        if (c->setup == SHARK_SETUP_DUSTYWAVE && (f & SHARK_FLAG_DRAG) && !(c->dust_K[k] > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "dust_K[%d] must be > 0", k);
+    }
+    return SHARK_OK;
+}
+
+template <typename T>
+void upload_cols(std::vector<T>& dst, const Columns& col) {
+    const std::vector<double>* src[8] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2,
+                                         &col.vol, &col.radc, &col.xpos, &col.cs};
+    const size_t n = col.dx1.size();
+    dst.resize(8 * n);
+    for (int a = 0; a < 8; ++a)
+        for (size_t i = 0; i < n; ++i) dst[a * n + i] = (T)(*src[a])[i];
+}
+
+int32_t release(shark_gpu_ctx* c) {
+    if (!c) return SHARK_OK;
+    cudaStreamSynchronize(c->stream);
+    for (void* p : {c->ubuf[0], c->ubuf[1], c->metrics}) if (p) cudaFree(p);
+    for (double* p : {c->metrics_d, c->species, c->dt_slots, c->staging, c->part, c->tot_out}) if (p) cudaFree(p);
+    if (c->status) cudaFree(c->status);
+    if (c->host_ring) cudaFreeHost(c->host_ring);
+    for (auto& e : c->ev_read) if (e) cudaEventDestroy(e);
+    for (auto& e : c->ev_time) if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return SHARK_OK;
+}
+
+bool is_mixed(const shark_gpu_ctx* c) { return c->cfg.precision == SHARK_PREC_MIXED; }
+
+cudaError_t do_step(shark_gpu_ctx* c, int slot) {
+    return is_mixed(c) ? shark::launch_step<float>(c->v, slot) : shark::launch_step<double>(c->v, slot);
+}
+
+// queue the readback of dt slot `slot` and of the status word into the pinned ring
+int32_t queue_readback(shark_gpu_ctx* c, int slot) {
+    CUDA_TRY(cudaMemcpyAsync(c->host_ring + slot, c->dt_slots + slot, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<unsigned int*>(c->host_ring + 2 + slot), c->status, sizeof(unsigned int),
+                             cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaEventRecord(c->ev_read[slot], c->stream));
+    c->pending_read[slot] = true;
+    return SHARK_OK;
+}
+
+int32_t wait_readback(shark_gpu_ctx* c, int slot, double* dt, unsigned int* st) {
+    if (!c->pending_read[slot]) return fail(SHARK_ERR_STATE, "no dt readback queued for slot %d", slot);
+    CUDA_TRY(cudaEventSynchronize(c->ev_read[slot]));
+    c->pending_read[slot] = false;
+    *dt = c->host_ring[slot];
+    *st = *reinterpret_cast<unsigned int*>(c->host_ring + 2 + slot);
+    c->status_seen |= *st;
+    return SHARK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t shark_gpu_abi_version(void) { return SHARK_GPU_ABI_VERSION; }
+
+const char* shark_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int32_t shark_gpu_config_defaults(shark_gpu_config* cfg) {
+    if (!cfg) return fail(SHARK_ERR_INVALID_ARG, "cfg is NULL");
+    std::memset(cfg, 0, sizeof *cfg);
+    cfg->abi_version = SHARK_GPU_ABI_VERSION;
+    cfg->nghost = 2;
+    cfg->ny = 1;
+    cfg->solver = 2;
+    cfg->solverdust = 0;
+    cfg->slope_type = 1;
+    cfg->iso_cs = -1;
+    cfg->precision = SHARK_PREC_FP64;
+    cfg->flags = SHARK_FLAG_DRAG | SHARK_FLAG_BACK_REACTION;
+    cfg->gamma = 1.66667;
+    cfg->cfl = 0.5;
+    cfg->smallr = 1e-27;
+    cfg->smallc = 1e-27;
+    cfg->smallp = cfg->smallr * cfg->smallc * cfg->smallc;
+    cfg->box_l = 1.0;
+    cfg->box_l_y = 1.0;
+    cfg->dust_ratio_min = 1e-11;
+    cfg->rhograin = 2.7;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
+    if (!out) return fail(SHARK_ERR_INVALID_ARG, "ctx_out is NULL");
+    *out = nullptr;
+    int32_t rc = validate(cfg);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SHARK_ERR_NO_DEVICE, "no CUDA device");
+    if (cfg->device < 0 || cfg->device >= ndev) return fail(SHARK_ERR_NO_DEVICE, "device %d not present", cfg->device);
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, cfg->device));
+    if (!(prop.major == 10 && prop.minor == 3))
+        return fail(SHARK_ERR_NO_DEVICE, "device %d is sm_%d%d; this library is built for sm_103a only", cfg->device,
+                    prop.major, prop.minor);
+    CUDA_TRY(cudaSetDevice(cfg->device));
+
+    shark_gpu_ctx* c = new (std::nothrow) shark_gpu_ctx();
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "out of host memory");
+    c->cfg = *cfg;
+    // the caller's grid pointers are only read here
+    c->cfg.dx = c->cfg.surf = c->cfg.vol = c->cfg.radii_c = c->cfg.position = c->cfg.cs = nullptr;
+    shark::DeviceView& v = c->v;
+    v.cfg = &c->cfg;
+    v.nx = cfg->nx; v.ny = cfg->ny; v.ng = cfg->nghost;
+    v.ndim = cfg->ny == 1 ? 1 : 2;
+    v.nx_max = cfg->nx + 2 * cfg->nghost;
+    v.ny_max = v.ndim == 1 ? 1 : cfg->ny + 2 * cfg->nghost;
+    v.ndust = cfg->ndust;
+    v.nvar = 5 + 4 * cfg->ndust;
+    v.pitch = (v.nx_max + 31) / 32 * 32;
+    v.plane = (long long)v.pitch * v.ny_max;
+    c->elem = is_mixed(c) ? 4 : 8;
+    c->state_bytes = (size_t)v.plane * v.nvar * c->elem;
+
+    Columns col;
+    if ((rc = build_columns(*cfg, v.nx_max, v.ny_max, col))) { release(c); return rc; }
+
+#define INIT_TRY(call)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            rc = fail(SHARK_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));                   \
+            release(c);                                                                           \
+            return rc;                                                                            \
+        }                                                                                         \
+    } while (0)
+    INIT_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    v.stream = c->stream;
+    for (auto& e : c->ev_read) INIT_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : c->ev_time) INIT_TRY(cudaEventCreate(&e));
+    for (int b = 0; b < 2; ++b) {
+        INIT_TRY(cudaMalloc(&c->ubuf[b], c->state_bytes));
+        INIT_TRY(cudaMemsetAsync(c->ubuf[b], 0, c->state_bytes, c->stream));
+        v.u[b] = c->ubuf[b];
+    }
+    v.cur = 0;
+    const size_t ncol = (size_t)v.nx_max;
+    INIT_TRY(cudaMalloc(&c->metrics, 8 * ncol * c->elem));
+    INIT_TRY(cudaMalloc(&c->metrics_d, 5 * ncol * sizeof(double)));
+    if (is_mixed(c)) {
+        std::vector<float> h;
+        upload_cols(h, col);
+        INIT_TRY(cudaMemcpy(c->metrics, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<double> h;
+        upload_cols(h, col);
+        INIT_TRY(cudaMemcpy(c->metrics, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    for (int a = 0; a < 8; ++a) v.m[a] = (const char*)c->metrics + a * ncol * c->elem;
+    {
+        std::vector<double> hd(5 * ncol);
+        const std::vector<double>* src[5] = {&col.dx1, &col.dx2, &col.radc, &col.xpos, &col.cs};
+        for (int a = 0; a < 5; ++a) std::memcpy(hd.data() + a * ncol, src[a]->data(), ncol * sizeof(double));
+        INIT_TRY(cudaMemcpy(c->metrics_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
+        for (int a = 0; a < 5; ++a) v.md[a] = c->metrics_d + a * ncol;
+    }
+    INIT_TRY(cudaMalloc(&c->species, 3 * SHARK_MAX_DUST * sizeof(double)));
+    INIT_TRY(cudaMemcpy(c->species, cfg->dust_K, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
+    INIT_TRY(cudaMemcpy(c->species + SHARK_MAX_DUST, cfg->dust_tstop, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
+    INIT_TRY(cudaMemcpy(c->species + 2 * SHARK_MAX_DUST, cfg->dust_size, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
+    v.dK = c->species;
+    v.dtstop = c->species + SHARK_MAX_DUST;
+    v.dsize = c->species + 2 * SHARK_MAX_DUST;
+    INIT_TRY(cudaMalloc(&c->dt_slots, 2 * sizeof(double)));
+    INIT_TRY(cudaMalloc(&c->status, sizeof(unsigned int)));
+    INIT_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
+    v.dt_slots = c->dt_slots;
+    v.status = c->status;
+    INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
+    std::memset(c->host_ring, 0, 4 * sizeof(double));
+    const long long nact = (long long)v.nx * (v.ndim == 2 ? v.ny : 1);
+    c->totals_blocks = (int)std::min<long long>(1024, std::max<long long>(1, nact / 256));
+    INIT_TRY(cudaMalloc(&c->part, (size_t)c->totals_blocks * 4 * (v.ndust + 1) * 2 * sizeof(double)));
+    INIT_TRY(cudaMalloc(&c->tot_out, 4 * (v.ndust + 1) * sizeof(double)));
+    for (int a = 0; a < 4; ++a) v.ev[a] = c->ev_time[a];
+    v.time_kernels = true;
+    INIT_TRY(cudaStreamSynchronize(c->stream));
+#undef INIT_TRY
+    *out = c;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_upload(shark_gpu_ctx* c, const double* u_prim, int64_t ncells, int32_t nvar) {
+    if (!c || !u_prim) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    const shark::DeviceView& v = c->v;
+    if (ncells != (int64_t)v.nx_max * v.ny_max || nvar != v.nvar)
+        return fail(SHARK_ERR_INVALID_ARG, "state is %lld x %d, context expects %lld x %d", (long long)ncells, nvar,
+                    (long long)v.nx_max * v.ny_max, v.nvar);
+    CUDA_TRY(cudaSetDevice(c->cfg.device));
+    // drain any readbacks still in flight: the new state starts a new dt sequence
+    for (int s = 0; s < 2; ++s) if (c->pending_read[s]) { cudaEventSynchronize(c->ev_read[s]); c->pending_read[s] = false; }
+    const size_t bytes = (size_t)ncells * nvar * sizeof(double);
+    if (!c->staging) CUDA_TRY(cudaMalloc(&c->staging, bytes));
+    CUDA_TRY(cudaMemcpyAsync(c->staging, u_prim, bytes, cudaMemcpyHostToDevice, c->stream));
+    c->v.cur = 0;
+    for (int b = 0; b < 2; ++b) {
+        cudaError_t e = is_mixed(c) ? shark::launch_from_fortran<float>(c->v, c->staging, c->ubuf[b])
+                                    : shark::launch_from_fortran<double>(c->v, c->staging, c->ubuf[b]);
+        if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "upload conversion: %s", cudaGetErrorString(e));
+    }
+    CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
+    c->status_seen = 0;
+    // first courant (src/solver/solve.f90:74) on the uploaded state -> dt slot 0
+    cudaError_t e = is_mixed(c) ? shark::launch_courant<float>(c->v, 0) : shark::launch_courant<double>(c->v, 0);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "courant: %s", cudaGetErrorString(e));
+    int32_t rc = queue_readback(c, 0);
+    if (rc) return rc;
+    c->nstep = 0;
+    c->uploaded = true;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_step(shark_gpu_ctx* c, double* dt_out, int32_t* status_out) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "step before upload");
+    const int slot = (int)(c->nstep & 1);
+    if (c->cfg.flags & SHARK_FLAG_STATIC) {
+        // static: solve returns before doing anything; dt keeps its value
+        double dt; unsigned st;
+        int32_t rc = wait_readback(c, slot, &dt, &st);
+        if (rc) return rc;
+        if ((rc = queue_readback(c, slot))) return rc;
+        if (dt_out) *dt_out = dt;
+        if (status_out) *status_out = (int32_t)c->status_seen;
+        return SHARK_OK;
+    }
+    cudaError_t e = do_step(c, slot);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+    c->v.cur = 1 - c->v.cur;
+    c->nstep++;
+    int32_t rc = queue_readback(c, 1 - slot);   // dt of the next step, written by k_finalize
+    if (rc) return rc;
+    double dt;
+    unsigned st;
+    if ((rc = wait_readback(c, slot, &dt, &st))) return rc;   // dt this step used (ready one step earlier)
+    if (dt_out) *dt_out = dt;
+    if (status_out) *status_out = (int32_t)c->status_seen;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_run(shark_gpu_ctx* c, int64_t nsteps, double tend, double* time_io, int64_t* steps_done,
+                      int32_t* status_out) {
+    if (!c || !time_io) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    double time = *time_io;
+    int64_t n = 0;
+    int32_t st = 0;
+    while (n < nsteps && !(time >= tend)) {
+        double dt;
+        int32_t rc = shark_gpu_step(c, &dt, &st);
+        if (rc) { *time_io = time; if (steps_done) *steps_done = n; return rc; }
+        time = time + dt;
+        ++n;
+    }
+    *time_io = time;
+    if (steps_done) *steps_done = n;
+    if (status_out) *status_out = st;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_sync(shark_gpu_ctx* c, int32_t* status_out) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    unsigned int st = 0;
+    CUDA_TRY(cudaMemcpy(&st, c->status, sizeof st, cudaMemcpyDeviceToHost));
+    c->status_seen |= st;
+    if (status_out) *status_out = (int32_t)c->status_seen;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_download(shark_gpu_ctx* c, double* u_prim, double* q) {
+    if (!c || (!u_prim && !q)) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "download before upload");
+    const shark::DeviceView& v = c->v;
+    const size_t n = (size_t)v.nx_max * v.ny_max * v.nvar;
+    if (!c->staging) CUDA_TRY(cudaMalloc(&c->staging, n * sizeof(double)));
+    if (u_prim) {
+        cudaError_t e = is_mixed(c) ? shark::launch_to_fortran<float>(v, v.u[v.cur], c->staging)
+                                    : shark::launch_to_fortran<double>(v, v.u[v.cur], c->staging);
+        if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "download conversion: %s", cudaGetErrorString(e));
+        CUDA_TRY(cudaMemcpyAsync(u_prim, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        CUDA_TRY(cudaStreamSynchronize(c->stream));
+    }
+    if (q) return shark_gpu_ctoprim(c, q, nullptr);
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_ctoprim(shark_gpu_ctx* c, double* q, double* cs) {
+    if (!c || !q) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "ctoprim before upload");
+    const shark::DeviceView& v = c->v;
+    const size_t ncells = (size_t)v.nx_max * v.ny_max;
+    const size_t n = ncells * v.nvar;
+    double* tmp = nullptr;
+    CUDA_TRY(cudaMalloc(&tmp, (n + ncells) * sizeof(double)));
+    cudaError_t e = is_mixed(c) ? shark::launch_ctoprim<float>(v, tmp, tmp + n) : shark::launch_ctoprim<double>(v, tmp, tmp + n);
+    if (e != cudaSuccess) { cudaFree(tmp); return fail(SHARK_ERR_CUDA, "ctoprim: %s", cudaGetErrorString(e)); }
+    e = cudaMemcpyAsync(q, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && cs) e = cudaMemcpyAsync(cs, tmp + n, ncells * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "ctoprim copy: %s", cudaGetErrorString(e));
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_totals(shark_gpu_ctx* c, double* out) {
+    if (!c || !out) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "totals before upload");
+    cudaError_t e = is_mixed(c) ? shark::launch_totals<float>(c->v, c->part, c->totals_blocks, c->tot_out)
+                                : shark::launch_totals<double>(c->v, c->part, c->totals_blocks, c->tot_out);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "totals: %s", cudaGetErrorString(e));
+    CUDA_TRY(cudaMemcpyAsync(out, c->tot_out, 4 * (c->v.ndust + 1) * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_last_step_ms(shark_gpu_ctx* c, float* ms_out) {
+    if (!c || !ms_out) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (c->nstep == 0) return fail(SHARK_ERR_STATE, "no step run yet");
+    CUDA_TRY(cudaEventSynchronize(c->ev_time[3]));
+    CUDA_TRY(cudaEventElapsedTime(&ms_out[0], c->ev_time[0], c->ev_time[1]));   // boundaries
+    CUDA_TRY(cudaEventElapsedTime(&ms_out[1], c->ev_time[1], c->ev_time[2]));   // flux/update
+    CUDA_TRY(cudaEventElapsedTime(&ms_out[2], c->ev_time[2], c->ev_time[3]));   // drag + dt
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_timed_run(shark_gpu_ctx* c, int64_t nsteps, double* time_io, float* ms_out) {
+    if (!c || !time_io || !ms_out) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "timed run before upload");
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const bool tk = c->v.time_kernels;
+    c->v.time_kernels = false;
+    CUDA_TRY(cudaEventRecord(e0, c->stream));
+    double time = *time_io;
+    int32_t rc = SHARK_OK;
+    for (int64_t n = 0; n < nsteps && rc == SHARK_OK; ++n) {
+        double dt;
+        rc = shark_gpu_step(c, &dt, nullptr);
+        time = time + dt;
+    }
+    c->v.time_kernels = tk;
+    if (rc == SHARK_OK) {
+        cudaEventRecord(e1, c->stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms_out, e0, e1);
+        if (e != cudaSuccess) rc = fail(SHARK_ERR_CUDA, "timed run: %s", cudaGetErrorString(e));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *time_io = time;
+    return rc;
+}
+
+int32_t shark_gpu_kernel_times(shark_gpu_ctx* c, int64_t nsteps, float* avg_ms) {
+    if (!c || !avg_ms || nsteps <= 0) return fail(SHARK_ERR_INVALID_ARG, "bad argument");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "kernel timing before upload");
+    std::vector<cudaEvent_t> ev((size_t)nsteps * 4, nullptr);
+    for (auto& e : ev) CUDA_TRY(cudaEventCreate(&e));
+    const bool tk = c->v.time_kernels;
+    int32_t rc = SHARK_OK;
+    for (int64_t n = 0; n < nsteps && rc == SHARK_OK; ++n) {
+        for (int a = 0; a < 4; ++a) c->v.ev[a] = ev[(size_t)n * 4 + a];
+        c->v.time_kernels = true;
+        rc = shark_gpu_step(c, nullptr, nullptr);
+    }
+    for (int a = 0; a < 4; ++a) c->v.ev[a] = c->ev_time[a];
+    c->v.time_kernels = tk;
+    double sum[4] = {0, 0, 0, 0};
+    if (rc == SHARK_OK) {
+        cudaError_t e = cudaStreamSynchronize(c->stream);
+        for (int64_t n = 0; n < nsteps && e == cudaSuccess; ++n) {
+            float t;
+            cudaEvent_t* E = &ev[(size_t)n * 4];
+            for (int a = 0; a < 3 && e == cudaSuccess; ++a) {
+                e = cudaEventElapsedTime(&t, E[a], E[a + 1]);
+                sum[a] += t;
+            }
+            if (e == cudaSuccess) { e = cudaEventElapsedTime(&t, E[0], E[3]); sum[3] += t; }
+        }
+        if (e != cudaSuccess) rc = fail(SHARK_ERR_CUDA, "kernel times: %s", cudaGetErrorString(e));
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int a = 0; a < 4; ++a) avg_ms[a] = (float)(sum[a] / (double)nsteps);
+    return rc;
+}
+
+int32_t shark_gpu_free(shark_gpu_ctx* c) { return release(c); }
+
+}  // extern "C"

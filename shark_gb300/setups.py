@@ -1,0 +1,311 @@
+"""Host-side setup builders: the run configuration and the initial conserved state of the
+in-scope problems, written with numpy the way the reference's ``setup`` routines build them.
+
+Each builder returns ``(cfg, u0)`` where ``cfg`` is a :class:`SharkConfig` and ``u0`` is the
+conserved state ``u_prim(1:ncells,1:nvar)`` in Fortran order flattened to a 1-D float64 array
+(variable-major, ``u0[v*ncells + i]``).  These are the inputs the Fortran driver would hand to
+the GPU library after its own ``setup``; they are not part of the per-step hot path.
+
+References: src/setups/SOD/setup.f90:1-46, src/setups/DUSTYWAVE/setup.f90:12-79,
+src/setups/SI/setup.f90:1-117, src/dust/dust_init.f90:11-103,164-197 (MRN bins),
+src/grid/grid.f90:104-173 (positions), src/solver/solve.f90:265-302 (primtoc).
+"""
+import numpy as np
+
+from .config import (SharkConfig, default_config, SETUP_SOD, SETUP_DUSTYWAVE, SETUP_SI,
+                     FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, PREC_FP64)
+
+PI = 3.141592653589793238462643383279          # src/commons/phys_const.f90:14
+F43 = float(np.float32(4.0) / np.float32(3.0))  # Fortran `4./3.` is a default-REAL quotient
+
+
+def _powi(x, n):
+    """x**n for integer n exactly as gfortran's __builtin_powi (square-and-multiply)."""
+    r = 1.0
+    a = float(x)
+    b = abs(int(n))
+    while True:
+        if b & 1:
+            r *= a
+        b //= 2
+        if b == 0:
+            break
+        a *= a
+    return 1.0 / r if n < 0 else r
+
+
+def positions(cfg):
+    """Cell positions (ncells, ndim) as gridinit builds them (grid.f90:104-173).
+
+    1D Cartesian: right cell edges accumulated over the active cells, ghosts at 0.
+    2D Cartesian: cell centres ((ix-first_active)+1/2)*L/nx.
+    """
+    nxm, nym, ng = cfg.nx_max, cfg.ny_max, cfg.nghost
+    if cfg.ny == 1:
+        pos = np.zeros((nxm, 1))
+        dx = cfg.box_l / float(np.float32(cfg.nx))
+        acc = 0.0
+        for ix in range(nxm):
+            if ng <= ix < ng + cfg.nx:
+                acc = acc + dx
+                pos[ix, 0] = acc
+        return pos
+    ix = np.arange(nxm)
+    iy = np.arange(nym)
+    px = ((ix - ng).astype(np.float64) + 0.5) * cfg.box_l / float(np.float32(cfg.nx))
+    py = ((iy - ng).astype(np.float64) + 0.5) * cfg.box_l_y / float(np.float32(cfg.ny))
+    pos = np.zeros((nym, nxm, 2))
+    pos[:, :, 0] = px[None, :]
+    pos[:, :, 1] = py[:, None]
+    return pos.reshape(-1, 2)
+
+
+def primtoc(cfg, q):
+    """Conservative from primitive variables (solve.f90:265-302); q has shape (nvar, ncells)."""
+    N = cfg.ndust
+    u = np.zeros_like(q)
+    r = q[0]
+    u[0] = r
+    u[1] = r * q[1]
+    u[2] = r * q[2]
+    u[3] = r * q[3]
+    u[4] = q[4] / (cfg.gamma - 1.0) + 0.5 * r * q[1] ** 2 + 0.5 * r * q[2] ** 2 + 0.5 * r * q[3] ** 2
+    for k in range(N):
+        rd = q[5 + k]
+        u[5 + k] = rd
+        u[5 + N + k] = rd * q[5 + N + k]
+        u[5 + 2 * N + k] = rd * q[5 + 2 * N + k]
+        u[5 + 3 * N + k] = rd * q[5 + 3 * N + k]
+    return u
+
+
+def _grid_view(cfg, u):
+    """(nvar, ny_max, nx_max) view of a flat state."""
+    return u.reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)
+
+
+def periodic_boundaries(cfg, u):
+    """periodic_boundaries (src/grid/boundary_types.f90:149-186) on a flat state, in place."""
+    g = _grid_view(cfg, u)
+    ng = cfg.nghost
+    if cfg.ny > 1:
+        g[:, :ng, ng:ng + cfg.nx] = g[:, cfg.ny:cfg.ny + ng, ng:ng + cfg.nx]
+        g[:, ng + cfg.ny:, ng:ng + cfg.nx] = g[:, ng:2 * ng, ng:ng + cfg.nx]
+    g[:, :, :ng] = g[:, :, cfg.nx:cfg.nx + ng]
+    g[:, :, ng + cfg.nx:] = g[:, :, ng:2 * ng]
+    return u
+
+
+def si_boundaries(cfg, u):
+    """SI apply_boundaries (src/setups/SI/boundaries.f90): periodic + shear in the vz momenta."""
+    periodic_boundaries(cfg, u)
+    g = _grid_view(cfg, u)
+    ng, N = cfg.nghost, cfg.ndust
+    nx = cfg.nx
+    # left ghosts take the right edge's values with vz momentum - rho q Omega L, and vice versa
+    g[3, :, :ng] = g[3, :, nx:nx + ng] - g[0, :, nx:nx + ng] * cfg.si_q_shear * cfg.si_omega * cfg.box_l
+    g[3, :, ng + nx:] = g[3, :, ng:2 * ng] + g[0, :, ng:2 * ng] * cfg.si_q_shear * cfg.si_omega * cfg.box_l
+    for k in range(N):
+        iz, ir = 5 + 3 * N + k, 5 + k
+        g[iz, :, :ng] = g[iz, :, nx:nx + ng] - g[ir, :, nx:nx + ng] * cfg.si_q_shear * cfg.si_omega * cfg.box_l
+        g[iz, :, ng + nx:] = g[iz, :, ng:2 * ng] + g[ir, :, ng:2 * ng] * cfg.si_q_shear * cfg.si_omega * cfg.box_l
+    return u
+
+
+# ---------------------------------------------------------------------------------------------
+# SOD
+# ---------------------------------------------------------------------------------------------
+def sod(nx=1000, ny=1, gamma=1.4, cfl=0.5, slope_type=1, solver=2, precision=PREC_FP64,
+        rho_l=1.0, rho_r=0.125, P_l=1.0, P_r=0.1):
+    """1D Sod shock tube (src/setups/SOD/setup.f90:1-46, boundaries.f90:49-77)."""
+    cfg = default_config()
+    cfg.nx, cfg.ny, cfg.ndust = nx, ny, 0
+    cfg.gamma, cfg.cfl, cfg.slope_type, cfg.solver = gamma, cfl, slope_type, solver
+    cfg.precision = precision
+    cfg.setup = SETUP_SOD
+    cfg.flags = 0
+    cfg.sod_rho_l, cfg.sod_rho_r, cfg.sod_P_l, cfg.sod_P_r = rho_l, rho_r, P_l, P_r
+    cfg.sod_direction = 0
+    pos = positions(cfg)
+    q = np.zeros((cfg.nvar, cfg.ncells))
+    right = pos[:, 0] > 0.5
+    q[0] = np.where(right, rho_r, rho_l)
+    q[4] = np.where(right, P_r, P_l)
+    u = primtoc(cfg, q).reshape(-1)
+    return cfg, u
+
+
+# ---------------------------------------------------------------------------------------------
+# DUSTYWAVE
+# ---------------------------------------------------------------------------------------------
+def dustywave(nx=2048, ndust=4, eps=None, tstop=None, K=None, cs0=1.0, rho_0=1.0,
+              delta=1e-4, vx_0=1e-4, kx_wave=1.0, cfl=0.8, slope_type=2, gamma=1.6666667,
+              precision=PREC_FP64):
+    """1D periodic dusty wave (src/setups/DUSTYWAVE/setup.f90:12-79).
+
+    Either ``K`` (the namelist drag constants) or ``tstop`` (stopping times, converted with
+    ts = rho_d/K, DUSTYWAVE/setup.f90:217) may be given.
+    """
+    cfg = default_config()
+    cfg.nx, cfg.ny, cfg.ndust = nx, 1, ndust
+    cfg.gamma, cfg.cfl, cfg.slope_type = gamma, cfl, slope_type
+    cfg.iso_cs = 1
+    cfg.precision = precision
+    cfg.setup = SETUP_DUSTYWAVE
+    cfg.flags = FLAG_DRAG | FLAG_BACK_REACTION
+    cfg.cs0 = cs0
+    cfg.dw_rho_0, cfg.dw_delta_rho, cfg.dw_vx_0, cfg.dw_kx_wave = rho_0, delta, vx_0, kx_wave
+    eps = np.full(ndust, 0.25) if eps is None else np.asarray(eps, dtype=np.float64)
+    if K is None:
+        tstop = np.logspace(-3, 0, ndust) if tstop is None else np.asarray(tstop, dtype=np.float64)
+        K = eps * rho_0 / tstop
+    for k in range(ndust):
+        cfg.dust_eps[k] = eps[k]
+        cfg.dust_K[k] = K[k]
+    pos = positions(cfg)
+    ph = np.sin(2.0 * PI * pos[:, 0] / cfg.box_l * kx_wave)
+    q = np.zeros((cfg.nvar, cfg.ncells))
+    q[0] = rho_0 * (1 + delta * ph)
+    q[1] = vx_0 * ph
+    q[4] = cs0 ** 2 * q[0]
+    N = ndust
+    for k in range(N):
+        q[5 + k] = eps[k] * q[0]
+        q[5 + N + k] = vx_0 * ph
+    # the reference calls apply_boundaries before primtoc, so the ghost cells keep the values of
+    # q at the ghosts' (zero) positions until the first solve refills them
+    u = primtoc(cfg, q).reshape(-1)
+    return cfg, u
+
+
+# ---------------------------------------------------------------------------------------------
+# SI shearing box
+# ---------------------------------------------------------------------------------------------
+def mrn_bins(ndust, smin, smax, scutmin, scut, dust2gas, mrn=3.5, rhograin=1.0,
+             dust_ratio_min=1e-11):
+    """distribution_dust(.true.) + mrn_distri (src/dust/dust_init.f90:11-103,164-197).
+
+    Returns (sdust, eps) per species (ice mantle excluded)."""
+    zeta = (smax / smin) ** (1.0 / ndust)
+    eta = zeta ** 3.0
+    m_min = F43 * PI * rhograin * smin ** 3.0
+    aminus = np.array([smin * _powi(zeta, k) for k in range(ndust)])
+    aplus = np.array([smin * _powi(zeta, k + 1) for k in range(ndust)])
+    sdust = np.sqrt(aminus * aplus)
+    massmin = m_min
+    mono1 = F43 * PI * rhograin * scutmin ** 3.0
+    mono2 = F43 * PI * rhograin * scut ** 3.0
+    icutmin = max(1, int(np.floor(np.log(mono1 / massmin) / np.log(eta) + 1)))
+    icutmax = min(int(np.floor(np.log(mono2 / massmin) / np.log(eta) + 1)), ndust)
+    eps = np.zeros(ndust)
+    norm = 0.0
+    for k in range(icutmin - 1, icutmax):
+        w = aplus[k] ** (4.0 - mrn) - aminus[k] ** (4.0 - mrn)
+        norm = norm + w
+        eps[k] = w
+    eps = dust2gas * eps / norm
+    eps = np.maximum(eps, dust_ratio_min)
+    return sdust, eps
+
+
+def si(n=1024, ndust=8, stokes_min=1e-3, stokes_max=1.0, stokes_cut=1.0, dust2gas=0.02,
+       hoverr=0.1, box_l=4.0, omega=1.0, q_shear=1.5, rho_init=1.0, rad0=1.0, theta_dust=1e-11,
+       noise=1e-3, seed=1, cfl=0.5, slope_type=3, gamma=1.666667, precision=PREC_FP64,
+       force_kick=True):
+    """2D streaming-instability shearing box (src/setups/SI/setup.f90:1-117, stokes_distrib).
+
+    Dust velocities get uniform white noise of amplitude ``noise*cs0`` from a counter-based hash
+    (seed ``seed``); the gas gets none.
+    """
+    cfg = default_config()
+    cfg.nx, cfg.ny, cfg.ndust = n, n, ndust
+    cfg.gamma, cfg.cfl, cfg.slope_type = gamma, cfl, slope_type
+    cfg.iso_cs = 1
+    cfg.precision = precision
+    cfg.setup = SETUP_SI
+    cfg.flags = FLAG_DRAG | FLAG_BACK_REACTION | (FLAG_FORCE_KICK if force_kick else 0)
+    eta_stream = float(np.float32(0.05)) * hoverr          # SI/setup.f90:24 (0.05 is REAL*4)
+    L = box_l * eta_stream * rad0
+    cfg.box_l = cfg.box_l_y = L
+    vkep = rad0 * omega
+    cs0 = hoverr * vkep
+    cfg.cs0 = cs0
+    rhograin = rho_init / theta_dust
+    cfg.rhograin = rhograin
+    cfg.si_q_shear, cfg.si_omega, cfg.si_eta_stream, cfg.si_rad0 = q_shear, omega, eta_stream, rad0
+    cfg.si_rho_init, cfg.si_hoverr = rho_init, hoverr
+    unit_s = rho_init * cs0 / rhograin / omega
+    smin = stokes_min * rho_init * cs0 / rhograin / omega
+    smax = stokes_max * rho_init * cs0 / rhograin / omega
+    scut = stokes_cut * rho_init * cs0 / rhograin / omega
+    scutmin = stokes_min * rho_init * cs0 / rhograin / omega
+    sdust, eps = mrn_bins(ndust, smin, smax, scutmin, scut, dust2gas, rhograin=rhograin,
+                          dust_ratio_min=cfg.dust_ratio_min)
+    stokes = sdust / unit_s
+    for k in range(ndust):
+        cfg.dust_size[k] = sdust[k]
+        cfg.dust_eps[k] = eps[k]
+        cfg.dust_stokes[k] = stokes[k]
+        cfg.dust_tstop[k] = rhograin * sdust[k] / rho_init / (rad0 * omega * hoverr)  # SI/setup.f90:394
+    u = si_ic(cfg, noise * cs0, seed)
+    return cfg, u
+
+
+def hash_uniform(seed, counter):
+    """Counter-based uniform deviate in [0,1): splitmix64 of (seed, counter) (vectorised)."""
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) * np.uint64(0x9E3779B97F4A7C15) + counter.astype(np.uint64)
+             + np.uint64(0x632BE59BD9B4E019))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def si_ic(cfg, noise_amp, seed):
+    """SI initial state: NSH equilibrium (SI/setup.f90:52-70) + noise on dust velocities."""
+    N = cfg.ndust
+    qs, om, eta, r0 = cfg.si_q_shear, cfg.si_omega, cfg.si_eta_stream, cfg.si_rad0
+    rho_init, cs0 = cfg.si_rho_init, cfg.cs0
+    vkep = r0 * om
+    A = 0.0
+    B = 1.0
+    for k in range(N):
+        e, St = cfg.dust_eps[k], cfg.dust_stokes[k]
+        A = A + e * St / (1.0 + St ** 2)
+        B = B + e / (1.0 + St ** 2)
+    vx_nak = 2.0 * eta * vkep * A / (A + B)
+    vy_nak = -eta * vkep * B / (A + B)
+    pos = positions(cfg)
+    xx = pos[:, 0] - 0.5 * cfg.box_l
+    nc = cfg.ncells
+    q = np.zeros((cfg.nvar, nc))
+    q[0] = rho_init
+    q[1] = vx_nak
+    q[2] = 0.0
+    q[3] = qs * om * xx + vy_nak
+    q[4] = q[0] * cs0 ** 2
+    cells = np.arange(nc, dtype=np.uint64)
+    for k in range(N):
+        St = cfg.dust_stokes[k]
+        ux = (vx_nak + 2.0 * St * vy_nak) / (1.0 + St ** 2)
+        uy = (vy_nak - 0.5 * St * vx_nak) / (1.0 + St ** 2)
+        q[5 + k] = cfg.dust_eps[k] * rho_init
+        if noise_amp > 0:
+            base = np.uint64(k * 3) * np.uint64(nc) + cells
+            nx_ = (2.0 * hash_uniform(seed, base) - 1.0) * noise_amp
+            ny_ = (2.0 * hash_uniform(seed, base + np.uint64(nc)) - 1.0) * noise_amp
+            nz_ = (2.0 * hash_uniform(seed, base + np.uint64(2 * nc)) - 1.0) * noise_amp
+        else:
+            nx_ = ny_ = nz_ = 0.0
+        q[5 + N + k] = nx_ + ux
+        q[5 + 2 * N + k] = ny_
+        q[5 + 3 * N + k] = nz_ + qs * om * xx + uy
+    u = primtoc(cfg, q).reshape(-1)
+    si_boundaries(cfg, u)
+    return u
+
+
+def build(name, **kw):
+    """Dispatch by setup name ('sod', 'dustywave', 'si')."""
+    return {"sod": sod, "dustywave": dustywave, "si": si}[name](**kw)

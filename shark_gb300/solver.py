@@ -1,0 +1,211 @@
+"""Host-side mirror of the reference's step interface over the C ABI (include/shark_gpu.h).
+
+The reference exposes one step as ``solve(verbose, outputing)`` (src/solver/solve.f90:10-181),
+the primitive recovery as ``ctoprim`` (src/solver/solve.f90:195-253) and the run loop as
+``time_loop`` (src/shark.f90:39-119).  :class:`Shark` offers the same calls over a device-resident
+state.  There is no CPU fallback: constructing a :class:`Shark` without the compiled library or
+without an sm_103 GPU raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from .config import SharkConfig, OK
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libshark_gpu.so")
+_lib = None
+
+# every symbol include/shark_gpu.h declares
+EXPORTS = [
+    "shark_gpu_abi_version", "shark_gpu_config_defaults", "shark_gpu_init", "shark_gpu_upload",
+    "shark_gpu_step", "shark_gpu_run", "shark_gpu_sync", "shark_gpu_download", "shark_gpu_ctoprim",
+    "shark_gpu_totals", "shark_gpu_last_step_ms", "shark_gpu_timed_run", "shark_gpu_kernel_times",
+    "shark_gpu_last_error", "shark_gpu_free",
+]
+
+
+class SharkError(RuntimeError):
+    def __init__(self, code, what, msg):
+        super().__init__(f"{what} returned {code}: {msg}")
+        self.code = code
+
+
+def load_library(path=None):
+    """Load libshark_gpu.so (built by shark_gb300.build).  Raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run shark_gb300.build.build() (nvcc, sm_103a)")
+    L = C.CDLL(path)
+    P = C.c_void_p
+    D = C.POINTER(C.c_double)
+    I32 = C.c_int32
+    L.shark_gpu_abi_version.restype = I32
+    L.shark_gpu_abi_version.argtypes = []
+    L.shark_gpu_config_defaults.restype = I32
+    L.shark_gpu_config_defaults.argtypes = [C.POINTER(SharkConfig)]
+    L.shark_gpu_init.restype = I32
+    L.shark_gpu_init.argtypes = [C.POINTER(SharkConfig), C.POINTER(P)]
+    L.shark_gpu_upload.restype = I32
+    L.shark_gpu_upload.argtypes = [P, D, C.c_int64, I32]
+    L.shark_gpu_step.restype = I32
+    L.shark_gpu_step.argtypes = [P, D, C.POINTER(I32)]
+    L.shark_gpu_run.restype = I32
+    L.shark_gpu_run.argtypes = [P, C.c_int64, C.c_double, D, C.POINTER(C.c_int64), C.POINTER(I32)]
+    L.shark_gpu_sync.restype = I32
+    L.shark_gpu_sync.argtypes = [P, C.POINTER(I32)]
+    L.shark_gpu_download.restype = I32
+    L.shark_gpu_download.argtypes = [P, D, D]
+    L.shark_gpu_ctoprim.restype = I32
+    L.shark_gpu_ctoprim.argtypes = [P, D, D]
+    L.shark_gpu_totals.restype = I32
+    L.shark_gpu_totals.argtypes = [P, D]
+    L.shark_gpu_last_step_ms.restype = I32
+    L.shark_gpu_last_step_ms.argtypes = [P, C.POINTER(C.c_float)]
+    L.shark_gpu_timed_run.restype = I32
+    L.shark_gpu_timed_run.argtypes = [P, C.c_int64, D, C.POINTER(C.c_float)]
+    L.shark_gpu_kernel_times.restype = I32
+    L.shark_gpu_kernel_times.argtypes = [P, C.c_int64, C.POINTER(C.c_float)]
+    L.shark_gpu_last_error.restype = C.c_char_p
+    L.shark_gpu_last_error.argtypes = []
+    L.shark_gpu_free.restype = I32
+    L.shark_gpu_free.argtypes = [P]
+    _lib = L
+    return L
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _check(rc, what):
+    if rc != OK:
+        msg = load_library().shark_gpu_last_error().decode(errors="replace")
+        raise SharkError(rc, what, msg)
+
+
+class Shark:
+    """One device-resident run.  ``Shark(cfg)`` = allocate_init + gridinit on the GPU."""
+
+    def __init__(self, cfg: SharkConfig):
+        L = load_library()
+        self.cfg = cfg.copy()
+        self._h = C.c_void_p()
+        _check(L.shark_gpu_init(C.byref(self.cfg), C.byref(self._h)), "shark_gpu_init")
+        self.ncells = self.cfg.ncells
+        self.nvar = self.cfg.nvar
+        self.time = 0.0
+        self.dt = 0.0
+        self.status = 0
+
+    # -- lifetime ------------------------------------------------------------------------------
+    def close(self):
+        if self._h:
+            load_library().shark_gpu_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state ---------------------------------------------------------------------------------
+    def upload(self, u_prim, time=0.0):
+        """Hand the conserved state (Fortran order, ncells*nvar) to the device."""
+        u = np.ascontiguousarray(u_prim, dtype=np.float64).reshape(-1)
+        if u.size != self.ncells * self.nvar:
+            raise ValueError(f"state has {u.size} values, expected {self.ncells * self.nvar}")
+        _check(load_library().shark_gpu_upload(self._h, _dptr(u), self.ncells, self.nvar), "shark_gpu_upload")
+        self.time = float(time)
+
+    def upload_ptr(self, ptr):
+        """Upload from a raw host pointer (e.g. pinned memory) without a copy in Python."""
+        _check(load_library().shark_gpu_upload(self._h, C.cast(ptr, C.POINTER(C.c_double)), self.ncells, self.nvar),
+               "shark_gpu_upload")
+
+    def download(self, out=None):
+        """u_prim as the host sees it (ghost cells included)."""
+        u = np.empty(self.ncells * self.nvar) if out is None else out
+        _check(load_library().shark_gpu_download(self._h, _dptr(u), None), "shark_gpu_download")
+        return u
+
+    def download_ptr(self, ptr):
+        _check(load_library().shark_gpu_download(self._h, C.cast(ptr, C.POINTER(C.c_double)), None),
+               "shark_gpu_download")
+
+    u_prim = property(download)
+
+    def ctoprim(self):
+        """(q, cs) of the current device state (src/solver/solve.f90:195-253)."""
+        q = np.empty(self.ncells * self.nvar)
+        cs = np.empty(self.ncells)
+        _check(load_library().shark_gpu_ctoprim(self._h, _dptr(q), _dptr(cs)), "shark_gpu_ctoprim")
+        return q, cs
+
+    def totals(self):
+        """Kahan-compensated FP64 [mass, px, py, pz] per species (gas first) over active cells."""
+        out = np.empty(4 * (self.cfg.ndust + 1))
+        _check(load_library().shark_gpu_totals(self._h, _dptr(out)), "shark_gpu_totals")
+        return out.reshape(self.cfg.ndust + 1, 4)
+
+    # -- stepping ------------------------------------------------------------------------------
+    def solve(self, verbose=False, outputing=False):
+        """One step; returns the dt that courant set for it (src/solver/solve.f90:10-181)."""
+        dt = C.c_double(0.0)
+        st = C.c_int32(0)
+        _check(load_library().shark_gpu_step(self._h, C.byref(dt), C.byref(st)), "shark_gpu_step")
+        self.dt = dt.value
+        self.status = st.value
+        return self.dt
+
+    def time_loop(self, tend, max_steps=1 << 62):
+        """Steps until time >= tend (dt is not clipped, as in src/shark.f90:71-110)."""
+        t = C.c_double(self.time)
+        n = C.c_int64(0)
+        st = C.c_int32(0)
+        _check(load_library().shark_gpu_run(self._h, int(max_steps), float(tend), C.byref(t), C.byref(n),
+                                            C.byref(st)), "shark_gpu_run")
+        self.time = t.value
+        self.status = st.value
+        return n.value
+
+    def run_steps(self, nsteps):
+        """Exactly nsteps steps (no end time)."""
+        return self.time_loop(float("inf"), max_steps=nsteps)
+
+    def sync(self):
+        st = C.c_int32(0)
+        _check(load_library().shark_gpu_sync(self._h, C.byref(st)), "shark_gpu_sync")
+        self.status = st.value
+        return st.value
+
+    def timed_run(self, nsteps):
+        """nsteps steps between two CUDA events on the library's stream; returns device ms."""
+        t = C.c_double(self.time)
+        ms = C.c_float(0.0)
+        _check(load_library().shark_gpu_timed_run(self._h, int(nsteps), C.byref(t), C.byref(ms)),
+               "shark_gpu_timed_run")
+        self.time = t.value
+        return ms.value
+
+    def kernel_times(self, nsteps):
+        """Mean device ms per launch: [boundaries, flux/update, drag+dt, whole step]."""
+        ms = (C.c_float * 4)()
+        _check(load_library().shark_gpu_kernel_times(self._h, int(nsteps), ms), "shark_gpu_kernel_times")
+        return list(ms)
+
+    def last_step_ms(self):
+        ms = (C.c_float * 3)()
+        _check(load_library().shark_gpu_last_step_ms(self._h, ms), "shark_gpu_last_step_ms")
+        return list(ms)

@@ -1,0 +1,93 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol include/shark_gpu.h
+declares, the ctypes mirror of shark_gpu_config has the C layout, and the error paths that run
+before any device call return the documented codes."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from shark_gb300 import build as gbuild, config as K, setups
+from shark_gb300.config import SharkConfig
+from shark_gb300 import solver
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "shark_gpu.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    gbuild.build()
+    return solver.load_library()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    text = open(HEADER).read()
+    declared = set(re.findall(r"\b(shark_gpu_\w+)\s*\(", text))
+    declared -= {"shark_gpu_config"}
+    assert declared == set(solver.EXPORTS), declared ^ set(solver.EXPORTS)
+    out = subprocess.run(["nm", "-D", "--defined-only", gbuild.LIB], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\b(shark_gpu_\w+)\b", out))
+    missing = declared - exported
+    assert not missing, missing
+    for name in declared:
+        getattr(lib, name)
+
+
+def test_config_struct_layout_matches_c(tmp_path):
+    fields = [f for f, _ in SharkConfig._fields_]
+    src = tmp_path / "probe.c"
+    body = "\n".join(f'  printf("{f} %zu\\n", offsetof(shark_gpu_config, {f}));' for f in fields)
+    src.write_text(f'#include <stdio.h>\n#include <stddef.h>\n#include "shark_gpu.h"\nint main(void){{\n'
+                   f'  printf("sizeof %zu\\n", sizeof(shark_gpu_config));\n{body}\n  return 0;}}\n')
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True).stdout.splitlines())
+    assert int(out["sizeof"]) == C.sizeof(SharkConfig)
+    for f in fields:
+        assert int(out[f]) == getattr(SharkConfig, f).offset, f
+
+
+def test_defaults_and_abi_version(lib):
+    assert lib.shark_gpu_abi_version() == K.ABI_VERSION
+    c = SharkConfig()
+    assert lib.shark_gpu_config_defaults(C.byref(c)) == K.OK
+    py = K.default_config()
+    for f, _ in SharkConfig._fields_:
+        a, b = getattr(c, f), getattr(py, f)
+        if isinstance(a, (int, float)):
+            assert a == b, f
+
+
+def test_invalid_configs_are_rejected_before_touching_a_device(lib):
+    cfg, _ = setups.sod(nx=64)
+    bad = cfg.copy()
+    bad.abi_version = 99
+    h = C.c_void_p()
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_INVALID_ARG
+    bad = cfg.copy()
+    bad.nghost = 3
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_UNSUPPORTED
+    bad = cfg.copy()
+    bad.flags |= K.FLAG_VISCOSITY
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_UNSUPPORTED
+    assert b"viscosity" in lib.shark_gpu_last_error()
+    bad = cfg.copy()
+    bad.slope_type = 7
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_INVALID_ARG
+    assert lib.shark_gpu_init(None, C.byref(h)) == K.ERR_INVALID_ARG
+    assert lib.shark_gpu_step(None, None, None) == K.ERR_INVALID_ARG
+    assert lib.shark_gpu_free(None) == K.OK
+
+
+def test_no_cpu_fallback_without_a_gpu(lib):
+    """On a machine without an sm_103 device the library refuses to run (no silent fallback)."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    cfg, _ = setups.sod(nx=64)
+    with pytest.raises(solver.SharkError) as e:
+        solver.Shark(cfg)
+    assert e.value.code == K.ERR_NO_DEVICE
