@@ -112,12 +112,19 @@ class ClockSampler:
 
 
 def rel_l1_max(cfg, a, b):
+    """Max over conserved fields of the relative L1 distance (densities/energy by their own L1
+    norm, momentum components by their species' momentum-magnitude L1 norm)."""
     g = cfg.nghost
     A = a.reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)[:, g:-g, g:-g]
     B = b.reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)[:, g:-g, g:-g]
+    N = cfg.ndust
+    sc = np.abs(B).sum(axis=(1, 2))
+    for c in [(1, 2, 3)] + [(5 + N + k, 5 + 2 * N + k, 5 + 3 * N + k) for k in range(N)]:
+        mag = np.sqrt(B[c[0]] ** 2 + B[c[1]] ** 2 + B[c[2]] ** 2).sum()
+        for v in c:
+            sc[v] = mag
     num = np.abs(A - B).sum(axis=(1, 2))
-    den = np.maximum(np.abs(B).sum(axis=(1, 2)), 1e-300)
-    return float((num / den).max())
+    return float((num / np.maximum(sc, 1e-300)).max())
 
 
 def cpu_oracle_rate(args, max_seconds=25.0, n_small=None):

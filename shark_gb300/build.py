@@ -2,7 +2,8 @@
 
 Three translation units compiled in parallel:
   kernels_f64.cu  -- FP64 step kernels, --fmad=false (round-for-round equal to the CPU oracle)
-  kernels_f32.cu  -- FP32 (mixed-precision) step kernels, FMA contraction on
+  kernels_f32.cu  -- FP32 (mixed-precision) step kernels, FMA contraction and approximate
+                     FP32 division on (the mixed path is held to 1e-5 L1 against FP64)
   shark_gpu.cu    -- host side of the C ABI (include/shark_gpu.h)
 """
 import os
@@ -20,7 +21,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
           "-I" + os.path.join(HERE, "..", "include")]
 UNITS = [
     ("kernels_f64.cu", ["--fmad=false"]),
-    ("kernels_f32.cu", ["--fmad=true"]),
+    ("kernels_f32.cu", ["--fmad=true", "-prec-div=false"]),
     ("shark_gpu.cu", []),
 ]
 

@@ -5,6 +5,8 @@
 #include "launch.h"
 #include "step_kernels.cuh"
 
+#include <type_traits>
+
 namespace shark {
 
 template <typename R>
@@ -22,6 +24,7 @@ static KParams<R> make_params(const DeviceView& v) {
     p.sod_rho_l = c.sod_rho_l; p.sod_rho_r = c.sod_rho_r; p.sod_P_l = c.sod_P_l; p.sod_P_r = c.sod_P_r;
     p.dx1 = (const R*)v.m[0]; p.dx2 = (const R*)v.m[1]; p.surf1 = (const R*)v.m[2]; p.surf2 = (const R*)v.m[3];
     p.vol = (const R*)v.m[4]; p.radc = (const R*)v.m[5]; p.xpos = (const R*)v.m[6]; p.cs = (const R*)v.m[7];
+    p.sfx = (const R*)v.m[8]; p.sfy = (const R*)v.m[9]; p.irp = (const R*)v.m[10]; p.rvol = (const R*)v.m[11];
     p.dx1d = v.md[0]; p.dx2d = v.md[1]; p.radcd = v.md[2]; p.xposd = v.md[3]; p.csd = v.md[4];
     p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize;
     p.dt = nullptr; p.dt_next = nullptr; p.status = v.status;
@@ -32,7 +35,8 @@ static KParams<R> make_params(const DeviceView& v) {
 
 template <typename R, int NS, int MODE>
 static void finalize_launch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
-    k_finalize<R, NS, MODE><<<grid, 256, 0, st>>>(p);
+    if constexpr (std::is_same<R, float>::value) k_finalize_mixed<NS, MODE><<<grid, 256, 0, st>>>(p);
+    else k_finalize<R, NS, MODE><<<grid, 256, 0, st>>>(p);
 }
 
 template <typename R, int MODE>
@@ -58,12 +62,58 @@ cudaError_t launch_boundaries(const DeviceView& v) {
 
 template <typename R, int NDIM>
 static cudaError_t flux_launch(const KParams<R>& p, cudaStream_t st) {
-    using T = Tile<NDIM>;
+    using T = Tile<R, NDIM>;
     const size_t smem = TileSmem<R, NDIM>::bytes;
     cudaError_t e = cudaFuncSetAttribute(k_flux<R, NDIM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((p.nx + T::TX - 1) / T::TX, NDIM == 2 ? (p.ny + T::TY - 1) / T::TY : 1, p.ndust + 1);
     k_flux<R, NDIM><<<grid, T::NT, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+template <typename R, bool IS_GAS, int ST, int SOLV>
+static void strip_kernel(const KParams<R>& p, dim3 grid, cudaStream_t st) {
+    k_flux_strip<R, IS_GAS, ST, SOLV><<<grid, 32 * STRIP_WARPS, 0, st>>>(p);
+}
+
+template <typename R, bool IS_GAS, int ST>
+static void strip_by_solver(const KParams<R>& p, dim3 grid, cudaStream_t st) {
+    switch (IS_GAS ? p.solver : p.solverdust) {
+        case 0: strip_kernel<R, IS_GAS, ST, 0>(p, grid, st); break;
+        case 1: strip_kernel<R, IS_GAS, ST, 1>(p, grid, st); break;
+        default: strip_kernel<R, IS_GAS, ST, 2>(p, grid, st); break;
+    }
+}
+
+template <typename R, bool IS_GAS>
+static void strip_dispatch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
+    switch (p.slope_type) {
+        case 0: strip_by_solver<R, IS_GAS, 0>(p, grid, st); break;
+        case 1: strip_by_solver<R, IS_GAS, 1>(p, grid, st); break;
+        case 2: strip_by_solver<R, IS_GAS, 2>(p, grid, st); break;
+        default: strip_by_solver<R, IS_GAS, 3>(p, grid, st); break;
+    }
+}
+
+// 2D K1: the dust species on the main stream and the gas concurrently on the side stream
+// (forked and joined with events), so the small gas grid does not run alone.
+template <typename R>
+static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
+    const int nbx = (p.nx + STRIP_UX - 1) / STRIP_UX;
+    const int nstrips = (p.ny + STRIP_H - 1) / STRIP_H;
+    dim3 grid(nbx, (nstrips + STRIP_WARPS - 1) / STRIP_WARPS, 1);
+    if (p.ndust > 0) {
+        cudaEventRecord(v.fork, v.stream);
+        cudaStreamWaitEvent(v.stream2, v.fork, 0);
+        strip_dispatch<R, true>(p, grid, v.stream2);
+        cudaEventRecord(v.join, v.stream2);
+        dim3 gd = grid;
+        gd.z = p.ndust;
+        strip_dispatch<R, false>(p, gd, v.stream);
+        cudaStreamWaitEvent(v.stream, v.join, 0);
+    } else {
+        strip_dispatch<R, true>(p, grid, v.stream);
+    }
     return cudaGetLastError();
 }
 
@@ -77,7 +127,7 @@ cudaError_t launch_step(const DeviceView& v, int slot) {
     if ((e = launch_boundaries<R>(v)) != cudaSuccess) return e;
     k_reset_dt<<<1, 1, 0, v.stream>>>(p.dt_next);
     if (v.time_kernels) cudaEventRecord(v.ev[1], v.stream);
-    e = (v.ndim == 2) ? flux_launch<R, 2>(p, v.stream) : flux_launch<R, 1>(p, v.stream);
+    e = (v.ndim == 2) ? strip_launch<R>(v, p) : flux_launch<R, 1>(p, v.stream);
     if (e != cudaSuccess) return e;
     if (v.time_kernels) cudaEventRecord(v.ev[2], v.stream);
     dim3 g2((v.nx + 255) / 256, v.ndim == 2 ? v.ny : 1, 1);

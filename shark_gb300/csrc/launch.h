@@ -16,7 +16,8 @@ struct DeviceView {
     const shark_gpu_config* cfg;
     void* u[2];                 // state ping-pong buffers (float or double)
     int cur;                    // index of the current state
-    const void* m[8];           // dx1, dx2, surf1, surf2, vol, radc, xpos, cs  (state precision)
+    const void* m[12];          // dx1, dx2, surf1, surf2, vol, radc, xpos, cs, sfx, sfy, irp, rvol
+                                // (state precision; the last four are derived tables)
     const double* md[5];        // dx1, dx2, radc, xpos, cs (FP64)
     const double* dK;           // per-species constants (device)
     const double* dtstop;
@@ -24,6 +25,8 @@ struct DeviceView {
     double* dt_slots;           // [2] dt of step n lives in slot n % 2
     unsigned int* status;       // OR of SHARK_STATUS_* bits
     cudaStream_t stream;
+    cudaStream_t stream2;       // side stream for the gas flux kernel (forked/joined per step)
+    cudaEvent_t fork, join;
     cudaEvent_t ev[4];          // timing: before boundaries, before flux, before finalize, end
     bool time_kernels;
 };

@@ -40,6 +40,13 @@ __device__ __forceinline__ R slope_limit(int slope_type, R l, R r) {
     return s;
 }
 
+// Compile-time limiter choice (0 = first order) for kernels specialised per configuration.
+template <int ST, typename R>
+__device__ __forceinline__ R slope_limit_t(R l, R r) {
+    if constexpr (ST == 0) return R(0);
+    else return slope_limit(ST, l, r);
+}
+
 template <typename R> struct GasFlux { R rho, mn, mt, mz, e; };
 template <typename R> struct DustFlux { R rho, mn, mt, mz; };
 

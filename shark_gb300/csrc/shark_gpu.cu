@@ -64,7 +64,7 @@ struct shark_gpu_ctx {
     size_t elem = 8;                 // bytes per state element
     size_t state_bytes = 0;          // one buffer
     void* ubuf[2] = {nullptr, nullptr};
-    void* metrics = nullptr;         // 8 arrays x nx_max in state precision
+    void* metrics = nullptr;         // 12 arrays x nx_max in state precision
     double* metrics_d = nullptr;     // 5 arrays x nx_max FP64
     double* species = nullptr;       // dK | dtstop | dsize (3 x SHARK_MAX_DUST)
     double* dt_slots = nullptr;      // [2]
@@ -76,6 +76,8 @@ struct shark_gpu_ctx {
     cudaEvent_t ev_read[2] = {nullptr, nullptr};
     cudaEvent_t ev_time[4] = {nullptr, nullptr, nullptr, nullptr};
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     long long nstep = 0;             // steps launched since upload
     bool uploaded = false;
     bool pending_read[2] = {false, false};
@@ -88,7 +90,22 @@ namespace {
 // ---- per-column grid metrics (src/grid/grid.f90:104-240) -----------------------------------
 struct Columns {
     std::vector<double> dx1, dx2, surf1, surf2, vol, radc, xpos, cs;
+    // derived tables used by the mixed-precision kernels (division-free slopes and update):
+    // sfx[i] = 2/(dx1[i]+dx1[i-1]), sfy[i] = 1/(dx2[i]*r_i), irp[i] = 1/r_i, rvol[i] = 1/vol[i]
+    std::vector<double> sfx, sfy, irp, rvol;
 };
+
+void derive_tables(const shark_gpu_config& c, Columns& col) {
+    const size_t n = col.dx1.size();
+    col.sfx.assign(n, 0.0); col.sfy.assign(n, 0.0); col.irp.assign(n, 1.0); col.rvol.assign(n, 0.0);
+    for (size_t i = 0; i < n; ++i) {
+        const double rp = (c.geom == 2) ? col.radc[i] : 1.0;
+        if (i > 0) col.sfx[i] = 2.0 / (col.dx1[i] + col.dx1[i - 1]);
+        col.sfy[i] = 2.0 / (col.dx2[i] + col.dx2[i]) / rp;
+        col.irp[i] = 1.0 / rp;
+        col.rvol[i] = col.vol[i] != 0.0 ? 1.0 / col.vol[i] : 0.0;
+    }
+}
 
 int32_t build_columns(const shark_gpu_config& c, int nx_max, int ny_max, Columns& col) {
     const int ng = c.nghost, nx = c.nx, ny = c.ny;
@@ -223,11 +240,11 @@ int32_t validate(const shark_gpu_config* c) {
 
 template <typename T>
 void upload_cols(std::vector<T>& dst, const Columns& col) {
-    const std::vector<double>* src[8] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2,
-                                         &col.vol, &col.radc, &col.xpos, &col.cs};
+    const std::vector<double>* src[12] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
+                                          &col.xpos, &col.cs, &col.sfx, &col.sfy, &col.irp, &col.rvol};
     const size_t n = col.dx1.size();
-    dst.resize(8 * n);
-    for (int a = 0; a < 8; ++a)
+    dst.resize(12 * n);
+    for (int a = 0; a < 12; ++a)
         for (size_t i = 0; i < n; ++i) dst[a * n + i] = (T)(*src[a])[i];
 }
 
@@ -240,6 +257,9 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->host_ring) cudaFreeHost(c->host_ring);
     for (auto& e : c->ev_read) if (e) cudaEventDestroy(e);
     for (auto& e : c->ev_time) if (e) cudaEventDestroy(e);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return SHARK_OK;
@@ -333,11 +353,17 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     v.nvar = 5 + 4 * cfg->ndust;
     v.pitch = (v.nx_max + 31) / 32 * 32;
     v.plane = (long long)v.pitch * v.ny_max;
+    if ((double)v.plane * v.nvar >= 2147483647.0) {
+        delete c;
+        return fail(SHARK_ERR_UNSUPPORTED, "state of %lld elements exceeds the 2^31 element indexing of the kernels",
+                    (long long)v.plane * v.nvar);
+    }
     c->elem = is_mixed(c) ? 4 : 8;
     c->state_bytes = (size_t)v.plane * v.nvar * c->elem;
 
     Columns col;
     if ((rc = build_columns(*cfg, v.nx_max, v.ny_max, col))) { release(c); return rc; }
+    derive_tables(*cfg, col);
 
 #define INIT_TRY(call)                                                                            \
     do {                                                                                          \
@@ -349,7 +375,13 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         }                                                                                         \
     } while (0)
     INIT_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    INIT_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+    INIT_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    INIT_TRY(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     v.stream = c->stream;
+    v.stream2 = c->stream2;
+    v.fork = c->ev_fork;
+    v.join = c->ev_join;
     for (auto& e : c->ev_read) INIT_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto& e : c->ev_time) INIT_TRY(cudaEventCreate(&e));
     for (int b = 0; b < 2; ++b) {
@@ -359,7 +391,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     }
     v.cur = 0;
     const size_t ncol = (size_t)v.nx_max;
-    INIT_TRY(cudaMalloc(&c->metrics, 8 * ncol * c->elem));
+    INIT_TRY(cudaMalloc(&c->metrics, 12 * ncol * c->elem));
     INIT_TRY(cudaMalloc(&c->metrics_d, 5 * ncol * sizeof(double)));
     if (is_mixed(c)) {
         std::vector<float> h;
@@ -370,7 +402,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         upload_cols(h, col);
         INIT_TRY(cudaMemcpy(c->metrics, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
-    for (int a = 0; a < 8; ++a) v.m[a] = (const char*)c->metrics + a * ncol * c->elem;
+    for (int a = 0; a < 12; ++a) v.m[a] = (const char*)c->metrics + a * ncol * c->elem;
     {
         std::vector<double> hd(5 * ncol);
         const std::vector<double>* src[5] = {&col.dx1, &col.dx2, &col.radc, &col.xpos, &col.cs};

@@ -31,6 +31,7 @@ struct KParams {
     double sod_rho_l, sod_rho_r, sod_P_l, sod_P_r;
     // per-column metrics (length nx_max), compute precision
     const R *dx1, *dx2, *surf1, *surf2, *vol, *radc, *xpos, *cs;
+    const R *sfx, *sfy, *irp, *rvol;   // division-free tables (mixed path)
     // per-column metrics in FP64 (courant, drag)
     const double *dx1d, *dx2d, *radcd, *xposd, *csd;
     // per-species constants
@@ -109,414 +110,52 @@ __global__ void k_boundaries(KParams<R> p, R* u) {
     (void)yg;
 }
 
-// ---------------------------------------------------------------------------------------------
-// K1: fused MUSCL-Hancock flux/update, one CTA per (tile, species)
-// ---------------------------------------------------------------------------------------------
-template <int NDIM> struct Tile;
-template <> struct Tile<2> {
-    static constexpr int TX = 32, TY = 8;
-    static constexpr int HX = TX + 4, HY = TY + 4, OX = 2, OY = 2;   // halo tile and origin offset
-    static constexpr int RX = TX + 2, RY = TY + 2;                    // predicted ring region
-    static constexpr int NT = TX * TY;
-};
-template <> struct Tile<1> {
-    static constexpr int TX = 128, TY = 1;
-    static constexpr int HX = TX + 4, HY = 1, OX = 2, OY = 0;
-    static constexpr int RX = TX + 2, RY = 1;
-    static constexpr int NT = TX;
-};
+}  // namespace shark
 
-template <typename R, int NDIM>
-struct TileSmem {
-    using T = Tile<NDIM>;
-    static constexpr int NV = 5;   // sized for the gas (dust uses the first 4 slots)
-    static constexpr size_t halo = (size_t)T::HX * T::HY;
-    static constexpr size_t ring = (size_t)T::RX * T::RY;
-    static constexpr size_t fxn = (size_t)(T::TX + 1) * T::TY;
-    static constexpr size_t fyn = (NDIM == 2) ? (size_t)T::TX * (T::TY + 1) : 0;
-    static constexpr size_t n_u = NV * halo, n_q = NV * halo, n_cs = halo;
-    static constexpr size_t n_face = NV * ring;   // each of qm_x, qp_x, qm_y, qp_y
-    static constexpr size_t n_fx = NV * fxn, n_fy = NV * fyn;
-    static constexpr size_t elems = n_u + n_q + n_cs + (NDIM == 2 ? 4 : 2) * n_face + n_fx + n_fy;
-    static constexpr size_t bytes = elems * sizeof(R);
-};
+#include "flux_tile.cuh"
+#include "flux_strip.cuh"
 
-// Force of the setup on a gas (s == 0) or dust (s > 0) element with primitive velocities
-// (vx, vy, vz) at column ix: update_force_setup of SI (src/setups/SI/setup.f90:335-368).  The
-// other in-scope setups have no force.  `drag` is on for every configuration that uses the force
-// (the !drag extra terms are rejected at init).
-template <typename R>
-__device__ __forceinline__ void setup_force(const KParams<R>& p, int s, int ix, R vx, R vz, R& f1, R& f2, R& f3) {
-    if (p.setup == SHARK_SETUP_SI) {
-        const R qs = R(p.si_q), om = R(p.si_om);
-        const R xc = p.xpos[ix] - R(0.5) * R(p.box_l);
-        if (s == 0)
-            f1 = R(2) * qs * sq(om) * xc - R(2) * om * vz - R(2) * R(p.si_r0) * om * R(p.si_eta);
-        else
-            f1 = R(2) * qs * sq(om) * xc - R(2) * om * vz;
-        f2 = R(0);
-        f3 = R(2) * om * vx;
-    } else {
-        f1 = f2 = f3 = R(0);
-    }
-}
-
-// One species of one tile.  IS_GAS selects the 5-variable gas (solver per p.solver) or a
-// 4-variable pressureless dust species (solver per p.solverdust).
-template <typename R, int NDIM, bool IS_GAS>
-__device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
-    using T = Tile<NDIM>;
-    using S = TileSmem<R, NDIM>;
-    constexpr int NV = IS_GAS ? 5 : 4;
-    const int N = p.ndust;
-    const int tid = threadIdx.x;
-    const int ax0 = blockIdx.x * T::TX + p.ng;                     // first active column of tile
-    const int ay0 = (NDIM == 2) ? blockIdx.y * T::TY + p.ng : 0;   // first active row of tile
-    const int hx0 = ax0 - T::OX, hy0 = ay0 - T::OY;                 // halo origin (global)
-    const R dt = R(*p.dt);
-    const R half = R(0.5);
-    const R gamma = R(p.gamma);
-    const bool fk = (p.flags & SHARK_FLAG_FORCE_KICK) != 0;
-    const bool polar = (p.geom == 2);
-    const bool iso = (p.iso == 1);
-
-    R* us = sm;                       // [NV][HY][HX] conserved
-    R* qs = us + S::n_u;              // [NV][HY][HX] primitive
-    R* css = qs + S::n_q;             // [HY][HX] sound speed (gas)
-    R* qmx = css + S::n_cs;           // [NV][RY][RX] right-face state in x  (qm(:,:,1))
-    R* qpx = qmx + S::n_face;         // [NV][RY][RX] left-face state in x   (qp(:,:,1))
-    R* qmy = qpx + S::n_face;         // y faces (2D only)
-    R* qpy = (NDIM == 2) ? qmy + S::n_face : qmy;
-    R* fxs = (NDIM == 2) ? qpy + S::n_face : qmy;  // [NV][TY][TX+1]
-    R* fys = fxs + S::n_fx;                        // [NV][TY+1][TX]
-
-    // ---- stage the halo tile of this species (coalesced rows) ------------------------------
-    for (int idx = tid; idx < NV * T::HY * T::HX; idx += T::NT) {
-        const int c = idx / (T::HY * T::HX);
-        const int r = idx - c * (T::HY * T::HX);
-        const int hy = r / T::HX, hx = r - hy * T::HX;
-        const int gx = hx0 + hx, gy = hy0 + hy;
-        R val = R(0);
-        if (gx < p.nx_max && gy < p.ny_max) val = p.u_cur[uidx(p, svar(s, c, N), gy, gx)];
-        us[idx] = val;
-    }
-    __syncthreads();
-
-    // ---- ctoprim on the halo tile (src/solver/solve.f90:195-253) ---------------------------
-    for (int r = tid; r < T::HY * T::HX; r += T::NT) {
-        const int hx = r % T::HX;
-        const int gx = min(hx0 + hx, p.nx_max - 1);
-        if (IS_GAS) {
-            const R rho = us[0 * S::halo + r];
-            const R px = us[1 * S::halo + r], py = us[2 * S::halo + r], pz = us[3 * S::halo + r];
-            qs[0 * S::halo + r] = fmax2(rho, R(p.smallr));
-            qs[1 * S::halo + r] = px / rho;
-            qs[2 * S::halo + r] = py / rho;
-            qs[3 * S::halo + r] = pz / rho;
-            const R ekin = half * rho * sq(px / rho) + half * rho * sq(py / rho) + half * rho * sq(pz / rho);
-            R P = fmax2((gamma - R(1)) * (us[4 * S::halo + r] - ekin - R(0)), R(p.smallp));
-            R cs;
-            if (!iso) cs = sqrt(gamma * P / qs[0 * S::halo + r]);
-            else { cs = p.cs[gx]; P = rho * sq(cs); }
-            qs[4 * S::halo + r] = P;
-            css[r] = cs;
-        } else {
-            const R rd = us[0 * S::halo + r];
-            qs[0 * S::halo + r] = rd;
-            qs[1 * S::halo + r] = us[1 * S::halo + r] / rd;
-            qs[2 * S::halo + r] = us[2 * S::halo + r] / rd;
-            qs[3 * S::halo + r] = us[3 * S::halo + r] / rd;
-        }
-    }
-    __syncthreads();
-
-    // ---- predictor on the ring region (src/solver/godunov.f90:7-629) -----------------------
-    for (int r = tid; r < T::RX * T::RY; r += T::NT) {
-        const int ry = r / T::RX, rx = r - ry * T::RX;
-        if (NDIM == 2 && (rx == 0 || rx == T::RX - 1) && (ry == 0 || ry == T::RY - 1)) continue;  // corners
-        const int hx = rx + 1, hy = (NDIM == 2) ? ry + 1 : 0;
-        const int gx = hx0 + hx;
-        if (gx >= p.nx_max - 1 || (NDIM == 2 && hy0 + hy >= p.ny_max - 1)) continue;  // beyond a partial tile
-        const int hc = hy * T::HX + hx;
-        const R radius_polar = polar ? p.radc[gx] : R(1);
-        R dqx[NV], dqy[NV];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) {
-            const R* qc = qs + c * S::halo;
-            dqx[c] = R(0);
-            dqy[c] = R(0);
-            if (p.slope_type > 0) {
-                dqx[c] = slope_limit(p.slope_type, R(2) * (qc[hc] - qc[hc - 1]) / (p.dx1[gx] + p.dx1[gx - 1]),
-                                     R(2) * (qc[hc + 1] - qc[hc]) / (p.dx1[gx + 1] + p.dx1[gx]));
-                if (NDIM == 2)
-                    dqy[c] = slope_limit(p.slope_type, R(2) * (qc[hc] - qc[hc - T::HX]) / (p.dx2[gx] + p.dx2[gx]),
-                                         R(2) * (qc[hc + T::HX] - qc[hc]) / (p.dx2[gx] + p.dx2[gx])) /
-                             radius_polar;
-            }
-        }
-        R r_rho = qs[0 * S::halo + hc];
-        R u = qs[1 * S::halo + hc], v = qs[2 * S::halo + hc], w = qs[3 * S::halo + hc];
-        const R drx = dqx[0], dux = dqx[1], dvx = dqx[2], dwx = dqx[3];
-        const R dry = dqy[0], duy = dqy[1], dvy = dqy[2], dwy = dqy[3];
-        R f1, f2, f3;
-        if (fk) {
-            // update_force_setup only writes active cells; ghost cells keep force = 0
-            // (src/setups/SI/setup.f90:339-340, the array is zeroed in allocate_init.f90:271)
-            const int gy = hy0 + hy;
-            const bool active = gx >= p.ng && gx < p.ng + p.nx && (NDIM == 1 || (gy >= p.ng && gy < p.ng + p.ny));
-            if (active) setup_force(p, s, gx, u, w, f1, f2, f3);
-            else f1 = f2 = f3 = R(0);
-            u = u + f1 * half * dt;
-            v = v + f2 * half * dt;
-            w = w + f3 * half * dt;
-        }
-        R sr0 = -u * drx - v * dry - (dux + dvy) * r_rho;
-        R su0, sv0, sw0;
-        R face[NV][4];   // [c][qm_x, qp_x, qm_y, qp_y]
-        const R dxl = p.dx1[gx];
-        const R dyl = radius_polar * p.dx2[gx];
-        if (IS_GAS) {
-            const R csi = css[hc];
-            R pp = qs[4 * S::halo + hc];
-            R dpx = dqx[4], dpy = dqy[4];
-            if (iso) {
-                pp = qs[0 * S::halo + hc] * sq(csi);
-                dpx = dqx[0] * sq(csi);
-                if (NDIM == 2) dpy = dqy[0] * sq(csi);
-            }
-            R sp0 = -u * dpx - v * dpy - (dux + dvy) * gamma * pp;
-            su0 = -u * dux - v * duy - (dpx) / r_rho;
-            sv0 = -u * dvx - v * dvy - (dpy) / r_rho;
-            sw0 = -u * dwx - v * dwy;
-            if (polar) {
-                sr0 = -u * drx - v * dry - (dux + dvy) * r_rho - r_rho * u / radius_polar;
-                sp0 = -u * dpx - v * dpy - (dux + dvy) * gamma * pp - gamma * pp * u / radius_polar;
-                su0 = -u * dux - v * duy - (dpx) / r_rho + (sq(v)) / radius_polar;
-                sv0 = -u * dvx - v * dvy - (dpy) / r_rho - u * v / radius_polar;
-                sw0 = -u * dwx - v * dwy;
-            }
-            const R smallP = R(p.smallp);
-            face[0][0] = r_rho + half * dt * sr0 + half * drx * dxl;
-            face[1][0] = u + half * dt * su0 + half * dux * dxl;
-            face[4][0] = fmax2(pp + half * dt * sp0 + half * dpx * dxl, smallP);
-            face[2][0] = v + half * dt * sv0 + half * dvx * dxl;
-            face[3][0] = w + half * dt * sw0 + half * dwx * dxl;
-            face[0][1] = r_rho + half * dt * sr0 - half * drx * dxl;
-            face[1][1] = u + half * dt * su0 - half * dux * dxl;
-            face[4][1] = fmax2(pp + half * dt * sp0 - half * dpx * dxl, smallP);
-            face[2][1] = v + half * dt * sv0 - half * dvx * dxl;
-            face[3][1] = w + half * dt * sw0 - half * dwx * dxl;
-            if (NDIM == 2) {
-                face[0][2] = r_rho + half * dt * sr0 + half * dry * dyl;
-                face[1][2] = u + half * dt * su0 + half * duy * dyl;
-                face[4][2] = fmax2(pp + half * dt * sp0 + half * dpy * dyl, smallP);
-                face[2][2] = v + half * dt * sv0 + half * dvy * dyl;
-                face[3][2] = w + half * dt * sw0 + half * dwy * dyl;
-                face[0][3] = r_rho + half * dt * sr0 - half * dry * dyl;
-                face[1][3] = u + half * dt * su0 - half * duy * dyl;
-                face[4][3] = fmax2(pp + half * dt * sp0 - half * dpy * dyl, smallP);
-                face[2][3] = v + half * dt * sv0 - half * dvy * dyl;
-                face[3][3] = w + half * dt * sw0 - half * dwy * dyl;
-            }
-            if (iso) {   // godunov.f90:606-611
-#pragma unroll
-                for (int d = 0; d < (NDIM == 2 ? 4 : 2); ++d) face[4][d] = sq(csi) * face[0][d];
-            }
-        } else {
-            su0 = -u * dux - v * duy;
-            sv0 = -u * dvx - v * dvy;
-            sw0 = -u * dwx - v * dwy;
-            if (polar) {
-                sr0 = sr0 - r_rho * u / radius_polar;
-                su0 = su0 + sq(v) / radius_polar;
-                sv0 = sv0 - u * v / radius_polar;
-            }
-            face[0][0] = r_rho + half * dt * sr0 + half * drx * dxl;
-            face[1][0] = u + half * dt * su0 + half * dux * dxl;
-            face[2][0] = v + half * dt * sv0 + half * dvx * dxl;
-            face[3][0] = w + half * dt * sw0 + half * dwx * dxl;
-            face[0][1] = r_rho + half * dt * sr0 - half * drx * dxl;
-            face[1][1] = u + half * dt * su0 - half * dux * dxl;
-            face[2][1] = v + half * dt * sv0 - half * dvx * dxl;
-            face[3][1] = w + half * dt * sw0 - half * dwx * dxl;
-            if (NDIM == 2) {
-                face[0][2] = r_rho + half * dt * sr0 + half * dry * dyl;
-                face[1][2] = u + half * dt * su0 + half * duy * dyl;
-                face[2][2] = v + half * dt * sv0 + half * dvy * dyl;
-                face[3][2] = w + half * dt * sw0 + half * dwy * dyl;
-                face[0][3] = r_rho + half * dt * sr0 - half * dry * dyl;
-                face[1][3] = u + half * dt * su0 - half * duy * dyl;
-                face[2][3] = v + half * dt * sv0 - half * dvy * dyl;
-                face[3][3] = w + half * dt * sw0 - half * dwy * dyl;
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < NV; ++c) {
-            qmx[c * S::ring + r] = face[c][0];
-            qpx[c * S::ring + r] = face[c][1];
-            if (NDIM == 2) {
-                qmy[c * S::ring + r] = face[c][2];
-                qpy[c * S::ring + r] = face[c][3];
-            }
-        }
-    }
-    __syncthreads();
-
-    // ---- Riemann fluxes (godunov.f90:659-722, solve_wrapper :768-833) ----------------------
-    // x faces: face fx (0..TX) of tile row fy sits between ring cells (fx, ry) and (fx+1, ry).
-    for (int f = tid; f < (T::TX + 1) * T::TY; f += T::NT) {
-        const int fy = f / (T::TX + 1), fx = f - fy * (T::TX + 1);
-        const int ry = (NDIM == 2) ? fy + 1 : 0;
-        const int rl = ry * T::RX + fx, rr = rl + 1;
-        const int gxl = hx0 + fx + 1;   // global column of the left cell
-        if (gxl + 1 > p.nx_max - 2) continue;
-        R fl[NV];
-        if (IS_GAS) {
-            R csl, csr;
-            const R rl0 = qmx[0 * S::ring + rl], rr0 = qpx[0 * S::ring + rr];
-            const R pl = qmx[4 * S::ring + rl], pr = qpx[4 * S::ring + rr];
-            if (iso) {
-                const int hy = (NDIM == 2) ? ry + 1 : 0;
-                csl = css[hy * T::HX + fx + 1];
-                csr = css[hy * T::HX + fx + 2];
-            } else {
-                csl = sqrt(gamma * pl / rl0);
-                csr = sqrt(gamma * pr / rr0);
-            }
-            GasFlux<R> g;
-            const R ul = qmx[1 * S::ring + rl], vl = qmx[2 * S::ring + rl], wl = qmx[3 * S::ring + rl];
-            const R ur = qpx[1 * S::ring + rr], vr = qpx[2 * S::ring + rr], wr = qpx[3 * S::ring + rr];
-            if (p.solver == 2) g = gas_hllc(gamma, rl0, ul, vl, wl, pl, rr0, ur, vr, wr, pr, csl, csr);
-            else if (p.solver == 1) g = gas_hll(gamma, rl0, ul, vl, wl, pl, rr0, ur, vr, wr, pr, csl, csr);
-            else g = gas_llf(gamma, rl0, ul, vl, wl, pl, rr0, ur, vr, wr, pr, csl, csr);
-            fl[0] = g.rho; fl[1] = g.mn; fl[2] = g.mt; fl[3] = g.mz; fl[4] = g.e;
-        } else {
-            DustFlux<R> d;
-            const R rl0 = qmx[0 * S::ring + rl], ul = qmx[1 * S::ring + rl], vl = qmx[2 * S::ring + rl], wl = qmx[3 * S::ring + rl];
-            const R rr0 = qpx[0 * S::ring + rr], ur = qpx[1 * S::ring + rr], vr = qpx[2 * S::ring + rr], wr = qpx[3 * S::ring + rr];
-            if (p.solverdust == 0) d = dust_hb(rl0, ul, vl, wl, rr0, ur, vr, wr);
-            else if (p.solverdust == 1) d = dust_llf(rl0, ul, vl, wl, rr0, ur, vr, wr);
-            else d = dust_hll(rl0, ul, vl, wl, rr0, ur, vr, wr);
-            fl[0] = d.rho; fl[1] = d.mn; fl[2] = d.mt; fl[3] = d.mz;
-        }
-#pragma unroll
-        for (int c = 0; c < NV; ++c) fxs[c * S::fxn + f] = fl[c];
-    }
-    if (NDIM == 2) {
-        // y faces: face fy (0..TY) of tile column fx sits between ring cells (fx+1, fy), (fx+1, fy+1)
-        for (int f = tid; f < T::TX * (T::TY + 1); f += T::NT) {
-            const int fy = f / T::TX, fx = f - fy * T::TX;
-            const int rl = fy * T::RX + fx + 1, rr = rl + T::RX;
-            const int gx = hx0 + fx + 2;
-            if (gx > p.nx_max - 3 || hy0 + fy + 2 > p.ny_max - 2) continue;
-            R fl[NV];
-            if (IS_GAS) {
-                R csl, csr;
-                const R rl0 = qmy[0 * S::ring + rl], rr0 = qpy[0 * S::ring + rr];
-                const R pl = qmy[4 * S::ring + rl], pr = qpy[4 * S::ring + rr];
-                if (iso) {
-                    csl = css[(fy + 1) * T::HX + fx + 2];
-                    csr = css[(fy + 2) * T::HX + fx + 2];
-                } else {
-                    csl = sqrt(gamma * pl / rl0);
-                    csr = sqrt(gamma * pr / rr0);
-                }
-                // idim = 2: normal velocity vy, transverse vx (index_vn/vt, allocate_init.f90:249-252)
-                const R ul = qmy[2 * S::ring + rl], vl = qmy[1 * S::ring + rl], wl = qmy[3 * S::ring + rl];
-                const R ur = qpy[2 * S::ring + rr], vr = qpy[1 * S::ring + rr], wr = qpy[3 * S::ring + rr];
-                GasFlux<R> g;
-                if (p.solver == 2) g = gas_hllc(gamma, rl0, ul, vl, wl, pl, rr0, ur, vr, wr, pr, csl, csr);
-                else if (p.solver == 1) g = gas_hll(gamma, rl0, ul, vl, wl, pl, rr0, ur, vr, wr, pr, csl, csr);
-                else g = gas_llf(gamma, rl0, ul, vl, wl, pl, rr0, ur, vr, wr, pr, csl, csr);
-                fl[0] = g.rho; fl[2] = g.mn; fl[1] = g.mt; fl[3] = g.mz; fl[4] = g.e;
-            } else {
-                const R rl0 = qmy[0 * S::ring + rl], ul = qmy[2 * S::ring + rl], vl = qmy[1 * S::ring + rl], wl = qmy[3 * S::ring + rl];
-                const R rr0 = qpy[0 * S::ring + rr], ur = qpy[2 * S::ring + rr], vr = qpy[1 * S::ring + rr], wr = qpy[3 * S::ring + rr];
-                DustFlux<R> d;
-                if (p.solverdust == 0) d = dust_hb(rl0, ul, vl, wl, rr0, ur, vr, wr);
-                else if (p.solverdust == 1) d = dust_llf(rl0, ul, vl, wl, rr0, ur, vr, wr);
-                else d = dust_hll(rl0, ul, vl, wl, rr0, ur, vr, wr);
-                fl[0] = d.rho; fl[2] = d.mn; fl[1] = d.mt; fl[3] = d.mz;
-            }
-#pragma unroll
-            for (int c = 0; c < NV; ++c) fys[c * S::fyn + f] = fl[c];
-        }
-    }
-    __syncthreads();
-
-    // ---- kick + conservative update + local source terms, one thread per active cell ----------
-    {
-        const int cy = tid / T::TX, cx = tid - cy * T::TX;
-        const int gx = ax0 + cx, gy = ay0 + cy;
-        if (gx >= p.ng + p.nx || (NDIM == 2 && gy >= p.ng + p.ny)) return;
-        const int hc = (cy + T::OY) * T::HX + cx + T::OX;
-        R uu[NV];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) uu[c] = us[c * S::halo + hc];
-        if (fk) {   // kick(1.0) (src/solver/force_kicks.f90:2-41) before the flux update
-            R f1, f2, f3;
-            setup_force(p, s, gx, qs[1 * S::halo + hc], qs[3 * S::halo + hc], f1, f2, f3);
-            const R rho = uu[0];
-            if (IS_GAS) {
-                const R eo = half * sq(uu[1]) / rho + half * sq(uu[2]) / rho + half * sq(uu[3]) / rho;
-                uu[1] = uu[1] + rho * R(1) * dt * f1;
-                uu[2] = uu[2] + rho * R(1) * dt * f2;
-                uu[3] = uu[3] + rho * R(1) * dt * f3;
-                const R en = half * sq(uu[1]) / rho + half * sq(uu[2]) / rho + half * sq(uu[3]) / rho;
-                uu[4] = uu[4] + (en - eo);
-            } else {
-                uu[1] = uu[1] + rho * R(1) * dt * f1;
-                uu[2] = uu[2] + rho * R(1) * dt * f2;
-                uu[3] = uu[3] + rho * R(1) * dt * f3;
-            }
-        }
-        const R s1l = p.surf1[gx], s1r = p.surf1[gx + 1], vol = p.vol[gx];
-        const int fxl = cy * (T::TX + 1) + cx;
-#pragma unroll
-        for (int c = 0; c < NV; ++c) {
-            const R* F = fxs + c * S::fxn;
-            if (NDIM == 1) {
-                uu[c] = uu[c] + (F[fxl] * s1l - F[fxl + 1] * s1r) / vol * dt;
-            } else {
-                const R* G = fys + c * S::fyn;
-                const R s2 = p.surf2[gx];
-                uu[c] = uu[c] + (F[fxl] * s1l - F[fxl + 1] * s1r) / vol * dt +
-                        (G[cy * T::TX + cx] * s2 - G[(cy + 1) * T::TX + cx] * s2) / vol * dt;
-            }
-        }
-        if (polar) {   // Source_terms, GEOM==2 (src/solver/source_terms.f90:37-47), on the OLD q
-            const R rc = p.radc[gx];
-            const R qr = qs[0 * S::halo + hc], qvx = qs[1 * S::halo + hc], qvy = qs[2 * S::halo + hc];
-            if (IS_GAS) {
-                uu[1] = uu[1] + dt * (qr * sq(qvy) + qs[4 * S::halo + hc]) / rc;
-                uu[2] = uu[2] + (R(0) - dt * (qr * qvy * qvx / rc));
-            } else {
-                uu[1] = uu[1] + dt * (qr * sq(qvy) / rc);
-                uu[2] = uu[2] + (R(0) - dt * (qr * qvy * qvx / rc));
-            }
-        }
-#pragma unroll
-        for (int c = 0; c < NV; ++c) p.u_next[uidx(p, svar(s, c, N), gy, gx)] = uu[c];
-    }
-}
-
-template <typename R, int NDIM>
-__global__ void __launch_bounds__(Tile<NDIM>::NT) k_flux(KParams<R> p) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    R* sm = reinterpret_cast<R*>(smem_raw);
-    const int s = blockIdx.z;
-    if (s == 0) flux_tile<R, NDIM, true>(p, 0, sm);
-    else flux_tile<R, NDIM, false>(p, s, sm);
-}
+namespace shark {
 
 // ---------------------------------------------------------------------------------------------
 // K2: drag + floor + inloop + status + next-step CFL dt, one thread per active cell.
 // NS > 0: compile-time species count (register arrays); NS < 0: run-time count.
 // MODE 0: full finalize; MODE 1: dt only (first step after an upload).
 // ---------------------------------------------------------------------------------------------
+
 __device__ __forceinline__ void atomic_min_dt(unsigned long long* a, double v) {
     // positive finite doubles order like their bit patterns
     atomicMin(a, (unsigned long long)__double_as_longlong(v));
+}
+
+// Block-wide min of the CFL candidates and OR of the status bits, then one atomic per block.
+// Every thread of the block must call it (no early return before it).
+__device__ __forceinline__ void block_reduce_dt(double dtc, unsigned int st, unsigned long long* dt_next,
+                                                unsigned int* status) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const double other = __shfl_xor_sync(0xffffffffu, dtc, o);
+        dtc = other < dtc ? other : dtc;
+        st |= __shfl_xor_sync(0xffffffffu, st, o);
+    }
+    __shared__ double wmin[32];
+    __shared__ unsigned int wst[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { wmin[wid] = dtc; wst[wid] = st; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        dtc = lane < nw ? wmin[lane] : 2e44;
+        st = lane < nw ? wst[lane] : 0u;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double other = __shfl_xor_sync(0xffffffffu, dtc, o);
+            dtc = other < dtc ? other : dtc;
+            st |= __shfl_xor_sync(0xffffffffu, st, o);
+        }
+        if (lane == 0) {
+            atomic_min_dt(dt_next, dtc);
+            if (st) atomicOr(status, st);
+        }
+    }
 }
 
 template <typename R, int NS, int MODE>
@@ -689,31 +328,180 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
         if (!isfinite(vx) || !isfinite(vy) || !isfinite(vz) || !isfinite(rho)) st |= SHARK_STATUS_NAN;
         if (!(dtc > 0.0) || !isfinite(dtc)) { st |= SHARK_STATUS_DT_UNDERFLOW; dtc = 2e44; }
     }
-    // block min of dtc and OR of status
-    for (int o = 16; o > 0; o >>= 1) {
-        const double other = __shfl_xor_sync(0xffffffffu, dtc, o);
-        dtc = other < dtc ? other : dtc;
-        st |= __shfl_xor_sync(0xffffffffu, st, o);
+    block_reduce_dt(dtc, st, p.dt_next, p.status);
+}
+
+// ---------------------------------------------------------------------------------------------
+// K2, mixed precision (FP32 state).  The stiff part of the implicit drag -- the coefficients
+// 1/(1+a_k) and a_k/(1+a_k) with a_k = dt/t_k, which carry the t_stop << dt limit -- is computed in
+// FP64 (once per block when t_k is a per-species constant, as in the SI box; per cell otherwise).
+// The per-cell barycentric combination (positive weights, no cancellation) and the CFL candidate
+// run in FP32 like the rest of the mixed path.  Same algorithm as dust_drag.f90:29-73.
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ void drag_coeffs(double a, float& r, float& w) {
+    const double d = 1.0 + a;
+    r = (float)(1.0 / d);
+    w = (float)(a / d);
+}
+
+template <int NS, int MODE>
+__global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
+    constexpr int NMAX = NS > 0 ? NS : 1;
+    const int N = NS >= 0 ? NS : p.ndust;
+    __shared__ float cr[SHARK_MAX_DUST], cw[SHARK_MAX_DUST];
+    const bool drag = MODE == 0 && N > 0 && (p.flags & SHARK_FLAG_DRAG);
+    const bool const_ts = p.setup == SHARK_SETUP_SI;
+    const double dt = *p.dt;
+    if (drag && const_ts) {
+        for (int k = threadIdx.x; k < N; k += blockDim.x) drag_coeffs(1.0 * dt / p.dtstop[k], cr[k], cw[k]);
+        __syncthreads();
     }
-    __shared__ double wmin[32];
-    __shared__ unsigned int wst[32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { wmin[wid] = dtc; wst[wid] = st; }
-    __syncthreads();
-    if (wid == 0) {
-        const int nw = (blockDim.x + 31) >> 5;
-        dtc = lane < nw ? wmin[lane] : 2e44;
-        st = lane < nw ? wst[lane] : 0u;
-        for (int o = 16; o > 0; o >>= 1) {
-            const double other = __shfl_xor_sync(0xffffffffu, dtc, o);
-            dtc = other < dtc ? other : dtc;
-            st |= __shfl_xor_sync(0xffffffffu, st, o);
+    const int gx = blockIdx.x * blockDim.x + threadIdx.x + p.ng;
+    const int gy = (p.ndim == 2) ? blockIdx.y + p.ng : 0;
+    float dtc = 2e38f;
+    unsigned int st = 0;
+    if (gx < p.ng + p.nx) {
+        float* u = p.u_next;
+        const float rho = u[uidx(p, 0, gy, gx)];
+        float px = u[uidx(p, 1, gy, gx)], py = u[uidx(p, 2, gy, gx)], pz = u[uidx(p, 3, gy, gx)];
+        if (drag) {
+            float rk[NMAX], wk[NMAX];
+            float rhon = rho, pnx = px, pny = py, pnz = pz;
+            const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
+            const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
+            for (int k = 0; k < N; ++k) {
+                float r, w;
+                if (const_ts) { r = cr[k]; w = cw[k]; }
+                else {
+                    double ts;
+                    if (p.setup == SHARK_SETUP_DUSTYWAVE) {
+                        const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
+                        ts = rd_old * qrho_old / p.dK[k] / qrho_old;
+                    } else {
+                        ts = sqrt(3.141592653589793238462643383279 * p.gamma / 8.0) * p.rhograin * p.dsize[k] /
+                             (qrho_old * p.csd[gx]);
+                    }
+                    drag_coeffs(1.0 * dt / ts, r, w);
+                }
+                if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
+                pnx += w * u[uidx(p, 5 + N + k, gy, gx)];
+                pny += w * u[uidx(p, 5 + 2 * N + k, gy, gx)];
+                pnz += w * u[uidx(p, 5 + 3 * N + k, gy, gx)];
+                rhon += w * u[uidx(p, 5 + k, gy, gx)];
+            }
+            const float irhon = 1.0f / rhon;
+            const float vbx = pnx * irhon, vby = pny * irhon, vbz = pnz * irhon;
+            for (int k = 0; k < N; ++k) {
+                float r, w;
+                if (NS > 0) { r = rk[k < NMAX ? k : 0]; w = wk[k < NMAX ? k : 0]; }
+                else if (const_ts) { r = cr[k]; w = cw[k]; }
+                else {
+                    double ts;
+                    if (p.setup == SHARK_SETUP_DUSTYWAVE) {
+                        const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
+                        ts = rd_old * qrho_old / p.dK[k] / qrho_old;
+                    } else {
+                        ts = sqrt(3.141592653589793238462643383279 * p.gamma / 8.0) * p.rhograin * p.dsize[k] /
+                             (qrho_old * p.csd[gx]);
+                    }
+                    drag_coeffs(1.0 * dt / ts, r, w);
+                }
+                const float rd = u[uidx(p, 5 + k, gy, gx)];
+                const long long ixx = uidx(p, 5 + N + k, gy, gx), iyy = uidx(p, 5 + 2 * N + k, gy, gx),
+                                izz = uidx(p, 5 + 3 * N + k, gy, gx);
+                const float wr = w * rd;
+                u[ixx] = u[ixx] * r + wr * vbx;
+                u[iyy] = u[iyy] * r + wr * vby;
+                u[izz] = u[izz] * r + wr * vbz;
+            }
+            if (p.flags & SHARK_FLAG_BACK_REACTION) {
+                px = vbx * rho; py = vby * rho; pz = vbz * rho;
+                u[uidx(p, 1, gy, gx)] = px;
+                u[uidx(p, 2, gy, gx)] = py;
+                u[uidx(p, 3, gy, gx)] = pz;
+            }
+            const float fl = rho * (float)p.dust_ratio_min;   // floor (dust_drag.f90:63-73)
+            for (int k = 0; k < N; ++k) {
+                const long long ir = uidx(p, 5 + k, gy, gx);
+                if (fl > u[ir]) u[ir] = fl;
+            }
         }
-        if (lane == 0) {
-            atomic_min_dt(p.dt_next, dtc);
-            if (st) atomicOr(p.status, st);
+        if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
+            // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
+            const float om = (float)p.si_om, qsh = (float)p.si_q;
+            const float Ohmdt = (float)(p.si_om * dt), O2 = Ohmdt * Ohmdt, inv = 1.0f / (1.0f + O2);
+            const float xc = p.xpos[gx] - 0.5f * (float)p.box_l;
+            float AA = 2.0f * qsh * om * xc - 2.0f * (float)p.si_r0 * (float)p.si_eta;
+            {
+                const float uz = pz / rho, vx = px / rho;
+                pz = rho * (uz * (1.f - O2) + 2.f * vx * Ohmdt + AA * O2) * inv;
+                px = rho * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
+                u[uidx(p, 3, gy, gx)] = pz;
+                u[uidx(p, 1, gy, gx)] = px;
+            }
+            AA = 2.0f * qsh * om * xc;
+            for (int k = 0; k < N; ++k) {
+                const long long iz = uidx(p, 5 + 3 * N + k, gy, gx), ixx = uidx(p, 5 + N + k, gy, gx);
+                const float d = u[uidx(p, 5 + k, gy, gx)];
+                const float uz = u[iz] / d, vx = u[ixx] / d;
+                u[iz] = d * (uz * (1.f - O2) + 2.f * vx * Ohmdt + AA * O2) * inv;
+                u[ixx] = d * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
+            }
         }
+        // ---- courant on the final state (src/solver/courant.f90:11-124), FP32 ----------------------
+        const float cfl = (float)p.cfl;
+        const float irho = 1.0f / rho;
+        const float vx = px * irho, vy = py * irho, vz = pz * irho;
+        float cs;
+        if (p.iso == 1) cs = p.cs[gx];
+        else {
+            const float E = u[uidx(p, 4, gy, gx)];
+            const float ekin = 0.5f * rho * (vx * vx) + 0.5f * rho * (vy * vy) + 0.5f * rho * (vz * vz);
+            const float P = fmaxf((float)(p.gamma - 1.0) * (E - ekin), (float)p.smallp);
+            cs = sqrtf((float)p.gamma * P / fmaxf(rho, (float)p.smallr));
+            if (!(E == E)) st |= SHARK_STATUS_NAN;
+        }
+        float dxx;
+        if (p.ndim == 1) dxx = p.dx1[gx];
+        else if (p.geom == 2) dxx = fminf(p.dx1[gx], p.radc[gx] * p.dx2[gx]);
+        else dxx = fminf(p.dx1[gx], p.dx2[gx]);
+        float vv = fabsf(vx) + fabsf(vy) + fabsf(vz);
+        float vmax = cs + vv;
+        float fmx = 0.f;
+        const bool fk = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
+        const float om = (float)p.si_om, qsh = (float)p.si_q;
+        const float xc = p.xpos[gx] - 0.5f * (float)p.box_l;
+        if (fk) {
+            const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vz - 2.0f * (float)p.si_r0 * om * (float)p.si_eta;
+            const float f3 = 2.0f * om * vx;
+            fmx = sqrtf(f1 * f1 + f3 * f3);
+        }
+        for (int k = 0; k < N; ++k) {
+            const float rd = u[uidx(p, 5 + k, gy, gx)];
+            const float ird = 1.0f / rd;
+            const float vdx = u[uidx(p, 5 + N + k, gy, gx)] * ird;
+            const float vdy = u[uidx(p, 5 + 2 * N + k, gy, gx)] * ird;
+            const float vdz = u[uidx(p, 5 + 3 * N + k, gy, gx)] * ird;
+            vv = fabsf(vdx) + fabsf(vdy) + fabsf(vdz);
+            vmax = fmaxf(vmax, vv);
+            if (fk) {
+                const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vdz;
+                const float f3 = 2.0f * om * vdx;
+                fmx = fmaxf(fmx, sqrtf(f1 * f1 + f3 * f3));
+            }
+            if (!(rd > 0.f)) st |= SHARK_STATUS_NEG_DENSITY;
+            if (!isfinite(vv)) st |= SHARK_STATUS_NAN;
+        }
+        dtc = cfl * dxx / fabsf(vmax);
+        if (fk && vv != 0.f) {
+            const float fratio = fmaxf(fmx * dxx / (vv * vv), 1e-3f);
+            dtc = fminf(dtc, cfl * dxx / vv * (sqrtf(1.0f + 2.0f * cfl * fratio) - 1.0f) / fratio);
+        }
+        if (!(rho > 0.f)) st |= SHARK_STATUS_NEG_DENSITY;
+        if (!isfinite(vx) || !isfinite(vy) || !isfinite(vz)) st |= SHARK_STATUS_NAN;
+        if (!(dtc > 0.f) || !isfinite(dtc)) { st |= SHARK_STATUS_DT_UNDERFLOW; dtc = 2e38f; }
     }
+    block_reduce_dt(dtc >= 2e38f ? 2e44 : (double)dtc, st, p.dt_next, p.status);
 }
 
 // Reset the next-dt slot before k_finalize runs (single thread).

@@ -24,14 +24,26 @@ def active(cfg, u):
     return g[:, cfg.nghost:cfg.nghost + cfg.ny, cfg.nghost:cfg.nghost + cfg.nx]
 
 
+def field_scales(cfg, B):
+    """L1 scale of every conserved field: densities and energy by their own L1 norm, each
+    momentum component by the L1 norm of its species' momentum magnitude (a component whose
+    mean is zero, e.g. the gas vertical momentum of the SI box, has no meaningful own scale)."""
+    N = cfg.ndust
+    sc = np.array([np.sum(np.abs(B[v])) for v in range(cfg.nvar)])
+    comps = [(1, 2, 3)] + [(5 + N + k, 5 + 2 * N + k, 5 + 3 * N + k) for k in range(N)]
+    for c in comps:
+        mag = np.sum(np.sqrt(B[c[0]] ** 2 + B[c[1]] ** 2 + B[c[2]] ** 2))
+        for v in c:
+            sc[v] = mag
+    return sc
+
+
 def rel_l1(cfg, a, b):
+    """Relative L1 error of a against b per conserved field over the active cells."""
     A, B = active(cfg, a), active(cfg, b)
-    out = []
-    for v in range(cfg.nvar):
-        den = np.sum(np.abs(B[v]))
-        num = np.sum(np.abs(A[v] - B[v]))
-        out.append(num / den if den > 0 else num)
-    return np.array(out)
+    sc = field_scales(cfg, B)
+    num = np.array([np.sum(np.abs(A[v] - B[v])) for v in range(cfg.nvar)])
+    return np.where(sc > 0, num / np.where(sc > 0, sc, 1.0), num)
 
 
 def run_pair(cfg, u0, nsteps):
