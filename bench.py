@@ -322,8 +322,8 @@ def run_gpu(args):
                  "mixed_over_fp64": value / world / value_fp64,
                  "l1_mixed_vs_fp64": l1, "l1_note": f"max relative L1 over the {nvar} conserved fields after "
                                                     f"{steps_done_m} steps from the same state",
-                 "kernel_ms": {"boundaries": kt_d[0], "flux_update": kt_d[1], "drag_dt": kt_d[2], "step": kt_d[3]}},
-        "kernel_ms": {"boundaries": kt[0], "flux_update": kt[1], "drag_dt": kt[2], "step": kt[3]},
+                 "kernel_ms": {"pre_flux": kt_d[0], "flux_update": kt_d[1], "drag_dt_ghosts": kt_d[2], "step": kt_d[3]}},
+        "kernel_ms": {"pre_flux": kt[0], "flux_update": kt[1], "drag_dt_ghosts": kt[2], "step": kt[3]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "kernel": "k_flux (K1 fused flux/update)",
                      "peak_kind": peak_kind,
@@ -336,7 +336,7 @@ def run_gpu(args):
                 "resident_note": "state kept on the device, per step shark_gpu_step with its 12-byte dt/status readback"},
         "cpu_baseline": cpu,
         "gpu_launches": 4 * args.steps,
-        "gpu_launches_note": "per step: k_boundaries, k_reset_dt, k_flux, k_finalize",
+        "gpu_launches_note": "per step: k_reset_dt, k_flux_strip (gas, side stream), k_flux_strip (dust), k_finalize",
         "status": st,
         "clocks": clocks.summary(),
     }

@@ -186,8 +186,9 @@ int32_t shark_gpu_ctoprim(shark_gpu_ctx* ctx, double* q, double* cs);
  * doubles.  Deterministic: fixed reduction tree. */
 int32_t shark_gpu_totals(shark_gpu_ctx* ctx, double* out);
 
-/* Device time of the last `step` in milliseconds: ms_out[0] boundaries, ms_out[1] flux/update
- * kernel, ms_out[2] drag + dt kernel (CUDA events on the context's stream; waits for the step). */
+/* Device time of the last `step` in milliseconds: ms_out[0] work before the flux kernel (the dt
+ * slot reset), ms_out[1] flux/update kernels (K1), ms_out[2] drag + dt + ghost-fill kernel (K2)
+ * (CUDA events on the context's stream; waits for the step). */
 int32_t shark_gpu_last_step_ms(shark_gpu_ctx* ctx, float* ms_out);
 
 /* Benchmark helper: synchronize, record a CUDA event on the context's stream, run nsteps steps
@@ -196,8 +197,9 @@ int32_t shark_gpu_last_step_ms(shark_gpu_ctx* ctx, float* ms_out);
 int32_t shark_gpu_timed_run(shark_gpu_ctx* ctx, int64_t nsteps, double* time_io, float* ms_out);
 
 /* Benchmark helper: run nsteps steps with CUDA events around every kernel on the context's
- * stream and return the mean device time per launch in milliseconds: avg_ms[0] boundaries,
- * avg_ms[1] flux/update (K1), avg_ms[2] drag + dt (K2), avg_ms[3] whole step. */
+ * stream and return the mean device time per launch in milliseconds: avg_ms[0] work before the
+ * flux kernel, avg_ms[1] flux/update (K1), avg_ms[2] drag + dt + ghost fill (K2), avg_ms[3] whole
+ * step. */
 int32_t shark_gpu_kernel_times(shark_gpu_ctx* ctx, int64_t nsteps, float* avg_ms);
 
 /* Human-readable message of the last error on this thread (static storage). */

@@ -59,12 +59,13 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
     const R vol = p.vol[gxc], rvol = p.rvol[gxc];
     const R cs_col = p.cs[gxc];
     const R dxl = dx1, dyl = (polar ? radc : R(1)) * dx2;
+    const R hdt = half * dt, hdx = half * dxl, hdy = half * dyl, dtv = dt * rvol;   // mixed path
 
     R q0[NV], q1[NV], q2[NV];       // primitive rows P-1, P, P+1 (P = row being predicted)
     R c0 = R(0), c1 = R(0), c2 = R(0);
     R qmy_prev[NV];                 // qm_y of the previous predicted row
     R g_prev[NV];                   // y flux at the bottom face of the previous predicted row
-    R fl_prev[NV], fr_prev[NV];     // x fluxes (left/right face) of the previous predicted row
+    R t_prev[NV];                   // previous row after kick + x-flux part of the update
     R c_prev = R(0);                // cs of the previous predicted row (isothermal y faces)
 
     // per-lane 32-bit element offsets of the species' planes (the context guarantees
@@ -123,13 +124,14 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
         to_prim(nxt, q2, c2);
         if (row < rend) fetch_row(row + 1, nxt);   // prefetch the next row (uniform branch)
         const int P = row - 1;    // predicted row, ay0-1 .. ylast+1
-        // own conserved values of the row updated in this iteration (row P-1, an L1/L2 hit)
+        // the update of row P starts in this iteration (kick + x fluxes) and ends in the next one
+        // (y flux above it); load its own conserved values now (an L1/L2 hit)
+        const bool start_upd = col_upd && P >= ay0 && P <= ylast;
+        const bool finish_upd = col_upd && P - 1 >= ay0 && P - 1 <= ylast;
         R uu[NV];
-        const int uy = P - 1;
-        const bool do_upd = row > ay0 && col_upd && uy >= ay0 && uy <= ylast;
-        if (do_upd) {
+        if (start_upd) {
 #pragma unroll
-            for (int k = 0; k < NV; ++k) uu[k] = __ldg(src + (voff[k] + uy * pitch));
+            for (int k = 0; k < NV; ++k) uu[k] = __ldg(src + (voff[k] + P * pitch));
         }
         // ---- predictor of (P, gx) -------------------------------------------------------------
         R dqx[NV], dqy[NV];
@@ -152,11 +154,10 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
         R r_rho = q1[0], u = q1[1], v = q1[2], w = q1[3];
         const R drx = dqx[0], dux = dqx[1], dvx = dqx[2], dwx = dqx[3];
         const R dry = dqy[0], duy = dqy[1], dvy = dqy[2], dwy = dqy[3];
+        R f1 = R(0), f2 = R(0), f3 = R(0);   // force of row P; the kick of row P below reuses it
         if (fk) {
-            R f1, f2, f3;
             const bool active = col_active && P >= p.ng && P < p.ng + p.ny;
-            if (active) setup_force(p, s, gxc, u, w, f1, f2, f3);
-            else f1 = f2 = f3 = R(0);   // ghost cells keep force = 0 (SI/setup.f90:339)
+            if (active) setup_force(p, s, gxc, u, w, f1, f2, f3);   // ghost cells keep force = 0 (SI/setup.f90:339)
             u = u + f1 * half * dt;
             v = v + f2 * half * dt;
             w = w + f3 * half * dt;
@@ -185,26 +186,40 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 sv0 = -u * dvx - v * dvy - dpy_r - over_r(u * v);
             }
             const R smallP = R(p.smallp);
-            qmx[0] = r_rho + half * dt * sr0 + half * drx * dxl;
-            qmx[1] = u + half * dt * su0 + half * dux * dxl;
-            qmx[4] = fmax2(pp + half * dt * sp0 + half * dpx * dxl, smallP);
-            qmx[2] = v + half * dt * sv0 + half * dvx * dxl;
-            qmx[3] = w + half * dt * sw0 + half * dwx * dxl;
-            qpx[0] = r_rho + half * dt * sr0 - half * drx * dxl;
-            qpx[1] = u + half * dt * su0 - half * dux * dxl;
-            qpx[4] = fmax2(pp + half * dt * sp0 - half * dpx * dxl, smallP);
-            qpx[2] = v + half * dt * sv0 - half * dvx * dxl;
-            qpx[3] = w + half * dt * sw0 - half * dwx * dxl;
-            qmy[0] = r_rho + half * dt * sr0 + half * dry * dyl;
-            qmy[1] = u + half * dt * su0 + half * duy * dyl;
-            qmy[4] = fmax2(pp + half * dt * sp0 + half * dpy * dyl, smallP);
-            qmy[2] = v + half * dt * sv0 + half * dvy * dyl;
-            qmy[3] = w + half * dt * sw0 + half * dwy * dyl;
-            qpy[0] = r_rho + half * dt * sr0 - half * dry * dyl;
-            qpy[1] = u + half * dt * su0 - half * duy * dyl;
-            qpy[4] = fmax2(pp + half * dt * sp0 - half * dpy * dyl, smallP);
-            qpy[2] = v + half * dt * sv0 - half * dvy * dyl;
-            qpy[3] = w + half * dt * sw0 - half * dwy * dyl;
+            if constexpr (FAST) {
+                const R b0 = r_rho + hdt * sr0, b1 = u + hdt * su0, b2 = v + hdt * sv0, b3 = w + hdt * sw0, b4 = pp + hdt * sp0;
+                qmx[0] = b0 + hdx * drx; qpx[0] = b0 - hdx * drx;
+                qmx[1] = b1 + hdx * dux; qpx[1] = b1 - hdx * dux;
+                qmx[2] = b2 + hdx * dvx; qpx[2] = b2 - hdx * dvx;
+                qmx[3] = b3 + hdx * dwx; qpx[3] = b3 - hdx * dwx;
+                qmx[4] = fmaxf(b4 + hdx * dpx, smallP); qpx[4] = fmaxf(b4 - hdx * dpx, smallP);
+                qmy[0] = b0 + hdy * dry; qpy[0] = b0 - hdy * dry;
+                qmy[1] = b1 + hdy * duy; qpy[1] = b1 - hdy * duy;
+                qmy[2] = b2 + hdy * dvy; qpy[2] = b2 - hdy * dvy;
+                qmy[3] = b3 + hdy * dwy; qpy[3] = b3 - hdy * dwy;
+                qmy[4] = fmaxf(b4 + hdy * dpy, smallP); qpy[4] = fmaxf(b4 - hdy * dpy, smallP);
+            } else {
+                qmx[0] = r_rho + half * dt * sr0 + half * drx * dxl;
+                qmx[1] = u + half * dt * su0 + half * dux * dxl;
+                qmx[4] = fmax2(pp + half * dt * sp0 + half * dpx * dxl, smallP);
+                qmx[2] = v + half * dt * sv0 + half * dvx * dxl;
+                qmx[3] = w + half * dt * sw0 + half * dwx * dxl;
+                qpx[0] = r_rho + half * dt * sr0 - half * drx * dxl;
+                qpx[1] = u + half * dt * su0 - half * dux * dxl;
+                qpx[4] = fmax2(pp + half * dt * sp0 - half * dpx * dxl, smallP);
+                qpx[2] = v + half * dt * sv0 - half * dvx * dxl;
+                qpx[3] = w + half * dt * sw0 - half * dwx * dxl;
+                qmy[0] = r_rho + half * dt * sr0 + half * dry * dyl;
+                qmy[1] = u + half * dt * su0 + half * duy * dyl;
+                qmy[4] = fmax2(pp + half * dt * sp0 + half * dpy * dyl, smallP);
+                qmy[2] = v + half * dt * sv0 + half * dvy * dyl;
+                qmy[3] = w + half * dt * sw0 + half * dwy * dyl;
+                qpy[0] = r_rho + half * dt * sr0 - half * dry * dyl;
+                qpy[1] = u + half * dt * su0 - half * duy * dyl;
+                qpy[4] = fmax2(pp + half * dt * sp0 - half * dpy * dyl, smallP);
+                qpy[2] = v + half * dt * sv0 - half * dvy * dyl;
+                qpy[3] = w + half * dt * sw0 - half * dwy * dyl;
+            }
             if (iso) {   // godunov.f90:606-611
                 qmx[4] = sq(c1) * qmx[0];
                 qpx[4] = sq(c1) * qpx[0];
@@ -220,22 +235,34 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 su0 = su0 + over_r(sq(v));
                 sv0 = sv0 - over_r(u * v);
             }
-            qmx[0] = r_rho + half * dt * sr0 + half * drx * dxl;
-            qmx[1] = u + half * dt * su0 + half * dux * dxl;
-            qmx[2] = v + half * dt * sv0 + half * dvx * dxl;
-            qmx[3] = w + half * dt * sw0 + half * dwx * dxl;
-            qpx[0] = r_rho + half * dt * sr0 - half * drx * dxl;
-            qpx[1] = u + half * dt * su0 - half * dux * dxl;
-            qpx[2] = v + half * dt * sv0 - half * dvx * dxl;
-            qpx[3] = w + half * dt * sw0 - half * dwx * dxl;
-            qmy[0] = r_rho + half * dt * sr0 + half * dry * dyl;
-            qmy[1] = u + half * dt * su0 + half * duy * dyl;
-            qmy[2] = v + half * dt * sv0 + half * dvy * dyl;
-            qmy[3] = w + half * dt * sw0 + half * dwy * dyl;
-            qpy[0] = r_rho + half * dt * sr0 - half * dry * dyl;
-            qpy[1] = u + half * dt * su0 - half * duy * dyl;
-            qpy[2] = v + half * dt * sv0 - half * dvy * dyl;
-            qpy[3] = w + half * dt * sw0 - half * dwy * dyl;
+            if constexpr (FAST) {
+                const R b0 = r_rho + hdt * sr0, b1 = u + hdt * su0, b2 = v + hdt * sv0, b3 = w + hdt * sw0;
+                qmx[0] = b0 + hdx * drx; qpx[0] = b0 - hdx * drx;
+                qmx[1] = b1 + hdx * dux; qpx[1] = b1 - hdx * dux;
+                qmx[2] = b2 + hdx * dvx; qpx[2] = b2 - hdx * dvx;
+                qmx[3] = b3 + hdx * dwx; qpx[3] = b3 - hdx * dwx;
+                qmy[0] = b0 + hdy * dry; qpy[0] = b0 - hdy * dry;
+                qmy[1] = b1 + hdy * duy; qpy[1] = b1 - hdy * duy;
+                qmy[2] = b2 + hdy * dvy; qpy[2] = b2 - hdy * dvy;
+                qmy[3] = b3 + hdy * dwy; qpy[3] = b3 - hdy * dwy;
+            } else {
+                qmx[0] = r_rho + half * dt * sr0 + half * drx * dxl;
+                qmx[1] = u + half * dt * su0 + half * dux * dxl;
+                qmx[2] = v + half * dt * sv0 + half * dvx * dxl;
+                qmx[3] = w + half * dt * sw0 + half * dwx * dxl;
+                qpx[0] = r_rho + half * dt * sr0 - half * drx * dxl;
+                qpx[1] = u + half * dt * su0 - half * dux * dxl;
+                qpx[2] = v + half * dt * sv0 - half * dvx * dxl;
+                qpx[3] = w + half * dt * sw0 - half * dwx * dxl;
+                qmy[0] = r_rho + half * dt * sr0 + half * dry * dyl;
+                qmy[1] = u + half * dt * su0 + half * duy * dyl;
+                qmy[2] = v + half * dt * sv0 + half * dvy * dyl;
+                qmy[3] = w + half * dt * sw0 + half * dwy * dyl;
+                qpy[0] = r_rho + half * dt * sr0 - half * dry * dyl;
+                qpy[1] = u + half * dt * su0 - half * duy * dyl;
+                qpy[2] = v + half * dt * sv0 - half * dvy * dyl;
+                qpy[3] = w + half * dt * sw0 - half * dwy * dyl;
+            }
         }
         (void)col_pred;
 
@@ -277,59 +304,62 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                                                 qpy[0], qpy[2], qpy[1], qpy[3]);
                 gb[0] = d.rho; gb[2] = d.mn; gb[1] = d.mt; gb[3] = d.mz;
             }
-            // ---- update row P-1 with its four fluxes ----------------------------------------------
-            if (do_upd) {
-                if (fk) {   // kick(1.0) before the flux update (force_kicks.f90:2-41), force of the OLD q
-                    R f1, f2, f3;
-                    // q of row uy is q0 here (rows P-1, P, P+1 = q0, q1, q2)
-                    setup_force(p, s, gxc, q0[1], q0[3], f1, f2, f3);
-                    const R rho = uu[0];
-                    if (IS_GAS) {
-                        R eo, en;
-                        if constexpr (FAST) {
-                            const R ir = R(1) / rho;
-                            eo = half * (sq(uu[1]) + sq(uu[2]) + sq(uu[3])) * ir;
-                            uu[1] = uu[1] + rho * dt * f1;
-                            uu[2] = uu[2] + rho * dt * f2;
-                            uu[3] = uu[3] + rho * dt * f3;
-                            en = half * (sq(uu[1]) + sq(uu[2]) + sq(uu[3])) * ir;
-                        } else {
-                            eo = half * sq(uu[1]) / rho + half * sq(uu[2]) / rho + half * sq(uu[3]) / rho;
-                            uu[1] = uu[1] + rho * R(1) * dt * f1;
-                            uu[2] = uu[2] + rho * R(1) * dt * f2;
-                            uu[3] = uu[3] + rho * R(1) * dt * f3;
-                            en = half * sq(uu[1]) / rho + half * sq(uu[2]) / rho + half * sq(uu[3]) / rho;
-                        }
-                        uu[4] = uu[4] + (en - eo);
+        }
+        // ---- finish row P-1: y-flux part, then the polar sources on its OLD q (= q0) ---------------
+        if (row > ay0 && finish_upd) {
+            R un[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k) {
+                if constexpr (FAST) un[k] = t_prev[k] + (g_prev[k] - gb[k]) * s2 * (dt * rvol);
+                else un[k] = t_prev[k] + (g_prev[k] * s2 - gb[k] * s2) / vol * dt;
+            }
+            if (polar) {   // Source_terms GEOM==2 (source_terms.f90:37-47)
+                const R qr = q0[0], qvx = q0[1], qvy = q0[2];
+                if constexpr (FAST) {
+                    const R dtr = dt * irp;
+                    if (IS_GAS) un[1] = un[1] + (qr * sq(qvy) + q0[4]) * dtr;
+                    else un[1] = un[1] + qr * sq(qvy) * dtr;
+                    un[2] = un[2] - qr * qvy * qvx * dtr;
+                } else {
+                    if (IS_GAS) un[1] = un[1] + dt * (qr * sq(qvy) + q0[4]) / radc;
+                    else un[1] = un[1] + dt * (qr * sq(qvy) / radc);
+                    un[2] = un[2] + (R(0) - dt * (qr * qvy * qvx / radc));
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NV; ++k) dst[voff[k] + (P - 1) * pitch] = un[k];
+        }
+        // ---- start row P: kick(1.0) with the force of its OLD q (= q1), then the x-flux part ------
+        if (start_upd) {
+            if (fk) {   // force_kicks.f90:2-41, before the flux update (force of this row's OLD q)
+                const R rho = uu[0];
+                if (IS_GAS) {
+                    R eo, en;
+                    if constexpr (FAST) {
+                        const R ir = R(1) / rho;
+                        eo = half * (sq(uu[1]) + sq(uu[2]) + sq(uu[3])) * ir;
+                        uu[1] = uu[1] + rho * dt * f1;
+                        uu[2] = uu[2] + rho * dt * f2;
+                        uu[3] = uu[3] + rho * dt * f3;
+                        en = half * (sq(uu[1]) + sq(uu[2]) + sq(uu[3])) * ir;
                     } else {
+                        eo = half * sq(uu[1]) / rho + half * sq(uu[2]) / rho + half * sq(uu[3]) / rho;
                         uu[1] = uu[1] + rho * R(1) * dt * f1;
                         uu[2] = uu[2] + rho * R(1) * dt * f2;
                         uu[3] = uu[3] + rho * R(1) * dt * f3;
+                        en = half * sq(uu[1]) / rho + half * sq(uu[2]) / rho + half * sq(uu[3]) / rho;
                     }
+                    uu[4] = uu[4] + (en - eo);
+                } else {
+                    uu[1] = uu[1] + rho * R(1) * dt * f1;
+                    uu[2] = uu[2] + rho * R(1) * dt * f2;
+                    uu[3] = uu[3] + rho * R(1) * dt * f3;
                 }
+            }
 #pragma unroll
-                for (int k = 0; k < NV; ++k) {
-                    if constexpr (FAST)
-                        uu[k] = uu[k] + ((fl_prev[k] * s1l - fr_prev[k] * s1r) + (g_prev[k] - gb[k]) * s2) * (dt * rvol);
-                    else
-                        uu[k] = uu[k] + (fl_prev[k] * s1l - fr_prev[k] * s1r) / vol * dt +
-                                (g_prev[k] * s2 - gb[k] * s2) / vol * dt;
-                }
-                if (polar) {   // Source_terms GEOM==2 on the OLD q (source_terms.f90:37-47)
-                    const R qr = q0[0], qvx = q0[1], qvy = q0[2];
-                    if constexpr (FAST) {
-                        const R dtr = dt * irp;
-                        if (IS_GAS) uu[1] = uu[1] + (qr * sq(qvy) + q0[4]) * dtr;
-                        else uu[1] = uu[1] + qr * sq(qvy) * dtr;
-                        uu[2] = uu[2] - qr * qvy * qvx * dtr;
-                    } else {
-                        if (IS_GAS) uu[1] = uu[1] + dt * (qr * sq(qvy) + q0[4]) / radc;
-                        else uu[1] = uu[1] + dt * (qr * sq(qvy) / radc);
-                        uu[2] = uu[2] + (R(0) - dt * (qr * qvy * qvx / radc));
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < NV; ++k) dst[voff[k] + uy * pitch] = uu[k];
+            for (int k = 0; k < NV; ++k) {
+                if constexpr (FAST) uu[k] = uu[k] + (fxl[k] * s1l - fxr[k] * s1r) * (dt * rvol);
+                else uu[k] = uu[k] + (fxl[k] * s1l - fxr[k] * s1r) / vol * dt;
             }
         }
         // ---- slide the window ---------------------------------------------------------------
@@ -337,8 +367,7 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
         for (int k = 0; k < NV; ++k) {
             qmy_prev[k] = qmy[k];
             g_prev[k] = gb[k];
-            fl_prev[k] = fxl[k];
-            fr_prev[k] = fxr[k];
+            t_prev[k] = uu[k];
             q0[k] = q1[k];
             q1[k] = q2[k];
         }

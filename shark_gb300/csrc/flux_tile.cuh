@@ -168,7 +168,8 @@ __device__ __forceinline__ GasFlux<R> gas_flux_t(R gamma, R inv_g1, R rl, R ul, 
 
 template <int SOLVERDUST, typename R>
 __device__ __forceinline__ DustFlux<R> dust_flux_t(R rl, R ul, R vl, R wl, R rr, R ur, R vr, R wr) {
-    if constexpr (SOLVERDUST == 0) return dust_hb(rl, ul, vl, wl, rr, ur, vr, wr);
+    if constexpr (SOLVERDUST == 0 && std::is_same<R, float>::value) return dust_hb_f(rl, ul, vl, wl, rr, ur, vr, wr);
+    else if constexpr (SOLVERDUST == 0) return dust_hb(rl, ul, vl, wl, rr, ur, vr, wr);
     else if constexpr (SOLVERDUST == 1) return dust_llf(rl, ul, vl, wl, rr, ur, vr, wr);
     else return dust_hll(rl, ul, vl, wl, rr, ur, vr, wr);
 }

@@ -27,7 +27,7 @@ static KParams<R> make_params(const DeviceView& v) {
     p.sfx = (const R*)v.m[8]; p.sfy = (const R*)v.m[9]; p.irp = (const R*)v.m[10]; p.rvol = (const R*)v.m[11];
     p.dx1d = v.md[0]; p.dx2d = v.md[1]; p.radcd = v.md[2]; p.xposd = v.md[3]; p.csd = v.md[4];
     p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize;
-    p.dt = nullptr; p.dt_next = nullptr; p.status = v.status;
+    p.dt = nullptr; p.dt_next = nullptr; p.status = v.status; p.coef = v.coef;
     p.u_cur = (const R*)v.u[v.cur];
     p.u_next = (R*)v.u[1 - v.cur];
     return p;
@@ -52,6 +52,8 @@ static void finalize_dispatch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
     }
 }
 
+// Full ghost fill of the current state (used after an upload; the steps themselves refill the
+// ghosts in k_finalize).
 template <typename R>
 cudaError_t launch_boundaries(const DeviceView& v) {
     KParams<R> p = make_params<R>(v);
@@ -123,9 +125,12 @@ cudaError_t launch_step(const DeviceView& v, int slot) {
     p.dt = v.dt_slots + slot;
     p.dt_next = reinterpret_cast<unsigned long long*>(v.dt_slots + (1 - slot));
     cudaError_t e;
+    // ghost cells of the current state were written by the previous step's k_finalize (or by
+    // launch_boundaries after an upload)
     if (v.time_kernels) cudaEventRecord(v.ev[0], v.stream);
-    if ((e = launch_boundaries<R>(v)) != cudaSuccess) return e;
-    k_reset_dt<<<1, 1, 0, v.stream>>>(p.dt_next);
+    k_prepare_step<<<1, SHARK_MAX_DUST, 0, v.stream>>>(p.dt_next, p.dt, p.dtstop, p.ndust,
+                                                      (p.setup == SHARK_SETUP_SI && std::is_same<R, float>::value) ? 1 : 0,
+                                                      p.coef);
     if (v.time_kernels) cudaEventRecord(v.ev[1], v.stream);
     e = (v.ndim == 2) ? strip_launch<R>(v, p) : flux_launch<R, 1>(p, v.stream);
     if (e != cudaSuccess) return e;
@@ -144,7 +149,7 @@ cudaError_t launch_courant(const DeviceView& v, int slot) {
     p.u_cur = (const R*)v.u[v.cur];
     p.dt = v.dt_slots + slot;   // unused in MODE 1 except by the drag (disabled)
     p.dt_next = reinterpret_cast<unsigned long long*>(v.dt_slots + slot);
-    k_reset_dt<<<1, 1, 0, v.stream>>>(p.dt_next);
+    k_prepare_step<<<1, 1, 0, v.stream>>>(p.dt_next, p.dt, p.dtstop, 0, 0, p.coef);
     dim3 g2((v.nx + 255) / 256, v.ndim == 2 ? v.ny : 1, 1);
     finalize_dispatch<R, 1>(p, g2, v.stream);
     return cudaGetLastError();

@@ -24,6 +24,7 @@ struct DeviceView {
     const double* dsize;
     double* dt_slots;           // [2] dt of step n lives in slot n % 2
     unsigned int* status;       // OR of SHARK_STATUS_* bits
+    float* coef;                // [2*SHARK_MAX_DUST] per-step drag coefficients (mixed path)
     cudaStream_t stream;
     cudaStream_t stream2;       // side stream for the gas flux kernel (forked/joined per step)
     cudaEvent_t fork, join;

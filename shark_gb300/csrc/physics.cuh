@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace shark {
 
 template <typename R> __device__ __forceinline__ R sq(R x) { return x * x; }
@@ -40,11 +42,34 @@ __device__ __forceinline__ R slope_limit(int slope_type, R l, R r) {
     return s;
 }
 
+// FP32 forms of the three limiters for the mixed path, equal to slope_limit in exact
+// arithmetic with fewer operations (single FMNMX min/max, copysign instead of a sign multiply):
+//   minmod: 0 if l*r < 0, else the argument of smaller modulus (the right one on ties)
+//   van Leer (harmonic): 0 if l*r <= 0, else 2 l r / (l + r)
+//   MC(1.5): 0 if l*r <= 0, else sign(l+r) min(1.5 min(|l|,|r|), |l+r|/2)
+__device__ __forceinline__ float limit_minmod_f(float l, float r) {
+    const float m = fabsf(r) < fabsf(l) ? r : l;
+    return l * r < 0.f ? 0.f : m;
+}
+__device__ __forceinline__ float limit_vl_f(float l, float r) {
+    const float p = l * r;
+    return p <= 0.f ? 0.f : 2.f * p / (l + r);
+}
+__device__ __forceinline__ float limit_mc_f(float l, float r) {
+    const float s = l + r;
+    const float m = fminf(1.5f * fminf(fabsf(l), fabsf(r)), 0.5f * fabsf(s));
+    return l * r <= 0.f ? 0.f : copysignf(m, s);
+}
+
 // Compile-time limiter choice (0 = first order) for kernels specialised per configuration.
 template <int ST, typename R>
 __device__ __forceinline__ R slope_limit_t(R l, R r) {
     if constexpr (ST == 0) return R(0);
-    else return slope_limit(ST, l, r);
+    else if constexpr (std::is_same<R, float>::value) {
+        if constexpr (ST == 1) return limit_minmod_f(l, r);
+        else if constexpr (ST == 2) return limit_vl_f(l, r);
+        else return limit_mc_f(l, r);
+    } else return slope_limit(ST, l, r);
 }
 
 template <typename R> struct GasFlux { R rho, mn, mt, mz, e; };
@@ -147,25 +172,48 @@ __device__ __forceinline__ GasFlux<R> gas_hllc(R gamma, R rho_lft, R u_lft, R v_
     return f;
 }
 
-// solver_dust_Huang_Bai (src/solver/solvers.f90:506-698): pressureless upwind, 4 cases (:654-694)
+// solver_dust_Huang_Bai (src/solver/solvers.f90:506-698): pressureless upwind, 4 cases (:654-694):
+// both velocities > 0 -> left flux; both < 0 -> right flux; converging (u_l > 0 > u_r) -> sum;
+// diverging or any exactly-zero velocity -> 0.  Written branch-free: the left flux enters when
+// u_l > 0 and u_r != 0, the right flux when u_r < 0 and u_l != 0 (same cases, same sums).
 template <typename R>
 __device__ __forceinline__ DustFlux<R> dust_hb(R rho_lft, R u_lft, R v_lft, R w_lft,
                                                R rho_rgt, R u_rgt, R v_rgt, R w_rgt) {
-    DustFlux<R> f{R(0), R(0), R(0), R(0)};
-    const bool lp = u_lft > R(0), ln = u_lft < R(0), rp = u_rgt > R(0), rn = u_rgt < R(0);
-    if (rp && lp) {
-        f.rho = rho_lft * u_lft; f.mn = rho_lft * sq(u_lft);
-        f.mt = rho_lft * u_lft * v_lft; f.mz = rho_lft * u_lft * w_lft;
-    } else if (ln && rn) {
-        f.rho = rho_rgt * u_rgt; f.mn = rho_rgt * sq(u_rgt);
-        f.mt = rho_rgt * u_rgt * v_rgt; f.mz = rho_rgt * u_rgt * w_rgt;
-    } else if (lp && rn) {
-        f.rho = rho_lft * u_lft + rho_rgt * u_rgt;
+    const bool takeL = (u_lft > R(0)) && (u_rgt != R(0));
+    const bool takeR = (u_rgt < R(0)) && (u_lft != R(0));
+    const R ml = takeL ? rho_lft * u_lft : R(0);
+    const R mr = takeR ? rho_rgt * u_rgt : R(0);
+    DustFlux<R> f;
+    if (takeL && takeR) {   // converging: flx_lft + flx_rgt (solvers.f90:687-691)
+        f.rho = ml + mr;
         f.mn = rho_lft * sq(u_lft) + rho_rgt * sq(u_rgt);
-        f.mt = rho_lft * u_lft * v_lft + rho_rgt * u_rgt * v_rgt;
-        f.mz = rho_lft * u_lft * w_lft + rho_rgt * u_rgt * w_rgt;
+        f.mt = ml * v_lft + mr * v_rgt;
+        f.mz = ml * w_lft + mr * w_rgt;
+    } else {
+        const R m = takeL ? ml : mr;
+        const R un = takeL ? u_lft : u_rgt, vt = takeL ? v_lft : v_rgt, wt = takeL ? w_lft : w_rgt;
+        const R rh = takeL ? rho_lft : rho_rgt;
+        f.rho = m;
+        f.mn = (takeL || takeR) ? rh * sq(un) : R(0);
+        f.mt = m * vt;
+        f.mz = m * wt;
     }
-    return f;   // diverging (ln && rp) or any zero velocity: zero flux
+    return f;
+}
+
+// FP32 Huang & Bai with selects only (mixed path); same cases as dust_hb.
+__device__ __forceinline__ DustFlux<float> dust_hb_f(float rho_lft, float u_lft, float v_lft, float w_lft,
+                                                     float rho_rgt, float u_rgt, float v_rgt, float w_rgt) {
+    const bool takeL = (u_lft > 0.f) && (u_rgt != 0.f);
+    const bool takeR = (u_rgt < 0.f) && (u_lft != 0.f);
+    const float ml = takeL ? rho_lft * u_lft : 0.f;
+    const float mr = takeR ? rho_rgt * u_rgt : 0.f;
+    DustFlux<float> f;
+    f.rho = ml + mr;
+    f.mn = ml * u_lft + mr * u_rgt;
+    f.mt = ml * v_lft + mr * v_rgt;
+    f.mz = ml * w_lft + mr * w_rgt;
+    return f;
 }
 
 // solver_dust_llf (src/solver/solvers.f90:840-1001), non-MHD

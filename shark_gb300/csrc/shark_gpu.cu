@@ -69,6 +69,7 @@ struct shark_gpu_ctx {
     double* species = nullptr;       // dK | dtstop | dsize (3 x SHARK_MAX_DUST)
     double* dt_slots = nullptr;      // [2]
     unsigned int* status = nullptr;
+    float* coef = nullptr;           // per-step drag coefficients
     double* staging = nullptr;       // ncells*nvar FP64 (Fortran order) for uploads/downloads
     double* part = nullptr;          // totals partials
     double* tot_out = nullptr;
@@ -254,6 +255,7 @@ int32_t release(shark_gpu_ctx* c) {
     for (void* p : {c->ubuf[0], c->ubuf[1], c->metrics}) if (p) cudaFree(p);
     for (double* p : {c->metrics_d, c->species, c->dt_slots, c->staging, c->part, c->tot_out}) if (p) cudaFree(p);
     if (c->status) cudaFree(c->status);
+    if (c->coef) cudaFree(c->coef);
     if (c->host_ring) cudaFreeHost(c->host_ring);
     for (auto& e : c->ev_read) if (e) cudaEventDestroy(e);
     for (auto& e : c->ev_time) if (e) cudaEventDestroy(e);
@@ -420,8 +422,11 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     INIT_TRY(cudaMalloc(&c->dt_slots, 2 * sizeof(double)));
     INIT_TRY(cudaMalloc(&c->status, sizeof(unsigned int)));
     INIT_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
+    INIT_TRY(cudaMalloc(&c->coef, 2 * SHARK_MAX_DUST * sizeof(float)));
+    INIT_TRY(cudaMemsetAsync(c->coef, 0, 2 * SHARK_MAX_DUST * sizeof(float), c->stream));
     v.dt_slots = c->dt_slots;
     v.status = c->status;
+    v.coef = c->coef;
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
     std::memset(c->host_ring, 0, 4 * sizeof(double));
     const long long nact = (long long)v.nx * (v.ndim == 2 ? v.ny : 1);
@@ -456,6 +461,13 @@ int32_t shark_gpu_upload(shark_gpu_ctx* c, const double* u_prim, int64_t ncells,
     }
     CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
     c->status_seen = 0;
+    // apply_boundaries of the first step on both buffers (fixed SOD ghosts are only ever set here)
+    for (int b = 0; b < 2; ++b) {
+        c->v.cur = b;
+        cudaError_t eb = is_mixed(c) ? shark::launch_boundaries<float>(c->v) : shark::launch_boundaries<double>(c->v);
+        if (eb != cudaSuccess) return fail(SHARK_ERR_CUDA, "boundaries: %s", cudaGetErrorString(eb));
+    }
+    c->v.cur = 0;
     // first courant (src/solver/solve.f90:74) on the uploaded state -> dt slot 0
     cudaError_t e = is_mixed(c) ? shark::launch_courant<float>(c->v, 0) : shark::launch_courant<double>(c->v, 0);
     if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "courant: %s", cudaGetErrorString(e));
@@ -573,7 +585,7 @@ int32_t shark_gpu_last_step_ms(shark_gpu_ctx* c, float* ms_out) {
     if (!c || !ms_out) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
     if (c->nstep == 0) return fail(SHARK_ERR_STATE, "no step run yet");
     CUDA_TRY(cudaEventSynchronize(c->ev_time[3]));
-    CUDA_TRY(cudaEventElapsedTime(&ms_out[0], c->ev_time[0], c->ev_time[1]));   // boundaries
+    CUDA_TRY(cudaEventElapsedTime(&ms_out[0], c->ev_time[0], c->ev_time[1]));   // dt slot reset
     CUDA_TRY(cudaEventElapsedTime(&ms_out[1], c->ev_time[1], c->ev_time[2]));   // flux/update
     CUDA_TRY(cudaEventElapsedTime(&ms_out[2], c->ev_time[2], c->ev_time[3]));   // drag + dt
     return SHARK_OK;

@@ -40,6 +40,7 @@ struct KParams {
     const double* dt;                 // dt of the current step
     unsigned long long* dt_next;      // bit image of the next dt (positive doubles order as u64)
     unsigned int* status;             // SHARK_STATUS_* bits
+    float* coef;                      // [2*SHARK_MAX_DUST] per-step drag coefficients 1/(1+a_k), a_k/(1+a_k)
     const R* u_cur;                   // state at the start of the step (read only)
     R* u_next;                        // state after the step
 };
@@ -122,6 +123,47 @@ namespace shark {
 // NS > 0: compile-time species count (register arrays); NS < 0: run-time count.
 // MODE 0: full finalize; MODE 1: dt only (first step after an upload).
 // ---------------------------------------------------------------------------------------------
+
+// Producer-side boundary fill: an active cell within nghost of a periodic or shear-periodic edge
+// writes its own ghost images (with the SI shear of the vz momenta for x images) from its final
+// values.  This is apply_boundaries of the next step (SI/boundaries.f90, boundary_types.f90:149-186,
+// SOD/boundaries.f90 periodic directions) done by the producer; fixed SOD ghosts never change after
+// the upload and are skipped.  Reads back this thread's own just-written values.
+template <typename R>
+__device__ __forceinline__ void fill_ghost_images(const KParams<R>& p, R* u, int gx, int gy) {
+    const int ng = p.ng, nx = p.nx, ny = p.ny;
+    const bool xper = !(p.setup == SHARK_SETUP_SOD && p.sod_dir == 0);
+    const bool yper = p.ndim == 2 && !(p.setup == SHARK_SETUP_SOD && p.sod_dir == 1);
+    int tx = -1, ty = -1;
+    if (xper) {
+        if (gx < 2 * ng) tx = gx + nx;            // source of a right ghost
+        else if (gx >= nx) tx = gx - nx;          // source of a left ghost
+    }
+    if (yper) {
+        if (gy < 2 * ng) ty = gy + ny;
+        else if (gy >= ny) ty = gy - ny;
+    }
+    if (tx < 0 && ty < 0) return;
+    const bool shear = p.setup == SHARK_SETUP_SI;
+    const R sgn = (tx >= 0 && tx > gx) ? R(1) : R(-1);   // right ghost: + rho q Omega L
+    const R qoL = R(p.si_q), om = R(p.si_om), L = R(p.box_l);
+    const int N = p.ndust;
+    for (int v = 0; v < p.nvar; ++v) {
+        R val = u[uidx(p, v, gy, gx)];
+        if (ty >= 0) u[uidx(p, v, ty, gx)] = val;               // y image (no shear)
+        if (tx >= 0) {
+            R xv = val;
+            if (shear) {
+                int vr = -1;
+                if (v == 3) vr = 0;
+                else if (v >= 5 + 3 * N) vr = v - 3 * N;         // vz momentum of dust species -> its density
+                if (vr >= 0) xv = val + sgn * (u[uidx(p, vr, gy, gx)] * qoL * om * L);
+            }
+            u[uidx(p, v, gy, tx)] = xv;                             // x image
+            if (ty >= 0) u[uidx(p, v, ty, tx)] = xv;                // corner image
+        }
+    }
+}
 
 __device__ __forceinline__ void atomic_min_dt(unsigned long long* a, double v) {
     // positive finite doubles order like their bit patterns
@@ -329,6 +371,7 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
         if (!(dtc > 0.0) || !isfinite(dtc)) { st |= SHARK_STATUS_DT_UNDERFLOW; dtc = 2e44; }
     }
     block_reduce_dt(dtc, st, p.dt_next, p.status);
+    if (MODE == 0 && gx < p.ng + p.nx) fill_ghost_images(p, p.u_next, gx, gy);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -348,14 +391,13 @@ template <int NS, int MODE>
 __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;
-    __shared__ float cr[SHARK_MAX_DUST], cw[SHARK_MAX_DUST];
     const bool drag = MODE == 0 && N > 0 && (p.flags & SHARK_FLAG_DRAG);
+    // constant stopping times (SI): the FP64 coefficients of this step were computed once by
+    // k_prepare_step; other setups compute them per cell below
     const bool const_ts = p.setup == SHARK_SETUP_SI;
+    const float* __restrict__ cr = p.coef;
+    const float* __restrict__ cw = p.coef + SHARK_MAX_DUST;
     const double dt = *p.dt;
-    if (drag && const_ts) {
-        for (int k = threadIdx.x; k < N; k += blockDim.x) drag_coeffs(1.0 * dt / p.dtstop[k], cr[k], cw[k]);
-        __syncthreads();
-    }
     const int gx = blockIdx.x * blockDim.x + threadIdx.x + p.ng;
     const int gy = (p.ndim == 2) ? blockIdx.y + p.ng : 0;
     float dtc = 2e38f;
@@ -502,11 +544,22 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
         if (!(dtc > 0.f) || !isfinite(dtc)) { st |= SHARK_STATUS_DT_UNDERFLOW; dtc = 2e38f; }
     }
     block_reduce_dt(dtc >= 2e38f ? 2e44 : (double)dtc, st, p.dt_next, p.status);
+    if (MODE == 0 && gx < p.ng + p.nx) fill_ghost_images(p, p.u_next, gx, gy);
 }
 
-// Reset the next-dt slot before k_finalize runs (single thread).
-static __global__ void k_reset_dt(unsigned long long* dt_next) {
-    *dt_next = (unsigned long long)__double_as_longlong(2e44);
+// Per-step preparation, one small block before the flux kernels: reset the next-dt slot and,
+// when the stopping times are per-species constants (SI box), compute the stiff drag
+// coefficients 1/(1+a_k) and a_k/(1+a_k), a_k = dt/t_k, once in FP64 (dust_drag.f90:29-46).
+static __global__ void k_prepare_step(unsigned long long* dt_next, const double* dt, const double* dtstop, int ndust,
+                                      int const_ts, float* coef) {
+    const int k = threadIdx.x;
+    if (k == 0) *dt_next = (unsigned long long)__double_as_longlong(2e44);
+    if (const_ts && k < ndust) {
+        float r, w;
+        drag_coeffs(1.0 * (*dt) / dtstop[k], r, w);
+        coef[k] = r;
+        coef[SHARK_MAX_DUST + k] = w;
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
