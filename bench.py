@@ -296,10 +296,12 @@ def run_gpu(args):
     achieved = alg_bytes_k1 / k1_s / 1e9
     alg_bytes_k2 = 4 * (7 * (args.ndust + 1) + args.ndust) * args.n * args.n
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "k_flux_traffic.json")
-    if os.path.exists(tfile):
+    tfile = os.path.join(ROOT, "profiles", "k_flux_traffic.txt")
+    if os.path.exists(tfile) and args.n == 1024 and args.ndust == 8:
         with open(tfile) as f:
-            traffic = json.load(f).get("bytes_per_launch_full_size")
+            for line in f:
+                if line.startswith("bytes_per_launch_full_size:"):
+                    traffic = int(line.split(":")[1])
 
     if rank != 0:
         return

@@ -1,0 +1,92 @@
+! shark_gpu_mod.f90 -- ISO_C_BINDING interface of libshark_gpu (include/shark_gpu.h).
+!
+! Compiled with the unchanged SHARK sources (add to MODOBJ in bin/Makefile, link -lshark_gpu).
+! The derived type mirrors struct shark_gpu_config field by field (bind(C) gives the C layout).
+module shark_gpu
+  use iso_c_binding
+  implicit none
+
+  integer(c_int32_t), parameter :: SHARK_GPU_ABI_VERSION = 1
+  integer, parameter :: SHARK_MAX_DUST = 64
+  integer(c_int32_t), parameter :: SHARK_OK = 0
+  integer(c_int32_t), parameter :: SHARK_SETUP_SOD = 1, SHARK_SETUP_DUSTYWAVE = 2, SHARK_SETUP_SI = 3
+  integer(c_int32_t), parameter :: SHARK_FLAG_DRAG = 1, SHARK_FLAG_BACK_REACTION = 2
+  integer(c_int32_t), parameter :: SHARK_FLAG_FORCE_KICK = 4, SHARK_FLAG_FARGO = 8
+  integer(c_int32_t), parameter :: SHARK_FLAG_GROWTH = 16, SHARK_FLAG_CHARGING = 32
+  integer(c_int32_t), parameter :: SHARK_FLAG_VISCOSITY = 64, SHARK_FLAG_STATIC = 128
+  integer(c_int32_t), parameter :: SHARK_PREC_FP64 = 0, SHARK_PREC_MIXED = 1
+
+  type, bind(C) :: shark_gpu_config
+    integer(c_int32_t) :: abi_version, nx, ny, nghost, ndust, geom, gridspace, solver, solverdust
+    integer(c_int32_t) :: slope_type, iso_cs, precision, setup, flags, device, pad0
+    real(c_double) :: gamma, cfl, smallr, smallc, smallp, box_l, box_l_y, inner_r, cs0
+    real(c_double) :: dust_ratio_min, rhograin
+    real(c_double) :: dust_size(SHARK_MAX_DUST), dust_K(SHARK_MAX_DUST), dust_tstop(SHARK_MAX_DUST)
+    real(c_double) :: dust_eps(SHARK_MAX_DUST), dust_stokes(SHARK_MAX_DUST)
+    real(c_double) :: sod_rho_l, sod_rho_r, sod_P_l, sod_P_r
+    integer(c_int32_t) :: sod_direction, pad1
+    real(c_double) :: dw_rho_0, dw_delta_rho, dw_vx_0, dw_kx_wave
+    real(c_double) :: si_q_shear, si_omega, si_eta_stream, si_rad0, si_rho_init, si_hoverr
+    real(c_double) :: disk_mstar, disk_hoverr, disk_sigma0, disk_r0, disk_rout
+    real(c_double) :: reserved(48)
+    type(c_ptr) :: dx, surf, vol, radii_c, position, cs
+  end type shark_gpu_config
+
+  interface
+    integer(c_int32_t) function shark_gpu_config_defaults(cfg) bind(C, name="shark_gpu_config_defaults")
+      import :: c_int32_t, shark_gpu_config
+      type(shark_gpu_config), intent(out) :: cfg
+    end function
+    integer(c_int32_t) function shark_gpu_init(cfg, ctx) bind(C, name="shark_gpu_init")
+      import :: c_int32_t, c_ptr, shark_gpu_config
+      type(shark_gpu_config), intent(in) :: cfg
+      type(c_ptr), intent(out) :: ctx
+    end function
+    integer(c_int32_t) function shark_gpu_upload(ctx, u_prim, ncells, nvar) bind(C, name="shark_gpu_upload")
+      import :: c_int32_t, c_int64_t, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: u_prim(*)
+      integer(c_int64_t), value :: ncells
+      integer(c_int32_t), value :: nvar
+    end function
+    integer(c_int32_t) function shark_gpu_step(ctx, dt, status) bind(C, name="shark_gpu_step")
+      import :: c_int32_t, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: dt
+      integer(c_int32_t), intent(out) :: status
+    end function
+    integer(c_int32_t) function shark_gpu_download(ctx, u_prim, q) bind(C, name="shark_gpu_download")
+      import :: c_int32_t, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: u_prim(*)
+      type(c_ptr), value :: q
+    end function
+    integer(c_int32_t) function shark_gpu_ctoprim(ctx, q, cs) bind(C, name="shark_gpu_ctoprim")
+      import :: c_int32_t, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: q(*), cs(*)
+    end function
+    integer(c_int32_t) function shark_gpu_totals(ctx, out) bind(C, name="shark_gpu_totals")
+      import :: c_int32_t, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: out(*)
+    end function
+    integer(c_int32_t) function shark_gpu_free(ctx) bind(C, name="shark_gpu_free")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+  end interface
+
+  type(c_ptr), save :: gpu_ctx = c_null_ptr
+  logical, save :: gpu_uploaded = .false.
+
+contains
+
+  ! Address of a contiguous real array for the config's grid pointers.  The library reads them
+  ! only inside shark_gpu_init, so the address need not outlive that call.
+  function shark_loc(a) result(p)
+    real(c_double), target, intent(in) :: a(*)
+    type(c_ptr) :: p
+    p = c_loc(a(1))
+  end function shark_loc
+end module shark_gpu
