@@ -202,6 +202,23 @@ int32_t shark_gpu_timed_run(shark_gpu_ctx* ctx, int64_t nsteps, double* time_io,
  * step. */
 int32_t shark_gpu_kernel_times(shark_gpu_ctx* ctx, int64_t nsteps, float* avg_ms);
 
+/* Totals without allocating: the same Kahan-compensated FP64 sums as shark_gpu_totals (layout
+ * out[4*s + 0..3] = mass, three momenta of species s, gas first) of a conserved state that the
+ * caller holds on the current device in the Fortran layout (u_dev: ncells*nvar doubles,
+ * nvar = 5 + 4*ndust), written to the caller's device array out_dev (4*(ndust+1) doubles).
+ * No counterpart in the reference: it exists for callers that cannot call cudaMalloc (a host
+ * application whose own allocator owns every device allocation, or a time loop that cannot take
+ * cudaMalloc's implicit synchronisation or a change of its device footprint), which rules out
+ * shark_gpu_totals because its context allocates.  It needs no context and allocates nothing:
+ * its partial sums live in a fixed device array of about 1 MiB compiled into the library, held by
+ * every GPU that loads it until the process exits.  Limit: ndust <= 64 (SHARK_ERR_INVALID_ARG
+ * beyond).  The kernels are queued on `stream` (a cudaStream_t, NULL = default stream) and the call
+ * returns without waiting.  The first call on a device looks up the array's device address with
+ * that device current, so make it before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race and give wrong results; order them on one stream. */
+int32_t shark_gpu_totals_noalloc(const double* u_dev, int32_t nx, int32_t ny, int32_t nghost, int32_t ndust,
+                                 double* out_dev, void* stream);
+
 /* Human-readable message of the last error on this thread (static storage). */
 const char* shark_gpu_last_error(void);
 

@@ -5,6 +5,7 @@ Three translation units compiled in parallel:
   kernels_f32.cu  -- FP32 (mixed-precision) step kernels, FMA contraction and approximate
                      FP32 division on (the mixed path is held to 1e-5 L1 against FP64)
   shark_gpu.cu    -- host side of the C ABI (include/shark_gpu.h)
+  noalloc.cu      -- shark_gpu_totals_noalloc (no allocations; fixed device scratch array)
 """
 import os
 import shutil
@@ -23,6 +24,7 @@ UNITS = [
     ("kernels_f64.cu", ["--fmad=false"]),
     ("kernels_f32.cu", ["--fmad=true", "-prec-div=false"]),
     ("shark_gpu.cu", []),
+    ("noalloc.cu", []),
 ]
 
 

@@ -32,6 +32,9 @@ struct DeviceView {
     bool time_kernels;
 };
 
+// Record `msg` as this thread's shark_gpu_last_error text and return `code`.
+int32_t set_error(int32_t code, const char* msg);
+
 // one full step on view.u[view.cur] -> view.u[1-cur]; dt read from slot `slot`, next dt written
 // to slot 1-slot.  Returns a cudaError_t.
 template <typename R> cudaError_t launch_step(const DeviceView& v, int slot);

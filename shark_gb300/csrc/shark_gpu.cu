@@ -58,6 +58,11 @@ double powi(double x, int n) {
 
 }  // namespace
 
+int32_t shark::set_error(int32_t code, const char* msg) {
+    g_last_error = msg ? msg : "";
+    return code;
+}
+
 struct shark_gpu_ctx {
     shark_gpu_config cfg;
     shark::DeviceView v;

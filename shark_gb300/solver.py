@@ -22,7 +22,7 @@ EXPORTS = [
     "shark_gpu_abi_version", "shark_gpu_config_defaults", "shark_gpu_init", "shark_gpu_upload",
     "shark_gpu_step", "shark_gpu_run", "shark_gpu_sync", "shark_gpu_download", "shark_gpu_ctoprim",
     "shark_gpu_totals", "shark_gpu_last_step_ms", "shark_gpu_timed_run", "shark_gpu_kernel_times",
-    "shark_gpu_last_error", "shark_gpu_free",
+    "shark_gpu_totals_noalloc", "shark_gpu_last_error", "shark_gpu_free",
 ]
 
 
@@ -70,6 +70,8 @@ def load_library(path=None):
     L.shark_gpu_timed_run.argtypes = [P, C.c_int64, D, C.POINTER(C.c_float)]
     L.shark_gpu_kernel_times.restype = I32
     L.shark_gpu_kernel_times.argtypes = [P, C.c_int64, C.POINTER(C.c_float)]
+    L.shark_gpu_totals_noalloc.restype = I32
+    L.shark_gpu_totals_noalloc.argtypes = [C.c_void_p, I32, I32, I32, I32, C.c_void_p, C.c_void_p]
     L.shark_gpu_last_error.restype = C.c_char_p
     L.shark_gpu_last_error.argtypes = []
     L.shark_gpu_free.restype = I32
@@ -86,6 +88,14 @@ def _check(rc, what):
     if rc != OK:
         msg = load_library().shark_gpu_last_error().decode(errors="replace")
         raise SharkError(rc, what, msg)
+
+
+def totals_noalloc(u_dev_ptr, nx, ny, nghost, ndust, out_dev_ptr, stream_ptr=None):
+    """shark_gpu_totals_noalloc on caller-owned device buffers (raw device pointers); queued on
+    `stream_ptr` (None = default stream), returns without synchronising."""
+    _check(load_library().shark_gpu_totals_noalloc(C.c_void_p(u_dev_ptr), nx, ny, nghost, ndust,
+                                                   C.c_void_p(out_dev_ptr), C.c_void_p(stream_ptr or 0)),
+           "shark_gpu_totals_noalloc")
 
 
 class Shark:
