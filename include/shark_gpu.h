@@ -120,9 +120,17 @@ typedef struct shark_gpu_config {
     double dw_rho_0, dw_delta_rho, dw_vx_0, dw_kx_wave;
     /* SI shearing box (src/setups/SI/setup_commons.f90) */
     double si_q_shear, si_omega, si_eta_stream, si_rad0, si_rho_init, si_hoverr;
-    /* polar disk / turbulence / charging / growth parameters (unused by the setups above) */
+    /* polar disk (src/setups/disk_polar/setup_commons.f90); code units AU, Msun, 1/Omega(1 AU).
+     * Sound speed cs(r) = h(r) sqrt(Mstar/r) with h(r) = disk_hoverr * r^((disk_temp_slope+1)/2),
+     * i.e. T ~ r^disk_temp_slope (the reference's constant H/R is disk_temp_slope = -1).
+     * Point-mass gravity -disk_mstar/r^2; stopping times Epstein on Sigma/(sqrt(2 pi) H);
+     * setup_inloop relaxes the cells with r < disk_r_relax towards the initial state over
+     * disk_n_rel orbits and resets the first active column; with SHARK_FLAG_FARGO the rings are
+     * remapped by the orbital velocity -sqrt(disk_mstar/r) every step.  ICs: Sigma =
+     * disk_sigma0 (disk_r0/r) exp(-r/disk_rout). */
     double disk_mstar, disk_hoverr, disk_sigma0, disk_r0, disk_rout;
-    double reserved[48];
+    double disk_r_relax, disk_n_rel, disk_temp_slope;
+    double reserved[45];
 
     /* Optional grid metrics from the caller (Fortran dx(ncells,ndim), surf(ncells,ndim),
      * vol(ncells), radii_c(ncells), position(ncells,ndim), cs(ncells)).  NULL: the library
@@ -152,7 +160,10 @@ int32_t shark_gpu_config_defaults(shark_gpu_config* cfg);
 int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** ctx_out);
 
 /* Copy the conserved state (ncells*nvar doubles, Fortran order) to the device.
- * ncells and nvar must match the context.  Also computes the first CFL dt. */
+ * ncells and nvar must match the context.  Also computes the first CFL dt.
+ * SHARK_SETUP_DISK_POLAR: the first state uploaded to a context is also kept as the initial
+ * state that setup_inloop relaxes towards (uprim_condinit, src/setups/disk_polar/setup.f90:79-83);
+ * later uploads (a restart) replace the state only. */
 int32_t shark_gpu_upload(shark_gpu_ctx* ctx, const double* u_prim, int64_t ncells, int32_t nvar);
 
 /* One full `solve` on the device (src/solver/solve.f90:10-181): boundaries, ctoprim, forces,

@@ -48,7 +48,7 @@ def lib():
                             ("oracle_apply_boundaries", []), ("oracle_ctoprim", []),
                             ("oracle_courant", [D]), ("oracle_set_dt", [C.c_double]),
                             ("oracle_dust_drag", [C.c_double]), ("oracle_compute_tstop", []),
-                            ("oracle_get_tstop", [D])]:
+                            ("oracle_get_tstop", [D]), ("oracle_fargo", [])]:
             f = getattr(L, name)
             f.restype = C.c_int32
             f.argtypes = [P] + extra
@@ -168,3 +168,7 @@ class Oracle:
 
     def apply_boundaries(self):
         self._chk(lib().oracle_apply_boundaries(self._h), "oracle_apply_boundaries")
+
+    def fargo(self):
+        """fargo_scheme alone on the current state with the dt last set (FARGO configs)."""
+        self._chk(lib().oracle_fargo(self._h), "oracle_fargo")

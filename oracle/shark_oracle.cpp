@@ -50,6 +50,8 @@ struct oracle_state {
     std::vector<double> dx, surf, vol, position, radii_c;
     std::vector<uint8_t> active, active_pred;
     std::vector<double> force, force_dust, tstop, sdust, epsilondust;
+    std::vector<double> u_init;     // disk_polar: uprim_condinit (state of the first upload / setup)
+    std::vector<double> fargo_v;    // fargo_velocity(ncells)
     double dt = 0.0, time = 0.0;
 
     // setup-derived scalars
@@ -335,10 +337,45 @@ void si_boundaries(oracle_state& s) {
         }
 }
 
+// disk_polar profile: aspect ratio h(r) = disk_hoverr r^((T slope + 1)/2), H = h r,
+// Omega = sqrt(Mstar/r^3), cs = Omega H (disk_polar/setup.f90:27-32 with constant h for slope -1)
+double disk_h(const shark_gpu_config& c, double r) { return c.disk_hoverr * std::pow(r, 0.5 * (c.disk_temp_slope + 1.0)); }
+double disk_cs(const shark_gpu_config& c, double r) {
+    return std::sqrt(c.disk_mstar / (r * r * r)) * (disk_h(c, r) * r);
+}
+
+// disk_polar apply_boundaries (disk_polar/boundaries.f90:1-70): periodic in phi over the active
+// radii, outflow in r with the radial velocities clipped to point out of the domain.  The
+// reference copies u_prim(first_active) / u_prim(last_active), i.e. one cell of the first row,
+// into every radial ghost (the cell index is used without icell); this restatement copies the
+// first/last active cell of the same row, the evident intent.  Accretion (off) is not restated.
+void disk_boundaries(oracle_state& s) {
+    const int ng = s.nghost;
+    for (int ix = s.first_active; ix <= s.last_active; ++ix)
+        for (int g = 0; g < ng; ++g) {
+            int64_t bl = s.icell(ix, g), br = s.icell(ix, s.ny_max - 1 - g);
+            int64_t al = s.icell(ix, s.last_active_y - ng + 1 + g), ar = s.icell(ix, s.first_active_y + ng - 1 - g);
+            for (int v = 0; v < s.nvar; ++v) { s.U(bl, v) = s.U(al, v); s.U(br, v) = s.U(ar, v); }
+        }
+    for (int g = 0; g < ng; ++g)
+        for (int iy = 0; iy < s.ny_max; ++iy) {
+            int64_t bl = s.icell(g, iy), br = s.icell(s.nx_max - 1 - g, iy);
+            int64_t al = s.icell(s.first_active, iy), ar = s.icell(s.last_active, iy);
+            for (int v = 0; v < s.nvar; ++v) { s.U(bl, v) = s.U(al, v); s.U(br, v) = s.U(ar, v); }
+            s.U(br, s.ivx) = fmin2(s.U(br, s.ivx), 0.0);
+            s.U(bl, s.ivx) = fmax2(s.U(bl, s.ivx), 0.0);
+            for (int k = 0; k < s.ndust; ++k) {
+                s.U(br, s.ivdx[k]) = fmin2(s.U(br, s.ivdx[k]), 0.0);
+                s.U(bl, s.ivdx[k]) = fmax2(s.U(bl, s.ivdx[k]), 0.0);
+            }
+        }
+}
+
 void apply_boundaries(oracle_state& s) {
     switch (s.cfg.setup) {
         case SHARK_SETUP_SOD: sod_boundaries(s); break;
         case SHARK_SETUP_SI: si_boundaries(s); break;
+        case SHARK_SETUP_DISK_POLAR: disk_boundaries(s); break;
         default: periodic_boundaries(s); break;   // DUSTYWAVE (DUSTYWAVE/boundaries.f90), dustyTurb
     }
 }
@@ -359,6 +396,12 @@ void compute_tstop(oracle_state& s) {
                 case SHARK_SETUP_SI:          // SI/setup.f90:389-397 (constant, precomputed on host)
                     ts = s.cfg.dust_tstop[k];
                     break;
+                case SHARK_SETUP_DISK_POLAR: {   // disk_polar/setup.f90:425-451, Epstein with Sigma/(sqrt(2 pi) H)
+                    const double H = disk_h(s.cfg, s.radii_c[i]) * s.radii_c[i];
+                    ts = std::sqrt(pi * s.cfg.gamma / 8.0) * (s.cfg.rhograin) * s.SDUST(i, k) /
+                         (s.Q(i, s.irho) / (std::sqrt(2.0 * pi) * H) * s.cs[i]);
+                    break;
+                }
                 default:                      // SOD/setup.f90:179-185, Epstein
                     ts = std::sqrt(pi * s.cfg.gamma / 8.0) * (s.cfg.rhograin) * s.SDUST(i, k) /
                          (s.Q(i, s.irho) * s.cs[i]);
@@ -369,8 +412,20 @@ void compute_tstop(oracle_state& s) {
     }
 }
 
-// update_force_setup (SI/setup.f90:335-368); the other in-scope setups leave force at zero.
+// update_force_setup of disk_polar (disk_polar/setup.f90:364-398) without planet/self-gravity:
+// point-mass gravity -Mstar/r^2 on gas and dust.
+void disk_force(oracle_state& s) {
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        const double g = -s.cfg.disk_mstar / sq(s.radii_c[i]);
+        s.FORCE(i, 0) = g; s.FORCE(i, 1) = 0.0; s.FORCE(i, 2) = 0.0;
+        for (int k = 0; k < s.ndust; ++k) { s.FDUST(i, 0, k) = g; s.FDUST(i, 1, k) = 0.0; s.FDUST(i, 2, k) = 0.0; }
+    }
+}
+
+// update_force_setup (SI/setup.f90:335-368); SOD and DUSTYWAVE leave force at zero.
 void update_force_setup(oracle_state& s) {
+    if (s.cfg.setup == SHARK_SETUP_DISK_POLAR) { disk_force(s); return; }
     if (s.cfg.setup != SHARK_SETUP_SI) return;
     const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, r0 = s.cfg.si_rad0, eta = s.cfg.si_eta_stream;
     const bool drag = s.flag(SHARK_FLAG_DRAG);
@@ -397,8 +452,41 @@ void update_force_setup(oracle_state& s) {
     }
 }
 
+// setup_inloop of disk_polar (disk_polar/setup.f90:206-284): relax density and in-plane velocities
+// of gas and dust towards the initial state inside r_relax with t_rel = n_rel orbits (measured
+// from the inner radius), then reset the radial ghosts and the first active column to the
+// initial state of the first active column.
+void disk_inloop(oracle_state& s) {
+    const double Mstar = s.cfg.disk_mstar, n_rel = s.cfg.disk_n_rel, r_relax = s.cfg.disk_r_relax;
+    const double sm = s.cfg.inner_r;
+    auto UI = [&](int64_t i, int v) { return s.u_init[(size_t)v * s.ncells + i]; };
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        const double rc = s.radii_c[i];
+        if (!(rc < r_relax)) continue;
+        const double t_rel = n_rel * 2.0 * pi / (std::sqrt(Mstar / powi(rc, 3))) - n_rel * 2.0 * pi / (std::sqrt(Mstar / powi(sm, 3)));
+        const double e = std::exp(-s.dt / t_rel);
+        auto relax = [&](int ir, int ivx_, int ivy_) {
+            const double rho_init = UI(i, ir), vx_init = UI(i, ivx_) / rho_init, vy_init = UI(i, ivy_) / rho_init;
+            const double rho_old = s.U(i, ir), vx_old = s.U(i, ivx_) / rho_old, vy_old = s.U(i, ivy_) / rho_old;
+            const double rho_new = (rho_init) * (1.0 - e) + rho_old * e;
+            const double vx_new = (vx_init) * (1.0 - e) + vx_old * e;
+            const double vy_new = (vy_init) * (1.0 - e) + vy_old * e;
+            s.U(i, ir) = rho_new;
+            s.U(i, ivx_) = rho_new * vx_new;
+            s.U(i, ivy_) = rho_new * vy_new;
+        };
+        relax(s.irho, s.ivx, s.ivy);
+        for (int k = 0; k < s.ndust; ++k) relax(s.irhod[k], s.ivdx[k], s.ivdy[k]);
+    }
+    for (int ix = 0; ix <= s.first_active; ++ix)
+        for (int iy = s.first_active_y; iy <= s.last_active_y; ++iy)
+            for (int v = 0; v < s.nvar; ++v) s.U(s.icell(ix, iy), v) = UI(s.icell(s.first_active, iy), v);
+}
+
 // setup_inloop (SI/setup.f90:299-332): Crank-Nicolson rotation, only without force_kick.
 void setup_inloop(oracle_state& s) {
+    if (s.cfg.setup == SHARK_SETUP_DISK_POLAR) { disk_inloop(s); return; }
     if (s.cfg.setup != SHARK_SETUP_SI) return;
     if (s.flag(SHARK_FLAG_FORCE_KICK)) return;
     const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, r0 = s.cfg.si_rad0, eta = s.cfg.si_eta_stream;
@@ -912,6 +1000,54 @@ void source_terms(oracle_state& s) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// fargo_scheme (src/solver/fargo_scheme.f90:2-81), with the reference's defects fixed:
+//   * `one` (undeclared, uninitialised) is 1 and `eps` is FP64 (it is an implicit REAL*4 there);
+//   * limited slopes of the conserved variables along phi are computed for every active cell
+//     (the reference loops ix=1..nx, iy=1..ny, missing the last active columns and rows), with
+//     the periodic wrap of the ring (what its apply_boundaries provides);
+//   * the source rows wrap modulo ny (the reference wraps once, i.e. assumes nshft < ny).
+// Per ring (fixed radius) the shift vk*dt splits into whole cells nshft and a residual eps; the
+// new value is the linear remap of the two donor cells plus their slope correction.
+// ---------------------------------------------------------------------------------------------
+void fargo_scheme(oracle_state& s) {
+    const int ny = s.ny, fy = s.first_active_y, st = s.cfg.slope_type;
+    const double forth = 0.25, one = 1.0;
+    const std::vector<double> uold = s.u;
+    auto UO = [&](int ix, int ay, int v) { return uold[(size_t)v * s.ncells + s.icell(ix, fy + ay)]; };
+#pragma omp parallel for schedule(static)
+    for (int ix = s.first_active; ix <= s.last_active; ++ix) {
+        const int64_t c0 = s.icell(ix, fy);
+        const double vk = s.fargo_v[c0];
+        const double dy_loc = s.DX(c0, 1) * s.radii_c[c0];
+        const double shift = std::fabs(vk * s.dt);
+        const int nshft = (int)(shift / dy_loc);
+        const double eps = std::fmod(shift, dy_loc) / dy_loc;
+        std::vector<double> du(ny);
+        for (int v = 0; v < s.nvar; ++v) {
+            for (int a = 0; a < ny; ++a) {
+                const double um = UO(ix, (a - 1 + ny) % ny, v), u0 = UO(ix, a, v), up = UO(ix, (a + 1) % ny, v);
+                du[a] = st > 0 ? slope_limit(st, u0 - um, up - u0) : 0.0;
+            }
+            for (int a = 0; a < ny; ++a) {
+                int j, jp;
+                double w0, w1;
+                if (vk > 0.0) {
+                    j = ((a - nshft - 1) % ny + ny) % ny;
+                    w0 = eps; w1 = one - eps;
+                } else {
+                    j = (a + nshft) % ny;
+                    w0 = one - eps; w1 = eps;
+                }
+                jp = (j + 1) % ny;
+                double un = UO(ix, j, v) * w0 + UO(ix, jp, v) * w1;
+                un = un + half * du[j] * (forth - sq(half - eps)) + half * du[jp] * (sq(half - eps) - forth);
+                s.U(s.icell(ix, fy + a), v) = un;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
 // dust_drag (src/dust/dust_drag.f90:2-75): Krapp et al. implicit multi-species drag + floor.
 // ---------------------------------------------------------------------------------------------
 void dust_drag(oracle_state& s, double coeffdt) {
@@ -972,6 +1108,7 @@ void solve(oracle_state& s) {
     predictor(s);
     add_delta_u(s);
     source_terms(s);
+    if (s.flag(SHARK_FLAG_FARGO)) fargo_scheme(s);
     if (s.ndust > 0 && s.flag(SHARK_FLAG_DRAG)) dust_drag(s, 1.0);
     setup_inloop(s);
 }
@@ -1083,6 +1220,45 @@ void setup_si(oracle_state& s, double noise_amp, uint64_t seed) {
     apply_boundaries(s);
 }
 
+// Polar disk initial state (disk_polar/setup.f90:12-84), re-specified for the GB300 workload:
+// T ~ r^disk_temp_slope through h(r), the matching pressure-supported rotation
+// v_phi = Omega r sqrt(1 - h^2 (1 - slope + r/R_out)) (the reference's sqrt(1 - h^2 (2 + r/R_out))
+// for slope -1), one grain size per bin (dust_size; the reference gives every bin scut), dust
+// starting at the full Keplerian azimuthal velocity with the reference's radial drift, and an
+// optional uniform density perturbation of relative amplitude noise_amp (counter-based hash).
+void setup_disk(oracle_state& s, double noise_amp, uint64_t seed) {
+    const shark_gpu_config& c = s.cfg;
+    const bool fargo = s.flag(SHARK_FLAG_FARGO);
+    std::fill(s.q.begin(), s.q.end(), 0.0);
+    for (int iy = 0; iy < s.ny_max; ++iy)
+        for (int ix = 0; ix < s.nx_max; ++ix) {
+            const int64_t i = s.icell(ix, iy);
+            const double rr = s.radii_c[i];
+            const double h = disk_h(c, rr), H = h * rr;
+            const double Omega = std::sqrt(c.disk_mstar / powi(rr, 3));
+            const double cs0 = Omega * H;
+            s.fargo_v[i] = fargo ? -Omega * rr : 0.0;
+            double sig = c.disk_sigma0 * (c.disk_r0 / rr) * std::exp(-rr / c.disk_rout);
+            if (noise_amp > 0) sig = sig * (1.0 + noise_amp * (2.0 * hash_uniform(seed, (uint64_t)i) - 1.0));
+            const double rot = std::sqrt(1.0 - sq(h) * (1.0 - c.disk_temp_slope + rr / c.disk_rout));
+            s.Q(i, s.irho) = sig;
+            s.Q(i, s.ivx) = 0.0;
+            s.Q(i, s.ivy) = Omega * rr * rot;
+            s.Q(i, s.iP) = sig * sq(cs0);
+            s.cs[i] = cs0;
+            for (int k = 0; k < s.ndust; ++k) {
+                s.Q(i, s.irhod[k]) = c.dust_eps[k] * sig;
+                const double ts = std::sqrt(pi * c.gamma / 8.0) * (c.rhograin) * c.dust_size[k] /
+                                  (sig / (std::sqrt(2.0 * pi) * H) * cs0);
+                const double St = ts * Omega;
+                s.Q(i, s.ivdx[k]) = (rot - 1.0) * Omega * rr / (St + 1.0 / St);
+                s.Q(i, s.ivdy[k]) = Omega * rr;
+            }
+        }
+    primtoc(s);
+    s.u_init = s.u;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------------------------
@@ -1142,9 +1318,18 @@ oracle_state* oracle_create(const shark_gpu_config* cfg) {
     s->box_l_y = cfg->box_l_y;
     get_active_cells(*s);
     gridinit(*s);
-    // isothermal sound speed: uniform cs0 unless the caller overrides it with oracle_set_cs
+    // isothermal sound speed: uniform cs0 (the disk: its radial profile) unless the caller
+    // overrides it with oracle_set_cs
+    s->fargo_v.assign(nc, 0.0);
     if (cfg->iso_cs == 1)
         for (size_t i = 0; i < nc; ++i) s->cs[i] = cfg->cs0;
+    if (cfg->setup == SHARK_SETUP_DISK_POLAR) {
+        for (size_t i = 0; i < nc; ++i) {
+            const double rr = s->radii_c[i];
+            s->cs[i] = disk_cs(*cfg, rr);
+            if (cfg->flags & SHARK_FLAG_FARGO) s->fargo_v[i] = -std::sqrt(cfg->disk_mstar / powi(rr, 3)) * rr;
+        }
+    }
     return s;
 }
 
@@ -1158,6 +1343,7 @@ int32_t oracle_setup_ic(oracle_state* s, double noise_amp, uint64_t seed) {
         case SHARK_SETUP_SOD: setup_sod(*s); break;
         case SHARK_SETUP_DUSTYWAVE: setup_dustywave(*s); break;
         case SHARK_SETUP_SI: setup_si(*s, noise_amp, seed); break;
+        case SHARK_SETUP_DISK_POLAR: setup_disk(*s, noise_amp, seed); break;
         default: return SHARK_ERR_UNSUPPORTED;
     }
     s->time = 0.0;
@@ -1172,6 +1358,7 @@ int32_t oracle_get_u(const oracle_state* s, double* u) {
 int32_t oracle_set_u(oracle_state* s, const double* u) {
     if (!s || !u) return SHARK_ERR_INVALID_ARG;
     std::memcpy(s->u.data(), u, s->u.size() * sizeof(double));
+    if (s->u_init.empty()) s->u_init = s->u;   // first state given = relaxation reference (disk)
     return SHARK_OK;
 }
 int32_t oracle_get_q(oracle_state* s, double* q, double* cs) {
@@ -1249,6 +1436,11 @@ int32_t oracle_totals(const oracle_state* s, double* out) {
 }
 
 int32_t oracle_apply_boundaries(oracle_state* s) { if (!s) return SHARK_ERR_INVALID_ARG; apply_boundaries(*s); return SHARK_OK; }
+int32_t oracle_fargo(oracle_state* s) {
+    if (!s || !s->flag(SHARK_FLAG_FARGO)) return SHARK_ERR_INVALID_ARG;
+    fargo_scheme(*s);
+    return SHARK_OK;
+}
 int32_t oracle_ctoprim(oracle_state* s) { if (!s) return SHARK_ERR_INVALID_ARG; ctoprim(*s); return SHARK_OK; }
 int32_t oracle_courant(oracle_state* s, double* dt_out) {
     if (!s) return SHARK_ERR_INVALID_ARG;

@@ -60,6 +60,7 @@ int32_t oracle_set_dt(oracle_state* s, double dt);
 int32_t oracle_dust_drag(oracle_state* s, double coeffdt);
 int32_t oracle_compute_tstop(oracle_state* s);
 int32_t oracle_get_tstop(const oracle_state* s, double* tstop); /* ncells*ndust */
+int32_t oracle_fargo(oracle_state* s);   /* fargo_scheme alone with the dt last set (needs FARGO) */
 
 int32_t oracle_set_threads(int32_t nthreads);
 

@@ -62,8 +62,8 @@ class SharkConfig(C.Structure):
         ("si_q_shear", _D), ("si_omega", _D), ("si_eta_stream", _D), ("si_rad0", _D),
         ("si_rho_init", _D), ("si_hoverr", _D),
         ("disk_mstar", _D), ("disk_hoverr", _D), ("disk_sigma0", _D), ("disk_r0", _D),
-        ("disk_rout", _D),
-        ("reserved", _D * 48),
+        ("disk_rout", _D), ("disk_r_relax", _D), ("disk_n_rel", _D), ("disk_temp_slope", _D),
+        ("reserved", _D * 45),
         ("dx", _P), ("surf", _P), ("vol", _P), ("radii_c", _P), ("position", _P), ("cs", _P),
     ]
 

@@ -58,9 +58,10 @@ struct TileSmem {
 };
 
 // Force of the setup on a gas (s == 0) or dust (s > 0) element with primitive velocities
-// (vx, vy, vz) at column ix: update_force_setup of SI (src/setups/SI/setup.f90:335-368).  The
-// other in-scope setups have no force.  `drag` is on for every configuration that uses the force
-// (the !drag extra terms are rejected at init).
+// (vx, vy, vz) at column ix: update_force_setup of SI (src/setups/SI/setup.f90:335-368) and of
+// the polar disk (point-mass gravity -Mstar/r^2, disk_polar/setup.f90:358-366, no planet or
+// self-gravity).  SOD and DUSTYWAVE have no force.  `drag` is on for every configuration that
+// uses the force (the !drag extra terms are rejected at init).
 template <typename R>
 __device__ __forceinline__ void setup_force(const KParams<R>& p, int s, int ix, R vx, R vz, R& f1, R& f2, R& f3) {
     if (p.setup == SHARK_SETUP_SI) {
@@ -72,6 +73,9 @@ __device__ __forceinline__ void setup_force(const KParams<R>& p, int s, int ix, 
             f1 = R(2) * qs * sq(om) * xc - R(2) * om * vz;
         f2 = R(0);
         f3 = R(2) * om * vx;
+    } else if (p.setup == SHARK_SETUP_DISK_POLAR) {
+        f1 = p.fgrav[ix];
+        f2 = f3 = R(0);
     } else {
         f1 = f2 = f3 = R(0);
     }

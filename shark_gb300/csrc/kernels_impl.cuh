@@ -4,6 +4,7 @@
 
 #include "launch.h"
 #include "step_kernels.cuh"
+#include "fargo.cuh"
 
 #include <type_traits>
 
@@ -25,11 +26,14 @@ static KParams<R> make_params(const DeviceView& v) {
     p.dx1 = (const R*)v.m[0]; p.dx2 = (const R*)v.m[1]; p.surf1 = (const R*)v.m[2]; p.surf2 = (const R*)v.m[3];
     p.vol = (const R*)v.m[4]; p.radc = (const R*)v.m[5]; p.xpos = (const R*)v.m[6]; p.cs = (const R*)v.m[7];
     p.sfx = (const R*)v.m[8]; p.sfy = (const R*)v.m[9]; p.irp = (const R*)v.m[10]; p.rvol = (const R*)v.m[11];
+    p.fgrav = (const R*)v.m[12];
     p.dx1d = v.md[0]; p.dx2d = v.md[1]; p.radcd = v.md[2]; p.xposd = v.md[3]; p.csd = v.md[4];
+    p.fgravd = v.md[5]; p.treld = v.md[6]; p.hsd = v.md[7]; p.vkd = v.md[8];
+    p.u_init = (const R*)v.u_init;
     p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize;
     p.dt = nullptr; p.dt_next = nullptr; p.status = v.status; p.coef = v.coef;
     p.u_cur = (const R*)v.u[v.cur];
-    p.u_next = (R*)v.u[1 - v.cur];
+    p.u_next = (R*)v.u[(v.cur + 1) % v.nbuf];
     return p;
 }
 
@@ -119,6 +123,28 @@ static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
     return cudaGetLastError();
 }
 
+// K3: FARGO remap of p.u_next into `dst` (polar disk with FARGO only)
+template <typename R>
+static cudaError_t fargo_launch(const KParams<R>& p, R* dst, cudaStream_t st) {
+    const size_t smem = Fargo<R>::smem_bytes(p.ny);
+    dim3 grid((p.nx + Fargo<R>::W - 1) / Fargo<R>::W, p.nvar, 1);
+    cudaError_t e = cudaSuccess;
+    switch (p.slope_type) {
+#define SHARK_FARGO_CASE(ST)                                                                       \
+    case ST:                                                                                      \
+        e = cudaFuncSetAttribute(k_fargo<R, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        if (e == cudaSuccess) k_fargo<R, ST><<<grid, Fargo<R>::THREADS, smem, st>>>(p, p.u_next, dst);  \
+        break;
+        SHARK_FARGO_CASE(0)
+        SHARK_FARGO_CASE(1)
+        SHARK_FARGO_CASE(2)
+        default: SHARK_FARGO_CASE(3)
+#undef SHARK_FARGO_CASE
+    }
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
 template <typename R>
 cudaError_t launch_step(const DeviceView& v, int slot) {
     KParams<R> p = make_params<R>(v);
@@ -134,6 +160,11 @@ cudaError_t launch_step(const DeviceView& v, int slot) {
     if (v.time_kernels) cudaEventRecord(v.ev[1], v.stream);
     e = (v.ndim == 2) ? strip_launch<R>(v, p) : flux_launch<R, 1>(p, v.stream);
     if (e != cudaSuccess) return e;
+    if (v.nbuf == 3) {   // fargo_scheme after source_terms (solve.f90:105), into the third buffer
+        R* dst = (R*)v.u[(v.cur + 2) % 3];
+        if ((e = fargo_launch<R>(p, dst, v.stream)) != cudaSuccess) return e;
+        p.u_next = dst;
+    }
     if (v.time_kernels) cudaEventRecord(v.ev[2], v.stream);
     dim3 g2((v.nx + 255) / 256, v.ndim == 2 ? v.ny : 1, 1);
     finalize_dispatch<R, 0>(p, g2, v.stream);

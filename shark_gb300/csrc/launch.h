@@ -14,11 +14,16 @@ struct DeviceView {
     int nx, ny, ng, nx_max, ny_max, pitch, ndim, nvar, ndust;
     long long plane;            // elements per variable plane
     const shark_gpu_config* cfg;
-    void* u[2];                 // state ping-pong buffers (float or double)
+    void* u[3];                 // state buffers (float or double): 2 in rotation, 3 with FARGO
+    int nbuf;                   // buffers in rotation
     int cur;                    // index of the current state
-    const void* m[12];          // dx1, dx2, surf1, surf2, vol, radc, xpos, cs, sfx, sfy, irp, rvol
-                                // (state precision; the last four are derived tables)
-    const double* md[5];        // dx1, dx2, radc, xpos, cs (FP64)
+    const void* u_init;         // relaxation reference state (polar disk), state precision
+    const void* m[13];          // dx1, dx2, surf1, surf2, vol, radc, xpos, cs, sfx, sfy, irp, rvol,
+                                // fgrav (state precision; sfx..rvol are derived tables, fgrav the
+                                // radial point-mass gravity of the polar disk)
+    const double* md[9];        // dx1, dx2, radc, xpos, cs, fgrav, trel, hs, vk (FP64): trel the
+                                // disk relaxation time (0 outside r_relax), hs = sqrt(2 pi) H,
+                                // vk the FARGO orbital velocity
     const double* dK;           // per-species constants (device)
     const double* dtstop;
     const double* dsize;
@@ -35,8 +40,12 @@ struct DeviceView {
 // Record `msg` as this thread's shark_gpu_last_error text and return `code`.
 int32_t set_error(int32_t code, const char* msg);
 
-// one full step on view.u[view.cur] -> view.u[1-cur]; dt read from slot `slot`, next dt written
-// to slot 1-slot.  Returns a cudaError_t.
+// Index of the state a step leaves: the flux kernel writes u[(cur+1) % nbuf]; with FARGO the
+// orbital remap moves that into u[(cur+2) % 3], where the finalize kernel completes the step.
+inline int next_cur(const DeviceView& v) { return v.nbuf == 3 ? (v.cur + 2) % 3 : 1 - v.cur; }
+
+// one full step on view.u[view.cur] -> view.u[next_cur(view)]; dt read from slot `slot`, next dt
+// written to slot 1-slot.  Returns a cudaError_t.
 template <typename R> cudaError_t launch_step(const DeviceView& v, int slot);
 // courant only on the current state into dt slot `slot`
 template <typename R> cudaError_t launch_courant(const DeviceView& v, int slot);

@@ -68,9 +68,11 @@ struct shark_gpu_ctx {
     shark::DeviceView v;
     size_t elem = 8;                 // bytes per state element
     size_t state_bytes = 0;          // one buffer
-    void* ubuf[2] = {nullptr, nullptr};
-    void* metrics = nullptr;         // 12 arrays x nx_max in state precision
-    double* metrics_d = nullptr;     // 5 arrays x nx_max FP64
+    void* ubuf[3] = {nullptr, nullptr, nullptr};
+    void* uinit = nullptr;           // polar disk: relaxation reference state (the first upload)
+    bool have_uinit = false;
+    void* metrics = nullptr;         // 13 arrays x nx_max in state precision
+    double* metrics_d = nullptr;     // 9 arrays x nx_max FP64
     double* species = nullptr;       // dK | dtstop | dsize (3 x SHARK_MAX_DUST)
     double* dt_slots = nullptr;      // [2]
     unsigned int* status = nullptr;
@@ -96,6 +98,9 @@ namespace {
 // ---- per-column grid metrics (src/grid/grid.f90:104-240) -----------------------------------
 struct Columns {
     std::vector<double> dx1, dx2, surf1, surf2, vol, radc, xpos, cs;
+    // polar disk (disk_polar/setup.f90): point-mass gravity -Mstar/r^2, relaxation time t_rel
+    // inside r_relax (0 elsewhere), sqrt(2 pi) H for the midplane density, FARGO velocity -Omega r
+    std::vector<double> fgrav, trel, hs, vk;
     // derived tables used by the mixed-precision kernels (division-free slopes and update):
     // sfx[i] = 2/(dx1[i]+dx1[i-1]), sfy[i] = 1/(dx2[i]*r_i), irp[i] = 1/r_i, rvol[i] = 1/vol[i]
     std::vector<double> sfx, sfy, irp, rvol;
@@ -198,6 +203,23 @@ int32_t build_columns(const shark_gpu_config& c, int nx_max, int ny_max, Columns
             for (int ix = 0; ix < nx_max; ++ix) col.xpos[ix] = col.radc[ix];
         }
     }
+    col.fgrav.assign(nx_max, 0.0); col.trel.assign(nx_max, 0.0);
+    col.hs.assign(nx_max, 0.0); col.vk.assign(nx_max, 0.0);
+    if (c.setup == SHARK_SETUP_DISK_POLAR) {
+        const double M = c.disk_mstar, tw = c.disk_n_rel * 2.0 * kPi;
+        for (int ix = 0; ix < nx_max; ++ix) {
+            const double r = col.radc[ix];
+            // aspect ratio h(r) = hoverr r^((T slope + 1)/2): the reference's constant h for slope -1
+            const double H = c.disk_hoverr * std::pow(r, 0.5 * (c.disk_temp_slope + 1.0)) * r;
+            col.cs[ix] = std::sqrt(M / (r * r * r)) * H;                          // Omega H
+            col.fgrav[ix] = -M / (r * r);                                         // setup.f90:362
+            col.hs[ix] = std::sqrt(2.0 * kPi) * H;
+            if (c.flags & SHARK_FLAG_FARGO) col.vk[ix] = -std::sqrt(M / powi(r, 3)) * r;   // setup.f90:33-36
+            const bool act = ix >= ng && ix < ng + nx;
+            if (act && r < c.disk_r_relax)                                        // setup.f90:226
+                col.trel[ix] = tw / (std::sqrt(M / powi(r, 3))) - tw / (std::sqrt(M / powi(c.inner_r, 3)));
+        }
+    }
     if (c.iso_cs == 1 && c.cs) {
         for (int ix = 0; ix < nx_max; ++ix) col.cs[ix] = c.cs[(one_d ? 0 : (long long)ng * nx_max) + ix];
         for (long long i = 0; i < ncells; ++i)
@@ -222,12 +244,30 @@ int32_t validate(const shark_gpu_config* c) {
     if (c->slope_type < 0 || c->slope_type > 3) return fail(SHARK_ERR_INVALID_ARG, "unknown slope limiter");
     if (c->precision != SHARK_PREC_FP64 && c->precision != SHARK_PREC_MIXED)
         return fail(SHARK_ERR_INVALID_ARG, "precision must be FP64 or MIXED");
-    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_SI)
+    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_DISK_POLAR)
         return fail(SHARK_ERR_UNSUPPORTED, "setup %d has no device hooks in this build", c->setup);
     const int f = c->flags;
     if (f & SHARK_FLAG_VISCOSITY) return fail(SHARK_ERR_UNSUPPORTED, "viscosity is not built");
-    if (f & (SHARK_FLAG_GROWTH | SHARK_FLAG_CHARGING | SHARK_FLAG_FARGO))
-        return fail(SHARK_ERR_UNSUPPORTED, "growth/charging/fargo are not enabled in this build");
+    if (f & (SHARK_FLAG_GROWTH | SHARK_FLAG_CHARGING))
+        return fail(SHARK_ERR_UNSUPPORTED, "growth/charging are not enabled in this build");
+    if (c->setup == SHARK_SETUP_DISK_POLAR) {
+        if (c->geom != 2) return fail(SHARK_ERR_UNSUPPORTED, "the polar disk needs geom 2");
+        if (c->iso_cs != 1) return fail(SHARK_ERR_UNSUPPORTED, "the polar disk is isothermal (iso_cs 1)");
+        if (!(c->disk_mstar > 0.0) || !(c->disk_hoverr > 0.0) || !(c->inner_r > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "disk_mstar, disk_hoverr and inner_r must be > 0");
+        if (c->disk_r_relax > c->inner_r && !(c->disk_n_rel > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "disk_n_rel must be > 0 when disk_r_relax > inner_r");
+        if ((f & SHARK_FLAG_DRAG) && c->ndust > 0 && !(c->rhograin > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "rhograin must be > 0");
+    }
+    if (f & SHARK_FLAG_FARGO) {
+        // the orbital velocity is defined by the disk setups only (allocate_init.f90:109-111)
+        if (c->setup != SHARK_SETUP_DISK_POLAR)
+            return fail(SHARK_ERR_UNSUPPORTED, "FARGO needs the polar disk setup");
+        const size_t ring = (size_t)c->ny * (c->precision == SHARK_PREC_MIXED ? 16 * 4 : 8 * 8);
+        if (ring > 200 * 1024)
+            return fail(SHARK_ERR_UNSUPPORTED, "FARGO ring of %d cells exceeds one CTA's shared memory", c->ny);
+    }
     if (c->ndust > 0 && (f & SHARK_FLAG_BACK_REACTION) && c->iso_cs < 1)
         return fail(SHARK_ERR_UNSUPPORTED, "adiabatic drag heating (source_terms.f90:88-97) is not built");
     if (c->setup == SHARK_SETUP_SI && c->ndust > 0 && !(f & SHARK_FLAG_DRAG) && (f & SHARK_FLAG_FORCE_KICK))
@@ -240,24 +280,26 @@ int32_t validate(const shark_gpu_config* c) {
             return fail(SHARK_ERR_INVALID_ARG, "dust_tstop[%d] must be > 0", k);
         if (c->setup == SHARK_SETUP_DUSTYWAVE && (f & SHARK_FLAG_DRAG) && !(c->dust_K[k] > 0.0))
             return fail(SHARK_ERR_INVALID_ARG, "dust_K[%d] must be > 0", k);
+        if (c->setup == SHARK_SETUP_DISK_POLAR && (f & SHARK_FLAG_DRAG) && !(c->dust_size[k] > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "dust_size[%d] must be > 0", k);
     }
     return SHARK_OK;
 }
 
 template <typename T>
 void upload_cols(std::vector<T>& dst, const Columns& col) {
-    const std::vector<double>* src[12] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
-                                          &col.xpos, &col.cs, &col.sfx, &col.sfy, &col.irp, &col.rvol};
+    const std::vector<double>* src[13] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
+                                          &col.xpos, &col.cs, &col.sfx, &col.sfy, &col.irp, &col.rvol, &col.fgrav};
     const size_t n = col.dx1.size();
-    dst.resize(12 * n);
-    for (int a = 0; a < 12; ++a)
+    dst.resize(13 * n);
+    for (int a = 0; a < 13; ++a)
         for (size_t i = 0; i < n; ++i) dst[a * n + i] = (T)(*src[a])[i];
 }
 
 int32_t release(shark_gpu_ctx* c) {
     if (!c) return SHARK_OK;
     cudaStreamSynchronize(c->stream);
-    for (void* p : {c->ubuf[0], c->ubuf[1], c->metrics}) if (p) cudaFree(p);
+    for (void* p : {c->ubuf[0], c->ubuf[1], c->ubuf[2], c->uinit, c->metrics}) if (p) cudaFree(p);
     for (double* p : {c->metrics_d, c->species, c->dt_slots, c->staging, c->part, c->tot_out}) if (p) cudaFree(p);
     if (c->status) cudaFree(c->status);
     if (c->coef) cudaFree(c->coef);
@@ -391,15 +433,22 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     v.join = c->ev_join;
     for (auto& e : c->ev_read) INIT_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto& e : c->ev_time) INIT_TRY(cudaEventCreate(&e));
-    for (int b = 0; b < 2; ++b) {
+    v.nbuf = (cfg->flags & SHARK_FLAG_FARGO) ? 3 : 2;
+    for (int b = 0; b < v.nbuf; ++b) {
         INIT_TRY(cudaMalloc(&c->ubuf[b], c->state_bytes));
         INIT_TRY(cudaMemsetAsync(c->ubuf[b], 0, c->state_bytes, c->stream));
         v.u[b] = c->ubuf[b];
     }
+    v.u[2] = c->ubuf[2];
     v.cur = 0;
+    if (cfg->setup == SHARK_SETUP_DISK_POLAR) {
+        INIT_TRY(cudaMalloc(&c->uinit, c->state_bytes));
+        INIT_TRY(cudaMemsetAsync(c->uinit, 0, c->state_bytes, c->stream));
+    }
+    v.u_init = c->uinit;
     const size_t ncol = (size_t)v.nx_max;
-    INIT_TRY(cudaMalloc(&c->metrics, 12 * ncol * c->elem));
-    INIT_TRY(cudaMalloc(&c->metrics_d, 5 * ncol * sizeof(double)));
+    INIT_TRY(cudaMalloc(&c->metrics, 13 * ncol * c->elem));
+    INIT_TRY(cudaMalloc(&c->metrics_d, 9 * ncol * sizeof(double)));
     if (is_mixed(c)) {
         std::vector<float> h;
         upload_cols(h, col);
@@ -409,13 +458,14 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         upload_cols(h, col);
         INIT_TRY(cudaMemcpy(c->metrics, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
-    for (int a = 0; a < 12; ++a) v.m[a] = (const char*)c->metrics + a * ncol * c->elem;
+    for (int a = 0; a < 13; ++a) v.m[a] = (const char*)c->metrics + a * ncol * c->elem;
     {
-        std::vector<double> hd(5 * ncol);
-        const std::vector<double>* src[5] = {&col.dx1, &col.dx2, &col.radc, &col.xpos, &col.cs};
-        for (int a = 0; a < 5; ++a) std::memcpy(hd.data() + a * ncol, src[a]->data(), ncol * sizeof(double));
+        std::vector<double> hd(9 * ncol);
+        const std::vector<double>* src[9] = {&col.dx1, &col.dx2, &col.radc, &col.xpos, &col.cs,
+                                             &col.fgrav, &col.trel, &col.hs, &col.vk};
+        for (int a = 0; a < 9; ++a) std::memcpy(hd.data() + a * ncol, src[a]->data(), ncol * sizeof(double));
         INIT_TRY(cudaMemcpy(c->metrics_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
-        for (int a = 0; a < 5; ++a) v.md[a] = c->metrics_d + a * ncol;
+        for (int a = 0; a < 9; ++a) v.md[a] = c->metrics_d + a * ncol;
     }
     INIT_TRY(cudaMalloc(&c->species, 3 * SHARK_MAX_DUST * sizeof(double)));
     INIT_TRY(cudaMemcpy(c->species, cfg->dust_K, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
@@ -459,15 +509,22 @@ int32_t shark_gpu_upload(shark_gpu_ctx* c, const double* u_prim, int64_t ncells,
     if (!c->staging) CUDA_TRY(cudaMalloc(&c->staging, bytes));
     CUDA_TRY(cudaMemcpyAsync(c->staging, u_prim, bytes, cudaMemcpyHostToDevice, c->stream));
     c->v.cur = 0;
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < c->v.nbuf; ++b) {
         cudaError_t e = is_mixed(c) ? shark::launch_from_fortran<float>(c->v, c->staging, c->ubuf[b])
                                     : shark::launch_from_fortran<double>(c->v, c->staging, c->ubuf[b]);
         if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "upload conversion: %s", cudaGetErrorString(e));
     }
+    if (c->uinit && !c->have_uinit) {
+        // the first state uploaded is the disk's initial state (uprim_condinit, setup.f90:79-83)
+        cudaError_t e = is_mixed(c) ? shark::launch_from_fortran<float>(c->v, c->staging, c->uinit)
+                                    : shark::launch_from_fortran<double>(c->v, c->staging, c->uinit);
+        if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "upload conversion: %s", cudaGetErrorString(e));
+        c->have_uinit = true;
+    }
     CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
     c->status_seen = 0;
-    // apply_boundaries of the first step on both buffers (fixed SOD ghosts are only ever set here)
-    for (int b = 0; b < 2; ++b) {
+    // apply_boundaries of the first step on every buffer (fixed SOD ghosts are only ever set here)
+    for (int b = 0; b < c->v.nbuf; ++b) {
         c->v.cur = b;
         cudaError_t eb = is_mixed(c) ? shark::launch_boundaries<float>(c->v) : shark::launch_boundaries<double>(c->v);
         if (eb != cudaSuccess) return fail(SHARK_ERR_CUDA, "boundaries: %s", cudaGetErrorString(eb));
@@ -499,7 +556,7 @@ int32_t shark_gpu_step(shark_gpu_ctx* c, double* dt_out, int32_t* status_out) {
     }
     cudaError_t e = do_step(c, slot);
     if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
-    c->v.cur = 1 - c->v.cur;
+    c->v.cur = shark::next_cur(c->v);
     c->nstep++;
     int32_t rc = queue_readback(c, 1 - slot);   // dt of the next step, written by k_finalize
     if (rc) return rc;

@@ -32,8 +32,13 @@ struct KParams {
     // per-column metrics (length nx_max), compute precision
     const R *dx1, *dx2, *surf1, *surf2, *vol, *radc, *xpos, *cs;
     const R *sfx, *sfy, *irp, *rvol;   // division-free tables (mixed path)
+    const R* fgrav;                    // polar disk: -Mstar/r^2 (0 for the other setups)
     // per-column metrics in FP64 (courant, drag)
     const double *dx1d, *dx2d, *radcd, *xposd, *csd;
+    // polar disk per-column FP64 tables: gravity, relaxation time (0 = no relaxation),
+    // sqrt(2 pi) H, FARGO orbital velocity
+    const double *fgravd, *treld, *hsd, *vkd;
+    const R* u_init;                   // polar disk relaxation reference state
     // per-species constants
     const double *dK, *dtstop, *dsize;
     // time step bookkeeping
@@ -98,6 +103,21 @@ __global__ void k_boundaries(KParams<R> p, R* u) {
             return;
         }
     }
+    if (p.setup == SHARK_SETUP_DISK_POLAR) {
+        // disk_polar/boundaries.f90:1-70: periodic in phi; a radial ghost takes the first (last)
+        // active cell of its row, phi image included, with the radial velocities clipped so that
+        // nothing flows in (the reference's row-less u_prim(first_active) read as the row's cell)
+        const int rx = ix < ng ? ng : (ix >= ng + nx ? ng + nx - 1 : ix);
+        for (int v = 0; v < p.nvar; ++v) u[uidx(p, v, iy, ix)] = u[uidx(p, v, sy, rx)];
+        if (xg) {
+            for (int k = -1; k < N; ++k) {
+                const long long i = uidx(p, k < 0 ? 1 : 5 + N + k, iy, ix);
+                const R val = u[i];
+                u[i] = ix < ng ? (val > R(0) ? val : R(0)) : (val < R(0) ? val : R(0));
+            }
+        }
+        return;
+    }
     for (int v = 0; v < p.nvar; ++v) u[uidx(p, v, iy, ix)] = u[uidx(p, v, sy, sx)];
     if (p.setup == SHARK_SETUP_SI && xg) {
         // shear: vz momentum -/+ rho * q * Omega * L (SI/boundaries.f90:60-74)
@@ -132,6 +152,30 @@ namespace shark {
 template <typename R>
 __device__ __forceinline__ void fill_ghost_images(const KParams<R>& p, R* u, int gx, int gy) {
     const int ng = p.ng, nx = p.nx, ny = p.ny;
+    if (p.setup == SHARK_SETUP_DISK_POLAR) {
+        // disk_polar/boundaries.f90:1-70 by the producer: phi images of the rows next to the
+        // periodic seam; the first/last active column also writes its radial ghosts (and their
+        // phi images) with the radial velocities clipped to outflow
+        const int ty = gy < 2 * ng ? gy + ny : (gy >= ny ? gy - ny : -1);
+        const bool left = gx == ng, right = gx == ng + nx - 1;
+        if (ty < 0 && !left && !right) return;
+        const int N = p.ndust;
+        for (int v = 0; v < p.nvar; ++v) {
+            const R val = u[uidx(p, v, gy, gx)];
+            if (ty >= 0) u[uidx(p, v, ty, gx)] = val;
+            if (left || right) {
+                R xv = val;
+                if (v == 1 || (v >= 5 + N && v < 5 + 2 * N))
+                    xv = left ? (val > R(0) ? val : R(0)) : (val < R(0) ? val : R(0));
+                for (int g = 0; g < ng; ++g) {
+                    const int col = left ? g : ng + nx + g;
+                    u[uidx(p, v, gy, col)] = xv;
+                    if (ty >= 0) u[uidx(p, v, ty, col)] = xv;
+                }
+            }
+        }
+        return;
+    }
     const bool xper = !(p.setup == SHARK_SETUP_SOD && p.sod_dir == 0);
     const bool yper = p.ndim == 2 && !(p.setup == SHARK_SETUP_SOD && p.sod_dir == 1);
     int tx = -1, ty = -1;
@@ -200,6 +244,54 @@ __device__ __forceinline__ void block_reduce_dt(double dtc, unsigned int st, uns
     }
 }
 
+// Stopping time of species k at cell (gx, gy) from the state at the start of the step
+// (compute_tstop runs before the update, solve.f90:34-35); qrho_old = max(rho_old, smallr).
+template <typename R>
+__device__ __forceinline__ double tstop_cell(const KParams<R>& p, int k, double qrho_old, int gx, int gy) {
+    constexpr double pi = 3.141592653589793238462643383279;
+    if (p.setup == SHARK_SETUP_SI) return p.dtstop[k];                       // SI/setup.f90:389-397
+    if (p.setup == SHARK_SETUP_DUSTYWAVE) {                                  // DUSTYWAVE/setup.f90:217
+        const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
+        return rd_old * qrho_old / p.dK[k] / (qrho_old);
+    }
+    if (p.setup == SHARK_SETUP_DISK_POLAR)   // Epstein on the midplane density Sigma/(sqrt(2 pi) H)
+        return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old / p.hsd[gx] * p.csd[gx]);
+    // Epstein (SOD/setup.f90:179-185); isothermal cs only (checked at init)
+    return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old * p.csd[gx]);
+}
+
+// setup_inloop of the polar disk (disk_polar/setup.f90:206-284) for one active cell, FP64 or
+// FP32 arithmetic: the first active column is reset to its initial state; inside r_relax the
+// density and in-plane velocities of gas and dust relax towards the initial state with
+// exp(-dt/t_rel).  Returns true when it changed the cell.
+template <typename R, typename C>
+__device__ __forceinline__ bool disk_inloop_cell(const KParams<R>& p, R* u, int gx, int gy, double dt) {
+    const int N = p.ndust;
+    if (gx == p.ng) {
+        for (int v = 0; v < p.nvar; ++v) u[uidx(p, v, gy, gx)] = p.u_init[uidx(p, v, gy, gx)];
+        return true;
+    }
+    const double trel = p.treld[gx];
+    if (!(trel > 0.0)) return false;
+    const C e = C(exp(-dt / trel));
+    for (int s = 0; s <= N; ++s) {
+        const int ir = svar(s, 0, N), ivx = svar(s, 1, N), ivy = svar(s, 2, N);
+        const C rho_init = C(p.u_init[uidx(p, ir, gy, gx)]);
+        const C vx_init = C(p.u_init[uidx(p, ivx, gy, gx)]) / rho_init;
+        const C vy_init = C(p.u_init[uidx(p, ivy, gy, gx)]) / rho_init;
+        const C rho_old = C(u[uidx(p, ir, gy, gx)]);
+        const C vx_old = C(u[uidx(p, ivx, gy, gx)]) / rho_old;
+        const C vy_old = C(u[uidx(p, ivy, gy, gx)]) / rho_old;
+        const C rho_new = (rho_init) * (C(1) - e) + rho_old * e;
+        const C vx_new = (vx_init) * (C(1) - e) + vx_old * e;
+        const C vy_new = (vy_init) * (C(1) - e) + vy_old * e;
+        u[uidx(p, ir, gy, gx)] = R(rho_new);
+        u[uidx(p, ivx, gy, gx)] = R(rho_new * vx_new);
+        u[uidx(p, ivy, gy, gx)] = R(rho_new * vy_new);
+    }
+    return true;
+}
+
 template <typename R, int NS, int MODE>
 __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
@@ -224,17 +316,7 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
             const double rho_old = (double)p.u_cur[uidx(p, 0, gy, gx)];
             const double qrho_old = rho_old > p.smallr ? rho_old : p.smallr;
             for (int k = 0; k < N; ++k) {
-                double ts;
-                if (p.setup == SHARK_SETUP_SI) {
-                    ts = p.dtstop[k];                                   // SI/setup.f90:389-397
-                } else if (p.setup == SHARK_SETUP_DUSTYWAVE) {
-                    const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
-                    ts = rd_old * qrho_old / p.dK[k] / (qrho_old);   // DUSTYWAVE/setup.f90:217
-                } else {
-                    // Epstein (SOD/setup.f90:179-185); isothermal cs only (checked at init)
-                    ts = sqrt(3.141592653589793238462643383279 * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] /
-                         (qrho_old * p.csd[gx]);
-                }
+                const double ts = tstop_cell(p, k, qrho_old, gx, gy);
                 const double a = 1.0 * dt / ts;
                 const double pdx = (double)u[uidx(p, 5 + N + k, gy, gx)];
                 const double pdy = (double)u[uidx(p, 5 + 2 * N + k, gy, gx)];
@@ -249,17 +331,7 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
             for (int k = 0; k < N; ++k) {
                 double a;
                 if (NS > 0) a = alpha[k < NMAX ? k : 0];
-                else {   // run-time species count: recompute alpha_k
-                    double ts;
-                    if (p.setup == SHARK_SETUP_SI) ts = p.dtstop[k];
-                    else if (p.setup == SHARK_SETUP_DUSTYWAVE) {
-                        const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
-                        ts = rd_old * qrho_old / p.dK[k] / (qrho_old);
-                    } else
-                        ts = sqrt(3.141592653589793238462643383279 * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] /
-                             (qrho_old * p.csd[gx]);
-                    a = 1.0 * dt / ts;
-                }
+                else a = 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy);   // run-time species count
                 const long long ix_ = uidx(p, 5 + N + k, gy, gx), iy_ = uidx(p, 5 + 2 * N + k, gy, gx),
                                 iz_ = uidx(p, 5 + 3 * N + k, gy, gx);
                 const double rd = (double)u[uidx(p, 5 + k, gy, gx)];
@@ -313,6 +385,12 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
                 u[ixx] = R(d * (vx * (1. - Ohmdt * Ohmdt) - 2. * uz * Ohmdt + AA * Ohmdt) / (1. + Ohmdt * Ohmdt));
             }
         }
+        if (MODE == 0 && p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<R, double>(p, u, gx, gy, dt)) {
+            rho = (double)u[uidx(p, 0, gy, gx)];
+            px = (double)u[uidx(p, 1, gy, gx)];
+            py = (double)u[uidx(p, 2, gy, gx)];
+            pz = (double)u[uidx(p, 3, gy, gx)];
+        }
         // ---- courant on the final state (src/solver/courant.f90:11-124) -----------------------
         const double cfl = p.cfl;
         const double qrho = rho > p.smallr ? rho : p.smallr;
@@ -340,6 +418,10 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
             const double f1 = 2.0 * qsh * (om * om) * xc - 2.0 * om * vz - 2.0 * p.si_r0 * om * p.si_eta;
             const double f3 = 2.0 * om * vx;
             fmax_d = sqrt(f1 * f1 + 0.0 * 0.0 + f3 * f3);
+        } else if (fk && p.setup == SHARK_SETUP_DISK_POLAR) {
+            // the same point-mass force acts on gas and every dust species
+            const double g = p.fgravd[gx];
+            fmax_d = sqrt(g * g + 0.0 * 0.0 + 0.0 * 0.0);
         }
         for (int k = 0; k < N; ++k) {
             const double rd = (double)u[uidx(p, 5 + k, gy, gx)];
@@ -404,7 +486,7 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
     unsigned int st = 0;
     if (gx < p.ng + p.nx) {
         float* u = p.u_next;
-        const float rho = u[uidx(p, 0, gy, gx)];
+        float rho = u[uidx(p, 0, gy, gx)];
         float px = u[uidx(p, 1, gy, gx)], py = u[uidx(p, 2, gy, gx)], pz = u[uidx(p, 3, gy, gx)];
         if (drag) {
             float rk[NMAX], wk[NMAX];
@@ -414,17 +496,7 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
             for (int k = 0; k < N; ++k) {
                 float r, w;
                 if (const_ts) { r = cr[k]; w = cw[k]; }
-                else {
-                    double ts;
-                    if (p.setup == SHARK_SETUP_DUSTYWAVE) {
-                        const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
-                        ts = rd_old * qrho_old / p.dK[k] / qrho_old;
-                    } else {
-                        ts = sqrt(3.141592653589793238462643383279 * p.gamma / 8.0) * p.rhograin * p.dsize[k] /
-                             (qrho_old * p.csd[gx]);
-                    }
-                    drag_coeffs(1.0 * dt / ts, r, w);
-                }
+                else drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
                 if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
                 pnx += w * u[uidx(p, 5 + N + k, gy, gx)];
                 pny += w * u[uidx(p, 5 + 2 * N + k, gy, gx)];
@@ -437,17 +509,7 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
                 float r, w;
                 if (NS > 0) { r = rk[k < NMAX ? k : 0]; w = wk[k < NMAX ? k : 0]; }
                 else if (const_ts) { r = cr[k]; w = cw[k]; }
-                else {
-                    double ts;
-                    if (p.setup == SHARK_SETUP_DUSTYWAVE) {
-                        const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
-                        ts = rd_old * qrho_old / p.dK[k] / qrho_old;
-                    } else {
-                        ts = sqrt(3.141592653589793238462643383279 * p.gamma / 8.0) * p.rhograin * p.dsize[k] /
-                             (qrho_old * p.csd[gx]);
-                    }
-                    drag_coeffs(1.0 * dt / ts, r, w);
-                }
+                else drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
                 const float rd = u[uidx(p, 5 + k, gy, gx)];
                 const long long ixx = uidx(p, 5 + N + k, gy, gx), iyy = uidx(p, 5 + 2 * N + k, gy, gx),
                                 izz = uidx(p, 5 + 3 * N + k, gy, gx);
@@ -490,6 +552,12 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
                 u[ixx] = d * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
             }
         }
+        if (MODE == 0 && p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<float, float>(p, u, gx, gy, dt)) {
+            rho = u[uidx(p, 0, gy, gx)];
+            px = u[uidx(p, 1, gy, gx)];
+            py = u[uidx(p, 2, gy, gx)];
+            pz = u[uidx(p, 3, gy, gx)];
+        }
         // ---- courant on the final state (src/solver/courant.f90:11-124), FP32 ----------------------
         const float cfl = (float)p.cfl;
         const float irho = 1.0f / rho;
@@ -510,13 +578,16 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
         float vv = fabsf(vx) + fabsf(vy) + fabsf(vz);
         float vmax = cs + vv;
         float fmx = 0.f;
-        const bool fk = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
+        const bool fk_si = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
+        const bool fk = fk_si || ((p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_DISK_POLAR);
         const float om = (float)p.si_om, qsh = (float)p.si_q;
         const float xc = p.xpos[gx] - 0.5f * (float)p.box_l;
-        if (fk) {
+        if (fk_si) {
             const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vz - 2.0f * (float)p.si_r0 * om * (float)p.si_eta;
             const float f3 = 2.0f * om * vx;
             fmx = sqrtf(f1 * f1 + f3 * f3);
+        } else if (fk) {
+            fmx = fabsf(p.fgrav[gx]);   // polar disk: the point-mass force, the same on gas and dust
         }
         for (int k = 0; k < N; ++k) {
             const float rd = u[uidx(p, 5 + k, gy, gx)];
@@ -526,7 +597,7 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
             const float vdz = u[uidx(p, 5 + 3 * N + k, gy, gx)] * ird;
             vv = fabsf(vdx) + fabsf(vdy) + fabsf(vdz);
             vmax = fmaxf(vmax, vv);
-            if (fk) {
+            if (fk_si) {
                 const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vdz;
                 const float f3 = 2.0f * om * vdx;
                 fmx = fmaxf(fmx, sqrtf(f1 * f1 + f3 * f3));

@@ -28,7 +28,8 @@ module shark_gpu
     real(c_double) :: dw_rho_0, dw_delta_rho, dw_vx_0, dw_kx_wave
     real(c_double) :: si_q_shear, si_omega, si_eta_stream, si_rad0, si_rho_init, si_hoverr
     real(c_double) :: disk_mstar, disk_hoverr, disk_sigma0, disk_r0, disk_rout
-    real(c_double) :: reserved(48)
+    real(c_double) :: disk_r_relax, disk_n_rel, disk_temp_slope
+    real(c_double) :: reserved(45)
     type(c_ptr) :: dx, surf, vol, radii_c, position, cs
   end type shark_gpu_config
 

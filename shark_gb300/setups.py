@@ -12,8 +12,10 @@ src/grid/grid.f90:104-173 (positions), src/solver/solve.f90:265-302 (primtoc).
 """
 import numpy as np
 
-from .config import (SharkConfig, default_config, SETUP_SOD, SETUP_DUSTYWAVE, SETUP_SI,
-                     FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, PREC_FP64)
+import math
+
+from .config import (SharkConfig, default_config, SETUP_SOD, SETUP_DUSTYWAVE, SETUP_SI, SETUP_DISK_POLAR,
+                     FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO, PREC_FP64)
 
 PI = 3.141592653589793238462643383279          # src/commons/phys_const.f90:14
 F43 = float(np.float32(4.0) / np.float32(3.0))  # Fortran `4./3.` is a default-REAL quotient
@@ -306,6 +308,101 @@ def si_ic(cfg, noise_amp, seed):
     return u
 
 
+# ---------------------------------------------------------------------------------------------
+# Polar disk
+# ---------------------------------------------------------------------------------------------
+def disk_radii(cfg):
+    """Cell-centre radius per column of gridinit_disk_log (src/grid/grid.f90:180-240): a log grid
+    from inner_r to box_l, ghost columns at inner_r/2 and box_l + dr_last/2."""
+    nx, ng = cfg.nx, cfg.nghost
+    zeta = math.pow(cfg.box_l / cfg.inner_r, 1.0 / float(nx - 1))
+    r = np.empty(cfg.nx_max)
+    dr = np.empty(cfg.nx_max)
+    for ix in range(cfg.nx_max):
+        k = ix - ng
+        r[ix] = cfg.inner_r * 0.5 * (_powi(zeta, k) + _powi(zeta, k + 1))
+        dr[ix] = cfg.inner_r * (_powi(zeta, k + 1) - _powi(zeta, k))
+    for g in range(ng):
+        r[g] = cfg.inner_r * 0.5
+        r[cfg.nx_max - 1 - g] = cfg.box_l + 0.5 * dr[ng + nx - 1]
+    return r
+
+
+def disk_polar(nr=128, nphi=128, ndust=4, stokes_min=1e-3, stokes_max=0.3, dust2gas=0.01, mstar=1.0,
+               hoverr=0.05, temp_slope=-1.0, sigma0=1e-3, r0=1.0, rout=40.0, rin=1.0, rmax=40.0,
+               r_relax=3.0, n_rel=8.0, rhograin=1.0, noise=0.0, seed=1, cfl=0.8, slope_type=1,
+               gamma=1.666666666666667, fargo=False, precision=PREC_FP64):
+    """Face-on polar disk around a point mass (src/setups/disk_polar/setup.f90:1-84) on the log
+    grid, in code units G = Mstar = 1 (r in AU, t in 1/Omega(1 AU)).
+
+    Sigma = sigma0 (r0/r) exp(-r/rout) with optional relative white noise ``noise``; isothermal
+    cs = h(r) sqrt(Mstar/r), h = hoverr r^((temp_slope+1)/2); gas rotation
+    Omega r sqrt(1 - h^2 (1 - temp_slope + r/rout)); dust in MRN bins between the grain sizes of
+    Stokes numbers ``stokes_min``/``stokes_max`` at r0, each bin with its own size, drifting
+    inwards at eta Omega r/(St + 1/St) with the full Keplerian azimuthal velocity.  The ghost
+    cells hold the initial state of their own radii, like the reference's setup.
+    """
+    cfg = default_config()
+    cfg.nx, cfg.ny, cfg.ndust = nr, nphi, ndust
+    cfg.geom, cfg.gridspace = 2, 1
+    cfg.gamma, cfg.cfl, cfg.slope_type = gamma, cfl, slope_type
+    cfg.iso_cs = 1
+    cfg.precision = precision
+    cfg.setup = SETUP_DISK_POLAR
+    cfg.flags = FLAG_DRAG | FLAG_BACK_REACTION | FLAG_FORCE_KICK | (FLAG_FARGO if fargo else 0)
+    cfg.box_l, cfg.inner_r = rmax, rin
+    cfg.box_l_y = 2.0 * PI
+    cfg.rhograin = rhograin
+    cfg.disk_mstar, cfg.disk_hoverr, cfg.disk_sigma0 = mstar, hoverr, sigma0
+    cfg.disk_r0, cfg.disk_rout = r0, rout
+    cfg.disk_r_relax, cfg.disk_n_rel, cfg.disk_temp_slope = r_relax, n_rel, temp_slope
+    sig0 = sigma0 * math.exp(-r0 / rout)
+    unit_s = sig0 / (math.sqrt(PI * gamma / 8.0) * math.sqrt(2.0 * PI) * rhograin)   # St = 1 at r0
+    if ndust > 0:
+        sdust, eps = mrn_bins(ndust, stokes_min * unit_s, stokes_max * unit_s, stokes_min * unit_s,
+                              stokes_max * unit_s, dust2gas, rhograin=rhograin,
+                              dust_ratio_min=cfg.dust_ratio_min)
+        for k in range(ndust):
+            cfg.dust_size[k] = sdust[k]
+            cfg.dust_eps[k] = eps[k]
+            cfg.dust_stokes[k] = sdust[k] / unit_s
+    cfg.cs0 = hoverr * math.sqrt(mstar / r0)
+    return cfg, disk_ic(cfg, noise, seed)
+
+
+def disk_ic(cfg, noise_amp, seed):
+    """Initial conserved state of the polar disk (disk_polar/setup.f90:27-74); see disk_polar."""
+    N = cfg.ndust
+    nxm, nym = cfg.nx_max, cfg.ny_max
+    r = disk_radii(cfg)
+    q = np.zeros((cfg.nvar, nym, nxm))
+    cells = np.arange(cfg.ncells, dtype=np.uint64).reshape(nym, nxm)
+    M, slope = cfg.disk_mstar, cfg.disk_temp_slope
+    for ix in range(nxm):
+        rr = float(r[ix])
+        h = cfg.disk_hoverr * math.pow(rr, 0.5 * (slope + 1.0))
+        H = h * rr
+        omega = math.sqrt(M / _powi(rr, 3))
+        cs0 = omega * H
+        sig = cfg.disk_sigma0 * (cfg.disk_r0 / rr) * math.exp(-rr / cfg.disk_rout)
+        if noise_amp > 0:
+            sig = sig * (1.0 + noise_amp * (2.0 * hash_uniform(seed, cells[:, ix]) - 1.0))
+        else:
+            sig = np.full(nym, sig)
+        rot = math.sqrt(1.0 - (h * h) * (1.0 - slope + rr / cfg.disk_rout))
+        q[0, :, ix] = sig
+        q[2, :, ix] = omega * rr * rot
+        q[4, :, ix] = sig * (cs0 * cs0)
+        hs = math.sqrt(2.0 * PI) * H
+        for k in range(N):
+            q[5 + k, :, ix] = cfg.dust_eps[k] * sig
+            ts = math.sqrt(PI * cfg.gamma / 8.0) * cfg.rhograin * cfg.dust_size[k] / (sig / hs * cs0)
+            St = ts * omega
+            q[5 + N + k, :, ix] = (rot - 1.0) * omega * rr / (St + 1.0 / St)
+            q[5 + 2 * N + k, :, ix] = omega * rr
+    return primtoc(cfg, q.reshape(cfg.nvar, -1)).reshape(-1)
+
+
 def build(name, **kw):
-    """Dispatch by setup name ('sod', 'dustywave', 'si')."""
-    return {"sod": sod, "dustywave": dustywave, "si": si}[name](**kw)
+    """Dispatch by setup name ('sod', 'dustywave', 'si', 'disk_polar')."""
+    return {"sod": sod, "dustywave": dustywave, "si": si, "disk_polar": disk_polar}[name](**kw)

@@ -82,6 +82,28 @@ def test_invalid_configs_are_rejected_before_touching_a_device(lib):
     assert lib.shark_gpu_free(None) == K.OK
 
 
+def test_disk_and_fargo_configs_are_checked_before_touching_a_device(lib):
+    h = C.c_void_p()
+    si, _ = setups.si(n=32, ndust=2)
+    bad = si.copy()
+    bad.flags |= K.FLAG_FARGO          # the orbital velocity exists for the disk setups only
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_UNSUPPORTED
+    assert b"FARGO" in lib.shark_gpu_last_error()
+    disk, _ = setups.disk_polar(nr=32, nphi=32, ndust=2, fargo=True)
+    bad = disk.copy()
+    bad.geom = 0
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_UNSUPPORTED
+    bad = disk.copy()
+    bad.ny = 8192                      # a ring that does not fit one CTA's shared memory
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_UNSUPPORTED
+    bad = disk.copy()
+    bad.disk_mstar = 0.0
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_INVALID_ARG
+    bad = disk.copy()
+    bad.dust_size[1] = 0.0
+    assert lib.shark_gpu_init(C.byref(bad), C.byref(h)) == K.ERR_INVALID_ARG
+
+
 def test_no_cpu_fallback_without_a_gpu(lib):
     """On a machine without an sm_103 device the library refuses to run (no silent fallback)."""
     import torch
