@@ -71,6 +71,13 @@ extern "C" {
 #define SHARK_FLAG_STATIC         0x80  /* static             src/commons/parameters.f90:48      */
 
 /* ---- precision of the device state and of the flux/update stage -------------------------- */
+#define SHARK_CHARGE_HIST 64   /* bins of the Newton iteration histogram (last bin: >= 63) */
+
+/* chg_mode bits */
+#define SHARK_CHARGE_RESISTIVITIES 1   /* also eta_o, eta_H, eta_a, gamma_d (res_Marchand)       */
+#define SHARK_CHARGE_ANALYTICAL    2   /* Fujii et al. per-species Newton (analytical_charge)    */
+#define SHARK_CHARGE_MLP_SEED      4   /* start the Marchand Newton from the trained network     */
+
 #define SHARK_PREC_FP64   0   /* everything FP64 (the FP64 GPU oracle run)                      */
 #define SHARK_PREC_MIXED  1   /* FP32 state + FP32 flux/update; FP64 drag, FARGO split, totals  */
 
@@ -130,7 +137,26 @@ typedef struct shark_gpu_config {
      * disk_sigma0 (disk_r0/r) exp(-r/disk_rout). */
     double disk_mstar, disk_hoverr, disk_sigma0, disk_r0, disk_rout;
     double disk_r_relax, disk_n_rel, disk_temp_slope;
-    double reserved[45];
+    /* Code units in cgs (0 = 1): length, density, time.  unit_m = unit_l^3 unit_d,
+     * unit_v = unit_l/unit_t, unit_nH = unit_d/(mu_gas mH) (dustyTurb/units.f90). */
+    double unit_l, unit_d, unit_t;
+    double mu_gas;                     /* mean molecular weight (setup_commons.f90: 2.31)        */
+    double T_cloud;                    /* dustyTurb gas temperature (K) for charging and growth  */
+    /* Charging (src/chemistry/ionisation_commons.f90): cosmic-ray ionisation rate x (s^-1),
+     * for the polar disk attenuated by exp(-Sigma/chg_sigma_att) (g cm^-2, 0 = none); ion mass
+     * (mH), electron sticking coefficient, Newton tolerance and iteration cap, B field
+     * normalisation of the resistivities (G at nH = 1e4 cm^-3). */
+    double chg_x, chg_sigma_att, chg_mu_ions, chg_stick_el, chg_eps, chg_B0;
+    int32_t chg_nitermax;
+    int32_t chg_mode;                  /* SHARK_CHARGE_* bits                                    */
+    /* dustyTurb (src/setups/dustyTurb/setup_commons.f90): mean density rho_0; stopping times
+     * t_k = dust_stokes[k] box_l rho_0 / cs / rho (setup.f90:456).  Ornstein-Uhlenbeck
+     * solenoidal forcing: target RMS Mach number, correlation time, wavenumber band (in 2 pi/box_l)
+     * and seed (turb_mach = 0: no forcing). */
+    double turb_rho0, turb_mach, turb_tcorr;
+    int32_t turb_kmin, turb_kmax;
+    int32_t turb_seed, pad2;
+    double reserved[28];
 
     /* Optional grid metrics from the caller (Fortran dx(ncells,ndim), surf(ncells,ndim),
      * vol(ncells), radii_c(ncells), position(ncells,ndim), cs(ncells)).  NULL: the library
@@ -234,6 +260,26 @@ int32_t shark_gpu_totals_noalloc(const double* u_dev, int32_t nx, int32_t ny, in
 const char* shark_gpu_last_error(void);
 
 /* Release the device state and the context. */
+/* ---- charging (SHARK_FLAG_CHARGING; src/chemistry/ionisation.f90:4-214) --------------------
+ * Each step charges every cell (ghosts included) from the state at the start of the step, after
+ * the stopping times (solve.f90:36-42), starting the Newton from the cell's previous psi
+ * (psi_old) or, on a cold start, from the reference's psi0 or the trained network
+ * (SHARK_CHARGE_MLP_SEED).  The charges do not feed back into the hydro state. */
+
+/* Charge the current state now (outside a step); synchronous. */
+int32_t shark_gpu_charge(shark_gpu_ctx* ctx);
+/* psi_old = 0 everywhere: the next charging call starts cold (ionisation.f90:71-73). */
+int32_t shark_gpu_charge_reset(shark_gpu_ctx* ctx);
+/* Newton iteration histogram of the last charging call (SHARK_CHARGE_HIST bins, the last one
+ * counting >= 63 iterations), the number of cells that hit chg_nitermax without reaching
+ * chg_eps, and the total iteration count.  Any pointer may be NULL. */
+int32_t shark_gpu_charge_stats(shark_gpu_ctx* ctx, int64_t* iters_hist, int64_t* nonconv, int64_t* total_iters);
+/* Last charging outputs in Fortran order: zd(ncells,N), ni(ncells), ne(ncells), psi_old(ncells),
+ * eta(ncells,3) = (eta_o, eta_H, eta_a), gamma_d(ncells,N) (the last two with
+ * SHARK_CHARGE_RESISTIVITIES).  Any pointer may be NULL. */
+int32_t shark_gpu_download_charge(shark_gpu_ctx* ctx, double* zd, double* ni, double* ne, double* psi,
+                                  double* eta, double* gamma_d);
+
 int32_t shark_gpu_free(shark_gpu_ctx* ctx);
 
 #ifdef __cplusplus

@@ -48,7 +48,10 @@ def lib():
                             ("oracle_apply_boundaries", []), ("oracle_ctoprim", []),
                             ("oracle_courant", [D]), ("oracle_set_dt", [C.c_double]),
                             ("oracle_dust_drag", [C.c_double]), ("oracle_compute_tstop", []),
-                            ("oracle_get_tstop", [D]), ("oracle_fargo", [])]:
+                            ("oracle_get_tstop", [D]), ("oracle_fargo", []),
+                            ("oracle_charge", [D, C.POINTER(C.c_int32)]),
+                            ("oracle_get_charge", [D, D, D, D, D, D]),
+                            ("oracle_reset_charge", []), ("oracle_charge_psi0", [D])]:
             f = getattr(L, name)
             f.restype = C.c_int32
             f.argtypes = [P] + extra
@@ -168,6 +171,32 @@ class Oracle:
 
     def apply_boundaries(self):
         self._chk(lib().oracle_apply_boundaries(self._h), "oracle_apply_boundaries")
+
+    def charge(self, seed=None):
+        """charge (ionisation.f90:4-214) on the current state; returns the Newton iteration
+        count per cell.  ``seed`` (ncells) overrides the start point where nonzero."""
+        it = np.zeros(self.ncells, dtype=np.int32)
+        sd = None if seed is None else _dptr(np.ascontiguousarray(seed, dtype=np.float64))
+        self._keep = seed
+        self._chk(lib().oracle_charge(self._h, sd, it.ctypes.data_as(C.POINTER(C.c_int32))), "oracle_charge")
+        return it
+
+    def get_charge(self):
+        """dict of zd (N, ncells), ni, ne, psi, eta (3, ncells: o, H, a), gamma_d (N, ncells)."""
+        N, nc = self.cfg.ndust, self.ncells
+        zd, gd = np.empty(N * nc), np.empty(N * nc)
+        ni, ne, psi, eta = np.empty(nc), np.empty(nc), np.empty(nc), np.empty(3 * nc)
+        self._chk(lib().oracle_get_charge(self._h, _dptr(zd), _dptr(ni), _dptr(ne), _dptr(psi), _dptr(eta),
+                                          _dptr(gd)), "oracle_get_charge")
+        return dict(zd=zd.reshape(N, nc), ni=ni, ne=ne, psi=psi, eta=eta.reshape(3, nc), gamma_d=gd.reshape(N, nc))
+
+    def reset_charge(self):
+        self._chk(lib().oracle_reset_charge(self._h), "oracle_reset_charge")
+
+    def charge_psi0(self):
+        v = C.c_double(0)
+        self._chk(lib().oracle_charge_psi0(self._h, C.byref(v)), "oracle_charge_psi0")
+        return v.value
 
     def fargo(self):
         """fargo_scheme alone on the current state with the dt last set (FARGO configs)."""

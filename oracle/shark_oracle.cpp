@@ -52,6 +52,11 @@ struct oracle_state {
     std::vector<double> force, force_dust, tstop, sdust, epsilondust;
     std::vector<double> u_init;     // disk_polar: uprim_condinit (state of the first upload / setup)
     std::vector<double> fargo_v;    // fargo_velocity(ncells)
+    // charging (ionisation_commons.f90): per cell psi_old, ni, ne, resistivities, Newton
+    // iteration count; per cell and species zd, gamma_d (species-major like sdust)
+    std::vector<double> psi_old, ni, ne, eta_o, eta_h, eta_a, zd, gamma_d;
+    std::vector<int32_t> chg_iters;
+    std::vector<double> chg_seed;   // optional Newton start per cell (0 = none)
     double dt = 0.0, time = 0.0;
 
     // setup-derived scalars
@@ -396,6 +401,9 @@ void compute_tstop(oracle_state& s) {
                 case SHARK_SETUP_SI:          // SI/setup.f90:389-397 (constant, precomputed on host)
                     ts = s.cfg.dust_tstop[k];
                     break;
+                case SHARK_SETUP_DUSTYTURB:   // dustyTurb/setup.f90:456
+                    ts = s.cfg.dust_stokes[k] * s.box_l * s.cfg.turb_rho0 / s.cs[i] / s.Q(i, s.irho);
+                    break;
                 case SHARK_SETUP_DISK_POLAR: {   // disk_polar/setup.f90:425-451, Epstein with Sigma/(sqrt(2 pi) H)
                     const double H = disk_h(s.cfg, s.radii_c[i]) * s.radii_c[i];
                     ts = std::sqrt(pi * s.cfg.gamma / 8.0) * (s.cfg.rhograin) * s.SDUST(i, k) /
@@ -408,6 +416,221 @@ void compute_tstop(oracle_state& s) {
                     break;
             }
             s.TSTOP(i, k) = ts;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Charging: Marchand et al. (2021) Newton on the reduced grain potential psi
+// (src/chemistry/ionisation.f90:4-214).  Constants of src/commons/phys_const.f90:5-13.
+// Fortran x**2., x**2.0 and x**3. are evaluated as products, x**4.0 as (x*x)*(x*x); SUM() in
+// index order.  The state -> (nH, T, zeta, n_k, a_k) map is per setup:
+//   dustyTurb (cgs code units): nH = rho unit_d/(mu_gas mH), T = T_cloud, zeta = chg_x,
+//     n_k = rho_k unit_d/(m_k unit_m), m_k = 4/3 pi rhograin s_k^3 (mrn_distri, dust_init.f90:192);
+//   polar disk (2D surface densities): the same on the midplane densities Sigma/(sqrt(2 pi) H),
+//     T from the isothermal sound speed through cs_eos (disk_polar/eos.f90), zeta =
+//     chg_x exp(-Sigma unit_d unit_l/chg_sigma_att).  The reference's disk has no temperature
+//     (its barotrop is empty) and a unit_nH without mu_gas mH; this is the re-specified form.
+// ---------------------------------------------------------------------------------------------
+namespace phys {
+constexpr double e_el = 4.8e-10, m_el = 9.109e-28, clight = 3e10, mH = 1.67e-24, kB = 1.38e-16;
+}
+double unit_or_1(double u) { return u != 0.0 ? u : 1.0; }
+double F43() { return (double)(4.0f / 3.0f); }   // Fortran 4./3. is a default-REAL quotient
+
+// Start point of the reference (ionisation.f90:33-52): Newton on the dust-free balance, from -2.5.
+double charge_psi0(double thetai) {
+    const double epsone = 0.99999;
+    double psi0 = -2.5, conv = 1e4;
+    int n = 0;
+    while (conv > 1e-6 && n < 1000) {
+        double psi = psi0;
+        const double f = (1.0 - psi) / (epsone * thetai) * std::exp(-psi) - 1.0;
+        const double df = -std::exp(-psi) / (epsone * thetai) - (1.0 - psi) / (epsone * thetai) * std::exp(-psi);
+        psi = psi - f / df;
+        conv = std::fabs(f);
+        n = n + 1;
+        psi0 = psi;
+    }
+    return psi0;
+}
+
+struct ChargeCell {
+    double nH, T, x, rho_cgs;
+    std::vector<double> nk, lk, mk_cgs;
+};
+
+void charge_inputs(oracle_state& s, int64_t i, ChargeCell& c) {
+    const shark_gpu_config& g = s.cfg;
+    const double ul = unit_or_1(g.unit_l), ud = unit_or_1(g.unit_d), ut = unit_or_1(g.unit_t);
+    const double um = ul * ul * ul * ud, uv = ul / ut, unH = ud / (g.mu_gas * phys::mH);
+    const int N = s.ndust;
+    double hs = 1.0;                                    // column-to-midplane factor
+    if (g.setup == SHARK_SETUP_DISK_POLAR) hs = std::sqrt(2.0 * pi) * (disk_h(g, s.radii_c[i]) * s.radii_c[i]);
+    const double rho = s.U(i, s.irho) / hs;
+    c.rho_cgs = rho * ud;
+    c.nH = rho * unH;
+    if (g.setup == SHARK_SETUP_DISK_POLAR) {
+        const double csc = s.cs[i] * uv;
+        c.T = g.mu_gas * phys::mH * (csc * csc) / (g.gamma * phys::kB);
+        c.x = g.chg_sigma_att > 0.0 ? g.chg_x * std::exp(-(s.U(i, s.irho) * ud * ul) / g.chg_sigma_att) : g.chg_x;
+    } else {
+        c.T = g.T_cloud;
+        c.x = g.chg_x;
+    }
+    c.nk.resize(N); c.lk.resize(N); c.mk_cgs.resize(N);
+    for (int k = 0; k < N; ++k) {
+        const double sk = s.cfg.dust_size[k];
+        const double mk = F43() * pi * g.rhograin * (sk * sk * sk);   // code mass (mrn_distri)
+        c.lk[k] = sk * ul;
+        c.mk_cgs[k] = mk * um;
+        c.nk[k] = (s.U(i, s.irhod[k]) / hs) * ud / (mk * um);
+    }
+}
+
+// One cell of `charge` (ionisation.f90:60-206).  psi_start: psi_old(i) or 0.  Returns the
+// iteration count; writes zd (N), ni, ne, psi_old and, with res, eta_o/h/a and gamma_d (N).
+int charge_cell(const shark_gpu_config& g, const ChargeCell& c, double psi0, double psi_start,
+                double* zd, double& ni_o, double& ne_o, double& psi_out, bool res,
+                double& eta_o, double& eta_h, double& eta_a, double* gamma_d) {
+    const int N = (int)c.nk.size();
+    const double mH = phys::mH, kB = phys::kB, e_el = phys::e_el, m_el = phys::m_el;
+    const double thetai = g.chg_stick_el * std::sqrt(g.chg_mu_ions * mH / m_el);
+    const double epsone = 0.99999, T = c.T, x = c.x, nH = c.nH;
+    std::vector<double> tau(N), alpha(N), l2(N);
+    const double sigmav_ie = (2e-7) / std::sqrt(T / 300.0);
+    for (int k = 0; k < N; ++k) {
+        tau[k] = c.lk[k] * kB * T / (e_el * e_el);
+        alpha[k] = std::sqrt(8.0 / (pi * tau[k]));
+        l2[k] = c.lk[k] * c.lk[k];
+    }
+    const double vi = std::sqrt(8.0 * kB * T / (pi * g.chg_mu_ions * mH));
+    const double th2 = thetai * thetai, th3 = thetai * thetai * thetai;
+    double conv = 1e4, psi = psi0;
+    int niter = 0;
+    if (psi_start != 0.0) psi = psi_start;
+    int lowT = 0;
+    double eps_psi, n_i = 0.0, fpsi;
+    while (conv > g.chg_eps && niter < g.chg_nitermax) {
+        eps_psi = (1.0 - psi) / thetai * std::exp(-psi);
+        const double et = eps_psi * thetai;
+        const double et2 = et * et;
+        n_i = 0.0;
+        for (int k = 0; k < N; ++k)
+            n_i = n_i + (-(psi * tau[k] + (1.0 - et2) / (1.0 + et * alpha[k] + et2)) * c.nk[k] / (1.0 - eps_psi));
+        double S1 = 0.0;
+        for (int k = 0; k < N; ++k)
+            S1 = S1 + c.nk[k] * pi * l2[k] * ((1.0 - psi) + (2.0 / tau[k]) * (et2 + et) / (1.0 + et * alpha[k] + et2));
+        fpsi = sigmav_ie * eps_psi * (n_i * n_i) / (x * nH) + n_i * vi / (x * nH) * (S1) - 1.0;
+        const double D = (-eps_psi * (2.0 - psi) / (1.0 - psi));
+        double S2 = 0.0, S3 = 0.0, S4 = 0.0, S5 = 0.0, S6 = 0.0;
+        for (int k = 0; k < N; ++k) {
+            const double den = 1.0 + et * alpha[k] + et2;
+            S2 = S2 + c.nk[k] * (-(et2 * et2) + (4.0 * th2 - th3 * alpha[k]) * (eps_psi * eps_psi) +
+                                 (2.0 * thetai * alpha[k] - 4.0 * th2) * eps_psi + 1.0 - thetai * alpha[k]) / (den * den);
+            S3 = S3 + c.nk[k] * tau[k];
+            S4 = S4 + c.nk[k] * pi * l2[k] / (tau[k] * den);
+            S5 = S5 + c.nk[k] * pi * l2[k] * (2.0 * eps_psi * th2 + thetai * alpha[k]) / (tau[k] * (den * den));
+            S6 = S6 + c.nk[k] * pi * l2[k];
+        }
+        const double om = 1.0 - eps_psi;
+        const double dni = -1.0 / (om * om) * (D) * (S2) - (psi / om * (D) + 1.0) * S3 / om;
+        const double dfdpsi =
+            sigmav_ie * n_i / (x * nH) * (n_i * (D) + 2.0 * eps_psi * dni) +
+            2.0 * n_i * vi / (x * nH) * (et2 + et) *
+                ((dni / n_i + (D) * (2.0 * et + 1.0) / (eps_psi * (1.0 + et))) * (S4) + ((D) * S5)) +
+            n_i * vi / (x * nH) * (dni / n_i * (1.0 - psi) - 1.0) * (S6);
+        psi = psi - fpsi / dfdpsi;
+        if (psi < psi0) {
+            psi = psi0 * 0.9999999;
+            lowT = 1;
+        } else if (psi > 0.0) {
+            psi = -1e-5;
+        }
+        conv = std::fabs(fpsi);   // the reference's interim values of conv are overwritten here
+        niter = niter + 1;
+    }
+    eps_psi = (1.0 - psi) / thetai * std::exp(-psi);
+    if (lowT > 0) eps_psi = epsone;
+    double nsum = 0.0;
+    for (int k = 0; k < N; ++k) {
+        zd[k] = psi * tau[k] + (1.0 - (eps_psi * eps_psi) * th2) / (1.0 + eps_psi * thetai * alpha[k] + (eps_psi * eps_psi) * th2);
+        nsum = nsum - zd[k] * c.nk[k] / (1.0 - eps_psi);
+        if (lowT > 0) nsum = std::sqrt(eps_psi * x * nH / sigmav_ie);
+    }
+    ni_o = nsum;
+    ne_o = eps_psi * ni_o;
+    psi_out = lowT > 0 ? psi0 : psi;
+    if (res) {
+        // resistivities (ionisation.f90:163-206); the grain stopping time uses the gas density
+        // and cs_eos(T) in cgs (the reference multiplies cs_eos, already cgs, by unit_v)
+        const double B = g.chg_B0 * std::sqrt(nH / 1e4);
+        const double cs_T = std::sqrt(g.gamma * kB * T / (g.mu_gas * mH));
+        const double mu_i = 2.0 * mH * g.chg_mu_ions * mH / (2.0 * mH + g.chg_mu_ions * mH);
+        const double mu_e = 2.0 * mH * m_el / (m_el + 2.0 * mH);
+        const double vrms_i = std::sqrt(8.0 * kB * T / (pi * mu_i)) * 1e-5;
+        const double vrms_el = std::sqrt(8.0 * kB * T / (pi * mu_e)) * 1e-5;
+        const double sigmav_el = 3.16e-11 * std::pow(vrms_el, 1.3);
+        const double sigmav_ions = 2.4e-9 * std::pow(vrms_i, 0.6);
+        const double as_He_ions = (double)1.14f, as_He_el = (double)1.16f;   // REAL*4 literals
+        const double t_sel = 1.0 / as_He_el * ((m_el + 2.0 * mH) / (2.0 * mH)) / sigmav_el / nH;
+        const double t_sions = 1.0 / as_He_ions * ((g.chg_mu_ions * mH + 2.0 * mH) / (2.0 * mH)) / sigmav_ions / nH;
+        const double sig_el = (ne_o) * (e_el * e_el) * t_sel / m_el;
+        const double sig_i = (ni_o) * (e_el * e_el) * t_sions / (g.chg_mu_ions * mH);
+        const double om_el = -e_el * B / phys::clight / m_el;
+        const double om_i = e_el * B / phys::clight / (g.chg_mu_ions * mH);
+        double so = 0.0, sp = 0.0, sh = 0.0;
+        for (int k = 0; k < N; ++k) {
+            const double t_sd = std::sqrt(pi * g.gamma / 8.0) * (g.rhograin * unit_or_1(g.unit_d)) * (c.lk[k]) / (c.rho_cgs * cs_T);
+            const double sd = c.nk[k] * ((zd[k] * e_el) * (zd[k] * e_el)) * t_sd / (c.mk_cgs[k]);
+            const double omd = zd[k] * e_el * B / phys::clight / (c.mk_cgs[k]);
+            so = so + sd;
+            sp = sp + sd / (1.0 + (omd * t_sd) * (omd * t_sd));
+            sh = sh + sd * (omd * t_sd) / (1.0 + (omd * t_sd) * (omd * t_sd));
+            gamma_d[k] = t_sd * omd;
+        }
+        const double sigma_o = so + sig_i + sig_el;
+        const double sigma_p = sig_i / (1.0 + (om_i * t_sions) * (om_i * t_sions)) +
+                               sig_el / (1.0 + (om_el * t_sel) * (om_el * t_sel)) + sp;
+        const double sigma_h = -sig_i * (om_i * t_sions) / (1.0 + (om_i * t_sions) * (om_i * t_sions)) -
+                               sig_el * (om_el * t_sel) / (1.0 + (om_el * t_sel) * (om_el * t_sel)) - sh;
+        eta_o = 1.0 / sigma_o;
+        eta_h = sigma_h / (sigma_p * 2. + sigma_h * sigma_h);   // as written in ionisation.f90:200
+        eta_a = sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - 1.0 / sigma_o;
+    }
+    return niter;
+}
+
+// charge over every cell, ghosts included (the reference's active-cell test is commented out)
+void charge(oracle_state& s) {
+    const shark_gpu_config& g = s.cfg;
+    const int N = s.ndust;
+    const double thetai = g.chg_stick_el * std::sqrt(g.chg_mu_ions * phys::mH / phys::m_el);
+    const double psi0 = charge_psi0(thetai);
+    const bool res = (g.chg_mode & SHARK_CHARGE_RESISTIVITIES) != 0;
+    const size_t nc = (size_t)s.ncells;
+    if (s.psi_old.size() != nc) {
+        s.psi_old.assign(nc, 0.0); s.ni.assign(nc, 0.0); s.ne.assign(nc, 0.0);
+        s.eta_o.assign(nc, 0.0); s.eta_h.assign(nc, 0.0); s.eta_a.assign(nc, 0.0);
+        s.zd.assign(nc * N, 0.0); s.gamma_d.assign(nc * N, 0.0); s.chg_iters.assign(nc, 0);
+    }
+#pragma omp parallel
+    {
+        ChargeCell c;
+        std::vector<double> zd(N), gd(N);
+#pragma omp for schedule(dynamic, 256)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            charge_inputs(s, i, c);
+            double start = s.psi_old[i];
+            if (!s.chg_seed.empty() && s.chg_seed[i] != 0.0) start = s.chg_seed[i];
+            double psi;
+            s.chg_iters[i] = charge_cell(g, c, psi0, start, zd.data(), s.ni[i], s.ne[i], psi, res,
+                                         s.eta_o[i], s.eta_h[i], s.eta_a[i], gd.data());
+            s.psi_old[i] = psi;
+            for (int k = 0; k < N; ++k) {
+                s.zd[(size_t)k * nc + i] = zd[k];
+                if (res) s.gamma_d[(size_t)k * nc + i] = gd[k];
+            }
         }
     }
 }
@@ -1102,6 +1325,7 @@ void solve(oracle_state& s) {
         for (int k = 0; k < s.ndust; ++k)
             for (int64_t i = 0; i < s.ncells; ++i) s.EPSD(i, k) = s.Q(i, s.irhod[k]) / s.Q(i, s.irho);
         compute_tstop(s);
+        if (s.flag(SHARK_FLAG_CHARGING)) charge(s);
     }
     courant(s);
     if (fk) kick(s, 1.0);
@@ -1436,6 +1660,40 @@ int32_t oracle_totals(const oracle_state* s, double* out) {
 }
 
 int32_t oracle_apply_boundaries(oracle_state* s) { if (!s) return SHARK_ERR_INVALID_ARG; apply_boundaries(*s); return SHARK_OK; }
+int32_t oracle_charge(oracle_state* s, const double* seed, int32_t* iters) {
+    if (!s || s->ndust == 0) return SHARK_ERR_INVALID_ARG;
+    if (seed) s->chg_seed.assign(seed, seed + s->ncells);
+    charge(*s);
+    s->chg_seed.clear();
+    if (iters) std::memcpy(iters, s->chg_iters.data(), s->chg_iters.size() * sizeof(int32_t));
+    return SHARK_OK;
+}
+int32_t oracle_get_charge(const oracle_state* s, double* zd, double* ni, double* ne, double* psi,
+                          double* eta /* 3 x ncells: o, h, a */, double* gamma_d) {
+    if (!s || s->psi_old.empty()) return SHARK_ERR_STATE;
+    const size_t nc = (size_t)s->ncells, nd = nc * s->ndust;
+    if (zd) std::memcpy(zd, s->zd.data(), nd * sizeof(double));
+    if (ni) std::memcpy(ni, s->ni.data(), nc * sizeof(double));
+    if (ne) std::memcpy(ne, s->ne.data(), nc * sizeof(double));
+    if (psi) std::memcpy(psi, s->psi_old.data(), nc * sizeof(double));
+    if (eta) {
+        std::memcpy(eta, s->eta_o.data(), nc * sizeof(double));
+        std::memcpy(eta + nc, s->eta_h.data(), nc * sizeof(double));
+        std::memcpy(eta + 2 * nc, s->eta_a.data(), nc * sizeof(double));
+    }
+    if (gamma_d) std::memcpy(gamma_d, s->gamma_d.data(), nd * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_reset_charge(oracle_state* s) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    std::fill(s->psi_old.begin(), s->psi_old.end(), 0.0);
+    return SHARK_OK;
+}
+int32_t oracle_charge_psi0(const oracle_state* s, double* psi0) {
+    if (!s || !psi0) return SHARK_ERR_INVALID_ARG;
+    *psi0 = charge_psi0(s->cfg.chg_stick_el * std::sqrt(s->cfg.chg_mu_ions * phys::mH / phys::m_el));
+    return SHARK_OK;
+}
 int32_t oracle_fargo(oracle_state* s) {
     if (!s || !s->flag(SHARK_FLAG_FARGO)) return SHARK_ERR_INVALID_ARG;
     fargo_scheme(*s);

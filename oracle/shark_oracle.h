@@ -61,6 +61,13 @@ int32_t oracle_dust_drag(oracle_state* s, double coeffdt);
 int32_t oracle_compute_tstop(oracle_state* s);
 int32_t oracle_get_tstop(const oracle_state* s, double* tstop); /* ncells*ndust */
 int32_t oracle_fargo(oracle_state* s);   /* fargo_scheme alone with the dt last set (needs FARGO) */
+/* charge (ionisation.f90:4-214) on the current state; seed (ncells, nullable) overrides the start
+ * point where nonzero; iters (ncells, nullable) receives the Newton iteration counts. */
+int32_t oracle_charge(oracle_state* s, const double* seed, int32_t* iters);
+int32_t oracle_get_charge(const oracle_state* s, double* zd, double* ni, double* ne, double* psi,
+                          double* eta, double* gamma_d);
+int32_t oracle_reset_charge(oracle_state* s);   /* psi_old = 0: the next call starts cold */
+int32_t oracle_charge_psi0(const oracle_state* s, double* psi0);
 
 int32_t oracle_set_threads(int32_t nthreads);
 

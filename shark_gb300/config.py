@@ -37,6 +37,10 @@ FLAG_CHARGING = 0x20
 FLAG_VISCOSITY = 0x40
 FLAG_STATIC = 0x80
 
+CHARGE_RESISTIVITIES = 0x1
+CHARGE_ANALYTICAL = 0x2
+CHARGE_MLP_SEED = 0x4
+
 PREC_FP64 = 0
 PREC_MIXED = 1
 
@@ -63,7 +67,12 @@ class SharkConfig(C.Structure):
         ("si_rho_init", _D), ("si_hoverr", _D),
         ("disk_mstar", _D), ("disk_hoverr", _D), ("disk_sigma0", _D), ("disk_r0", _D),
         ("disk_rout", _D), ("disk_r_relax", _D), ("disk_n_rel", _D), ("disk_temp_slope", _D),
-        ("reserved", _D * 45),
+        ("unit_l", _D), ("unit_d", _D), ("unit_t", _D), ("mu_gas", _D), ("T_cloud", _D),
+        ("chg_x", _D), ("chg_sigma_att", _D), ("chg_mu_ions", _D), ("chg_stick_el", _D),
+        ("chg_eps", _D), ("chg_B0", _D), ("chg_nitermax", _I), ("chg_mode", _I),
+        ("turb_rho0", _D), ("turb_mach", _D), ("turb_tcorr", _D), ("turb_kmin", _I), ("turb_kmax", _I),
+        ("turb_seed", _I), ("pad2", _I),
+        ("reserved", _D * 28),
         ("dx", _P), ("surf", _P), ("vol", _P), ("radii_c", _P), ("position", _P), ("cs", _P),
     ]
 
@@ -115,4 +124,14 @@ def default_config():
     c.box_l_y = 1.0
     c.dust_ratio_min = 1e-11
     c.rhograin = 2.7
+    c.unit_l = c.unit_d = c.unit_t = 1.0
+    c.mu_gas = 2.31                           # setups' setup_commons.f90
+    c.T_cloud = 10.0                          # dustyTurb/setup_commons.f90:18
+    c.chg_x = 5e-17                           # ionisation_commons.f90:73-77
+    c.chg_mu_ions = 25.0
+    c.chg_stick_el = 0.5
+    c.chg_eps = 1e-6
+    c.chg_nitermax = 1000
+    c.chg_B0 = 3e-5
+    c.chg_mode = CHARGE_RESISTIVITIES         # res_Marchand = .true.
     return c

@@ -5,6 +5,7 @@
 #include "launch.h"
 #include "step_kernels.cuh"
 #include "fargo.cuh"
+#include "charge.cuh"
 
 #include <type_traits>
 
@@ -30,7 +31,7 @@ static KParams<R> make_params(const DeviceView& v) {
     p.dx1d = v.md[0]; p.dx2d = v.md[1]; p.radcd = v.md[2]; p.xposd = v.md[3]; p.csd = v.md[4];
     p.fgravd = v.md[5]; p.treld = v.md[6]; p.hsd = v.md[7]; p.vkd = v.md[8];
     p.u_init = (const R*)v.u_init;
-    p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize;
+    p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize; p.dstokes = v.dstokes; p.turb_rho0 = c.turb_rho0;
     p.dt = nullptr; p.dt_next = nullptr; p.status = v.status; p.coef = v.coef;
     p.u_cur = (const R*)v.u[v.cur];
     p.u_next = (R*)v.u[(v.cur + 1) % v.nbuf];
@@ -157,6 +158,7 @@ cudaError_t launch_step(const DeviceView& v, int slot) {
     k_prepare_step<<<1, SHARK_MAX_DUST, 0, v.stream>>>(p.dt_next, p.dt, p.dtstop, p.ndust,
                                                       (p.setup == SHARK_SETUP_SI && std::is_same<R, float>::value) ? 1 : 0,
                                                       p.coef);
+    if (v.chg.on && (e = launch_charge<R>(v)) != cudaSuccess) return e;   // charge: solve.f90:36-42
     if (v.time_kernels) cudaEventRecord(v.ev[1], v.stream);
     e = (v.ndim == 2) ? strip_launch<R>(v, p) : flux_launch<R, 1>(p, v.stream);
     if (e != cudaSuccess) return e;
@@ -220,6 +222,35 @@ cudaError_t launch_totals(const DeviceView& v, double* part_dev, int nblocks, do
     return cudaGetLastError();
 }
 
+template <typename R>
+cudaError_t launch_charge(const DeviceView& v) {
+    const ChargeView& c = v.chg;
+    ChargeParams<R> q;
+    q.u = (const R*)v.u[v.cur];
+    q.plane = v.plane; q.pitch = v.pitch; q.nx_max = v.nx_max; q.ny_max = v.ny_max;
+    q.ndust = v.ndust; q.nvar = v.nvar;
+    q.t_per_col = c.t_per_col; q.res = c.res; q.use_seed = c.use_seed;
+    q.hs = c.hs; q.trow = c.trow; q.tau = c.tau; q.alpha = c.alpha; q.l2 = c.l2; q.mkum = c.mkum; q.ak = c.ak;
+    q.unH = c.unH; q.ud = c.ud; q.ul = c.ul; q.x0 = c.x0; q.sig_att = c.sig_att;
+    q.thetai = c.thetai; q.th2 = c.th2; q.th3 = c.th3; q.psi0 = c.psi0; q.eps = c.eps; q.B0 = c.B0;
+    q.mu_ions = c.mu_ions; q.nitermax = c.nitermax;
+    q.psi_old = c.psi_old; q.zd = (R*)c.zd; q.ni = (R*)c.ni; q.ne = (R*)c.ne; q.eta = (R*)c.eta;
+    q.gamma_d = (R*)c.gamma_d; q.seed = c.seed; q.hist = c.hist;
+    cudaError_t e = cudaMemsetAsync(c.hist, 0, (CHARGE_HIST + 2) * sizeof(unsigned long long), v.stream);
+    if (e != cudaSuccess) return e;
+    const long long n = (long long)v.nx_max * v.ny_max;
+    k_charge<R><<<(unsigned)((n + 127) / 128), 128, 0, v.stream>>>(q);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int count, double* dst_dev) {
+    const long long n = (long long)v.nx_max * v.ny_max * count;
+    k_to_fortran<R><<<(unsigned)((n + 255) / 256), 256, 0, v.stream>>>((const R*)src, dst_dev, v.nx_max, v.ny_max,
+                                                                        v.pitch, v.plane, count);
+    return cudaGetLastError();
+}
+
 #define SHARK_INSTANTIATE(R)                                                                       \
     template cudaError_t launch_step<R>(const DeviceView&, int);                                   \
     template cudaError_t launch_courant<R>(const DeviceView&, int);                                \
@@ -227,6 +258,8 @@ cudaError_t launch_totals(const DeviceView& v, double* part_dev, int nblocks, do
     template cudaError_t launch_from_fortran<R>(const DeviceView&, const double*, void*);          \
     template cudaError_t launch_to_fortran<R>(const DeviceView&, const void*, double*);            \
     template cudaError_t launch_ctoprim<R>(const DeviceView&, double*, double*);                   \
-    template cudaError_t launch_totals<R>(const DeviceView&, double*, int, double*);
+    template cudaError_t launch_totals<R>(const DeviceView&, double*, int, double*);               \
+    template cudaError_t launch_charge<R>(const DeviceView&);                                      \
+    template cudaError_t launch_planes_to_fortran<R>(const DeviceView&, const void*, int, double*);
 
 }  // namespace shark

@@ -8,6 +8,19 @@
 
 namespace shark {
 
+// Charging (K5) tables, outputs and constants; see charge.cuh.
+struct ChargeView {
+    bool on;
+    int res, use_seed, t_per_col;
+    const double *hs, *trow, *tau, *alpha, *l2, *mkum, *ak;
+    double unH, ud, ul, x0, sig_att, thetai, th2, th3, psi0, eps, B0, mu_ions;
+    int nitermax;
+    double* psi_old;                        // FP64 [plane]
+    void *zd, *ni, *ne, *eta, *gamma_d;     // state precision, plane layout
+    const float* seed;                      // network start points [plane] or nullptr
+    unsigned long long* hist;               // [CHARGE_HIST + 2]
+};
+
 // Device-side view of a context, shared by both precisions.  Metric arrays come in two copies:
 // `m` in the state precision (flux/update) and `md` in FP64 (drag, courant).
 struct DeviceView {
@@ -27,6 +40,7 @@ struct DeviceView {
     const double* dK;           // per-species constants (device)
     const double* dtstop;
     const double* dsize;
+    const double* dstokes;
     double* dt_slots;           // [2] dt of step n lives in slot n % 2
     unsigned int* status;       // OR of SHARK_STATUS_* bits
     float* coef;                // [2*SHARK_MAX_DUST] per-step drag coefficients (mixed path)
@@ -35,6 +49,7 @@ struct DeviceView {
     cudaEvent_t fork, join;
     cudaEvent_t ev[4];          // timing: before boundaries, before flux, before finalize, end
     bool time_kernels;
+    ChargeView chg;
 };
 
 // Record `msg` as this thread's shark_gpu_last_error text and return `code`.
@@ -54,5 +69,9 @@ template <typename R> cudaError_t launch_from_fortran(const DeviceView& v, const
 template <typename R> cudaError_t launch_to_fortran(const DeviceView& v, const void* src, double* dst_dev);
 template <typename R> cudaError_t launch_ctoprim(const DeviceView& v, double* q_dev, double* cs_dev);
 template <typename R> cudaError_t launch_totals(const DeviceView& v, double* part_dev, int nblocks, double* out_dev);
+// charging (K5) on the current state; resets the iteration histogram first
+template <typename R> cudaError_t launch_charge(const DeviceView& v);
+// plane-layout array of `count` planes -> Fortran-order FP64 (ncells per plane)
+template <typename R> cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int count, double* dst_dev);
 
 }  // namespace shark

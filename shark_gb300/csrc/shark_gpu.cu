@@ -73,7 +73,7 @@ struct shark_gpu_ctx {
     bool have_uinit = false;
     void* metrics = nullptr;         // 13 arrays x nx_max in state precision
     double* metrics_d = nullptr;     // 9 arrays x nx_max FP64
-    double* species = nullptr;       // dK | dtstop | dsize (3 x SHARK_MAX_DUST)
+    double* species = nullptr;       // dK | dtstop | dsize | dstokes (4 x SHARK_MAX_DUST)
     double* dt_slots = nullptr;      // [2]
     unsigned int* status = nullptr;
     float* coef = nullptr;           // per-step drag coefficients
@@ -86,6 +86,12 @@ struct shark_gpu_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // charging: tables (FP64) and outputs
+    double* chg_tables = nullptr;
+    double* chg_psi = nullptr;
+    void* chg_out = nullptr;         // zd | ni | ne | eta | gamma_d in state precision
+    unsigned long long* chg_hist = nullptr;
+    float* chg_seed = nullptr;       // network start points (plane layout)
     long long nstep = 0;             // steps launched since upload
     bool uploaded = false;
     bool pending_read[2] = {false, false};
@@ -244,12 +250,33 @@ int32_t validate(const shark_gpu_config* c) {
     if (c->slope_type < 0 || c->slope_type > 3) return fail(SHARK_ERR_INVALID_ARG, "unknown slope limiter");
     if (c->precision != SHARK_PREC_FP64 && c->precision != SHARK_PREC_MIXED)
         return fail(SHARK_ERR_INVALID_ARG, "precision must be FP64 or MIXED");
-    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_DISK_POLAR)
+    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_DUSTYTURB)
         return fail(SHARK_ERR_UNSUPPORTED, "setup %d has no device hooks in this build", c->setup);
     const int f = c->flags;
     if (f & SHARK_FLAG_VISCOSITY) return fail(SHARK_ERR_UNSUPPORTED, "viscosity is not built");
-    if (f & (SHARK_FLAG_GROWTH | SHARK_FLAG_CHARGING))
-        return fail(SHARK_ERR_UNSUPPORTED, "growth/charging are not enabled in this build");
+    if (f & SHARK_FLAG_GROWTH) return fail(SHARK_ERR_UNSUPPORTED, "growth is not enabled in this build");
+    if (f & SHARK_FLAG_CHARGING) {
+        if (c->ndust < 1) return fail(SHARK_ERR_INVALID_ARG, "charging needs dust species");
+        if (c->setup != SHARK_SETUP_DISK_POLAR && c->setup != SHARK_SETUP_DUSTYTURB)
+            return fail(SHARK_ERR_UNSUPPORTED, "charging needs the cgs map of the polar disk or dustyTurb setup");
+        if (c->chg_mode & SHARK_CHARGE_ANALYTICAL)
+            return fail(SHARK_ERR_UNSUPPORTED, "analytical (Fujii) charging is not built");
+        if (!(c->chg_x > 0.0) || !(c->chg_mu_ions > 0.0) || !(c->chg_stick_el > 0.0) || !(c->chg_eps > 0.0) ||
+            c->chg_nitermax < 1 || !(c->mu_gas > 0.0) || !(c->rhograin > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "charging parameters must be positive");
+        if (c->setup == SHARK_SETUP_DUSTYTURB && !(c->T_cloud > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "T_cloud must be > 0");
+        for (int k = 0; k < c->ndust; ++k)
+            if (!(c->dust_size[k] > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "dust_size[%d] must be > 0", k);
+    }
+    if (c->setup == SHARK_SETUP_DUSTYTURB) {
+        if (c->geom != 0) return fail(SHARK_ERR_UNSUPPORTED, "dustyTurb is Cartesian");
+        if (c->iso_cs != 1) return fail(SHARK_ERR_UNSUPPORTED, "dustyTurb is isothermal (iso_cs 1)");
+        if ((f & SHARK_FLAG_DRAG) && c->ndust > 0 && !(c->turb_rho0 > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "turb_rho0 must be > 0");
+        for (int k = 0; k < c->ndust; ++k)
+            if ((f & SHARK_FLAG_DRAG) && !(c->dust_stokes[k] > 0.0))
+                return fail(SHARK_ERR_INVALID_ARG, "dust_stokes[%d] must be > 0", k);
+    }
     if (c->setup == SHARK_SETUP_DISK_POLAR) {
         if (c->geom != 2) return fail(SHARK_ERR_UNSUPPORTED, "the polar disk needs geom 2");
         if (c->iso_cs != 1) return fail(SHARK_ERR_UNSUPPORTED, "the polar disk is isothermal (iso_cs 1)");
@@ -286,6 +313,99 @@ int32_t validate(const shark_gpu_config* c) {
     return SHARK_OK;
 }
 
+// ---- charging tables (src/chemistry/ionisation.f90:4-214, phys_const.f90:5-13) ----------------
+constexpr double kEl = 4.8e-10, kMel = 9.109e-28, kMH = 1.67e-24, kKB = 1.38e-16;
+double unit1(double u) { return u != 0.0 ? u : 1.0; }
+
+// start point of the reference's Newton (ionisation.f90:33-52)
+double charge_psi0(double thetai) {
+    const double epsone = 0.99999;
+    double psi0 = -2.5, conv = 1e4;
+    int n = 0;
+    while (conv > 1e-6 && n < 1000) {
+        double psi = psi0;
+        const double f = (1.0 - psi) / (epsone * thetai) * std::exp(-psi) - 1.0;
+        const double df = -std::exp(-psi) / (epsone * thetai) - (1.0 - psi) / (epsone * thetai) * std::exp(-psi);
+        psi = psi - f / df;
+        conv = std::fabs(f);
+        n = n + 1;
+        psi0 = psi;
+    }
+    return psi0;
+}
+
+// Host tables of the charging kernel: [hs | trow | tau | alpha | l2 | mkum | ak] and the
+// constants of the view.  Temperature rows: one per column for the polar disk (T from the
+// isothermal cs through cs_eos), one row (T_cloud) for dustyTurb.
+void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_max, std::vector<double>& h,
+                         shark::ChargeView& cv, size_t off[7]) {
+    const int N = c.ndust;
+    const double ul = unit1(c.unit_l), ud = unit1(c.unit_d), ut = unit1(c.unit_t);
+    const double um = ul * ul * ul * ud, uv = ul / ut;
+    const bool disk = c.setup == SHARK_SETUP_DISK_POLAR;
+    const int rows = disk ? nx_max : 1;
+    off[0] = 0;                               // hs
+    off[1] = off[0] + nx_max;                 // trow
+    off[2] = off[1] + (size_t)rows * 8;       // tau
+    off[3] = off[2] + (size_t)rows * N;       // alpha
+    off[4] = off[3] + (size_t)rows * N;       // l2
+    off[5] = off[4] + N;                      // mkum
+    off[6] = off[5] + N;                      // ak
+    h.assign(off[6] + N, 0.0);
+    for (int ix = 0; ix < nx_max; ++ix) h[off[0] + ix] = disk ? col.hs[ix] : 1.0;
+    const double mu = c.chg_mu_ions;
+    const double as_He_ions = (double)1.14f, as_He_el = (double)1.16f;   // REAL*4 literals
+    for (int r = 0; r < rows; ++r) {
+        double T = c.T_cloud;
+        if (disk) {
+            const double csc = col.cs[r] * uv;
+            T = c.mu_gas * kMH * (csc * csc) / (c.gamma * kKB);
+        }
+        double* tr = &h[off[1] + (size_t)r * 8];
+        tr[0] = T;
+        tr[1] = (2e-7) / std::sqrt(T / 300.0);
+        tr[2] = std::sqrt(8.0 * kKB * T / (kPi * mu * kMH));
+        tr[3] = std::sqrt(c.gamma * kKB * T / (c.mu_gas * kMH));
+        const double mu_i = 2.0 * kMH * mu * kMH / (2.0 * kMH + mu * kMH);
+        const double mu_e = 2.0 * kMH * kMel / (kMel + 2.0 * kMH);
+        const double vrms_i = std::sqrt(8.0 * kKB * T / (kPi * mu_i)) * 1e-5;
+        const double vrms_el = std::sqrt(8.0 * kKB * T / (kPi * mu_e)) * 1e-5;
+        tr[6] = 3.16e-11 * std::pow(vrms_el, 1.3);
+        tr[7] = 2.4e-9 * std::pow(vrms_i, 0.6);
+        tr[4] = 1.0 / as_He_el * ((kMel + 2.0 * kMH) / (2.0 * kMH)) / tr[6];
+        tr[5] = 1.0 / as_He_ions * ((mu * kMH + 2.0 * kMH) / (2.0 * kMH)) / tr[7];
+        for (int k = 0; k < N; ++k) {
+            const double lk = c.dust_size[k] * ul;
+            const double tau = lk * kKB * T / (kEl * kEl);
+            h[off[2] + (size_t)r * N + k] = tau;
+            h[off[3] + (size_t)r * N + k] = std::sqrt(8.0 / (kPi * tau));
+        }
+    }
+    const double f43 = (double)(4.0f / 3.0f);   // Fortran 4./3. is a default-REAL quotient
+    for (int k = 0; k < N; ++k) {
+        const double sk = c.dust_size[k], lk = sk * ul;
+        h[off[4] + k] = lk * lk;
+        h[off[5] + k] = (f43 * kPi * c.rhograin * (sk * sk * sk)) * um;
+        h[off[6] + k] = std::sqrt(kPi * c.gamma / 8.0) * (c.rhograin * ud) * (lk);
+    }
+    cv.t_per_col = disk ? 1 : 0;
+    cv.res = (c.chg_mode & SHARK_CHARGE_RESISTIVITIES) ? 1 : 0;
+    cv.use_seed = 0;
+    cv.unH = ud / (c.mu_gas * kMH);
+    cv.ud = ud;
+    cv.ul = ul;
+    cv.x0 = c.chg_x;
+    cv.sig_att = disk ? c.chg_sigma_att : 0.0;
+    cv.thetai = c.chg_stick_el * std::sqrt(mu * kMH / kMel);
+    cv.th2 = cv.thetai * cv.thetai;
+    cv.th3 = cv.thetai * cv.thetai * cv.thetai;
+    cv.psi0 = charge_psi0(cv.thetai);
+    cv.eps = c.chg_eps;
+    cv.B0 = c.chg_B0;
+    cv.mu_ions = mu;
+    cv.nitermax = c.chg_nitermax;
+}
+
 template <typename T>
 void upload_cols(std::vector<T>& dst, const Columns& col) {
     const std::vector<double>* src[13] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
@@ -309,6 +429,11 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->ev_fork) cudaEventDestroy(c->ev_fork);
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream2) cudaStreamDestroy(c->stream2);
+    if (c->chg_tables) cudaFree(c->chg_tables);
+    if (c->chg_psi) cudaFree(c->chg_psi);
+    if (c->chg_out) cudaFree(c->chg_out);
+    if (c->chg_hist) cudaFree(c->chg_hist);
+    if (c->chg_seed) cudaFree(c->chg_seed);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return SHARK_OK;
@@ -369,6 +494,16 @@ int32_t shark_gpu_config_defaults(shark_gpu_config* cfg) {
     cfg->box_l_y = 1.0;
     cfg->dust_ratio_min = 1e-11;
     cfg->rhograin = 2.7;
+    cfg->unit_l = cfg->unit_d = cfg->unit_t = 1.0;
+    cfg->mu_gas = 2.31;                 // setup_commons.f90 of the setups
+    cfg->T_cloud = 10.0;                // dustyTurb/setup_commons.f90:18
+    cfg->chg_x = 5e-17;                 // ionisation_commons.f90:73-77
+    cfg->chg_mu_ions = 25.0;
+    cfg->chg_stick_el = 0.5;
+    cfg->chg_eps = 1e-6;
+    cfg->chg_nitermax = 1000;
+    cfg->chg_B0 = 3e-5;
+    cfg->chg_mode = SHARK_CHARGE_RESISTIVITIES;   // res_Marchand = .true.
     return SHARK_OK;
 }
 
@@ -467,13 +602,15 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         INIT_TRY(cudaMemcpy(c->metrics_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
         for (int a = 0; a < 9; ++a) v.md[a] = c->metrics_d + a * ncol;
     }
-    INIT_TRY(cudaMalloc(&c->species, 3 * SHARK_MAX_DUST * sizeof(double)));
+    INIT_TRY(cudaMalloc(&c->species, 4 * SHARK_MAX_DUST * sizeof(double)));
+    INIT_TRY(cudaMemcpy(c->species + 3 * SHARK_MAX_DUST, cfg->dust_stokes, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
     INIT_TRY(cudaMemcpy(c->species, cfg->dust_K, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
     INIT_TRY(cudaMemcpy(c->species + SHARK_MAX_DUST, cfg->dust_tstop, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
     INIT_TRY(cudaMemcpy(c->species + 2 * SHARK_MAX_DUST, cfg->dust_size, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
     v.dK = c->species;
     v.dtstop = c->species + SHARK_MAX_DUST;
     v.dsize = c->species + 2 * SHARK_MAX_DUST;
+    v.dstokes = c->species + 3 * SHARK_MAX_DUST;
     INIT_TRY(cudaMalloc(&c->dt_slots, 2 * sizeof(double)));
     INIT_TRY(cudaMalloc(&c->status, sizeof(unsigned int)));
     INIT_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
@@ -482,6 +619,34 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     v.dt_slots = c->dt_slots;
     v.status = c->status;
     v.coef = c->coef;
+    v.chg = shark::ChargeView{};
+    if (cfg->flags & SHARK_FLAG_CHARGING) {
+        std::vector<double> h;
+        size_t off[7];
+        build_charge_tables(*cfg, col, v.nx_max, h, v.chg, off);
+        INIT_TRY(cudaMalloc(&c->chg_tables, h.size() * sizeof(double)));
+        INIT_TRY(cudaMemcpy(c->chg_tables, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        v.chg.hs = c->chg_tables + off[0]; v.chg.trow = c->chg_tables + off[1]; v.chg.tau = c->chg_tables + off[2];
+        v.chg.alpha = c->chg_tables + off[3]; v.chg.l2 = c->chg_tables + off[4]; v.chg.mkum = c->chg_tables + off[5];
+        v.chg.ak = c->chg_tables + off[6];
+        const size_t pl = (size_t)v.plane;
+        INIT_TRY(cudaMalloc(&c->chg_psi, pl * sizeof(double)));
+        INIT_TRY(cudaMemsetAsync(c->chg_psi, 0, pl * sizeof(double), c->stream));
+        const size_t nplanes = 2 * (size_t)v.ndust + 5;   // zd N | ni | ne | eta 3 | gamma_d N
+        INIT_TRY(cudaMalloc(&c->chg_out, nplanes * pl * c->elem));
+        INIT_TRY(cudaMemsetAsync(c->chg_out, 0, nplanes * pl * c->elem, c->stream));
+        char* b = (char*)c->chg_out;
+        v.chg.zd = b;
+        v.chg.ni = b + (size_t)v.ndust * pl * c->elem;
+        v.chg.ne = b + ((size_t)v.ndust + 1) * pl * c->elem;
+        v.chg.eta = b + ((size_t)v.ndust + 2) * pl * c->elem;
+        v.chg.gamma_d = b + ((size_t)v.ndust + 5) * pl * c->elem;
+        v.chg.psi_old = c->chg_psi;
+        INIT_TRY(cudaMalloc(&c->chg_hist, (SHARK_CHARGE_HIST + 2) * sizeof(unsigned long long)));
+        INIT_TRY(cudaMemsetAsync(c->chg_hist, 0, (SHARK_CHARGE_HIST + 2) * sizeof(unsigned long long), c->stream));
+        v.chg.hist = c->chg_hist;
+        v.chg.on = true;
+    }
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
     std::memset(c->host_ring, 0, 4 * sizeof(double));
     const long long nact = (long long)v.nx * (v.ndim == 2 ? v.ny : 1);
@@ -714,6 +879,61 @@ int32_t shark_gpu_kernel_times(shark_gpu_ctx* c, int64_t nsteps, float* avg_ms) 
     for (auto& e : ev) cudaEventDestroy(e);
     for (int a = 0; a < 4; ++a) avg_ms[a] = (float)(sum[a] / (double)nsteps);
     return rc;
+}
+
+int32_t shark_gpu_charge(shark_gpu_ctx* c) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "charge before upload");
+    cudaError_t e = is_mixed(c) ? shark::launch_charge<float>(c->v) : shark::launch_charge<double>(c->v);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "charge: %s", cudaGetErrorString(e));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_charge_reset(shark_gpu_ctx* c) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
+    CUDA_TRY(cudaMemsetAsync(c->chg_psi, 0, (size_t)c->v.plane * sizeof(double), c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_charge_stats(shark_gpu_ctx* c, int64_t* hist, int64_t* nonconv, int64_t* total_iters) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
+    unsigned long long h[SHARK_CHARGE_HIST + 2];
+    CUDA_TRY(cudaMemcpyAsync(h, c->chg_hist, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (hist) for (int b = 0; b < SHARK_CHARGE_HIST; ++b) hist[b] = (int64_t)h[b];
+    if (nonconv) *nonconv = (int64_t)h[SHARK_CHARGE_HIST];
+    if (total_iters) *total_iters = (int64_t)h[SHARK_CHARGE_HIST + 1];
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_download_charge(shark_gpu_ctx* c, double* zd, double* ni, double* ne, double* psi, double* eta,
+                                  double* gamma_d) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
+    const shark::DeviceView& v = c->v;
+    const size_t nc = (size_t)v.nx_max * v.ny_max;
+    const int N = v.ndust;
+    double* tmp = nullptr;
+    CUDA_TRY(cudaMalloc(&tmp, nc * (size_t)N * sizeof(double)));
+    struct Part { double* dst; const void* src; int count; bool fp64; };
+    const Part parts[6] = {{zd, v.chg.zd, N, false}, {ni, v.chg.ni, 1, false}, {ne, v.chg.ne, 1, false},
+                           {psi, v.chg.psi_old, 1, true}, {eta, v.chg.eta, 3, false}, {gamma_d, v.chg.gamma_d, N, false}};
+    cudaError_t e = cudaSuccess;
+    for (const Part& q : parts) {
+        if (!q.dst || e != cudaSuccess) continue;
+        if (q.fp64 || !is_mixed(c)) e = shark::launch_planes_to_fortran<double>(v, q.src, q.count, tmp);
+        else e = shark::launch_planes_to_fortran<float>(v, q.src, q.count, tmp);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(q.dst, tmp, nc * q.count * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    }
+    cudaFree(tmp);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "download_charge: %s", cudaGetErrorString(e));
+    return SHARK_OK;
 }
 
 int32_t shark_gpu_free(shark_gpu_ctx* c) { return release(c); }

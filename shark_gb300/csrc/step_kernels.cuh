@@ -40,7 +40,8 @@ struct KParams {
     const double *fgravd, *treld, *hsd, *vkd;
     const R* u_init;                   // polar disk relaxation reference state
     // per-species constants
-    const double *dK, *dtstop, *dsize;
+    const double *dK, *dtstop, *dsize, *dstokes;
+    double turb_rho0;
     // time step bookkeeping
     const double* dt;                 // dt of the current step
     unsigned long long* dt_next;      // bit image of the next dt (positive doubles order as u64)
@@ -254,6 +255,8 @@ __device__ __forceinline__ double tstop_cell(const KParams<R>& p, int k, double 
         const double rd_old = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
         return rd_old * qrho_old / p.dK[k] / (qrho_old);
     }
+    if (p.setup == SHARK_SETUP_DUSTYTURB)    // dustyTurb/setup.f90:456
+        return p.dstokes[k] * p.box_l * p.turb_rho0 / p.csd[gx] / qrho_old;
     if (p.setup == SHARK_SETUP_DISK_POLAR)   // Epstein on the midplane density Sigma/(sqrt(2 pi) H)
         return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old / p.hsd[gx] * p.csd[gx]);
     // Epstein (SOD/setup.f90:179-185); isothermal cs only (checked at init)

@@ -15,6 +15,8 @@ module shark_gpu
   integer(c_int32_t), parameter :: SHARK_FLAG_GROWTH = 16, SHARK_FLAG_CHARGING = 32
   integer(c_int32_t), parameter :: SHARK_FLAG_VISCOSITY = 64, SHARK_FLAG_STATIC = 128
   integer(c_int32_t), parameter :: SHARK_PREC_FP64 = 0, SHARK_PREC_MIXED = 1
+  integer(c_int32_t), parameter :: SHARK_CHARGE_RESISTIVITIES = 1, SHARK_CHARGE_ANALYTICAL = 2
+  integer(c_int32_t), parameter :: SHARK_CHARGE_MLP_SEED = 4
 
   type, bind(C) :: shark_gpu_config
     integer(c_int32_t) :: abi_version, nx, ny, nghost, ndust, geom, gridspace, solver, solverdust
@@ -29,7 +31,12 @@ module shark_gpu
     real(c_double) :: si_q_shear, si_omega, si_eta_stream, si_rad0, si_rho_init, si_hoverr
     real(c_double) :: disk_mstar, disk_hoverr, disk_sigma0, disk_r0, disk_rout
     real(c_double) :: disk_r_relax, disk_n_rel, disk_temp_slope
-    real(c_double) :: reserved(45)
+    real(c_double) :: unit_l, unit_d, unit_t, mu_gas, T_cloud
+    real(c_double) :: chg_x, chg_sigma_att, chg_mu_ions, chg_stick_el, chg_eps, chg_B0
+    integer(c_int32_t) :: chg_nitermax, chg_mode
+    real(c_double) :: turb_rho0, turb_mach, turb_tcorr
+    integer(c_int32_t) :: turb_kmin, turb_kmax, turb_seed, pad2
+    real(c_double) :: reserved(28)
     type(c_ptr) :: dx, surf, vol, radii_c, position, cs
   end type shark_gpu_config
 

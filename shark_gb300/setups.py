@@ -15,7 +15,12 @@ import numpy as np
 import math
 
 from .config import (SharkConfig, default_config, SETUP_SOD, SETUP_DUSTYWAVE, SETUP_SI, SETUP_DISK_POLAR,
-                     FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO, PREC_FP64)
+                     SETUP_DUSTYTURB, FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO,
+                     FLAG_CHARGING, PREC_FP64)
+
+MH = 1.67e-24        # src/commons/phys_const.f90:8
+KB = 1.38e-16        # src/commons/phys_const.f90:9
+PC = 3e18            # src/commons/phys_const.f90:12
 
 PI = 3.141592653589793238462643383279          # src/commons/phys_const.f90:14
 F43 = float(np.float32(4.0) / np.float32(3.0))  # Fortran `4./3.` is a default-REAL quotient
@@ -328,10 +333,15 @@ def disk_radii(cfg):
     return r
 
 
+AU = 1.5e13          # src/commons/phys_const.f90:11
+MSUN = 2e33          # src/commons/phys_const.f90:13
+GRAV = 6.67e-8       # src/commons/phys_const.f90:10
+
+
 def disk_polar(nr=128, nphi=128, ndust=4, stokes_min=1e-3, stokes_max=0.3, dust2gas=0.01, mstar=1.0,
                hoverr=0.05, temp_slope=-1.0, sigma0=1e-3, r0=1.0, rout=40.0, rin=1.0, rmax=40.0,
                r_relax=3.0, n_rel=8.0, rhograin=1.0, noise=0.0, seed=1, cfl=0.8, slope_type=1,
-               gamma=1.666666666666667, fargo=False, precision=PREC_FP64):
+               gamma=1.666666666666667, fargo=False, precision=PREC_FP64, sizes=None, charging=False):
     """Face-on polar disk around a point mass (src/setups/disk_polar/setup.f90:1-84) on the log
     grid, in code units G = Mstar = 1 (r in AU, t in 1/Omega(1 AU)).
 
@@ -356,17 +366,38 @@ def disk_polar(nr=128, nphi=128, ndust=4, stokes_min=1e-3, stokes_max=0.3, dust2
     cfg.disk_mstar, cfg.disk_hoverr, cfg.disk_sigma0 = mstar, hoverr, sigma0
     cfg.disk_r0, cfg.disk_rout = r0, rout
     cfg.disk_r_relax, cfg.disk_n_rel, cfg.disk_temp_slope = r_relax, n_rel, temp_slope
+    cfg.flags |= FLAG_CHARGING if charging else 0
     sig0 = sigma0 * math.exp(-r0 / rout)
     unit_s = sig0 / (math.sqrt(PI * gamma / 8.0) * math.sqrt(2.0 * PI) * rhograin)   # St = 1 at r0
     if ndust > 0:
-        sdust, eps = mrn_bins(ndust, stokes_min * unit_s, stokes_max * unit_s, stokes_min * unit_s,
-                              stokes_max * unit_s, dust2gas, rhograin=rhograin,
+        smin, smax = sizes if sizes is not None else (stokes_min * unit_s, stokes_max * unit_s)
+        sdust, eps = mrn_bins(ndust, smin, smax, smin, smax, dust2gas, rhograin=rhograin,
                               dust_ratio_min=cfg.dust_ratio_min)
         for k in range(ndust):
             cfg.dust_size[k] = sdust[k]
             cfg.dust_eps[k] = eps[k]
             cfg.dust_stokes[k] = sdust[k] / unit_s
     cfg.cs0 = hoverr * math.sqrt(mstar / r0)
+    return cfg, disk_ic(cfg, noise, seed)
+
+
+def disk_polar_au(nr=512, nphi=1024, ndust=16, smin_cm=1e-4, smax_cm=1.0, sigma0_cgs=1700.0,
+                  rhograin_cgs=2.7, rin=1.0, rmax=100.0, hoverr=0.05, temp_slope=-0.5, dust2gas=0.01,
+                  zeta=1e-17, sigma_att=96.0, noise=1e-3, seed=2, fargo=True, charging=True,
+                  precision=PREC_FP64, **kw):
+    """The polar disk in the reference's disk units (disk_polar/units.f90: AU, Msun, G = 1):
+    Sigma = sigma0_cgs (1 AU/r) g cm^-2 without outer taper, T ~ r^temp_slope, grains from
+    smin_cm to smax_cm, cosmic-ray ionisation zeta exp(-Sigma/sigma_att)."""
+    unit_l = AU
+    unit_d = MSUN / AU ** 3
+    unit_t = 1.0 / math.sqrt(GRAV * MSUN / AU ** 3)
+    cfg, _ = disk_polar(nr=nr, nphi=nphi, ndust=ndust, dust2gas=dust2gas, hoverr=hoverr, temp_slope=temp_slope,
+                        sigma0=sigma0_cgs / (unit_d * unit_l), r0=1.0, rout=float("inf"), rin=rin, rmax=rmax,
+                        rhograin=rhograin_cgs / unit_d, fargo=fargo, precision=precision,
+                        sizes=(smin_cm / unit_l, smax_cm / unit_l), charging=charging, **kw)
+    cfg.unit_l, cfg.unit_d, cfg.unit_t = unit_l, unit_d, unit_t
+    cfg.chg_x = zeta
+    cfg.chg_sigma_att = sigma_att
     return cfg, disk_ic(cfg, noise, seed)
 
 
@@ -403,6 +434,108 @@ def disk_ic(cfg, noise_amp, seed):
     return primtoc(cfg, q.reshape(cfg.nvar, -1)).reshape(-1)
 
 
+# ---------------------------------------------------------------------------------------------
+# Dusty turbulence
+# ---------------------------------------------------------------------------------------------
+def dusty_turb(n=256, ndust=32, smin=1e-6, smax=0.1, dust2gas=0.01, nH=1e9, T=10.0, box_pc=0.1,
+               mach=1.0, kmin=1, kmax=3, seed=3, tcorr=None, rhograin=2.7, gamma=1.66667, cfl=0.5,
+               slope_type=1, charging=False, forcing=False, precision=PREC_FP64):
+    """2D periodic isothermal dusty box in cgs units (src/setups/dustyTurb/setup.f90, units.f90).
+
+    Gas of number density ``nH`` (cm^-3, mu_gas = 2.31) at ``T`` K; grains in ``ndust`` MRN bins
+    between radii ``smin`` and ``smax`` (cm), total dust-to-gas ratio ``dust2gas``.  The stopping
+    time law of the reference, t_k = St_0,k box_l rho_0/cs/rho, takes St_0,k from the Epstein
+    time of grain k at rho_0.  Gas and dust start with the same solenoidal velocity field: a sum
+    of Fourier modes of the stream function with wavenumbers kmin <= |k| L/(2 pi) <= kmax,
+    seeded amplitudes and phases, scaled to RMS Mach ``mach``.  ``forcing`` enables the
+    Ornstein-Uhlenbeck driving of the same band with correlation time ``tcorr`` (default one
+    sound crossing time of the box).
+    """
+    cfg = default_config()
+    cfg.nx = cfg.ny = n
+    cfg.ndust = ndust
+    cfg.gamma, cfg.cfl, cfg.slope_type = gamma, cfl, slope_type
+    cfg.iso_cs = 1
+    cfg.precision = precision
+    cfg.setup = SETUP_DUSTYTURB
+    cfg.flags = FLAG_DRAG | FLAG_BACK_REACTION | (FLAG_CHARGING if charging else 0)
+    L = box_pc * PC
+    cfg.box_l = cfg.box_l_y = L
+    cfg.mu_gas = 2.31
+    cfg.T_cloud = T
+    rho0 = nH * cfg.mu_gas * MH
+    cfg.turb_rho0 = rho0
+    cs = math.sqrt(KB * T / (cfg.mu_gas * MH))
+    cfg.cs0 = cs
+    cfg.rhograin = rhograin
+    if ndust > 0:
+        sdust, eps = mrn_bins(ndust, smin, smax, smin, smax, dust2gas, rhograin=rhograin,
+                              dust_ratio_min=cfg.dust_ratio_min)
+        for k in range(ndust):
+            cfg.dust_size[k] = sdust[k]
+            cfg.dust_eps[k] = eps[k]
+            cfg.dust_stokes[k] = math.sqrt(PI * gamma / 8.0) * rhograin * sdust[k] / (rho0 * L)
+    cfg.turb_mach = mach if forcing else 0.0
+    cfg.turb_tcorr = tcorr if tcorr is not None else L / cs
+    cfg.turb_kmin, cfg.turb_kmax, cfg.turb_seed = kmin, kmax, seed
+    return cfg, turb_ic(cfg, mach, seed, kmin, kmax)
+
+
+def solenoidal_modes(kmin, kmax):
+    """Integer wave vectors (kx, ky), one per +-k pair, with kmin <= |k| <= kmax."""
+    modes = []
+    for kx in range(0, kmax + 1):
+        for ky in range(-kmax, kmax + 1):
+            if kx == 0 and ky <= 0:
+                continue
+            kk = math.hypot(kx, ky)
+            if kmin <= kk <= kmax:
+                modes.append((kx, ky))
+    return modes
+
+
+def turb_ic(cfg, mach, seed, kmin, kmax):
+    """Initial conserved state of the dusty box (see dusty_turb)."""
+    N = cfg.ndust
+    pos = positions(cfg)
+    L = cfg.box_l
+    x, y = pos[:, 0], pos[:, 1]
+    vx = np.zeros(cfg.ncells)
+    vy = np.zeros(cfg.ncells)
+    modes = solenoidal_modes(kmin, kmax)
+    cnt = np.arange(2 * len(modes), dtype=np.uint64)
+    u = hash_uniform(seed, cnt)
+    for m, (kx, ky) in enumerate(modes):
+        amp = u[2 * m] + 0.5
+        ph = 2.0 * PI * u[2 * m + 1]
+        kxp, kyp = 2.0 * PI * kx / L, 2.0 * PI * ky / L
+        c = np.cos(kxp * x + kyp * y + ph)
+        # stream function amp sin(k.x + ph)/|k|: v = (d/dy, -d/dx)
+        kk = math.hypot(kxp, kyp)
+        vx += amp * kyp / kk * c
+        vy -= amp * kxp / kk * c
+    ng = cfg.nghost
+    act = np.zeros((cfg.ny_max, cfg.nx_max), bool)
+    act[ng:ng + cfg.ny, ng:ng + cfg.nx] = True
+    act = act.reshape(-1)
+    rms = math.sqrt(float(np.mean(vx[act] ** 2 + vy[act] ** 2)))
+    scale = mach * cfg.cs0 / rms if rms > 0 else 0.0
+    vx *= scale
+    vy *= scale
+    q = np.zeros((cfg.nvar, cfg.ncells))
+    q[0] = cfg.turb_rho0
+    q[1], q[2] = vx, vy
+    q[4] = q[0] * cfg.cs0 ** 2
+    for k in range(N):
+        q[5 + k] = cfg.dust_eps[k] * cfg.turb_rho0
+        q[5 + N + k] = vx
+        q[5 + 2 * N + k] = vy
+    u0 = primtoc(cfg, q).reshape(-1)
+    periodic_boundaries(cfg, u0)
+    return u0
+
+
 def build(name, **kw):
-    """Dispatch by setup name ('sod', 'dustywave', 'si', 'disk_polar')."""
-    return {"sod": sod, "dustywave": dustywave, "si": si, "disk_polar": disk_polar}[name](**kw)
+    """Dispatch by setup name ('sod', 'dustywave', 'si', 'disk_polar', 'dusty_turb')."""
+    return {"sod": sod, "dustywave": dustywave, "si": si, "disk_polar": disk_polar,
+            "dusty_turb": dusty_turb}[name](**kw)

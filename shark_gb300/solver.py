@@ -23,7 +23,9 @@ EXPORTS = [
     "shark_gpu_step", "shark_gpu_run", "shark_gpu_sync", "shark_gpu_download", "shark_gpu_ctoprim",
     "shark_gpu_totals", "shark_gpu_last_step_ms", "shark_gpu_timed_run", "shark_gpu_kernel_times",
     "shark_gpu_totals_noalloc", "shark_gpu_last_error", "shark_gpu_free",
+    "shark_gpu_charge", "shark_gpu_charge_reset", "shark_gpu_charge_stats", "shark_gpu_download_charge",
 ]
+CHARGE_HIST = 64   # SHARK_CHARGE_HIST
 
 
 class SharkError(RuntimeError):
@@ -76,6 +78,13 @@ def load_library(path=None):
     L.shark_gpu_last_error.argtypes = []
     L.shark_gpu_free.restype = I32
     L.shark_gpu_free.argtypes = [P]
+    I64P = C.POINTER(C.c_int64)
+    for name, args in [("shark_gpu_charge", [P]), ("shark_gpu_charge_reset", [P]),
+                       ("shark_gpu_charge_stats", [P, I64P, I64P, I64P]),
+                       ("shark_gpu_download_charge", [P, D, D, D, D, D, D])]:
+        f = getattr(L, name)
+        f.restype = I32
+        f.argtypes = args
     _lib = L
     return L
 
@@ -219,3 +228,29 @@ class Shark:
         ms = (C.c_float * 3)()
         _check(load_library().shark_gpu_last_step_ms(self._h, ms), "shark_gpu_last_step_ms")
         return list(ms)
+
+    # ---- charging (SHARK_FLAG_CHARGING) ---------------------------------------------------------
+    def charge(self):
+        """Charge the current state now (src/chemistry/ionisation.f90:4-214)."""
+        _check(load_library().shark_gpu_charge(self._h), "shark_gpu_charge")
+
+    def charge_reset(self):
+        """psi_old = 0: the next charging call starts cold."""
+        _check(load_library().shark_gpu_charge_reset(self._h), "shark_gpu_charge_reset")
+
+    def charge_stats(self):
+        """(iteration histogram[64], non-converged cells, total iterations) of the last call."""
+        h = np.zeros(CHARGE_HIST, dtype=np.int64)
+        nc, tot = C.c_int64(0), C.c_int64(0)
+        _check(load_library().shark_gpu_charge_stats(self._h, h.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                     C.byref(nc), C.byref(tot)), "shark_gpu_charge_stats")
+        return h, nc.value, tot.value
+
+    def download_charge(self):
+        """dict of zd (N, ncells), ni, ne, psi, eta (3, ncells), gamma_d (N, ncells)."""
+        N, nc = self.cfg.ndust, self.ncells
+        zd, gd = np.empty(N * nc), np.empty(N * nc)
+        ni, ne, psi, eta = np.empty(nc), np.empty(nc), np.empty(nc), np.empty(3 * nc)
+        _check(load_library().shark_gpu_download_charge(self._h, _dptr(zd), _dptr(ni), _dptr(ne), _dptr(psi),
+                                                        _dptr(eta), _dptr(gd)), "shark_gpu_download_charge")
+        return dict(zd=zd.reshape(N, nc), ni=ni, ne=ne, psi=psi, eta=eta.reshape(3, nc), gamma_d=gd.reshape(N, nc))

@@ -1,0 +1,103 @@
+"""Grain charging on the GPU (K5, src/chemistry/ionisation.f90:4-214) against the CPU oracle on
+the same states: the FP64 kernel follows the oracle operation by operation (only exp() may differ
+in the last bit), so psi, Z_k, n_i, n_e agree to 1e-10 relative and the Newton iteration counts
+agree cell by cell (a last-bit difference may move a borderline cell by one iteration); the
+mixed-precision kernel iterates in FP32 to the same residual tolerance."""
+import numpy as np
+import pytest
+
+from shark_gb300 import config as K, setups
+from shark_gb300.solver import Shark
+from oracle.oracle import Oracle
+from tests.test_charge_cpu import _noisy_turb
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))
+
+
+def _compare(cfg, u0, tol, iters_exact=True):
+    o = Oracle(cfg)
+    o.set_u(u0)
+    it_o = o.charge()
+    co = o.get_charge()
+    with Shark(cfg) as g:
+        g.upload(u0)
+        g.charge()
+        hist, nonconv, total = g.charge_stats()
+        cg = g.download_charge()
+    assert total == int(it_o.sum()) or not iters_exact
+    ho = np.bincount(np.minimum(it_o, 63), minlength=64)
+    if iters_exact:
+        assert np.abs(hist - ho).sum() <= max(2, it_o.size // 1000)
+    assert nonconv == int(np.sum(it_o >= cfg.chg_nitermax)) or not iters_exact
+    conv = it_o < cfg.chg_nitermax
+    assert _rel(cg["psi"][conv], co["psi"][conv]) <= tol
+    assert _rel(cg["zd"][:, conv], co["zd"][:, conv]) <= tol
+    assert _rel(cg["ni"][conv], co["ni"][conv]) <= tol
+    assert _rel(cg["ne"][conv], co["ne"][conv]) <= tol
+    return co, cg, it_o, hist
+
+
+def test_charge_fp64_dusty_box():
+    cfg, u0 = _noisy_turb(n=40, ndust=8)
+    co, cg, it, hist = _compare(cfg, u0, 1e-10)
+    conv = it < cfg.chg_nitermax
+    assert _rel(cg["eta"][:, conv], co["eta"][:, conv]) <= 1e-9
+    assert _rel(cg["gamma_d"][:, conv], co["gamma_d"][:, conv]) <= 1e-9
+
+
+def test_charge_fp64_runtime_species_count():
+    cfg, u0 = _noisy_turb(n=24, ndust=13)
+    _compare(cfg, u0, 1e-10)
+
+
+def test_charge_fp64_polar_disk_temperature_per_column():
+    cfg, u0 = setups.disk_polar_au(nr=40, nphi=24, ndust=6, noise=1e-2)
+    _compare(cfg, u0, 1e-10)
+
+
+def test_charge_mixed_dusty_box():
+    cfg, u0 = _noisy_turb(n=40, ndust=8)
+    cfg.precision = K.PREC_MIXED
+    co, cg, it, hist = _compare(cfg, u0, 2e-4, iters_exact=False)
+    # every cell the FP64 oracle converges also converges in FP32, in about as many iterations
+    assert hist[63] == 0
+    assert abs(int((hist * np.arange(64)).sum()) - int(it.sum())) <= 0.2 * it.sum()
+
+
+def test_charging_inside_the_step_matches_the_oracle():
+    cfg, u0 = _noisy_turb(n=32, ndust=4, amp=0.3)
+    o = Oracle(cfg)
+    o.set_u(u0)
+    with Shark(cfg) as g:
+        g.upload(u0)
+        for _ in range(5):
+            assert g.solve() == pytest.approx(o.solve(), rel=1e-13)
+        cg = g.download_charge()
+        u_g = g.download()
+        hist, nonconv, total = g.charge_stats()
+    co = o.get_charge()
+    assert _rel(cg["psi"], co["psi"]) <= 1e-10
+    assert _rel(cg["zd"], co["zd"]) <= 1e-10
+    # warm starts: after the first step every cell converges in a couple of iterations
+    assert total <= 3 * u0.size // cfg.nvar
+    from tests.test_gpu_parity import rel_l1
+    assert rel_l1(cfg, u_g, o.get_u()).max() <= 1e-10
+
+
+def test_charge_reset_restarts_cold():
+    cfg, u0 = _noisy_turb(n=16, ndust=4)
+    with Shark(cfg) as g:
+        g.upload(u0)
+        g.charge()
+        _, _, cold = g.charge_stats()
+        g.charge()
+        _, _, warm = g.charge_stats()
+        g.charge_reset()
+        g.charge()
+        _, _, again = g.charge_stats()
+    assert again == cold
+    assert warm < cold / 5
