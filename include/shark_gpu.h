@@ -276,9 +276,9 @@ int32_t shark_gpu_charge_reset(shark_gpu_ctx* ctx);
 int32_t shark_gpu_charge_stats(shark_gpu_ctx* ctx, int64_t* iters_hist, int64_t* nonconv, int64_t* total_iters);
 /* Last charging outputs in Fortran order: zd(ncells,N), ni(ncells), ne(ncells), psi_old(ncells),
  * eta(ncells,3) = (eta_o, eta_H, eta_a), gamma_d(ncells,N) (the last two with
- * SHARK_CHARGE_RESISTIVITIES).  Any pointer may be NULL. */
+ * SHARK_CHARGE_RESISTIVITIES), Newton iterations per cell.  Any pointer may be NULL. */
 int32_t shark_gpu_download_charge(shark_gpu_ctx* ctx, double* zd, double* ni, double* ne, double* psi,
-                                  double* eta, double* gamma_d);
+                                  double* eta, double* gamma_d, int32_t* iters);
 
 int32_t shark_gpu_free(shark_gpu_ctx* ctx);
 

@@ -49,6 +49,7 @@ struct ChargeParams {
     R* eta;                      // [3][plane] (o, H, a)
     R* gamma_d;                  // [N][plane]
     const float* seed;           // [plane] network start points (nullptr: none)
+    int32_t* iters;              // [plane] Newton iterations of the last call
     unsigned long long* hist;    // [CHARGE_HIST + 2]: histogram, non-converged cells, total iterations
 };
 
@@ -187,6 +188,7 @@ __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
             p.eta[p.plane + c] = sigma_h / (sigma_p * two + sigma_h * sigma_h);
             p.eta[2 * p.plane + c] = sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - one / sigma_o;
         }
+        p.iters[c] = niter;
         atomicAdd(&s_hist[niter < CHARGE_HIST - 1 ? niter : CHARGE_HIST - 1], 1u);
         if (conv > R(p.eps)) atomicAdd(&s_hist[CHARGE_HIST], 1u);
         atomicAdd(&s_iter, (unsigned long long)niter);

@@ -235,7 +235,7 @@ cudaError_t launch_charge(const DeviceView& v) {
     q.thetai = c.thetai; q.th2 = c.th2; q.th3 = c.th3; q.psi0 = c.psi0; q.eps = c.eps; q.B0 = c.B0;
     q.mu_ions = c.mu_ions; q.nitermax = c.nitermax;
     q.psi_old = c.psi_old; q.zd = (R*)c.zd; q.ni = (R*)c.ni; q.ne = (R*)c.ne; q.eta = (R*)c.eta;
-    q.gamma_d = (R*)c.gamma_d; q.seed = c.seed; q.hist = c.hist;
+    q.gamma_d = (R*)c.gamma_d; q.seed = c.seed; q.hist = c.hist; q.iters = c.iters;
     cudaError_t e = cudaMemsetAsync(c.hist, 0, (CHARGE_HIST + 2) * sizeof(unsigned long long), v.stream);
     if (e != cudaSuccess) return e;
     const long long n = (long long)v.nx_max * v.ny_max;

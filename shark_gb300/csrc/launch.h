@@ -18,6 +18,7 @@ struct ChargeView {
     double* psi_old;                        // FP64 [plane]
     void *zd, *ni, *ne, *eta, *gamma_d;     // state precision, plane layout
     const float* seed;                      // network start points [plane] or nullptr
+    int32_t* iters;                         // Newton iterations per cell [plane]
     unsigned long long* hist;               // [CHARGE_HIST + 2]
 };
 

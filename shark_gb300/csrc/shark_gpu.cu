@@ -92,6 +92,7 @@ struct shark_gpu_ctx {
     void* chg_out = nullptr;         // zd | ni | ne | eta | gamma_d in state precision
     unsigned long long* chg_hist = nullptr;
     float* chg_seed = nullptr;       // network start points (plane layout)
+    int32_t* chg_iters = nullptr;    // Newton iterations per cell (plane layout)
     long long nstep = 0;             // steps launched since upload
     bool uploaded = false;
     bool pending_read[2] = {false, false};
@@ -434,6 +435,7 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->chg_out) cudaFree(c->chg_out);
     if (c->chg_hist) cudaFree(c->chg_hist);
     if (c->chg_seed) cudaFree(c->chg_seed);
+    if (c->chg_iters) cudaFree(c->chg_iters);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return SHARK_OK;
@@ -645,6 +647,9 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         INIT_TRY(cudaMalloc(&c->chg_hist, (SHARK_CHARGE_HIST + 2) * sizeof(unsigned long long)));
         INIT_TRY(cudaMemsetAsync(c->chg_hist, 0, (SHARK_CHARGE_HIST + 2) * sizeof(unsigned long long), c->stream));
         v.chg.hist = c->chg_hist;
+        INIT_TRY(cudaMalloc(&c->chg_iters, pl * sizeof(int32_t)));
+        INIT_TRY(cudaMemsetAsync(c->chg_iters, 0, pl * sizeof(int32_t), c->stream));
+        v.chg.iters = c->chg_iters;
         v.chg.on = true;
     }
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
@@ -912,7 +917,7 @@ int32_t shark_gpu_charge_stats(shark_gpu_ctx* c, int64_t* hist, int64_t* nonconv
 }
 
 int32_t shark_gpu_download_charge(shark_gpu_ctx* c, double* zd, double* ni, double* ne, double* psi, double* eta,
-                                  double* gamma_d) {
+                                  double* gamma_d, int32_t* iters) {
     if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
     if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
     const shark::DeviceView& v = c->v;
@@ -932,6 +937,15 @@ int32_t shark_gpu_download_charge(shark_gpu_ctx* c, double* zd, double* ni, doub
         if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     }
     cudaFree(tmp);
+    if (e == cudaSuccess && iters) {
+        std::vector<int32_t> h((size_t)v.plane);
+        e = cudaMemcpyAsync(h.data(), c->chg_iters, h.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e == cudaSuccess)
+            for (int iy = 0; iy < v.ny_max; ++iy)
+                for (int ix = 0; ix < v.nx_max; ++ix)
+                    iters[(size_t)iy * v.nx_max + ix] = h[(size_t)iy * v.pitch + ix];
+    }
     if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "download_charge: %s", cudaGetErrorString(e));
     return SHARK_OK;
 }

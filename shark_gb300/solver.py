@@ -81,7 +81,7 @@ def load_library(path=None):
     I64P = C.POINTER(C.c_int64)
     for name, args in [("shark_gpu_charge", [P]), ("shark_gpu_charge_reset", [P]),
                        ("shark_gpu_charge_stats", [P, I64P, I64P, I64P]),
-                       ("shark_gpu_download_charge", [P, D, D, D, D, D, D])]:
+                       ("shark_gpu_download_charge", [P, D, D, D, D, D, D, C.POINTER(C.c_int32)])]:
         f = getattr(L, name)
         f.restype = I32
         f.argtypes = args
@@ -247,10 +247,13 @@ class Shark:
         return h, nc.value, tot.value
 
     def download_charge(self):
-        """dict of zd (N, ncells), ni, ne, psi, eta (3, ncells), gamma_d (N, ncells)."""
+        """dict of zd (N, ncells), ni, ne, psi, eta (3, ncells), gamma_d (N, ncells), iters."""
         N, nc = self.cfg.ndust, self.ncells
         zd, gd = np.empty(N * nc), np.empty(N * nc)
         ni, ne, psi, eta = np.empty(nc), np.empty(nc), np.empty(nc), np.empty(3 * nc)
+        it = np.zeros(nc, dtype=np.int32)
         _check(load_library().shark_gpu_download_charge(self._h, _dptr(zd), _dptr(ni), _dptr(ne), _dptr(psi),
-                                                        _dptr(eta), _dptr(gd)), "shark_gpu_download_charge")
-        return dict(zd=zd.reshape(N, nc), ni=ni, ne=ne, psi=psi, eta=eta.reshape(3, nc), gamma_d=gd.reshape(N, nc))
+                                                        _dptr(eta), _dptr(gd), it.ctypes.data_as(C.POINTER(C.c_int32))),
+               "shark_gpu_download_charge")
+        return dict(zd=zd.reshape(N, nc), ni=ni, ne=ne, psi=psi, eta=eta.reshape(3, nc), gamma_d=gd.reshape(N, nc),
+                    iters=it)

@@ -23,6 +23,7 @@ def _noisy_turb(n=16, ndust=8, seed=5, amp=0.6, nH=1e9):
     for k in range(ndust):
         for c in range(4):
             g[5 + c * ndust + k] *= f * fd[k]
+    setups.periodic_boundaries(cfg, u0)
     return cfg, u0
 
 
