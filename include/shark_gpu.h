@@ -72,6 +72,10 @@ extern "C" {
 
 /* ---- precision of the device state and of the flux/update stage -------------------------- */
 #define SHARK_CHARGE_HIST 64   /* bins of the Newton iteration histogram (last bin: >= 63) */
+/* charging network: features per cell, trainable parameters, whole parameter blob */
+#define SHARK_MLP_NFEAT  6
+#define SHARK_MLP_NPARAM 5313  /* W1[64][16] b1[64] W2[64][64] b2[64] w3[64] b3[1]            */
+#define SHARK_MLP_NBLOB  5327  /* + feature mean[6], sd[6], target mean, sd                   */
 
 /* chg_mode bits */
 #define SHARK_CHARGE_RESISTIVITIES 1   /* also eta_o, eta_H, eta_a, gamma_d (res_Marchand)       */
@@ -279,6 +283,34 @@ int32_t shark_gpu_charge_stats(shark_gpu_ctx* ctx, int64_t* iters_hist, int64_t*
  * SHARK_CHARGE_RESISTIVITIES), Newton iterations per cell.  Any pointer may be NULL. */
 int32_t shark_gpu_download_charge(shark_gpu_ctx* ctx, double* zd, double* ni, double* ne, double* psi,
                                   double* eta, double* gamma_d, int32_t* iters);
+
+/* ---- charging network (SHARK_CHARGE_MLP_SEED) ----------------------------------------------
+ * A 6 -> 64 -> 64 -> 1 tanh MLP (BF16 tensor-core GEMMs, FP32 accumulate) maps a cell's
+ * log10 nH, log10 T, log10 zeta and grain moments log10(sum n_k pi a_k^2/nH), log10(sum n_k a_k/nH),
+ * log10(sum n_k/nH) to t = psi/psi0 - 1, the start point of the charging Newton on a cold start.
+ * Parameter blob (SHARK_MLP_NBLOB floats): W1[64][16] b1[64] W2[64][64] b2[64] w3[64] b3, then
+ * the feature means[6], standard deviations[6], target mean, standard deviation. */
+
+/* Charge the current state cold (psi_old = 0, the reference's start point) and append the
+ * (features, t) pairs of every converged cell to the training set, allocated on the first call
+ * with room for `capacity` pairs.  *count receives the fill level. */
+int32_t shark_gpu_mlp_collect(shark_gpu_ctx* ctx, int64_t capacity, int64_t* count);
+/* Adam on the mean squared error of the normalised target, `steps` mini-batches of `batch`
+ * pairs drawn without replacement (shuffled with `seed`), on the GPU.  The normalisation comes
+ * from the training set on the first training of a context without loaded weights.
+ * loss_curve (steps floats, nullable) receives the mini-batch losses. */
+int32_t shark_gpu_mlp_train(shark_gpu_ctx* ctx, int32_t steps, int32_t batch, float lr, uint64_t seed,
+                            float* loss_curve);
+int32_t shark_gpu_mlp_save(shark_gpu_ctx* ctx, float* blob, int64_t n);
+int32_t shark_gpu_mlp_load(shark_gpu_ctx* ctx, const float* blob, int64_t n);
+/* Network on host-given raw features (n x SHARK_MLP_NFEAT): out (n, nullable) receives t; with
+ * target (n) and grad (SHARK_MLP_NPARAM) also the gradient of sum((y - y*)^2)/n over the
+ * normalised outputs, without updating the weights (and *loss the sum of squares). */
+int32_t shark_gpu_mlp_eval(shark_gpu_ctx* ctx, const float* feat, const float* target, int64_t n, float* out,
+                           float* grad, float* loss);
+/* Network features of every cell of the current state, (ncells x SHARK_MLP_NFEAT), cells in
+ * Fortran order. */
+int32_t shark_gpu_mlp_features(shark_gpu_ctx* ctx, float* feat);
 
 int32_t shark_gpu_free(shark_gpu_ctx* ctx);
 

@@ -6,6 +6,7 @@ Three translation units compiled in parallel:
                      FP32 division on (the mixed path is held to 1e-5 L1 against FP64)
   shark_gpu.cu    -- host side of the C ABI (include/shark_gpu.h)
   noalloc.cu      -- shark_gpu_totals_noalloc (no allocations; fixed device scratch array)
+  mlp.cu          -- the charging network (tcgen05 BF16 GEMMs, TMEM accumulators, Adam)
 """
 import os
 import shutil
@@ -25,6 +26,7 @@ UNITS = [
     ("kernels_f32.cu", ["--fmad=true", "-prec-div=false"]),
     ("shark_gpu.cu", []),
     ("noalloc.cu", []),
+    ("mlp.cu", []),
 ]
 
 

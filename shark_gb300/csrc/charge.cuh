@@ -199,4 +199,58 @@ __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
     if (threadIdx.x == 0 && s_iter) atomicAdd(&p.hist[CHARGE_HIST + 1], s_iter);
 }
 
+// Network features of the cells (SHARK_MLP_NFEAT floats per cell, plane layout [plane][F]):
+// log10 nH, log10 T, log10 zeta, log10 of the grain cross-section, radius and number per H
+// (sum_k n_k pi a_k^2 / nH, sum_k n_k a_k / nH, sum_k n_k / nH).  The same state -> input map as
+// k_charge.  Pad columns of the plane get zeros.
+template <typename R>
+__global__ void __launch_bounds__(128) k_charge_features(ChargeParams<R> p, float* __restrict__ feat) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= p.plane) return;
+    const int iy = (int)(t / p.pitch), ix = (int)(t - (long long)iy * p.pitch);
+    float* f = feat + t * SHARK_MLP_NFEAT;
+    if (ix >= p.nx_max) {
+        for (int i = 0; i < SHARK_MLP_NFEAT; ++i) f[i] = 0.0f;
+        return;
+    }
+    const int N = p.ndust;
+    const int row = p.t_per_col ? ix : 0;
+    const double T = p.trow[(size_t)row * 8];
+    const double hs = p.hs ? p.hs[ix] : 1.0;
+    const double rho = (double)p.u[t] / hs;
+    const double nH = rho * p.unH;
+    double x = p.x0;
+    if (p.sig_att > 0.0) x = p.x0 * exp(-((double)p.u[t] * p.ud * p.ul) / p.sig_att);
+    double s2 = 0.0, s1 = 0.0, s0 = 0.0;
+    for (int k = 0; k < N; ++k) {
+        const double n = ((double)p.u[(long long)(5 + k) * p.plane + t] / hs) * p.ud / p.mkum[k];
+        s2 += n * chg::pi * p.l2[k];
+        s1 += n * sqrt(p.l2[k]);
+        s0 += n;
+    }
+    f[0] = (float)log10(nH);
+    f[1] = (float)log10(T);
+    f[2] = (float)log10(x);
+    f[3] = (float)log10(s2 / nH);
+    f[4] = (float)log10(s1 / nH);
+    f[5] = (float)log10(s0 / nH);
+}
+
+// Append (features, t = psi/psi0 - 1) of every cell the last charging call converged to the
+// network's training set (cap rows of SHARK_MLP_NFEAT + 1 floats; `count` is the fill level).
+template <typename R>
+__global__ void k_charge_collect(ChargeParams<R> p, const float* __restrict__ feat, float* __restrict__ out,
+                                 unsigned long long* count, long long cap) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= p.plane) return;
+    const int iy = (int)(t / p.pitch), ix = (int)(t - (long long)iy * p.pitch);
+    if (ix >= p.nx_max || iy >= p.ny_max) return;
+    if (p.iters[t] >= p.nitermax) return;
+    const unsigned long long slot = atomicAdd(count, 1ull);
+    if ((long long)slot >= cap) return;
+    float* o = out + slot * (SHARK_MLP_NFEAT + 1);
+    for (int i = 0; i < SHARK_MLP_NFEAT; ++i) o[i] = feat[t * SHARK_MLP_NFEAT + i];
+    o[SHARK_MLP_NFEAT] = (float)(p.psi_old[t] / p.psi0 - 1.0);
+}
+
 }  // namespace shark

@@ -223,7 +223,7 @@ cudaError_t launch_totals(const DeviceView& v, double* part_dev, int nblocks, do
 }
 
 template <typename R>
-cudaError_t launch_charge(const DeviceView& v) {
+static ChargeParams<R> charge_params(const DeviceView& v) {
     const ChargeView& c = v.chg;
     ChargeParams<R> q;
     q.u = (const R*)v.u[v.cur];
@@ -236,10 +236,32 @@ cudaError_t launch_charge(const DeviceView& v) {
     q.mu_ions = c.mu_ions; q.nitermax = c.nitermax;
     q.psi_old = c.psi_old; q.zd = (R*)c.zd; q.ni = (R*)c.ni; q.ne = (R*)c.ne; q.eta = (R*)c.eta;
     q.gamma_d = (R*)c.gamma_d; q.seed = c.seed; q.hist = c.hist; q.iters = c.iters;
+    return q;
+}
+
+template <typename R>
+cudaError_t launch_charge(const DeviceView& v) {
+    const ChargeView& c = v.chg;
+    ChargeParams<R> q = charge_params<R>(v);
     cudaError_t e = cudaMemsetAsync(c.hist, 0, (CHARGE_HIST + 2) * sizeof(unsigned long long), v.stream);
     if (e != cudaSuccess) return e;
     const long long n = (long long)v.nx_max * v.ny_max;
     k_charge<R><<<(unsigned)((n + 127) / 128), 128, 0, v.stream>>>(q);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_charge_features(const DeviceView& v, float* feat) {
+    ChargeParams<R> q = charge_params<R>(v);
+    k_charge_features<R><<<(unsigned)((v.plane + 127) / 128), 128, 0, v.stream>>>(q, feat);
+    return cudaGetLastError();
+}
+
+template <typename R>
+cudaError_t launch_charge_collect(const DeviceView& v, const float* feat, float* out, unsigned long long* count,
+                                  long long cap) {
+    ChargeParams<R> q = charge_params<R>(v);
+    k_charge_collect<R><<<(unsigned)((v.plane + 255) / 256), 256, 0, v.stream>>>(q, feat, out, count, cap);
     return cudaGetLastError();
 }
 
@@ -260,6 +282,8 @@ cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int c
     template cudaError_t launch_ctoprim<R>(const DeviceView&, double*, double*);                   \
     template cudaError_t launch_totals<R>(const DeviceView&, double*, int, double*);               \
     template cudaError_t launch_charge<R>(const DeviceView&);                                      \
+    template cudaError_t launch_charge_features<R>(const DeviceView&, float*);                     \
+    template cudaError_t launch_charge_collect<R>(const DeviceView&, const float*, float*, unsigned long long*, long long); \
     template cudaError_t launch_planes_to_fortran<R>(const DeviceView&, const void*, int, double*);
 
 }  // namespace shark

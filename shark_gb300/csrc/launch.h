@@ -72,6 +72,11 @@ template <typename R> cudaError_t launch_ctoprim(const DeviceView& v, double* q_
 template <typename R> cudaError_t launch_totals(const DeviceView& v, double* part_dev, int nblocks, double* out_dev);
 // charging (K5) on the current state; resets the iteration histogram first
 template <typename R> cudaError_t launch_charge(const DeviceView& v);
+// network features of every cell of the current state ([plane][SHARK_MLP_NFEAT] floats)
+template <typename R> cudaError_t launch_charge_features(const DeviceView& v, float* feat);
+// append (features, t) of the cells the last charging call converged to a training buffer
+template <typename R>
+cudaError_t launch_charge_collect(const DeviceView& v, const float* feat, float* out, unsigned long long* count, long long cap);
 // plane-layout array of `count` planes -> Fortran-order FP64 (ncells per plane)
 template <typename R> cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int count, double* dst_dev);
 

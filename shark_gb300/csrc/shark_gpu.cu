@@ -17,6 +17,9 @@
 
 #include "../../include/shark_gpu.h"
 #include "launch.h"
+#include "mlp.h"
+
+#include <random>
 
 namespace {
 
@@ -93,6 +96,22 @@ struct shark_gpu_ctx {
     unsigned long long* chg_hist = nullptr;
     float* chg_seed = nullptr;       // network start points (plane layout)
     int32_t* chg_iters = nullptr;    // Newton iterations per cell (plane layout)
+    bool chg_cold = true;            // psi_old is zero everywhere (no charging call since reset)
+    // charging network
+    float* mlp_blob = nullptr;       // SHARK_MLP_NBLOB FP32
+    uint8_t* mlp_packed = nullptr;   // BF16 operand packs
+    float* mlp_grad = nullptr;       // SHARK_MLP_NPARAM
+    float* mlp_adam = nullptr;       // m | v (2 x SHARK_MLP_NPARAM)
+    int mlp_step = 0;
+    bool mlp_ready = false;          // weights loaded or trained
+    float* mlp_feat = nullptr;       // [plane][SHARK_MLP_NFEAT]
+    float* mlp_train = nullptr;      // [cap][SHARK_MLP_NFEAT + 1] training pairs
+    long long mlp_cap = 0;
+    unsigned long long* mlp_count = nullptr;
+    int32_t* mlp_perm = nullptr;     // [cap]
+    float* mlp_scratch = nullptr;    // losses / eval inputs
+    size_t mlp_scratch_n = 0;
+    unsigned int* mlp_err = nullptr;
     long long nstep = 0;             // steps launched since upload
     bool uploaded = false;
     bool pending_read[2] = {false, false};
@@ -436,6 +455,10 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->chg_hist) cudaFree(c->chg_hist);
     if (c->chg_seed) cudaFree(c->chg_seed);
     if (c->chg_iters) cudaFree(c->chg_iters);
+    for (void* p : {(void*)c->mlp_blob, (void*)c->mlp_packed, (void*)c->mlp_grad, (void*)c->mlp_adam,
+                    (void*)c->mlp_feat, (void*)c->mlp_train, (void*)c->mlp_count, (void*)c->mlp_perm,
+                    (void*)c->mlp_scratch, (void*)c->mlp_err})
+        if (p) cudaFree(p);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return SHARK_OK;
@@ -464,6 +487,87 @@ int32_t wait_readback(shark_gpu_ctx* c, int slot, double* dt, unsigned int* st) 
     *dt = c->host_ring[slot];
     *st = *reinterpret_cast<unsigned int*>(c->host_ring + 2 + slot);
     c->status_seen |= *st;
+    return SHARK_OK;
+}
+
+// ---- charging network (mlp.cu) ------------------------------------------------------------
+namespace nn {
+constexpr int F = SHARK_MLP_NFEAT, KIN = 16, H = 64;
+constexpr int OFF_W1 = 0, OFF_B1 = H * KIN, OFF_W2 = OFF_B1 + H, OFF_B2 = OFF_W2 + H * H, OFF_W3 = OFF_B2 + H;
+constexpr int OFF_B3 = OFF_W3 + H, OFF_XMU = SHARK_MLP_NPARAM, OFF_XSD = OFF_XMU + F, OFF_TMU = OFF_XSD + F;
+constexpr int OFF_TSD = OFF_TMU + 1;
+}  // namespace nn
+
+int32_t mlp_alloc(shark_gpu_ctx* c) {
+    if (c->mlp_blob) return SHARK_OK;
+    CUDA_TRY(cudaMalloc(&c->mlp_blob, SHARK_MLP_NBLOB * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&c->mlp_packed, shark::mlp_packed_bytes()));
+    CUDA_TRY(cudaMalloc(&c->mlp_grad, SHARK_MLP_NPARAM * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&c->mlp_adam, 2 * SHARK_MLP_NPARAM * sizeof(float)));
+    CUDA_TRY(cudaMalloc(&c->mlp_count, sizeof(unsigned long long)));
+    CUDA_TRY(cudaMalloc(&c->mlp_err, sizeof(unsigned int)));
+    CUDA_TRY(cudaMemsetAsync(c->mlp_count, 0, sizeof(unsigned long long), c->stream));
+    CUDA_TRY(cudaMemsetAsync(c->mlp_err, 0, sizeof(unsigned int), c->stream));
+    // Glorot-uniform initial weights from a fixed seed, zero biases, identity normalisation
+    std::vector<float> b(SHARK_MLP_NBLOB, 0.0f);
+    std::mt19937 rng(12345u);
+    auto uni = [&](float lim) { return std::uniform_real_distribution<float>(-lim, lim)(rng); };
+    const float l1 = std::sqrt(6.0f / (nn::F + nn::H)), l2 = std::sqrt(6.0f / (2 * nn::H)), l3 = std::sqrt(6.0f / (nn::H + 1));
+    for (int j = 0; j < nn::H; ++j)
+        for (int i = 0; i < nn::F; ++i) b[nn::OFF_W1 + j * nn::KIN + i] = uni(l1);
+    for (int e = 0; e < nn::H * nn::H; ++e) b[nn::OFF_W2 + e] = uni(l2);
+    for (int j = 0; j < nn::H; ++j) b[nn::OFF_W3 + j] = uni(l3);
+    for (int i = 0; i < nn::F; ++i) b[nn::OFF_XSD + i] = 1.0f;
+    b[nn::OFF_TSD] = 1.0f;
+    CUDA_TRY(cudaMemcpy(c->mlp_blob, b.data(), b.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemsetAsync(c->mlp_adam, 0, 2 * SHARK_MLP_NPARAM * sizeof(float), c->stream));
+    cudaError_t e = shark::mlp_pack(c->mlp_blob, c->mlp_packed, c->stream);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "mlp pack: %s", cudaGetErrorString(e));
+    c->mlp_step = 0;
+    return SHARK_OK;
+}
+
+int32_t mlp_scratch(shark_gpu_ctx* c, size_t n) {
+    if (c->mlp_scratch_n >= n) return SHARK_OK;
+    if (c->mlp_scratch) cudaFree(c->mlp_scratch);
+    c->mlp_scratch = nullptr;
+    c->mlp_scratch_n = 0;
+    CUDA_TRY(cudaMalloc(&c->mlp_scratch, n * sizeof(float)));
+    c->mlp_scratch_n = n;
+    return SHARK_OK;
+}
+
+int32_t features(shark_gpu_ctx* c) {
+    if (!c->mlp_feat) CUDA_TRY(cudaMalloc(&c->mlp_feat, (size_t)c->v.plane * SHARK_MLP_NFEAT * sizeof(float)));
+    cudaError_t e = is_mixed(c) ? shark::launch_charge_features<float>(c->v, c->mlp_feat)
+                                : shark::launch_charge_features<double>(c->v, c->mlp_feat);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "charge features: %s", cudaGetErrorString(e));
+    return SHARK_OK;
+}
+
+// Network start points for the next charging call (SHARK_CHARGE_MLP_SEED on a cold start).
+int32_t seed_charges(shark_gpu_ctx* c) {
+    shark::ChargeView& cv = c->v.chg;
+    cv.use_seed = 0;
+    cv.seed = nullptr;
+    if (!(c->cfg.chg_mode & SHARK_CHARGE_MLP_SEED) || !c->chg_cold) return SHARK_OK;
+    if (!c->mlp_ready) return fail(SHARK_ERR_STATE, "SHARK_CHARGE_MLP_SEED without trained or loaded weights");
+    int32_t rc = features(c);
+    if (rc) return rc;
+    if (!c->chg_seed) CUDA_TRY(cudaMalloc(&c->chg_seed, (size_t)c->v.plane * sizeof(float)));
+    shark::MlpArgs a{};
+    a.feat = c->mlp_feat;
+    a.feat_stride = SHARK_MLP_NFEAT;
+    a.n = (int)c->v.plane;
+    a.blob = c->mlp_blob;
+    a.packed = c->mlp_packed;
+    a.seed = c->chg_seed;
+    a.psi0 = cv.psi0;
+    a.err = c->mlp_err;
+    cudaError_t e = shark::mlp_forward(a, c->stream);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "mlp forward: %s", cudaGetErrorString(e));
+    cv.use_seed = 1;
+    cv.seed = c->chg_seed;
     return SHARK_OK;
 }
 
@@ -724,8 +828,13 @@ int32_t shark_gpu_step(shark_gpu_ctx* c, double* dt_out, int32_t* status_out) {
         if (status_out) *status_out = (int32_t)c->status_seen;
         return SHARK_OK;
     }
+    if (c->v.chg.on) {
+        int32_t rs = seed_charges(c);
+        if (rs) return rs;
+    }
     cudaError_t e = do_step(c, slot);
     if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+    c->chg_cold = false;
     c->v.cur = shark::next_cur(c->v);
     c->nstep++;
     int32_t rc = queue_readback(c, 1 - slot);   // dt of the next step, written by k_finalize
@@ -890,9 +999,12 @@ int32_t shark_gpu_charge(shark_gpu_ctx* c) {
     if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
     if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
     if (!c->uploaded) return fail(SHARK_ERR_STATE, "charge before upload");
+    int32_t rc = seed_charges(c);
+    if (rc) return rc;
     cudaError_t e = is_mixed(c) ? shark::launch_charge<float>(c->v) : shark::launch_charge<double>(c->v);
     if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "charge: %s", cudaGetErrorString(e));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->chg_cold = false;
     return SHARK_OK;
 }
 
@@ -901,6 +1013,199 @@ int32_t shark_gpu_charge_reset(shark_gpu_ctx* c) {
     if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
     CUDA_TRY(cudaMemsetAsync(c->chg_psi, 0, (size_t)c->v.plane * sizeof(double), c->stream));
     CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->chg_cold = true;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_mlp_load(shark_gpu_ctx* c, const float* blob, int64_t n) {
+    if (!c || !blob) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (n != SHARK_MLP_NBLOB) return fail(SHARK_ERR_INVALID_ARG, "blob has %lld floats, expected %d", (long long)n, SHARK_MLP_NBLOB);
+    int32_t rc = mlp_alloc(c);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(c->mlp_blob, blob, SHARK_MLP_NBLOB * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    cudaError_t e = shark::mlp_pack(c->mlp_blob, c->mlp_packed, c->stream);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "mlp pack: %s", cudaGetErrorString(e));
+    CUDA_TRY(cudaMemsetAsync(c->mlp_adam, 0, 2 * SHARK_MLP_NPARAM * sizeof(float), c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    c->mlp_step = 0;
+    c->mlp_ready = true;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_mlp_save(shark_gpu_ctx* c, float* blob, int64_t n) {
+    if (!c || !blob) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (n != SHARK_MLP_NBLOB) return fail(SHARK_ERR_INVALID_ARG, "blob has %lld floats, expected %d", (long long)n, SHARK_MLP_NBLOB);
+    int32_t rc = mlp_alloc(c);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemcpyAsync(blob, c->mlp_blob, SHARK_MLP_NBLOB * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_mlp_collect(shark_gpu_ctx* c, int64_t capacity, int64_t* count) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "collect before upload");
+    int32_t rc = mlp_alloc(c);
+    if (rc) return rc;
+    if (!c->mlp_train) {
+        if (capacity <= 0) return fail(SHARK_ERR_INVALID_ARG, "capacity must be > 0");
+        CUDA_TRY(cudaMalloc(&c->mlp_train, (size_t)capacity * (SHARK_MLP_NFEAT + 1) * sizeof(float)));
+        CUDA_TRY(cudaMalloc(&c->mlp_perm, (size_t)capacity * sizeof(int32_t)));
+        c->mlp_cap = capacity;
+    }
+    // the plain Newton from the reference's cold start gives the converged solutions
+    CUDA_TRY(cudaMemsetAsync(c->chg_psi, 0, (size_t)c->v.plane * sizeof(double), c->stream));
+    shark::ChargeView& cv = c->v.chg;
+    cv.use_seed = 0;
+    cv.seed = nullptr;
+    cudaError_t e = is_mixed(c) ? shark::launch_charge<float>(c->v) : shark::launch_charge<double>(c->v);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "charge: %s", cudaGetErrorString(e));
+    c->chg_cold = false;
+    if ((rc = features(c))) return rc;
+    e = is_mixed(c) ? shark::launch_charge_collect<float>(c->v, c->mlp_feat, c->mlp_train, c->mlp_count, c->mlp_cap)
+                    : shark::launch_charge_collect<double>(c->v, c->mlp_feat, c->mlp_train, c->mlp_count, c->mlp_cap);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "collect: %s", cudaGetErrorString(e));
+    unsigned long long n = 0;
+    CUDA_TRY(cudaMemcpyAsync(&n, c->mlp_count, sizeof n, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if ((long long)n > c->mlp_cap) {
+        n = (unsigned long long)c->mlp_cap;
+        CUDA_TRY(cudaMemcpy(c->mlp_count, &n, sizeof n, cudaMemcpyHostToDevice));
+    }
+    if (count) *count = (int64_t)n;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_mlp_train(shark_gpu_ctx* c, int32_t steps, int32_t batch, float lr, uint64_t seed, float* loss_curve) {
+    if (!c) return fail(SHARK_ERR_INVALID_ARG, "ctx is NULL");
+    if (steps <= 0 || batch <= 0 || !(lr > 0.0f)) return fail(SHARK_ERR_INVALID_ARG, "steps, batch and lr must be > 0");
+    if (!c->mlp_train) return fail(SHARK_ERR_STATE, "no training samples: call shark_gpu_mlp_collect first");
+    unsigned long long n = 0;
+    CUDA_TRY(cudaMemcpy(&n, c->mlp_count, sizeof n, cudaMemcpyDeviceToHost));
+    if (n < (unsigned long long)batch) return fail(SHARK_ERR_STATE, "%llu samples < batch %d", n, batch);
+    const int F = SHARK_MLP_NFEAT;
+    // normalisation of the features and of the target from the training set (first training only)
+    std::vector<float> h((size_t)n * (F + 1));
+    CUDA_TRY(cudaMemcpy(h.data(), c->mlp_train, h.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    if (!c->mlp_ready) {
+        std::vector<float> nb(F * 2 + 2);
+        for (int i = 0; i <= F; ++i) {
+            double s = 0.0, s2 = 0.0;
+            for (size_t r = 0; r < n; ++r) { const double x = h[r * (F + 1) + i]; s += x; s2 += x * x; }
+            const double mu = s / (double)n, var = std::max(s2 / (double)n - mu * mu, 0.0);
+            const double sd = std::sqrt(var) > 1e-12 ? std::sqrt(var) : 1.0;
+            if (i < F) { nb[i] = (float)mu; nb[F + i] = (float)sd; }
+            else { nb[2 * F] = (float)mu; nb[2 * F + 1] = (float)sd; }
+        }
+        CUDA_TRY(cudaMemcpy(c->mlp_blob + nn::OFF_XMU, nb.data(), nb.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    int32_t rc = mlp_scratch(c, (size_t)steps);
+    if (rc) return rc;
+    CUDA_TRY(cudaMemsetAsync(c->mlp_scratch, 0, (size_t)steps * sizeof(float), c->stream));
+    std::mt19937_64 rng(seed);
+    std::vector<int32_t> perm(n);
+    for (size_t i = 0; i < n; ++i) perm[i] = (int32_t)i;
+    size_t pos = n;
+    shark::MlpArgs a{};
+    a.feat = c->mlp_train;
+    a.target = c->mlp_train;
+    a.feat_stride = F + 1;
+    a.n = batch;
+    a.blob = c->mlp_blob;
+    a.packed = c->mlp_packed;
+    a.grad = c->mlp_grad;
+    a.inv_n = 1.0f / (float)batch;
+    a.err = c->mlp_err;
+    for (int s = 0; s < steps; ++s) {
+        if (pos + (size_t)batch > n) {
+            std::shuffle(perm.begin(), perm.end(), rng);
+            CUDA_TRY(cudaMemcpyAsync(c->mlp_perm, perm.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+            CUDA_TRY(cudaStreamSynchronize(c->stream));
+            pos = 0;
+        }
+        a.index = c->mlp_perm + pos;
+        a.loss = c->mlp_scratch + s;
+        pos += (size_t)batch;
+        CUDA_TRY(cudaMemsetAsync(c->mlp_grad, 0, SHARK_MLP_NPARAM * sizeof(float), c->stream));
+        cudaError_t e = shark::mlp_backward(a, c->stream);
+        if (e == cudaSuccess) e = shark::mlp_adam(c->mlp_blob, c->mlp_grad, c->mlp_adam, c->mlp_adam + SHARK_MLP_NPARAM, lr,
+                                                  ++c->mlp_step, c->stream);
+        if (e == cudaSuccess) e = shark::mlp_pack(c->mlp_blob, c->mlp_packed, c->stream);
+        if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "mlp training step: %s", cudaGetErrorString(e));
+    }
+    unsigned int err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, c->mlp_err, sizeof err, cudaMemcpyDeviceToHost, c->stream));
+    if (loss_curve) CUDA_TRY(cudaMemcpyAsync(loss_curve, c->mlp_scratch, (size_t)steps * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (err) return fail(SHARK_ERR_CUDA, "a tensor-core completion wait of the network gave up");
+    if (loss_curve) for (int s = 0; s < steps; ++s) loss_curve[s] /= (float)batch;
+    c->mlp_ready = true;
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_mlp_eval(shark_gpu_ctx* c, const float* feat, const float* target, int64_t n, float* out, float* grad,
+                           float* loss) {
+    if (!c || !feat || n <= 0 || n > (1 << 30)) return fail(SHARK_ERR_INVALID_ARG, "bad argument");
+    int32_t rc = mlp_alloc(c);
+    if (rc) return rc;
+    const int F = SHARK_MLP_NFEAT;
+    if ((rc = mlp_scratch(c, (size_t)n * (F + 1) + (size_t)n + 1))) return rc;
+    std::vector<float> h((size_t)n * (F + 1), 0.0f);
+    for (int64_t r = 0; r < n; ++r) {
+        for (int i = 0; i < F; ++i) h[r * (F + 1) + i] = feat[r * F + i];
+        if (target) h[r * (F + 1) + F] = target[r];
+    }
+    float* d_in = c->mlp_scratch;
+    float* d_out = c->mlp_scratch + (size_t)n * (F + 1);
+    float* d_loss = d_out + n;
+    CUDA_TRY(cudaMemcpyAsync(d_in, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    shark::MlpArgs a{};
+    a.feat = d_in;
+    a.target = d_in;
+    a.feat_stride = F + 1;
+    a.n = (int)n;
+    a.blob = c->mlp_blob;
+    a.packed = c->mlp_packed;
+    a.err = c->mlp_err;
+    a.out = d_out;
+    cudaError_t e = shark::mlp_forward(a, c->stream);
+    if (e == cudaSuccess && target && grad) {
+        a.out = nullptr;
+        a.grad = c->mlp_grad;
+        a.loss = d_loss;
+        a.inv_n = 1.0f / (float)n;
+        e = cudaMemsetAsync(c->mlp_grad, 0, SHARK_MLP_NPARAM * sizeof(float), c->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_loss, 0, sizeof(float), c->stream);
+        if (e == cudaSuccess) e = shark::mlp_backward(a, c->stream);
+    }
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "mlp eval: %s", cudaGetErrorString(e));
+    if (out) CUDA_TRY(cudaMemcpyAsync(out, d_out, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (target && grad) {
+        CUDA_TRY(cudaMemcpyAsync(grad, c->mlp_grad, SHARK_MLP_NPARAM * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+        if (loss) CUDA_TRY(cudaMemcpyAsync(loss, d_loss, sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    }
+    unsigned int err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, c->mlp_err, sizeof err, cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (err) return fail(SHARK_ERR_CUDA, "a tensor-core completion wait of the network gave up");
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_mlp_features(shark_gpu_ctx* c, float* feat) {
+    if (!c || !feat) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (!c->v.chg.on) return fail(SHARK_ERR_STATE, "charging is not enabled in this context");
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "features before upload");
+    int32_t rc = features(c);
+    if (rc) return rc;
+    const shark::DeviceView& v = c->v;
+    std::vector<float> h((size_t)v.plane * SHARK_MLP_NFEAT);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), c->mlp_feat, h.size() * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    for (int iy = 0; iy < v.ny_max; ++iy)
+        for (int ix = 0; ix < v.nx_max; ++ix)
+            for (int i = 0; i < SHARK_MLP_NFEAT; ++i)
+                feat[((size_t)iy * v.nx_max + ix) * SHARK_MLP_NFEAT + i] = h[((size_t)iy * v.pitch + ix) * SHARK_MLP_NFEAT + i];
     return SHARK_OK;
 }
 

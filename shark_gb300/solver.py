@@ -24,7 +24,10 @@ EXPORTS = [
     "shark_gpu_totals", "shark_gpu_last_step_ms", "shark_gpu_timed_run", "shark_gpu_kernel_times",
     "shark_gpu_totals_noalloc", "shark_gpu_last_error", "shark_gpu_free",
     "shark_gpu_charge", "shark_gpu_charge_reset", "shark_gpu_charge_stats", "shark_gpu_download_charge",
+    "shark_gpu_mlp_collect", "shark_gpu_mlp_train", "shark_gpu_mlp_save", "shark_gpu_mlp_load",
+    "shark_gpu_mlp_eval", "shark_gpu_mlp_features",
 ]
+MLP_NFEAT, MLP_NPARAM, MLP_NBLOB = 6, 5313, 5327
 CHARGE_HIST = 64   # SHARK_CHARGE_HIST
 
 
@@ -79,9 +82,15 @@ def load_library(path=None):
     L.shark_gpu_free.restype = I32
     L.shark_gpu_free.argtypes = [P]
     I64P = C.POINTER(C.c_int64)
+    FP = C.POINTER(C.c_float)
     for name, args in [("shark_gpu_charge", [P]), ("shark_gpu_charge_reset", [P]),
                        ("shark_gpu_charge_stats", [P, I64P, I64P, I64P]),
-                       ("shark_gpu_download_charge", [P, D, D, D, D, D, D, C.POINTER(C.c_int32)])]:
+                       ("shark_gpu_download_charge", [P, D, D, D, D, D, D, C.POINTER(C.c_int32)]),
+                       ("shark_gpu_mlp_collect", [P, C.c_int64, I64P]),
+                       ("shark_gpu_mlp_train", [P, I32, I32, C.c_float, C.c_uint64, FP]),
+                       ("shark_gpu_mlp_save", [P, FP, C.c_int64]), ("shark_gpu_mlp_load", [P, FP, C.c_int64]),
+                       ("shark_gpu_mlp_eval", [P, FP, FP, C.c_int64, FP, FP, FP]),
+                       ("shark_gpu_mlp_features", [P, FP])]:
         f = getattr(L, name)
         f.restype = I32
         f.argtypes = args
@@ -257,3 +266,53 @@ class Shark:
                "shark_gpu_download_charge")
         return dict(zd=zd.reshape(N, nc), ni=ni, ne=ne, psi=psi, eta=eta.reshape(3, nc), gamma_d=gd.reshape(N, nc),
                     iters=it)
+
+    # ---- charging network (SHARK_CHARGE_MLP_SEED) -----------------------------------------------
+    def mlp_collect(self, capacity=1 << 22):
+        """Cold-charge the current state and add its converged (features, t) pairs to the
+        training set; returns the number of pairs held."""
+        n = C.c_int64(0)
+        _check(load_library().shark_gpu_mlp_collect(self._h, int(capacity), C.byref(n)), "shark_gpu_mlp_collect")
+        return n.value
+
+    def mlp_train(self, steps, batch=4096, lr=1e-3, seed=1):
+        """Train on the GPU; returns the mini-batch loss curve."""
+        loss = np.zeros(steps, dtype=np.float32)
+        _check(load_library().shark_gpu_mlp_train(self._h, int(steps), int(batch), float(lr), int(seed),
+                                                  loss.ctypes.data_as(C.POINTER(C.c_float))), "shark_gpu_mlp_train")
+        return loss
+
+    def mlp_save(self):
+        b = np.zeros(MLP_NBLOB, dtype=np.float32)
+        _check(load_library().shark_gpu_mlp_save(self._h, b.ctypes.data_as(C.POINTER(C.c_float)), MLP_NBLOB),
+               "shark_gpu_mlp_save")
+        return b
+
+    def mlp_load(self, blob):
+        b = np.ascontiguousarray(blob, dtype=np.float32)
+        _check(load_library().shark_gpu_mlp_load(self._h, b.ctypes.data_as(C.POINTER(C.c_float)), b.size),
+               "shark_gpu_mlp_load")
+
+    def mlp_eval(self, feat, target=None):
+        """(t per sample, gradient or None, loss or None) of the network on raw features."""
+        f = np.ascontiguousarray(feat, dtype=np.float32).reshape(-1, MLP_NFEAT)
+        n = f.shape[0]
+        out = np.zeros(n, dtype=np.float32)
+        FPt = C.POINTER(C.c_float)
+        if target is None:
+            _check(load_library().shark_gpu_mlp_eval(self._h, f.ctypes.data_as(FPt), None, n,
+                                                     out.ctypes.data_as(FPt), None, None), "shark_gpu_mlp_eval")
+            return out, None, None
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        g = np.zeros(MLP_NPARAM, dtype=np.float32)
+        loss = C.c_float(0)
+        _check(load_library().shark_gpu_mlp_eval(self._h, f.ctypes.data_as(FPt), t.ctypes.data_as(FPt), n,
+                                                 out.ctypes.data_as(FPt), g.ctypes.data_as(FPt), C.byref(loss)),
+               "shark_gpu_mlp_eval")
+        return out, g, loss.value
+
+    def mlp_features(self):
+        f = np.zeros(self.ncells * MLP_NFEAT, dtype=np.float32)
+        _check(load_library().shark_gpu_mlp_features(self._h, f.ctypes.data_as(C.POINTER(C.c_float))),
+               "shark_gpu_mlp_features")
+        return f.reshape(self.ncells, MLP_NFEAT)

@@ -1,0 +1,123 @@
+"""The charging network on the GPU: tcgen05 BF16 forward/backward kernels against the numpy
+oracle (oracle/mlp_oracle.py, same BF16 rounding points), the device feature map against numpy,
+GPU training on (state, converged psi) pairs from the charging solver, and the gain it brings:
+fewer Newton iterations from a cold start at the same residual tolerance.
+
+Tolerances: the forward output within 2e-3 of the target scale and every gradient group within
+1e-2 relative L2 of the oracle (FP32 accumulation order of the tensor cores, tanhf vs numpy tanh
+moving a few BF16 roundings by one unit)."""
+import math
+
+import numpy as np
+import pytest
+
+from shark_gb300 import config as K, setups
+from shark_gb300.solver import Shark
+from oracle import mlp_oracle as M
+from tests.test_charge_cpu import _noisy_turb
+from tests.test_mlp_cpu import _blob
+
+pytestmark = pytest.mark.gpu
+
+MH = 1.67e-24
+
+
+def _ctx(n=32, ndust=8, seed_mode=False):
+    cfg, u0 = _noisy_turb(n=n, ndust=ndust)
+    if seed_mode:
+        cfg.chg_mode |= K.CHARGE_MLP_SEED
+    return cfg, u0, Shark(cfg)
+
+
+def test_forward_matches_oracle():
+    cfg, u0, g = _ctx(n=8)
+    with g:
+        blob = _blob(2).astype(np.float32)
+        g.mlp_load(blob)
+        rng = np.random.default_rng(1)
+        feat = (rng.standard_normal((1000, M.F)) * 1.3 + blob[M.OFF_XMU:M.OFF_XSD]).astype(np.float32)
+        out, _, _ = g.mlp_eval(feat)
+    ref, _ = M.forward(blob, feat)
+    assert np.max(np.abs(out - ref)) <= 2e-3 * blob[M.OFF_TSD]
+
+
+def test_gradient_matches_oracle():
+    cfg, u0, g = _ctx(n=8)
+    with g:
+        blob = _blob(4).astype(np.float32)
+        g.mlp_load(blob)
+        rng = np.random.default_rng(2)
+        feat = (rng.standard_normal((1000, M.F)) + blob[M.OFF_XMU:M.OFF_XSD]).astype(np.float32)
+        target = rng.standard_normal(1000).astype(np.float32)
+        _, grad, loss = g.mlp_eval(feat, target)
+    ref, ref_loss = M.gradient(blob, feat, target)
+    assert loss == pytest.approx(ref_loss, rel=1e-2)
+    groups = dict(W1=(M.OFF_W1, M.OFF_B1), b1=(M.OFF_B1, M.OFF_W2), W2=(M.OFF_W2, M.OFF_B2), b2=(M.OFF_B2, M.OFF_W3),
+                  w3=(M.OFF_W3, M.OFF_B3), b3=(M.OFF_B3, M.NPARAM))
+    for name, (a, b) in groups.items():
+        err = np.linalg.norm(grad[a:b] - ref[a:b]) / max(np.linalg.norm(ref[a:b]), 1e-30)
+        assert err <= 1e-2, (name, err)
+
+
+def test_features_match_numpy():
+    cfg, u0, g = _ctx(n=16)
+    with g:
+        g.upload(u0)
+        f = g.mlp_features()
+    N = cfg.ndust
+    q = u0.reshape(cfg.nvar, -1)
+    nH = q[0] / (cfg.mu_gas * MH)
+    a = np.array(cfg.dust_size[:N])
+    m = float(np.float32(4.0) / np.float32(3.0)) * math.pi * cfg.rhograin * a ** 3
+    nk = q[5:5 + N] / m[:, None]
+    ref = np.stack([np.log10(nH), np.full_like(nH, math.log10(cfg.T_cloud)), np.full_like(nH, math.log10(cfg.chg_x)),
+                    np.log10((nk * math.pi * a[:, None] ** 2).sum(0) / nH), np.log10((nk * a[:, None]).sum(0) / nH),
+                    np.log10(nk.sum(0) / nH)], axis=1)
+    np.testing.assert_allclose(f, ref, rtol=1e-5, atol=1e-5)
+
+
+def _train_on_varied_states(g, cfg, u0, factors, seeds):
+    n = 0
+    for f in factors:
+        for s in seeds:
+            _, u = _noisy_turb(n=cfg.nx, ndust=cfg.ndust, seed=s, amp=0.5)
+            g.upload(u * f)
+            n = g.mlp_collect(capacity=1 << 20)
+    loss1 = g.mlp_train(3000, batch=2048, lr=2e-3, seed=7)
+    loss2 = g.mlp_train(3000, batch=2048, lr=3e-4, seed=8)
+    return n, np.concatenate([loss1, loss2])
+
+
+def test_trained_network_cuts_cold_start_newton_iterations():
+    factors = [0.03, 0.1, 0.3, 1.0, 3.0, 10.0, 30.0]
+    cfg, u0, g = _ctx(n=48, ndust=8)
+    with g:
+        n, loss = _train_on_varied_states(g, cfg, u0, factors, seeds=[11, 12])
+        blob = g.mlp_save()
+        assert n > 20000
+        assert loss[-200:].mean() < 0.02 * loss[:50].mean()
+        # held-out states: new noise, densities between the training ones
+        res = []
+        for f in (0.5, 2.0, 5.0):
+            _, u = _noisy_turb(n=48, ndust=8, seed=99, amp=0.5)
+            u = u * f
+            g.upload(u)
+            g.charge_reset()
+            g.charge()
+            _, nc_ref, it_ref = g.charge_stats()
+            ref = g.download_charge()
+            cfg_s = cfg.copy()
+            cfg_s.chg_mode |= K.CHARGE_MLP_SEED
+            with Shark(cfg_s) as s:
+                s.mlp_load(blob)
+                s.upload(u)
+                s.charge()
+                _, nc_mlp, it_mlp = s.charge_stats()
+                got = s.download_charge()
+            conv = ref["iters"] < cfg.chg_nitermax
+            # same converged tolerance: the same cells converge, to the same potential
+            assert nc_mlp == nc_ref
+            assert np.max(np.abs(got["psi"][conv] - ref["psi"][conv]) / np.abs(ref["psi"][conv])) < 1e-5
+            res.append((it_ref, it_mlp))
+    ratio = sum(r for r, _ in res) / sum(m for _, m in res)
+    assert ratio >= 3.0, res
