@@ -9,8 +9,8 @@
 //   T    = per temperature row (one row, or one per column for the disk), with the T-only
 //          constants sigmav_ie, vi, tau_k, alpha_k tabulated on the host
 //   zeta = chg_x, attenuated by exp(-Sigma unit_d unit_l/chg_sigma_att) for the disk.
-// R = double follows the CPU oracle operation by operation (nvcc --fmad=false); R = float is
-// the mixed-precision form of the same iteration.  Outputs: psi_old (FP64, the warm start of the
+// R = double follows the CPU oracle operation by operation (nvcc --fmad=false); R = float
+// (mixed precision) runs the cold part of the iteration in FP32 and finishes it in FP64.  Outputs: psi_old (FP64, the warm start of the
 // next call), zd (N planes), ni, ne, and with SHARK_CHARGE_RESISTIVITIES eta_o/H/a and gamma_d,
 // plus the per-call histogram of Newton iteration counts.
 #pragma once
@@ -67,6 +67,65 @@ __device__ __forceinline__ R dsqrt_(R x);
 template <> __device__ __forceinline__ double dsqrt_<double>(double x) { return sqrt(x); }
 template <> __device__ __forceinline__ float dsqrt_<float>(float x) { return sqrtf(x); }
 
+// One Newton iteration loop of ionisation.f90:79-135 in arithmetic C: iterates while
+// |f(psi)| > tol and niter < nitermax, updating psi, niter, lowT and conv (|f| of the last
+// evaluation).  `nk(k)` gives the grain number density of species k in C.  With stall = true the
+// loop also stops when an update leaves psi unchanged (no further progress in C).
+template <typename C, typename R, typename NK>
+__device__ __forceinline__ void charge_newton(const ChargeParams<R>& p, const double* tau, const double* alp, NK nk,
+                                              C nH, C x, C sigmav_ie, C vi, C tol, bool stall, C& psi, int& niter,
+                                              int& lowT, C& conv) {
+    const int N = p.ndust;
+    const C pi = C(chg::pi);
+    const C thetai = C(p.thetai), th2 = C(p.th2), th3 = C(p.th3), psi0 = C(p.psi0);
+    const C one = C(1), two = C(2);
+    const C xnH = x * nH;
+    while (conv > tol && niter < p.nitermax) {
+        const C eps_psi = (one - psi) / thetai * dexp<C>(-psi);
+        const C et = eps_psi * thetai;
+        const C et2 = et * et;
+        const C om = one - eps_psi;
+        const C D = (-eps_psi * (two - psi) / (one - psi));
+        C S1 = C(0), S2 = C(0), S3 = C(0), S4 = C(0), S5 = C(0), S6 = C(0);
+        C n_i = C(0);
+        for (int k = 0; k < N; ++k) {
+            const C n = nk(k), tk = C(tau[k]), ak = C(alp[k]), l2 = C(p.l2[k]);
+            const C den = one + et * ak + et2;
+            n_i = n_i + (-(psi * tk + (one - et2) / den) * n / om);
+            const C npl = n * pi * l2;
+            S1 = S1 + npl * ((one - psi) + (two / tk) * (et2 + et) / den);
+            S2 = S2 + n * (-(et2 * et2) + (C(4) * th2 - th3 * ak) * (eps_psi * eps_psi) +
+                           (two * thetai * ak - C(4) * th2) * eps_psi + one - thetai * ak) / (den * den);
+            S3 = S3 + n * tk;
+            S4 = S4 + npl / (tk * den);
+            S5 = S5 + npl * (two * eps_psi * th2 + thetai * ak) / (tk * (den * den));
+            S6 = S6 + npl;
+        }
+        const C fpsi = sigmav_ie * eps_psi * (n_i * n_i) / (xnH) + n_i * vi / (xnH) * (S1) - one;
+        const C dni = -one / (om * om) * (D) * (S2) - (psi / om * (D) + one) * S3 / om;
+        const C dfdpsi = sigmav_ie * n_i / (xnH) * (n_i * (D) + two * eps_psi * dni) +
+                         two * n_i * vi / (xnH) * (et2 + et) *
+                             ((dni / n_i + (D) * (two * et + one) / (eps_psi * (one + et))) * (S4) + ((D) * S5)) +
+                         n_i * vi / (xnH) * (dni / n_i * (one - psi) - one) * (S6);
+        const C prev = psi;
+        psi = psi - fpsi / dfdpsi;
+        if (psi < psi0) {
+            psi = psi0 * C(0.9999999);
+            lowT = 1;
+        } else if (psi > C(0)) {
+            psi = C(-1e-5);
+        }
+        conv = fabs(fpsi);
+        niter = niter + 1;
+        if (stall && psi == prev) break;
+    }
+}
+
+// K5.  R = double: the reference loop in FP64 (parity path).  R = float (mixed precision): from a
+// cold or network start, FP32 Newton steps until |f| < 1e-3 or psi stops moving in FP32, then FP64
+// steps to the reference tolerance chg_eps; a warm start (psi_old, FP64) goes to FP64 directly.
+// The residual is steep (|df/dpsi| ~ 1e2-1e3 at the root), so an FP32 psi pins f only to ~1e-4:
+// the last digits need FP64.  The iteration count is the sum of both phases.
 template <typename R>
 __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
     const int N = p.ndust;
@@ -84,113 +143,82 @@ __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
         const double* tr = p.trow + (size_t)row * 8;
         const double* tau = p.tau + (size_t)row * N;
         const double* alp = p.alpha + (size_t)row * N;
-        const R pi = R(chg::pi);
-        const R hs = p.hs ? R(p.hs[ix]) : R(1);
-        const R rho = p.u[c] / hs;
-        const R nH = rho * R(p.unH);
-        R x = R(p.x0);
-        if (p.sig_att > 0.0) x = R(p.x0) * dexp<R>(-(p.u[c] * R(p.ud) * R(p.ul)) / R(p.sig_att));
-        const R sigmav_ie = R(tr[1]), vi = R(tr[2]);
-        const R thetai = R(p.thetai), th2 = R(p.th2), th3 = R(p.th3), psi0 = R(p.psi0);
-        const R one = R(1), two = R(2);
-        const R xnH = x * nH;
-        // n_k of this cell
-        auto nk = [&](int k) -> R { return (p.u[(long long)(5 + k) * p.plane + c] / hs) * R(p.ud) / R(p.mkum[k]); };
-        R conv = R(1e4);
-        R psi = psi0;
-        int niter = 0;
+        // cell inputs in FP64 (the FP64 path reproduces the oracle's operation order)
+        const double hs = p.hs ? p.hs[ix] : 1.0;
+        const double u0 = (double)p.u[c];
+        const double rho = u0 / hs;
+        const double nH = rho * p.unH;
+        double x = p.x0;
+        if (p.sig_att > 0.0) x = p.x0 * exp(-(u0 * p.ud * p.ul) / p.sig_att);
+        auto nk64 = [&](int k) -> double { return ((double)p.u[(long long)(5 + k) * p.plane + c] / hs) * p.ud / p.mkum[k]; };
+        const double sigmav_ie = tr[1], vi = tr[2];
+        const double thetai = p.thetai, th2 = p.th2, psi0 = p.psi0;
+        double psi = psi0, conv = 1e4;
+        int niter = 0, lowT = 0;
         const double pold = p.psi_old[c];
-        if (pold != 0.0) psi = R(pold);
+        bool cold = true;
+        if (pold != 0.0) { psi = pold; cold = false; }
         if (p.seed && (p.use_seed == 2 || (p.use_seed == 1 && pold == 0.0))) {
             const float sd = p.seed[c];
-            if (sd < 0.0f) psi = R(sd);
+            if (sd < 0.0f) { psi = (double)sd; cold = true; }
         }
-        int lowT = 0;
-        R eps_psi, n_i = R(0);
-        while (conv > R(p.eps) && niter < p.nitermax) {
-            eps_psi = (one - psi) / thetai * dexp<R>(-psi);
-            const R et = eps_psi * thetai;
-            const R et2 = et * et;
-            const R om = one - eps_psi;
-            const R D = (-eps_psi * (two - psi) / (one - psi));
-            R S1 = R(0), S2 = R(0), S3 = R(0), S4 = R(0), S5 = R(0), S6 = R(0);
-            n_i = R(0);
-            for (int k = 0; k < N; ++k) {
-                const R n = nk(k), tk = R(tau[k]), ak = R(alp[k]), l2 = R(p.l2[k]);
-                const R den = one + et * ak + et2;
-                n_i = n_i + (-(psi * tk + (one - et2) / den) * n / om);
-                const R npl = n * pi * l2;
-                S1 = S1 + npl * ((one - psi) + (two / tk) * (et2 + et) / den);
-                S2 = S2 + n * (-(et2 * et2) + (R(4) * th2 - th3 * ak) * (eps_psi * eps_psi) +
-                               (two * thetai * ak - R(4) * th2) * eps_psi + one - thetai * ak) / (den * den);
-                S3 = S3 + n * tk;
-                S4 = S4 + npl / (tk * den);
-                S5 = S5 + npl * (two * eps_psi * th2 + thetai * ak) / (tk * (den * den));
-                S6 = S6 + npl;
-            }
-            const R fpsi = sigmav_ie * eps_psi * (n_i * n_i) / (xnH) + n_i * vi / (xnH) * (S1) - one;
-            const R dni = -one / (om * om) * (D) * (S2) - (psi / om * (D) + one) * S3 / om;
-            const R dfdpsi = sigmav_ie * n_i / (xnH) * (n_i * (D) + two * eps_psi * dni) +
-                             two * n_i * vi / (xnH) * (et2 + et) *
-                                 ((dni / n_i + (D) * (two * et + one) / (eps_psi * (one + et))) * (S4) + ((D) * S5)) +
-                             n_i * vi / (xnH) * (dni / n_i * (one - psi) - one) * (S6);
-            psi = psi - fpsi / dfdpsi;
-            if (psi < psi0) {
-                psi = psi0 * R(0.9999999);
-                lowT = 1;
-            } else if (psi > R(0)) {
-                psi = R(-1e-5);
-            }
-            conv = fabs(fpsi);
-            niter = niter + 1;
+        if (sizeof(R) == 4 && cold) {
+            float psif = (float)psi, convf = 1e4f;
+            auto nk32 = [&](int k) -> float { return (float)nk64(k); };
+            charge_newton<float>(p, tau, alp, nk32, (float)nH, (float)x, (float)sigmav_ie, (float)vi,
+                                 fmaxf((float)p.eps, 1e-3f), true, psif, niter, lowT, convf);
+            psi = (double)psif;
+            conv = 1e4;   // the FP64 phase re-evaluates the residual
         }
-        eps_psi = (one - psi) / thetai * dexp<R>(-psi);
-        if (lowT > 0) eps_psi = R(0.99999);
-        R nsum = R(0);
+        charge_newton<double>(p, tau, alp, nk64, nH, x, sigmav_ie, vi, p.eps, false, psi, niter, lowT, conv);
+        double eps_psi = (1.0 - psi) / thetai * exp(-psi);
+        if (lowT > 0) eps_psi = 0.99999;
+        double nsum = 0.0;
         for (int k = 0; k < N; ++k) {
-            const R tk = R(tau[k]), ak = R(alp[k]);
-            const R z = psi * tk + (one - (eps_psi * eps_psi) * th2) / (one + eps_psi * thetai * ak + (eps_psi * eps_psi) * th2);
-            p.zd[(long long)k * p.plane + c] = z;
-            nsum = nsum - z * nk(k) / (one - eps_psi);
+            const double tk = tau[k], ak = alp[k];
+            const double z = psi * tk + (1.0 - (eps_psi * eps_psi) * th2) / (1.0 + eps_psi * thetai * ak + (eps_psi * eps_psi) * th2);
+            p.zd[(long long)k * p.plane + c] = R(z);
+            nsum = nsum - z * nk64(k) / (1.0 - eps_psi);
         }
-        if (lowT > 0 && N > 0) nsum = dsqrt_<R>(eps_psi * x * nH / sigmav_ie);
-        p.ni[c] = nsum;
-        p.ne[c] = eps_psi * nsum;
-        p.psi_old[c] = lowT > 0 ? p.psi0 : (double)psi;
+        if (lowT > 0 && N > 0) nsum = sqrt(eps_psi * x * nH / sigmav_ie);
+        p.ni[c] = R(nsum);
+        p.ne[c] = R(eps_psi * nsum);
+        p.psi_old[c] = lowT > 0 ? p.psi0 : psi;
         if (p.res) {
             // resistivities (ionisation.f90:163-206)
-            const R e = R(chg::e_el), cl = R(chg::clight), mel = R(chg::m_el), mi = R(p.mu_ions * chg::mH);
-            const R B = R(p.B0) * dsqrt_<R>(nH / R(1e4));
-            const R cs_T = R(tr[3]);
-            const R t_sel = R(tr[4]) / nH, t_sions = R(tr[5]) / nH;
-            const R rho_cgs = rho * R(p.ud);
-            const R sig_el = (eps_psi * nsum) * (e * e) * t_sel / mel;
-            const R sig_i = (nsum) * (e * e) * t_sions / mi;
-            const R om_el = -e * B / cl / mel;
-            const R om_i = e * B / cl / mi;
-            R so = R(0), sp = R(0), sh = R(0);
+            const double e = chg::e_el, cl = chg::clight, mel = chg::m_el, mi = p.mu_ions * chg::mH;
+            const double B = p.B0 * sqrt(nH / 1e4);
+            const double cs_T = tr[3];
+            const double t_sel = tr[4] / nH, t_sions = tr[5] / nH;
+            const double rho_cgs = rho * p.ud;
+            const double sig_el = (eps_psi * nsum) * (e * e) * t_sel / mel;
+            const double sig_i = (nsum) * (e * e) * t_sions / mi;
+            const double om_el = -e * B / cl / mel;
+            const double om_i = e * B / cl / mi;
+            double so = 0.0, sp = 0.0, sh = 0.0;
             for (int k = 0; k < N; ++k) {
-                const R z = p.zd[(long long)k * p.plane + c];
-                const R t_sd = R(p.ak[k]) / (rho_cgs * cs_T);
-                const R sd = nk(k) * ((z * e) * (z * e)) * t_sd / R(p.mkum[k]);
-                const R omd = z * e * B / cl / R(p.mkum[k]);
-                const R wt = omd * t_sd;
+                const double tk = tau[k], ak = alp[k];
+                const double z = psi * tk + (1.0 - (eps_psi * eps_psi) * th2) / (1.0 + eps_psi * thetai * ak + (eps_psi * eps_psi) * th2);
+                const double t_sd = p.ak[k] / (rho_cgs * cs_T);
+                const double sd = nk64(k) * ((z * e) * (z * e)) * t_sd / p.mkum[k];
+                const double omd = z * e * B / cl / p.mkum[k];
+                const double wt = omd * t_sd;
                 so = so + sd;
-                sp = sp + sd / (one + wt * wt);
-                sh = sh + sd * wt / (one + wt * wt);
-                p.gamma_d[(long long)k * p.plane + c] = t_sd * omd;
+                sp = sp + sd / (1.0 + wt * wt);
+                sh = sh + sd * wt / (1.0 + wt * wt);
+                p.gamma_d[(long long)k * p.plane + c] = R(t_sd * omd);
             }
-            const R wi = om_i * t_sions, we = om_el * t_sel;
-            const R sigma_o = so + sig_i + sig_el;
-            const R sigma_p = sig_i / (one + wi * wi) + sig_el / (one + we * we) + sp;
-            const R sigma_h = -sig_i * (wi) / (one + wi * wi) - sig_el * (we) / (one + we * we) - sh;
-            p.eta[c] = one / sigma_o;
-            p.eta[p.plane + c] = sigma_h / (sigma_p * two + sigma_h * sigma_h);
-            p.eta[2 * p.plane + c] = sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - one / sigma_o;
+            const double wi = om_i * t_sions, we = om_el * t_sel;
+            const double sigma_o = so + sig_i + sig_el;
+            const double sigma_p = sig_i / (1.0 + wi * wi) + sig_el / (1.0 + we * we) + sp;
+            const double sigma_h = -sig_i * (wi) / (1.0 + wi * wi) - sig_el * (we) / (1.0 + we * we) - sh;
+            p.eta[c] = R(1.0 / sigma_o);
+            p.eta[p.plane + c] = R(sigma_h / (sigma_p * 2.0 + sigma_h * sigma_h));
+            p.eta[2 * p.plane + c] = R(sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - 1.0 / sigma_o);
         }
         p.iters[c] = niter;
         atomicAdd(&s_hist[niter < CHARGE_HIST - 1 ? niter : CHARGE_HIST - 1], 1u);
-        if (conv > R(p.eps)) atomicAdd(&s_hist[CHARGE_HIST], 1u);
+        if (conv > p.eps) atomicAdd(&s_hist[CHARGE_HIST], 1u);
         atomicAdd(&s_iter, (unsigned long long)niter);
     }
     __syncthreads();

@@ -171,8 +171,11 @@ __global__ void __launch_bounds__(TILE, 1) k_mlp(MlpArgs a) {
     if (!TRAIN) {
         if (valid && a.out) a.out[idx] = y * P[OFF_TSD] + P[OFF_TMU];
         if (valid && a.seed) {
-            // start point psi = psi0 (1 + t); only a negative potential is a usable start
-            const float ps = (float)(a.psi0 * (1.0 + (double)(y * P[OFF_TSD] + P[OFF_TMU])));
+            // start point psi = psi0 (1 + t) inside the reference's admissible range [psi0, 0):
+            // an iterate below psi0 is clamped and flagged low-temperature (ionisation.f90:119-125),
+            // so t > 0 starts from psi0 itself; psi >= 0 is no start (the kernel falls back to psi0)
+            const double tt = fmin((double)(y * P[OFF_TSD] + P[OFF_TMU]), 0.0);
+            const float ps = (float)(a.psi0 * (1.0 + tt));
             a.seed[sample] = ps < 0.0f ? ps : 0.0f;
         }
     } else {
