@@ -82,6 +82,13 @@ extern "C" {
 #define SHARK_CHARGE_ANALYTICAL    2   /* Fujii et al. per-species Newton (analytical_charge)    */
 #define SHARK_CHARGE_MLP_SEED      4   /* start the Marchand Newton from the trained network     */
 
+/* grw_mode bits (dust_commons.f90:9-13) */
+#define SHARK_GROWTH_FRAGMENTATION 1
+#define SHARK_GROWTH_DRIFT         2
+#define SHARK_GROWTH_TURB          4
+#define SHARK_GROWTH_BROWNIAN      8
+#define SHARK_GROWTH_AMBIPOLAR     16
+
 #define SHARK_PREC_FP64   0   /* everything FP64 (the FP64 GPU oracle run)                      */
 #define SHARK_PREC_MIXED  1   /* FP32 state + FP32 flux/update; FP64 drag, FARGO split, totals  */
 
@@ -160,7 +167,17 @@ typedef struct shark_gpu_config {
     double turb_rho0, turb_mach, turb_tcorr;
     int32_t turb_kmin, turb_kmax;
     int32_t turb_seed, pad2;
-    double reserved[28];
+    /* Dust growth (src/dust/dust_commons.f90): size grid smin..smax (cm, the bins' edges
+     * smin zeta^(k-1), smin zeta^k with zeta = (smax/smin)^(1/N)), sticking efficiency,
+     * clustered fraction, sub-cycle CFL, coagulation / fragmentation dust-to-gas thresholds, fixed
+     * sub-step (years, <= 0: none), ambipolar drift factor, turbulence alpha, monomer size (cm)
+     * and fragment slope, Blum & Wurm A, grain surface energy (erg cm^-2) and Young modulus. */
+    double grw_smin, grw_smax, grw_sticking, grw_clustered, grw_cfl, grw_eps_thr, grw_eps_thr_frag;
+    double grw_dtcontrol, grw_delta_vambi, grw_alpha_turb, grw_size_mono, grw_slope_mono, grw_Abr;
+    double grw_gamma_grains, grw_estar_grains;
+    int32_t grw_kernel;                /* 0 physical, 1 constant, 2 additive (kernel_type)     */
+    int32_t grw_mode;                  /* SHARK_GROWTH_* bits                                   */
+    double reserved[12];
 
     /* Optional grid metrics from the caller (Fortran dx(ncells,ndim), surf(ncells,ndim),
      * vol(ncells), radii_c(ncells), position(ncells,ndim), cs(ncells)).  NULL: the library

@@ -51,7 +51,8 @@ def lib():
                             ("oracle_get_tstop", [D]), ("oracle_fargo", []),
                             ("oracle_charge", [D, C.POINTER(C.c_int32)]),
                             ("oracle_get_charge", [D, D, D, D, D, D]),
-                            ("oracle_reset_charge", []), ("oracle_charge_psi0", [D])]:
+                            ("oracle_reset_charge", []), ("oracle_charge_psi0", [D]),
+                            ("oracle_growth", [C.POINTER(C.c_int32)]), ("oracle_growth_grid", [D, D, D])]:
             f = getattr(L, name)
             f.restype = C.c_int32
             f.argtypes = [P] + extra
@@ -197,6 +198,20 @@ class Oracle:
         v = C.c_double(0)
         self._chk(lib().oracle_charge_psi0(self._h, C.byref(v)), "oracle_charge_psi0")
         return v.value
+
+    def growth(self):
+        """dust_growth alone with the dt last set; returns the sub-steps per cell."""
+        it = np.zeros(self.ncells, dtype=np.int32)
+        self._chk(lib().oracle_growth(self._h, it.ctypes.data_as(C.POINTER(C.c_int32))), "oracle_growth")
+        return it
+
+    def growth_grid(self):
+        """(zeta, eta, massmin), bin masses m_k, fragment shares redis[ifrag][k]."""
+        z = np.zeros(3)
+        N = self.cfg.ndust
+        mk, rd = np.zeros(N), np.zeros(N * N)
+        self._chk(lib().oracle_growth_grid(self._h, _dptr(z), _dptr(mk), _dptr(rd)), "oracle_growth_grid")
+        return z, mk, rd.reshape(N, N)
 
     def fargo(self):
         """fargo_scheme alone on the current state with the dt last set (FARGO configs)."""

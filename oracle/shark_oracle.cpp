@@ -635,6 +635,237 @@ void charge(oracle_state& s) {
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Dust growth (src/dust/dust_growth.f90:3-256): Smoluchowski coagulation (and fragmentation) on
+// the mass grid of dust_init.f90:11-45, sub-cycled per cell with dt_growth = CFL_growth
+// rho_k/|drho_k/dt|.  Re-specified where the reference has no definition, with the reason:
+//   temperature: dustyTurb T_cloud, polar disk T(r) from its isothermal cs (the reference calls
+//     the empty barotrop of these setups);
+//   polar disk: densities, Reynolds number and Jeans length on the midplane Sigma/(sqrt(2 pi) H),
+//     the large-eddy time 1/Omega(r), and the surface-density rate K Sigma_i Sigma_j/(sqrt(2 pi) H
+//     m_i m_j) (the reference's disk branch is empty);
+//   velocities: cs_eos(T) is cgs and is divided by unit_v where a code velocity is meant.
+// x**3. and zeta**3. are evaluated as products; the REAL*4 literals 3.2, 1./2.6, 1.6 of the
+// Stokes function keep their single-precision values.  A cell that needs more than 100000
+// sub-steps stops there (the reference loops on).
+// ---------------------------------------------------------------------------------------------
+namespace phys_g { constexpr double grav = 6.67e-8; }
+
+struct GrowthGrid {
+    double zeta, eta, massmin, m_mono, Ebr_mono;
+    std::vector<double> aminus, aplus, mk, sk, redis;   // redis[ifrag * N + k]: share of bin k
+};
+
+GrowthGrid growth_grid(const shark_gpu_config& g) {
+    const int N = g.ndust;
+    const double ul = unit_or_1(g.unit_l), ud = unit_or_1(g.unit_d), ut = unit_or_1(g.unit_t);
+    const double um = ul * ul * ul * ud, uv = ul / ut;
+    const double rg_cgs = g.rhograin * ud;
+    GrowthGrid G;
+    G.zeta = std::pow(g.grw_smax / g.grw_smin, 1.0 / N);
+    G.eta = G.zeta * G.zeta * G.zeta;
+    G.massmin = (g.grw_kernel == 0) ? F43() * pi * rg_cgs * (g.grw_smin * g.grw_smin * g.grw_smin) / um
+                                    : g.grw_smin * g.grw_smin * g.grw_smin;
+    const double a_mu = g.grw_size_mono / 2.0;
+    G.Ebr_mono = g.grw_Abr * std::pow(g.grw_gamma_grains, 5.0 / 3.0) * std::pow(a_mu, 4.0 / 3.0) /
+                 std::pow(g.grw_estar_grains, 2.0 / 3.0) / (uv * uv * um);
+    G.m_mono = 4.0 / 3.0 * pi * rg_cgs * (g.grw_size_mono * g.grw_size_mono * g.grw_size_mono) / um;
+    G.aminus.resize(N); G.aplus.resize(N); G.mk.resize(N); G.sk.resize(N);
+    for (int k = 0; k < N; ++k) {
+        G.aminus[k] = g.grw_smin * powi(G.zeta, k) / ul;
+        G.aplus[k] = g.grw_smin * powi(G.zeta, k + 1) / ul;
+        const double s = g.dust_size[k];
+        G.sk[k] = s;
+        G.mk[k] = (g.grw_kernel == 0) ? F43() * pi * g.rhograin * (s * s * s) : s * s * s;
+    }
+    const double e4 = 4.0 - g.grw_slope_mono;
+    G.redis.assign((size_t)N * N, 0.0);
+    for (int i = 0; i < N; ++i) {
+        double sum = 0.0;
+        for (int j = 0; j <= i; ++j) {
+            const double r = (std::pow(G.aplus[j], e4) - std::pow(G.aminus[j], e4)) /
+                             (std::pow(G.aplus[i], e4) - std::pow(G.aminus[0], e4));
+            G.redis[(size_t)i * N + j] = r;
+        }
+        for (int j = 0; j < N; ++j) sum += G.redis[(size_t)i * N + j];
+        for (int j = 0; j < N; ++j) G.redis[(size_t)i * N + j] = G.redis[(size_t)i * N + j] / sum;
+    }
+    return G;
+}
+
+// x_stokes-dependent factor of the turbulent relative velocity (dust_growth.f90:94)
+double growth_f_stokes(double x) {
+    return (double)3.2f - 1.0 - x + 2.0 / (1. + x) * ((double)(1.0f / 2.6f) + (x * x * x) / ((double)1.6f + x));
+}
+
+// pairwise relative velocity dv(k, j) of one cell (dust_growth.f90:88-114)
+struct GrowthCell {
+    double T, rho, rho_cgs, cs_v, t_L, t_eta, Re, vambi, hs;
+};
+
+double growth_dv(const shark_gpu_config& g, const GrowthGrid& G, const GrowthCell& c, const double* ts,
+                 const double* vx, const double* vy, const double* vz, const double* gam, int k, int j) {
+    const double ul = unit_or_1(g.unit_l), ud = unit_or_1(g.unit_d), ut = unit_or_1(g.unit_t);
+    const double um = ul * ul * ul * ud, uv = ul / ut;
+    const double x_stokes = ts[j] / ts[k];
+    const double f_Stokes = growth_f_stokes(x_stokes);
+    const double St1 = ts[k] / c.t_L, St2 = ts[j] / c.t_L;
+    const double a = g.grw_alpha_turb;
+    const double rm = std::pow(c.Re, -0.5);
+    const double vclass1 = a * c.cs_v * std::sqrt((St1 - St2) / (St1 + St2)) *
+                           std::sqrt(St1 * St1 / (St1 + rm) - St2 * St2 / (St2 + rm));
+    const double vclass2 = a * c.cs_v * std::sqrt(f_Stokes * St1);
+    const double vclass3 = a * c.cs_v * std::sqrt(1.0 / (1.0 + St1) + 1.0 / (1.0 + St2));
+    double vturb = vclass2;
+    if (ts[k] < c.t_eta) vturb = vclass1;
+    if (ts[k] > c.t_L) vturb = vclass3;
+    const double X = (8.0 * phys::kB * c.T / pi) * (G.mk[k] * um + G.mk[j] * um) / (G.mk[k] * G.mk[j] * (um * um)) / (uv * uv);
+    const double sX = std::sqrt(X);
+    const double vbrow = std::sqrt(sX * sX);
+    const double dxv = vx[k] - vx[j], dyv = vy[k] - vy[j], dzv = vz[k] - vz[j];
+    const double vhydro = std::sqrt(dxv * dxv + dyv * dyv + dzv * dzv);
+    double vad = 0.0;
+    if (gam) {
+        const double d = c.vambi / uv * (std::fabs(gam[k]) / std::sqrt(1.0 + gam[k] * gam[k]) -
+                                         std::fabs(gam[j]) / std::sqrt(1.0 + gam[j] * gam[j]));
+        vad = std::sqrt(d * d);
+    }
+    double dv = 0.0;
+    if (g.grw_mode & SHARK_GROWTH_TURB) dv = vturb;
+    if (g.grw_mode & SHARK_GROWTH_BROWNIAN) dv = std::sqrt(dv * dv + vbrow * vbrow);
+    if (g.grw_mode & SHARK_GROWTH_DRIFT) dv = std::sqrt(dv * dv + vhydro * vhydro);
+    if (g.grw_mode & SHARK_GROWTH_AMBIPOLAR) dv = std::sqrt(dv * dv + vad * vad);
+    return dv;
+}
+
+int growth_bin(double m, double massmin, double eta, int cap) {
+    const int b = (int)std::floor(std::log(m / massmin) / std::log(eta) + 1);
+    return std::max(std::min(b, cap), 1);
+}
+
+// One cell's sub-cycled update of rho_k (1-based bin numbers as in the reference); returns the
+// number of sub-steps.
+int growth_cell(const shark_gpu_config& g, const GrowthGrid& G, const GrowthCell& c, double dt, double rho_gas,
+                double* rd, const double* ts, const double* vx, const double* vy, const double* vz,
+                const double* gam, std::vector<double>& drhodt) {
+    const int N = g.ndust;
+    const bool frag = (g.grw_mode & SHARK_GROWTH_FRAGMENTATION) != 0;
+    const double ut = unit_or_1(g.unit_t);
+    double time_growth = 0.0;
+    int niter = 0;
+    while (time_growth < dt && niter < 100000) {
+        std::fill(drhodt.begin(), drhodt.end(), 0.0);
+        niter = niter + 1;
+        for (int k = 0; k < N; ++k) {
+            const double m1 = G.mk[k], s1 = G.sk[k];
+            for (int j = 0; j <= k; ++j) {
+                const double m2 = G.mk[j], s2 = G.sk[j];
+                const double dv = g.grw_kernel == 0 ? growth_dv(g, G, c, ts, vx, vy, vz, gam, k, j) : 0.0;
+                double f_frag = 0.0, p_coag = 1.0;
+                if (frag) {
+                    const double Ecol = 0.5 * (m1 * m2) / (m1 + m2) * (dv * dv);
+                    const double Ebr = (m1 + m2) / G.m_mono * G.Ebr_mono;
+                    f_frag = fmax2(fmin2((Ecol - 0.1 * Ebr) / (4.9 * Ebr), 1.0), 0.0);
+                }
+                double dndt = (g.grw_clustered * g.grw_clustered) * pi * ((s1 + s2) * (s1 + s2)) * dv * rd[k] * rd[j] / m1 / m2;
+                if (g.grw_kernel == 1) { p_coag = 1.0; f_frag = 0.0; dndt = rd[k] * rd[j] / m1 / m2; }
+                else if (g.grw_kernel == 2) { p_coag = 1.0; f_frag = 0.0; dndt = (m1 + m2) * rd[k] * rd[j] / m1 / m2; }
+                dndt = dndt / c.hs;
+                if (k == j) dndt = dndt / 2.0;
+                if (g.grw_kernel == 0) {
+                    if (g.grw_eps_thr > 0.0 && (rd[k] < g.grw_eps_thr * rho_gas)) p_coag = 0.0;
+                    if (g.grw_eps_thr > 0.0 && (rd[j] < g.grw_eps_thr * rho_gas)) p_coag = 0.0;
+                    if (g.grw_eps_thr_frag > 0.0 && (rd[k] < g.grw_eps_thr_frag * rho_gas)) f_frag = 0.0;
+                    if (g.grw_eps_thr_frag > 0.0 && (rd[j] < g.grw_eps_thr_frag * rho_gas)) f_frag = 0.0;
+                }
+                const double mc = (1.0 - f_frag) * (m1 + m2);
+                const int ic1 = growth_bin(mc, G.massmin, G.eta, N);
+                const int ic2 = std::max(std::min((int)std::floor(std::log(mc / G.massmin) / std::log(G.eta) + 1) + 1, N), 1);
+                double eps_m = 1.0;
+                if (ic1 < ic2) eps_m = fmin2((G.mk[ic2 - 1] - (1.0 - f_frag) * (m1 + m2)) / (G.mk[ic2 - 1] - G.mk[ic1 - 1]), 1.0);
+                if (p_coag >= 0.0) {
+                    const double st = g.grw_sticking;
+                    drhodt[k] = drhodt[k] - p_coag * (1.0 - f_frag) * m1 * dndt * st - p_coag * f_frag * m1 * dndt;
+                    drhodt[j] = drhodt[j] - p_coag * (1.0 - f_frag) * m2 * dndt * st - p_coag * f_frag * m2 * dndt;
+                    if (f_frag < 1.0) {
+                        drhodt[ic1 - 1] = drhodt[ic1 - 1] + eps_m * p_coag * (1.0 - f_frag) * (m1 + m2) * dndt * st;
+                        drhodt[ic2 - 1] = drhodt[ic2 - 1] + (1. - eps_m) * p_coag * (1.0 - f_frag) * (m1 + m2) * dndt * st;
+                    }
+                }
+                if ((frag && f_frag > 0.0) && p_coag > 0.) {
+                    const int ifrag2 = std::max(std::min((int)std::floor(std::log(0.1 * f_frag * (m1 + m2) / G.massmin) /
+                                                                         std::log(G.eta) + 1), ic1), 1);
+                    for (int kd = 0; kd < ifrag2; ++kd)
+                        drhodt[kd] = drhodt[kd] + p_coag * f_frag * (m1 + m2) * dndt * G.redis[(size_t)(ifrag2 - 1) * N + kd];
+                }
+            }
+        }
+        double dtg = 1e32;
+        for (int k = 0; k < N; ++k)
+            if (std::fabs(drhodt[k]) != 0.0) dtg = fmin2(dtg, rd[k] / std::fabs(drhodt[k]) * g.grw_cfl);
+        dtg = fmin2(dtg, dt - time_growth);
+        if (g.grw_dtcontrol > 0.0) dtg = fmin2(g.grw_dtcontrol * (double)365.25f * 3600 * 24 / ut, dt - time_growth);
+        for (int k = 0; k < N; ++k) rd[k] = fmax2(rd[k] + drhodt[k] * dtg, rho_gas * g.dust_ratio_min);
+        time_growth = time_growth + dtg;
+    }
+    return niter;
+}
+
+// per-cell inputs of the growth kernel for the setup (see the header comment)
+void growth_inputs(oracle_state& s, int64_t i, GrowthCell& c) {
+    const shark_gpu_config& g = s.cfg;
+    const double ud = unit_or_1(g.unit_d), ut = unit_or_1(g.unit_t), ul = unit_or_1(g.unit_l);
+    const double uv = ul / ut;
+    c.hs = 1.0;
+    if (g.setup == SHARK_SETUP_DISK_POLAR) {
+        c.hs = std::sqrt(2.0 * pi) * (disk_h(g, s.radii_c[i]) * s.radii_c[i]);
+        const double csc = s.cs[i] * uv;
+        c.T = g.mu_gas * phys::mH * (csc * csc) / (g.gamma * phys::kB);
+    } else {
+        c.T = g.T_cloud;
+    }
+    c.rho = s.Q(i, s.irho) / c.hs;
+    c.rho_cgs = c.rho * ud;
+    const double cs_T = std::sqrt(g.gamma * phys::kB * c.T / (g.mu_gas * phys::mH));
+    c.cs_v = cs_T / uv;
+    const double lambJ = std::sqrt(3. * pi / (32. * phys_g::grav * c.rho_cgs)) * cs_T;
+    c.vambi = 0.0;
+    if (!s.eta_a.empty()) c.vambi = g.grw_delta_vambi * (phys::clight * phys::clight) * s.eta_a[i] / lambJ / (4.0 * pi);
+    c.Re = 6.2e7 * std::sqrt(c.rho_cgs / (g.mu_gas * phys::mH) / 1e5) * std::sqrt(c.T / 10.0);
+    if (g.setup == SHARK_SETUP_DISK_POLAR) c.t_L = 1.0 / std::sqrt(g.disk_mstar / powi(s.radii_c[i], 3));
+    else c.t_L = std::sqrt(3. * pi / (32. * phys_g::grav * c.rho_cgs)) / ut;
+    c.t_eta = c.t_L / std::sqrt(c.Re);
+}
+
+std::vector<int32_t> g_growth_iters;   // sub-steps per cell of the last growth call
+
+void dust_growth(oracle_state& s) {
+    const int N = s.ndust;
+    const shark_gpu_config& g = s.cfg;
+    const GrowthGrid G = growth_grid(g);
+    const bool ambi = (g.grw_mode & SHARK_GROWTH_AMBIPOLAR) && !s.gamma_d.empty();
+    if ((int64_t)g_growth_iters.size() != s.ncells) g_growth_iters.assign(s.ncells, 0);
+#pragma omp parallel
+    {
+        std::vector<double> rd(N), ts(N), vx(N), vy(N), vz(N), gam(N), drhodt(N);
+        GrowthCell c;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            if (!s.active[i]) continue;
+            growth_inputs(s, i, c);
+            for (int k = 0; k < N; ++k) {
+                rd[k] = s.U(i, s.irhod[k]);
+                ts[k] = s.TSTOP(i, k);
+                vx[k] = s.Q(i, s.ivdx[k]); vy[k] = s.Q(i, s.ivdy[k]); vz[k] = s.Q(i, s.ivdz[k]);
+                if (ambi) gam[k] = s.gamma_d[(size_t)k * s.ncells + i];
+            }
+            g_growth_iters[i] = growth_cell(g, G, c, s.dt, s.U(i, s.irho), rd.data(), ts.data(), vx.data(), vy.data(),
+                                            vz.data(), ambi ? gam.data() : nullptr, drhodt);
+            for (int k = 0; k < N; ++k) s.U(i, s.irhod[k]) = rd[k];
+        }
+    }
+}
+
 // update_force_setup of disk_polar (disk_polar/setup.f90:364-398) without planet/self-gravity:
 // point-mass gravity -Mstar/r^2 on gas and dust.
 void disk_force(oracle_state& s) {
@@ -1334,6 +1565,7 @@ void solve(oracle_state& s) {
     source_terms(s);
     if (s.flag(SHARK_FLAG_FARGO)) fargo_scheme(s);
     if (s.ndust > 0 && s.flag(SHARK_FLAG_DRAG)) dust_drag(s, 1.0);
+    if (s.ndust > 0 && s.flag(SHARK_FLAG_GROWTH)) dust_growth(s);
     setup_inloop(s);
 }
 
@@ -1692,6 +1924,22 @@ int32_t oracle_reset_charge(oracle_state* s) {
 int32_t oracle_charge_psi0(const oracle_state* s, double* psi0) {
     if (!s || !psi0) return SHARK_ERR_INVALID_ARG;
     *psi0 = charge_psi0(s->cfg.chg_stick_el * std::sqrt(s->cfg.chg_mu_ions * phys::mH / phys::m_el));
+    return SHARK_OK;
+}
+int32_t oracle_growth(oracle_state* s, int32_t* substeps) {
+    if (!s || s->ndust == 0) return SHARK_ERR_INVALID_ARG;
+    ctoprim(*s);
+    compute_tstop(*s);
+    dust_growth(*s);
+    if (substeps) std::memcpy(substeps, g_growth_iters.data(), g_growth_iters.size() * sizeof(int32_t));
+    return SHARK_OK;
+}
+int32_t oracle_growth_grid(const oracle_state* s, double* zeta_eta_massmin, double* mk, double* redis) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    const GrowthGrid G = growth_grid(s->cfg);
+    if (zeta_eta_massmin) { zeta_eta_massmin[0] = G.zeta; zeta_eta_massmin[1] = G.eta; zeta_eta_massmin[2] = G.massmin; }
+    if (mk) std::memcpy(mk, G.mk.data(), G.mk.size() * sizeof(double));
+    if (redis) std::memcpy(redis, G.redis.data(), G.redis.size() * sizeof(double));
     return SHARK_OK;
 }
 int32_t oracle_fargo(oracle_state* s) {

@@ -68,6 +68,10 @@ int32_t oracle_get_charge(const oracle_state* s, double* zd, double* ni, double*
                           double* eta, double* gamma_d);
 int32_t oracle_reset_charge(oracle_state* s);   /* psi_old = 0: the next call starts cold */
 int32_t oracle_charge_psi0(const oracle_state* s, double* psi0);
+/* dust_growth (dust_growth.f90:3-256) alone, with the dt last set, on the current state (ctoprim
+ * and compute_tstop first); substeps (ncells, nullable) receives the sub-steps per cell. */
+int32_t oracle_growth(oracle_state* s, int32_t* substeps);
+int32_t oracle_growth_grid(const oracle_state* s, double* zeta_eta_massmin, double* mk, double* redis);
 
 int32_t oracle_set_threads(int32_t nthreads);
 

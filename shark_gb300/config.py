@@ -41,6 +41,12 @@ CHARGE_RESISTIVITIES = 0x1
 CHARGE_ANALYTICAL = 0x2
 CHARGE_MLP_SEED = 0x4
 
+GROWTH_FRAGMENTATION = 0x1
+GROWTH_DRIFT = 0x2
+GROWTH_TURB = 0x4
+GROWTH_BROWNIAN = 0x8
+GROWTH_AMBIPOLAR = 0x10
+
 PREC_FP64 = 0
 PREC_MIXED = 1
 
@@ -72,7 +78,11 @@ class SharkConfig(C.Structure):
         ("chg_eps", _D), ("chg_B0", _D), ("chg_nitermax", _I), ("chg_mode", _I),
         ("turb_rho0", _D), ("turb_mach", _D), ("turb_tcorr", _D), ("turb_kmin", _I), ("turb_kmax", _I),
         ("turb_seed", _I), ("pad2", _I),
-        ("reserved", _D * 28),
+        ("grw_smin", _D), ("grw_smax", _D), ("grw_sticking", _D), ("grw_clustered", _D), ("grw_cfl", _D),
+        ("grw_eps_thr", _D), ("grw_eps_thr_frag", _D), ("grw_dtcontrol", _D), ("grw_delta_vambi", _D),
+        ("grw_alpha_turb", _D), ("grw_size_mono", _D), ("grw_slope_mono", _D), ("grw_Abr", _D),
+        ("grw_gamma_grains", _D), ("grw_estar_grains", _D), ("grw_kernel", _I), ("grw_mode", _I),
+        ("reserved", _D * 12),
         ("dx", _P), ("surf", _P), ("vol", _P), ("radii_c", _P), ("position", _P), ("cs", _P),
     ]
 
@@ -134,4 +144,17 @@ def default_config():
     c.chg_nitermax = 1000
     c.chg_B0 = 3e-5
     c.chg_mode = CHARGE_RESISTIVITIES         # res_Marchand = .true.
+    c.grw_sticking = 1.0                      # dust_commons.f90:17-63
+    c.grw_clustered = 1.0
+    c.grw_cfl = 0.1
+    c.grw_eps_thr = 1e-10
+    c.grw_eps_thr_frag = 1e-10
+    c.grw_dtcontrol = -1.0
+    c.grw_delta_vambi = 1.0
+    c.grw_alpha_turb = 1.5
+    c.grw_size_mono = 1e-5
+    c.grw_slope_mono = 3.5
+    c.grw_Abr = 2.8e3
+    c.grw_gamma_grains = 25.0
+    c.grw_estar_grains = 2.8e11
     return c

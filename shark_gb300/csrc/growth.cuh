@@ -1,0 +1,192 @@
+// growth.cuh -- dust growth (src/dust/dust_growth.f90:3-256) of one cell inside K2, after the
+// drag and its floor and before setup_inloop and the CFL dt (solve.f90:112-113).
+//
+// Smoluchowski coagulation (and fragmentation) on the mass grid of dust_init.f90:11-45,
+// sub-cycled per cell with dt_growth = CFL_growth rho_k/|drho_k/dt|.  The pair relative velocity
+// (turbulent, Brownian, drift, ambipolar) is formed from the state at the start of the step
+// (q velocities, stopping times) exactly as the CPU oracle (oracle/shark_oracle.cpp, growth_*)
+// forms it; per-pair constants that involve no state -- the collision cross-section factor, the
+// Brownian mass factor, and without fragmentation the target bins and their mass split -- are
+// tabulated on the host with the oracle's operations.  Arithmetic: FP64 in both precisions (the
+// densities are read from and written to the state in its precision).  A cell needing more than
+// 100000 sub-steps stops there and raises SHARK_STATUS_GROWTH.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/shark_gpu.h"
+
+namespace shark {
+
+struct GrowthDev {
+    int on, kernel, mode, t_per_col;
+    const double* pA;        // [N*N] (clustered^2 pi)(s_k + s_j)^2
+    const double* pS;        // [N*N] m_k unit_m + m_j unit_m
+    const double* pD;        // [N*N] m_k m_j unit_m^2
+    const int32_t* pic;      // [N*N*2] target bins ic1, ic2 (1-based) without fragmentation
+    const double* peps;      // [N*N] mass share of ic1 without fragmentation
+    const double* mk;        // [N] grain masses (code)
+    const double* sk;        // [N] grain sizes (code)
+    const double* redis;     // [N*N] fragment shares: redis[ifrag * N + k]
+    const double* col;       // [rows][4]: T, cs_T (cgs), cs_v (code), t_L (disk; 0 otherwise)
+    double massmin, eta, m_mono, Ebr_mono, uv, uv2, ud, ut, mu_gas, dtctl, cfl, sticking, eps_thr, eps_thr_frag;
+    double delta_vambi, alpha_turb, dust_ratio_min;
+};
+
+namespace grw {
+constexpr double pi = 3.141592653589793238462643383279;
+constexpr double kB = 1.38e-16, mH = 1.67e-24, grav = 6.67e-8, clight = 3e10;
+constexpr int MAX_SUB = 100000;
+}
+
+__device__ __forceinline__ double growth_f_stokes_d(double x) {
+    return (double)3.2f - 1.0 - x + 2.0 / (1. + x) * ((double)(1.0f / 2.6f) + (x * x * x) / ((double)1.6f + x));
+}
+
+__device__ __forceinline__ int growth_bin_d(double mc, double massmin, double eta, int add, int cap) {
+    const int b = (int)floor(log(mc / massmin) / log(eta) + 1) + add;
+    return max(min(b, cap), 1);
+}
+
+// Relative velocity of species k and j <= k (dust_growth.f90:88-114).
+__device__ __forceinline__ double growth_dv_d(const GrowthDev& g, int N, int k, int j, double T, double cs_v,
+                                              double t_L, double t_eta, double rm, double vambi, const double* ts,
+                                              const double* vx, const double* vy, const double* vz,
+                                              const double* gam) {
+    const double x_stokes = ts[j] / ts[k];
+    const double f_Stokes = growth_f_stokes_d(x_stokes);
+    const double St1 = ts[k] / t_L, St2 = ts[j] / t_L;
+    const double a = g.alpha_turb;
+    double dv = 0.0;
+    if (g.mode & SHARK_GROWTH_TURB) {
+        double vturb = a * cs_v * sqrt(f_Stokes * St1);
+        if (ts[k] < t_eta)
+            vturb = a * cs_v * sqrt((St1 - St2) / (St1 + St2)) * sqrt(St1 * St1 / (St1 + rm) - St2 * St2 / (St2 + rm));
+        if (ts[k] > t_L) vturb = a * cs_v * sqrt(1.0 / (1.0 + St1) + 1.0 / (1.0 + St2));
+        dv = vturb;
+    }
+    if (g.mode & SHARK_GROWTH_BROWNIAN) {
+        const double X = (8.0 * grw::kB * T / grw::pi) * g.pS[k * N + j] / g.pD[k * N + j] / g.uv2;
+        const double sX = sqrt(X);
+        const double vbrow = sqrt(sX * sX);
+        dv = sqrt(dv * dv + vbrow * vbrow);
+    }
+    if (g.mode & SHARK_GROWTH_DRIFT) {
+        const double dxv = vx[k] - vx[j], dyv = vy[k] - vy[j], dzv = vz[k] - vz[j];
+        const double vh = sqrt(dxv * dxv + dyv * dyv + dzv * dzv);
+        dv = sqrt(dv * dv + vh * vh);
+    }
+    if ((g.mode & SHARK_GROWTH_AMBIPOLAR) && gam) {
+        const double d = vambi / g.uv * (fabs(gam[k]) / sqrt(1.0 + gam[k] * gam[k]) -
+                                                fabs(gam[j]) / sqrt(1.0 + gam[j] * gam[j]));
+        const double vad = sqrt(d * d);
+        dv = sqrt(dv * dv + vad * vad);
+    }
+    return dv;
+}
+
+// Sub-cycled growth of one cell: rd[N] in/out (dust densities after the drag), rho_gas the
+// conserved gas density, rho_q the floored gas density at the start of the step (q(irho)).
+// Returns false if the sub-step cap was reached.
+static __device__ bool growth_cell_d(const GrowthDev& g, int N, int ix, double dt, double rho_gas, double rho_q, double hs,
+                              double* rd, const double* ts, const double* vx, const double* vy, const double* vz,
+                              const double* gam, double eta_a) {
+    const int row = g.t_per_col ? ix : 0;
+    const double* cc = g.col + (size_t)row * 4;
+    const double T = cc[0], cs_T = cc[1], cs_v = cc[2];
+    const double rho = rho_q / hs;
+    const double rho_cgs = rho * g.ud;
+    const double lambJ = sqrt(3. * grw::pi / (32. * grw::grav * rho_cgs)) * cs_T;
+    const double vambi = g.delta_vambi * (grw::clight * grw::clight) * eta_a / lambJ / (4.0 * grw::pi);
+    const double Re = 6.2e7 * sqrt(rho_cgs / (g.mu_gas * grw::mH) / 1e5) * sqrt(T / 10.0);
+    const double t_L = g.t_per_col ? cc[3] : sqrt(3. * grw::pi / (32. * grw::grav * rho_cgs)) / g.ut;
+    const double t_eta = t_L / sqrt(Re);
+    const double rm = pow(Re, -0.5);
+    const bool frag = (g.mode & SHARK_GROWTH_FRAGMENTATION) != 0;
+    double drhodt[SHARK_MAX_DUST];
+    double time_growth = 0.0;
+    int niter = 0;
+    while (time_growth < dt && niter < grw::MAX_SUB) {
+        for (int k = 0; k < N; ++k) drhodt[k] = 0.0;
+        niter = niter + 1;
+        for (int k = 0; k < N; ++k) {
+            const double m1 = g.mk[k];
+            for (int j = 0; j <= k; ++j) {
+                const double m2 = g.mk[j];
+                const double dv = g.kernel == 0 ? growth_dv_d(g, N, k, j, T, cs_v, t_L, t_eta, rm, vambi, ts, vx, vy, vz, gam)
+                                                : 0.0;
+                double f_frag = 0.0, p_coag = 1.0;
+                if (frag) {
+                    const double Ecol = 0.5 * (m1 * m2) / (m1 + m2) * (dv * dv);
+                    const double Ebr = (m1 + m2) / g.m_mono * g.Ebr_mono;
+                    const double fr = (Ecol - 0.1 * Ebr) / (4.9 * Ebr);
+                    const double lo = fr < 1.0 ? fr : 1.0;
+                    f_frag = lo > 0.0 ? lo : 0.0;
+                }
+                double dndt;
+                if (g.kernel == 1) dndt = rd[k] * rd[j] / m1 / m2;
+                else if (g.kernel == 2) dndt = (m1 + m2) * rd[k] * rd[j] / m1 / m2;
+                else dndt = g.pA[k * N + j] * dv * rd[k] * rd[j] / m1 / m2;
+                dndt = dndt / hs;
+                if (k == j) dndt = dndt / 2.0;
+                if (g.kernel == 0) {
+                    if (g.eps_thr > 0.0 && (rd[k] < g.eps_thr * rho_gas)) p_coag = 0.0;
+                    if (g.eps_thr > 0.0 && (rd[j] < g.eps_thr * rho_gas)) p_coag = 0.0;
+                    if (g.eps_thr_frag > 0.0 && (rd[k] < g.eps_thr_frag * rho_gas)) f_frag = 0.0;
+                    if (g.eps_thr_frag > 0.0 && (rd[j] < g.eps_thr_frag * rho_gas)) f_frag = 0.0;
+                }
+                int ic1, ic2;
+                double eps_m;
+                if (f_frag == 0.0) {
+                    ic1 = g.pic[(k * N + j) * 2];
+                    ic2 = g.pic[(k * N + j) * 2 + 1];
+                    eps_m = g.peps[k * N + j];
+                } else {
+                    const double mc = (1.0 - f_frag) * (m1 + m2);
+                    ic1 = growth_bin_d(mc, g.massmin, g.eta, 0, N);
+                    ic2 = growth_bin_d(mc, g.massmin, g.eta, 1, N);
+                    eps_m = 1.0;
+                    if (ic1 < ic2) {
+                        const double e = (g.mk[ic2 - 1] - (1.0 - f_frag) * (m1 + m2)) / (g.mk[ic2 - 1] - g.mk[ic1 - 1]);
+                        eps_m = e < 1.0 ? e : 1.0;
+                    }
+                }
+                if (p_coag >= 0.0) {
+                    const double st = g.sticking;
+                    drhodt[k] = drhodt[k] - p_coag * (1.0 - f_frag) * m1 * dndt * st - p_coag * f_frag * m1 * dndt;
+                    drhodt[j] = drhodt[j] - p_coag * (1.0 - f_frag) * m2 * dndt * st - p_coag * f_frag * m2 * dndt;
+                    if (f_frag < 1.0) {
+                        drhodt[ic1 - 1] = drhodt[ic1 - 1] + eps_m * p_coag * (1.0 - f_frag) * (m1 + m2) * dndt * st;
+                        drhodt[ic2 - 1] = drhodt[ic2 - 1] + (1. - eps_m) * p_coag * (1.0 - f_frag) * (m1 + m2) * dndt * st;
+                    }
+                }
+                if ((frag && f_frag > 0.0) && p_coag > 0.) {
+                    const int b = (int)floor(log(0.1 * f_frag * (m1 + m2) / g.massmin) / log(g.eta) + 1);
+                    const int ifrag2 = max(min(b, ic1), 1);
+                    for (int kd = 0; kd < ifrag2; ++kd)
+                        drhodt[kd] = drhodt[kd] + p_coag * f_frag * (m1 + m2) * dndt * g.redis[(ifrag2 - 1) * N + kd];
+                }
+            }
+        }
+        double dtg = 1e32;
+        for (int k = 0; k < N; ++k)
+            if (fabs(drhodt[k]) != 0.0) {
+                const double c = rd[k] / fabs(drhodt[k]) * g.cfl;
+                dtg = dtg < c ? dtg : c;
+            }
+        {
+            const double rest = dt - time_growth;
+            dtg = dtg < rest ? dtg : rest;
+            if (g.dtctl > 0.0) dtg = g.dtctl < rest ? g.dtctl : rest;
+        }
+        for (int k = 0; k < N; ++k) {
+            const double a = rd[k] + drhodt[k] * dtg, fl = rho_gas * g.dust_ratio_min;
+            rd[k] = a > fl ? a : fl;
+        }
+        time_growth = time_growth + dtg;
+    }
+    return time_growth >= dt;
+}
+
+}  // namespace shark

@@ -31,6 +31,9 @@ static KParams<R> make_params(const DeviceView& v) {
     p.dx1d = v.md[0]; p.dx2d = v.md[1]; p.radcd = v.md[2]; p.xposd = v.md[3]; p.csd = v.md[4];
     p.fgravd = v.md[5]; p.treld = v.md[6]; p.hsd = v.md[7]; p.vkd = v.md[8];
     p.u_init = (const R*)v.u_init;
+    p.gw = v.gw;
+    p.chg_eta = (const R*)v.chg.eta;
+    p.chg_gamma_d = (const R*)v.chg.gamma_d;
     p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize; p.dstokes = v.dstokes; p.turb_rho0 = c.turb_rho0;
     p.dt = nullptr; p.dt_next = nullptr; p.status = v.status; p.coef = v.coef;
     p.u_cur = (const R*)v.u[v.cur];
@@ -38,14 +41,18 @@ static KParams<R> make_params(const DeviceView& v) {
     return p;
 }
 
-template <typename R, int NS, int MODE>
+template <typename R, int NS, int MODE, bool GROW = false>
 static void finalize_launch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
-    if constexpr (std::is_same<R, float>::value) k_finalize_mixed<NS, MODE><<<grid, 256, 0, st>>>(p);
-    else k_finalize<R, NS, MODE><<<grid, 256, 0, st>>>(p);
+    if constexpr (std::is_same<R, float>::value) k_finalize_mixed<NS, MODE, GROW><<<grid, 256, 0, st>>>(p);
+    else k_finalize<R, NS, MODE, GROW><<<grid, 256, 0, st>>>(p);
 }
 
 template <typename R, int MODE>
 static void finalize_dispatch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
+    if (MODE == 0 && p.gw.on) {   // dust growth: run-time species count, growth in the epilogue
+        finalize_launch<R, -1, MODE, true>(p, grid, st);
+        return;
+    }
     switch (p.ndust) {
         case 0: finalize_launch<R, 0, MODE>(p, grid, st); break;
         case 1: finalize_launch<R, 1, MODE>(p, grid, st); break;

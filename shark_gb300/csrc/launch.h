@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "../../include/shark_gpu.h"
+#include "growth.cuh"
 
 namespace shark {
 
@@ -51,6 +52,7 @@ struct DeviceView {
     cudaEvent_t ev[4];          // timing: before boundaries, before flux, before finalize, end
     bool time_kernels;
     ChargeView chg;
+    GrowthDev gw;               // dust growth (gw.on = 0: off)
 };
 
 // Record `msg` as this thread's shark_gpu_last_error text and return `code`.

@@ -96,6 +96,8 @@ struct shark_gpu_ctx {
     unsigned long long* chg_hist = nullptr;
     float* chg_seed = nullptr;       // network start points (plane layout)
     int32_t* chg_iters = nullptr;    // Newton iterations per cell (plane layout)
+    double* grw_d = nullptr;         // dust growth tables (FP64)
+    int32_t* grw_i = nullptr;        // dust growth target bins
     bool chg_cold = true;            // psi_old is zero everywhere (no charging call since reset)
     // charging network
     float* mlp_blob = nullptr;       // SHARK_MLP_NBLOB FP32
@@ -274,7 +276,23 @@ int32_t validate(const shark_gpu_config* c) {
         return fail(SHARK_ERR_UNSUPPORTED, "setup %d has no device hooks in this build", c->setup);
     const int f = c->flags;
     if (f & SHARK_FLAG_VISCOSITY) return fail(SHARK_ERR_UNSUPPORTED, "viscosity is not built");
-    if (f & SHARK_FLAG_GROWTH) return fail(SHARK_ERR_UNSUPPORTED, "growth is not enabled in this build");
+    if (f & SHARK_FLAG_GROWTH) {
+        if (c->ndust < 1) return fail(SHARK_ERR_INVALID_ARG, "growth needs dust species");
+        if (c->setup != SHARK_SETUP_DISK_POLAR && c->setup != SHARK_SETUP_DUSTYTURB)
+            return fail(SHARK_ERR_UNSUPPORTED, "growth needs the temperature of the polar disk or dustyTurb setup");
+        if (c->grw_kernel < 0 || c->grw_kernel > 2) return fail(SHARK_ERR_INVALID_ARG, "grw_kernel must be 0, 1 or 2");
+        if (!(c->grw_smin > 0.0) || !(c->grw_smax > c->grw_smin) || !(c->grw_cfl > 0.0) || !(c->mu_gas > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "growth needs 0 < grw_smin < grw_smax, grw_cfl > 0 and mu_gas > 0");
+        if (c->grw_kernel == 0 && !(c->rhograin > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "rhograin must be > 0");
+        if ((c->grw_mode & SHARK_GROWTH_AMBIPOLAR) &&
+            (!(f & SHARK_FLAG_CHARGING) || !(c->chg_mode & SHARK_CHARGE_RESISTIVITIES)))
+            return fail(SHARK_ERR_INVALID_ARG, "ambipolar growth needs charging with resistivities");
+        if (c->grw_kernel == 0 && (c->grw_mode & SHARK_GROWTH_FRAGMENTATION) &&
+            !(c->grw_size_mono > 0.0 && c->grw_Abr > 0.0 && c->grw_gamma_grains > 0.0 && c->grw_estar_grains > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "fragmentation needs positive monomer and binding parameters");
+        for (int k = 0; k < c->ndust; ++k)
+            if (!(c->dust_size[k] > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "dust_size[%d] must be > 0", k);
+    }
     if (f & SHARK_FLAG_CHARGING) {
         if (c->ndust < 1) return fail(SHARK_ERR_INVALID_ARG, "charging needs dust species");
         if (c->setup != SHARK_SETUP_DISK_POLAR && c->setup != SHARK_SETUP_DUSTYTURB)
@@ -426,6 +444,108 @@ void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     cv.nitermax = c.chg_nitermax;
 }
 
+// ---- dust growth tables (src/dust/dust_growth.f90:3-256, dust_init.f90:11-45) --------------------
+// The operations follow the CPU oracle's growth_grid so the tables are bit-identical to it.
+void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_max, std::vector<double>& hd,
+                         std::vector<int32_t>& hi, shark::GrowthDev& g, size_t off[8]) {
+    const int N = c.ndust;
+    const double ul = unit1(c.unit_l), ud = unit1(c.unit_d), ut = unit1(c.unit_t);
+    const double um = ul * ul * ul * ud, uv = ul / ut;
+    const double rg_cgs = c.rhograin * ud;
+    const double f43 = (double)(4.0f / 3.0f);
+    const bool disk = c.setup == SHARK_SETUP_DISK_POLAR;
+    const int rows = disk ? nx_max : 1;
+    const size_t NN = (size_t)N * N;
+    off[0] = 0;                  // pA
+    off[1] = off[0] + NN;        // pS
+    off[2] = off[1] + NN;        // pD
+    off[3] = off[2] + NN;        // peps
+    off[4] = off[3] + NN;        // mk
+    off[5] = off[4] + N;         // sk
+    off[6] = off[5] + N;         // redis
+    off[7] = off[6] + NN;        // col
+    hd.assign(off[7] + (size_t)rows * 4, 0.0);
+    hi.assign(NN * 2, 1);
+    const double zeta = std::pow(c.grw_smax / c.grw_smin, 1.0 / N);
+    const double eta = zeta * zeta * zeta;
+    const double massmin = (c.grw_kernel == 0) ? f43 * kPi * rg_cgs * (c.grw_smin * c.grw_smin * c.grw_smin) / um
+                                               : c.grw_smin * c.grw_smin * c.grw_smin;
+    std::vector<double> am(N), ap(N), mk(N);
+    for (int k = 0; k < N; ++k) {
+        am[k] = c.grw_smin * powi(zeta, k) / ul;
+        ap[k] = c.grw_smin * powi(zeta, k + 1) / ul;
+        const double sz = c.dust_size[k];
+        mk[k] = (c.grw_kernel == 0) ? f43 * kPi * c.rhograin * (sz * sz * sz) : sz * sz * sz;
+        hd[off[4] + k] = mk[k];
+        hd[off[5] + k] = sz;
+    }
+    const double e4 = 4.0 - c.grw_slope_mono;
+    for (int i = 0; i < N; ++i) {
+        double* r = &hd[off[6] + (size_t)i * N];
+        for (int j = 0; j <= i; ++j)
+            r[j] = (std::pow(ap[j], e4) - std::pow(am[j], e4)) / (std::pow(ap[i], e4) - std::pow(am[0], e4));
+        double sum = 0.0;
+        for (int j = 0; j < N; ++j) sum += r[j];
+        for (int j = 0; j < N; ++j) r[j] = r[j] / sum;
+    }
+    const double cl = c.grw_clustered;
+    for (int k = 0; k < N; ++k)
+        for (int j = 0; j <= k; ++j) {
+            const size_t q = (size_t)k * N + j;
+            const double sk = c.dust_size[k], sj = c.dust_size[j];
+            hd[off[0] + q] = (cl * cl) * kPi * ((sk + sj) * (sk + sj));
+            hd[off[1] + q] = mk[k] * um + mk[j] * um;
+            hd[off[2] + q] = mk[k] * mk[j] * (um * um);
+            const double mc = (1.0 - 0.0) * (mk[k] + mk[j]);
+            const int b = (int)std::floor(std::log(mc / massmin) / std::log(eta) + 1);
+            const int ic1 = std::max(std::min(b, N), 1), ic2 = std::max(std::min(b + 1, N), 1);
+            hi[q * 2] = ic1;
+            hi[q * 2 + 1] = ic2;
+            double e = 1.0;
+            if (ic1 < ic2) {
+                const double v = (mk[ic2 - 1] - (1.0 - 0.0) * (mk[k] + mk[j])) / (mk[ic2 - 1] - mk[ic1 - 1]);
+                e = v < 1.0 ? v : 1.0;
+            }
+            hd[off[3] + q] = e;
+        }
+    for (int r = 0; r < rows; ++r) {
+        double T = c.T_cloud;
+        if (disk) {
+            const double csc = col.cs[r] * uv;
+            T = c.mu_gas * kMH * (csc * csc) / (c.gamma * kKB);
+        }
+        const double cs_T = std::sqrt(c.gamma * kKB * T / (c.mu_gas * kMH));
+        double* cc = &hd[off[7] + (size_t)r * 4];
+        cc[0] = T;
+        cc[1] = cs_T;
+        cc[2] = cs_T / uv;
+        cc[3] = disk ? 1.0 / std::sqrt(c.disk_mstar / powi(col.radc[r], 3)) : 0.0;
+    }
+    g.on = 1;
+    g.kernel = c.grw_kernel;
+    g.mode = c.grw_mode;
+    g.t_per_col = disk ? 1 : 0;
+    g.massmin = massmin;
+    g.eta = eta;
+    const double a_mu = c.grw_size_mono / 2.0;
+    g.Ebr_mono = c.grw_Abr * std::pow(c.grw_gamma_grains, 5.0 / 3.0) * std::pow(a_mu, 4.0 / 3.0) /
+                 std::pow(c.grw_estar_grains, 2.0 / 3.0) / (uv * uv * um);
+    g.m_mono = 4.0 / 3.0 * kPi * rg_cgs * (c.grw_size_mono * c.grw_size_mono * c.grw_size_mono) / um;
+    g.uv = uv;
+    g.uv2 = uv * uv;
+    g.ud = ud;
+    g.ut = ut;
+    g.mu_gas = c.mu_gas;
+    g.dtctl = c.grw_dtcontrol > 0.0 ? c.grw_dtcontrol * (double)365.25f * 3600 * 24 / ut : -1.0;
+    g.cfl = c.grw_cfl;
+    g.sticking = c.grw_sticking;
+    g.eps_thr = c.grw_eps_thr;
+    g.eps_thr_frag = c.grw_eps_thr_frag;
+    g.delta_vambi = c.grw_delta_vambi;
+    g.alpha_turb = c.grw_alpha_turb;
+    g.dust_ratio_min = c.dust_ratio_min;
+}
+
 template <typename T>
 void upload_cols(std::vector<T>& dst, const Columns& col) {
     const std::vector<double>* src[13] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
@@ -455,6 +575,8 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->chg_hist) cudaFree(c->chg_hist);
     if (c->chg_seed) cudaFree(c->chg_seed);
     if (c->chg_iters) cudaFree(c->chg_iters);
+    if (c->grw_d) cudaFree(c->grw_d);
+    if (c->grw_i) cudaFree(c->grw_i);
     for (void* p : {(void*)c->mlp_blob, (void*)c->mlp_packed, (void*)c->mlp_grad, (void*)c->mlp_adam,
                     (void*)c->mlp_feat, (void*)c->mlp_train, (void*)c->mlp_count, (void*)c->mlp_perm,
                     (void*)c->mlp_scratch, (void*)c->mlp_err})
@@ -610,6 +732,19 @@ int32_t shark_gpu_config_defaults(shark_gpu_config* cfg) {
     cfg->chg_nitermax = 1000;
     cfg->chg_B0 = 3e-5;
     cfg->chg_mode = SHARK_CHARGE_RESISTIVITIES;   // res_Marchand = .true.
+    cfg->grw_sticking = 1.0;            // dust_commons.f90:17-63
+    cfg->grw_clustered = 1.0;
+    cfg->grw_cfl = 0.1;
+    cfg->grw_eps_thr = 1e-10;
+    cfg->grw_eps_thr_frag = 1e-10;
+    cfg->grw_dtcontrol = -1.0;
+    cfg->grw_delta_vambi = 1.0;
+    cfg->grw_alpha_turb = 1.5;
+    cfg->grw_size_mono = 1e-5;
+    cfg->grw_slope_mono = 3.5;
+    cfg->grw_Abr = 2.8e3;
+    cfg->grw_gamma_grains = 25.0;
+    cfg->grw_estar_grains = 2.8e11;
     return SHARK_OK;
 }
 
@@ -755,6 +890,20 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         INIT_TRY(cudaMemsetAsync(c->chg_iters, 0, pl * sizeof(int32_t), c->stream));
         v.chg.iters = c->chg_iters;
         v.chg.on = true;
+    }
+    v.gw = shark::GrowthDev{};
+    if (cfg->flags & SHARK_FLAG_GROWTH) {
+        std::vector<double> hd;
+        std::vector<int32_t> hi;
+        size_t off[8];
+        build_growth_tables(*cfg, col, v.nx_max, hd, hi, v.gw, off);
+        INIT_TRY(cudaMalloc(&c->grw_d, hd.size() * sizeof(double)));
+        INIT_TRY(cudaMemcpy(c->grw_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
+        INIT_TRY(cudaMalloc(&c->grw_i, hi.size() * sizeof(int32_t)));
+        INIT_TRY(cudaMemcpy(c->grw_i, hi.data(), hi.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+        v.gw.pA = c->grw_d + off[0]; v.gw.pS = c->grw_d + off[1]; v.gw.pD = c->grw_d + off[2];
+        v.gw.peps = c->grw_d + off[3]; v.gw.mk = c->grw_d + off[4]; v.gw.sk = c->grw_d + off[5];
+        v.gw.redis = c->grw_d + off[6]; v.gw.col = c->grw_d + off[7]; v.gw.pic = c->grw_i;
     }
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
     std::memset(c->host_ring, 0, 4 * sizeof(double));

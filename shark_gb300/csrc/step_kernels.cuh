@@ -15,6 +15,7 @@
 #pragma once
 
 #include "physics.cuh"
+#include "growth.cuh"
 #include "../../include/shark_gpu.h"
 
 namespace shark {
@@ -39,6 +40,9 @@ struct KParams {
     // sqrt(2 pi) H, FARGO orbital velocity
     const double *fgravd, *treld, *hsd, *vkd;
     const R* u_init;                   // polar disk relaxation reference state
+    GrowthDev gw;                      // dust growth tables and constants
+    const R* chg_eta;                  // charging outputs: eta (3 planes), gamma_d (N planes)
+    const R* chg_gamma_d;
     // per-species constants
     const double *dK, *dtstop, *dsize, *dstokes;
     double turb_rho0;
@@ -295,7 +299,35 @@ __device__ __forceinline__ bool disk_inloop_cell(const KParams<R>& p, R* u, int 
     return true;
 }
 
-template <typename R, int NS, int MODE>
+// dust_growth of one active cell of K2 (growth.cuh); u holds the post-drag state.  Returns the
+// status bits it raises.
+template <typename R>
+__device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int gx, int gy, double dt) {
+    const int N = p.ndust;
+    double rd[SHARK_MAX_DUST], ts[SHARK_MAX_DUST], vx[SHARK_MAX_DUST], vy[SHARK_MAX_DUST], vz[SHARK_MAX_DUST];
+    double gam[SHARK_MAX_DUST];
+    const double rho_old = (double)p.u_cur[uidx(p, 0, gy, gx)];
+    const double qrho_old = rho_old > p.smallr ? rho_old : p.smallr;
+    const bool ambi = (p.gw.mode & SHARK_GROWTH_AMBIPOLAR) && p.chg_gamma_d;
+    const long long c = (long long)gy * p.pitch + gx;
+    for (int k = 0; k < N; ++k) {
+        rd[k] = (double)u[uidx(p, 5 + k, gy, gx)];
+        ts[k] = tstop_cell(p, k, qrho_old, gx, gy);
+        const double r0 = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
+        vx[k] = (double)p.u_cur[uidx(p, 5 + N + k, gy, gx)] / r0;
+        vy[k] = (double)p.u_cur[uidx(p, 5 + 2 * N + k, gy, gx)] / r0;
+        vz[k] = (double)p.u_cur[uidx(p, 5 + 3 * N + k, gy, gx)] / r0;
+        gam[k] = ambi ? (double)p.chg_gamma_d[(long long)k * p.plane + c] : 0.0;
+    }
+    const double eta_a = ambi ? (double)p.chg_eta[2 * p.plane + c] : 0.0;
+    const double hs = p.setup == SHARK_SETUP_DISK_POLAR ? p.hsd[gx] : 1.0;
+    const double rho_gas = (double)u[uidx(p, 0, gy, gx)];
+    const bool ok = growth_cell_d(p.gw, N, gx, dt, rho_gas, qrho_old, hs, rd, ts, vx, vy, vz, ambi ? gam : nullptr, eta_a);
+    for (int k = 0; k < N; ++k) u[uidx(p, 5 + k, gy, gx)] = R(rd[k]);
+    return ok ? 0u : (unsigned)SHARK_STATUS_GROWTH;
+}
+
+template <typename R, int NS, int MODE, bool GROW = false>
 __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;
@@ -364,6 +396,7 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
                 if (fl > rd) u[ir] = R(fl);
             }
         }
+        if (GROW && MODE == 0) st |= grow_in_finalize(p, u, gx, gy, dt);   // dust_growth (solve.f90:113)
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
             const double om = p.si_om, qsh = p.si_q;
@@ -472,7 +505,7 @@ __device__ __forceinline__ void drag_coeffs(double a, float& r, float& w) {
     w = (float)(a / d);
 }
 
-template <int NS, int MODE>
+template <int NS, int MODE, bool GROW = false>
 __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;
@@ -533,6 +566,7 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
                 if (fl > u[ir]) u[ir] = fl;
             }
         }
+        if (GROW && MODE == 0) st |= grow_in_finalize(p, u, gx, gy, dt);   // dust_growth (solve.f90:113)
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
             const float om = (float)p.si_om, qsh = (float)p.si_q;

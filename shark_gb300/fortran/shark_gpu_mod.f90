@@ -36,7 +36,11 @@ module shark_gpu
     integer(c_int32_t) :: chg_nitermax, chg_mode
     real(c_double) :: turb_rho0, turb_mach, turb_tcorr
     integer(c_int32_t) :: turb_kmin, turb_kmax, turb_seed, pad2
-    real(c_double) :: reserved(28)
+    real(c_double) :: grw_smin, grw_smax, grw_sticking, grw_clustered, grw_cfl, grw_eps_thr
+    real(c_double) :: grw_eps_thr_frag, grw_dtcontrol, grw_delta_vambi, grw_alpha_turb, grw_size_mono
+    real(c_double) :: grw_slope_mono, grw_Abr, grw_gamma_grains, grw_estar_grains
+    integer(c_int32_t) :: grw_kernel, grw_mode
+    real(c_double) :: reserved(12)
     type(c_ptr) :: dx, surf, vol, radii_c, position, cs
   end type shark_gpu_config
 

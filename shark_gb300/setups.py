@@ -16,7 +16,9 @@ import math
 
 from .config import (SharkConfig, default_config, SETUP_SOD, SETUP_DUSTYWAVE, SETUP_SI, SETUP_DISK_POLAR,
                      SETUP_DUSTYTURB, FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO,
-                     FLAG_CHARGING, PREC_FP64)
+                     FLAG_CHARGING, FLAG_GROWTH, GROWTH_TURB, GROWTH_BROWNIAN, GROWTH_DRIFT, PREC_FP64)
+
+GROWTH_DEFAULT = GROWTH_TURB | GROWTH_BROWNIAN | GROWTH_DRIFT
 
 MH = 1.67e-24        # src/commons/phys_const.f90:8
 KB = 1.38e-16        # src/commons/phys_const.f90:9
@@ -384,7 +386,7 @@ def disk_polar(nr=128, nphi=128, ndust=4, stokes_min=1e-3, stokes_max=0.3, dust2
 def disk_polar_au(nr=512, nphi=1024, ndust=16, smin_cm=1e-4, smax_cm=1.0, sigma0_cgs=1700.0,
                   rhograin_cgs=2.7, rin=1.0, rmax=100.0, hoverr=0.05, temp_slope=-0.5, dust2gas=0.01,
                   zeta=1e-17, sigma_att=96.0, noise=1e-3, seed=2, fargo=True, charging=True,
-                  precision=PREC_FP64, **kw):
+                  growth=False, growth_mode=GROWTH_DEFAULT, precision=PREC_FP64, **kw):
     """The polar disk in the reference's disk units (disk_polar/units.f90: AU, Msun, G = 1):
     Sigma = sigma0_cgs (1 AU/r) g cm^-2 without outer taper, T ~ r^temp_slope, grains from
     smin_cm to smax_cm, cosmic-ray ionisation zeta exp(-Sigma/sigma_att)."""
@@ -398,6 +400,9 @@ def disk_polar_au(nr=512, nphi=1024, ndust=16, smin_cm=1e-4, smax_cm=1.0, sigma0
     cfg.unit_l, cfg.unit_d, cfg.unit_t = unit_l, unit_d, unit_t
     cfg.chg_x = zeta
     cfg.chg_sigma_att = sigma_att
+    if growth:
+        cfg.flags |= FLAG_GROWTH
+    cfg.grw_smin, cfg.grw_smax, cfg.grw_mode = smin_cm, smax_cm, growth_mode
     return cfg, disk_ic(cfg, noise, seed)
 
 
@@ -439,7 +444,8 @@ def disk_ic(cfg, noise_amp, seed):
 # ---------------------------------------------------------------------------------------------
 def dusty_turb(n=256, ndust=32, smin=1e-6, smax=0.1, dust2gas=0.01, nH=1e9, T=10.0, box_pc=0.1,
                mach=1.0, kmin=1, kmax=3, seed=3, tcorr=None, rhograin=2.7, gamma=1.66667, cfl=0.5,
-               slope_type=1, charging=False, forcing=False, precision=PREC_FP64):
+               slope_type=1, charging=False, forcing=False, growth=False, growth_mode=GROWTH_DEFAULT,
+               precision=PREC_FP64):
     """2D periodic isothermal dusty box in cgs units (src/setups/dustyTurb/setup.f90, units.f90).
 
     Gas of number density ``nH`` (cm^-3, mu_gas = 2.31) at ``T`` K; grains in ``ndust`` MRN bins
@@ -458,7 +464,8 @@ def dusty_turb(n=256, ndust=32, smin=1e-6, smax=0.1, dust2gas=0.01, nH=1e9, T=10
     cfg.iso_cs = 1
     cfg.precision = precision
     cfg.setup = SETUP_DUSTYTURB
-    cfg.flags = FLAG_DRAG | FLAG_BACK_REACTION | (FLAG_CHARGING if charging else 0)
+    cfg.flags = FLAG_DRAG | FLAG_BACK_REACTION | (FLAG_CHARGING if charging else 0) | (FLAG_GROWTH if growth else 0)
+    cfg.grw_smin, cfg.grw_smax, cfg.grw_mode = smin, smax, growth_mode
     L = box_pc * PC
     cfg.box_l = cfg.box_l_y = L
     cfg.mu_gas = 2.31
