@@ -601,6 +601,82 @@ int charge_cell(const shark_gpu_config& g, const ChargeCell& c, double psi0, dou
     return niter;
 }
 
+// analytical_charge (ionisation.f90:809-922, functions_NR.f90:15-128, newton_raphson.f90:7-97):
+// per cell and species, Newton on the grain charge Z from -1 until |f| < 1e-14 (at most 1e5
+// iterations) of the Fujii et al. (2011) balance; n_i, n_e of the cell are those of the last
+// species (the reference overwrites them in the species loop).  Cell inputs in cgs through the
+// setup map of charge_inputs (q(irho) is the floored density, as in the reference).
+double fujii_f(double y, double zeta, double rho, double m_d, double rho_d, double s_d, double T, double mu_gas,
+               double mu_ions, double* fp) {
+    const double mH = phys::mH, kB = phys::kB, e = phys::e_el;
+    const double m_i = mu_ions * mH, m_e = phys::m_el;
+    const double k_e = pi * (s_d * s_d) * std::sqrt(8 * kB * T / (pi * m_e)) * std::exp((e * e) * y / (s_d * kB * T));
+    const double k_i = pi * (s_d * s_d) * std::sqrt(8 * kB * T / (pi * m_i)) * (1 - (e * e) * y / (s_d * kB * T));
+    const double a = m_d * rho / (rho_d * mu_gas * mH);
+    const double f = mu_gas * mH * zeta / rho * (a * a) * ((1 / k_i) - (1 / k_e)) - y;
+    if (fp) {
+        const double kp_e = pi * s_d * std::sqrt(8 * kB * T / pi / m_e) * (e * e) / kB / T * std::exp((e * e) * (y) / s_d / kB / T);
+        const double kp_i = -pi * s_d * std::sqrt(8 * kB * T / pi / m_i) * (e * e) / kB / T;
+        const double b = m_d * rho / rho_d / mu_gas / mH;
+        *fp = mu_gas * mH * zeta / rho * (b * b) * (kp_e / (k_e * k_e) - kp_i / (k_i * k_i)) - 1;
+    }
+    return f;
+}
+
+int fujii_solve(double zeta, double rho, double m_d, double rho_d, double s_d, double T, double mu_gas, double mu_ions,
+                double& y, bool& converged) {
+    y = -1.0;
+    int k;
+    converged = false;
+    for (k = 1; k <= 100000; ++k) {
+        double fp;
+        const double fy = fujii_f(y, zeta, rho, m_d, rho_d, s_d, T, mu_gas, mu_ions, &fp);
+        if (std::fabs(fy) < 1.e-14) { converged = true; break; }
+        const double dy = fy / fp;
+        y = y - dy;
+    }
+    if (!converged) {
+        const double fy = fujii_f(y, zeta, rho, m_d, rho_d, s_d, T, mu_gas, mu_ions, nullptr);
+        converged = std::fabs(fy) <= 1.e-14;
+    }
+    return k - 1;
+}
+
+void analytical_charge(oracle_state& s) {
+    const shark_gpu_config& g = s.cfg;
+    const int N = s.ndust;
+    const size_t nc = (size_t)s.ncells;
+    const double ul = unit_or_1(g.unit_l), ud = unit_or_1(g.unit_d), um = ul * ul * ul * ud;
+    const double mH = phys::mH, kB = phys::kB, e = phys::e_el;
+#pragma omp parallel
+    {
+        ChargeCell c;
+#pragma omp for schedule(dynamic, 64)
+        for (int64_t i = 0; i < s.ncells; ++i) {
+            charge_inputs(s, i, c);
+            double hs = 1.0;
+            if (g.setup == SHARK_SETUP_DISK_POLAR) hs = std::sqrt(2.0 * pi) * (disk_h(g, s.radii_c[i]) * s.radii_c[i]);
+            const double rho = s.Q(i, s.irho) / hs * ud;
+            int total = 0;
+            for (int k = 0; k < N; ++k) {
+                const double m_d = F43() * pi * g.rhograin * (g.dust_size[k] * g.dust_size[k] * g.dust_size[k]) * um;
+                const double rho_d = s.Q(i, s.irhod[k]) / hs * ud;
+                const double s_d = g.dust_size[k] * ul;
+                double y;
+                bool conv;
+                total += fujii_solve(c.x, rho, m_d, rho_d, s_d, c.T, g.mu_gas, g.chg_mu_ions, y, conv);
+                s.zd[(size_t)k * nc + i] = y;
+                const double m_i = g.chg_mu_ions * mH, m_e = phys::m_el;
+                const double k_e = pi * (s_d * s_d) * std::sqrt(8 * kB * c.T / (pi * m_e)) * std::exp((e * e) * y / (s_d * kB * c.T));
+                const double k_i = pi * (s_d * s_d) * std::sqrt(8 * kB * c.T / (pi * m_i)) * (1 - (e * e) * y / (s_d * kB * c.T));
+                s.ni[i] = c.x * rho * m_d / (k_i * g.mu_gas * mH * rho_d);
+                s.ne[i] = c.x * rho * m_d / (k_e * g.mu_gas * mH * rho_d);
+            }
+            s.chg_iters[i] = total;
+        }
+    }
+}
+
 // charge over every cell, ghosts included (the reference's active-cell test is commented out)
 void charge(oracle_state& s) {
     const shark_gpu_config& g = s.cfg;
@@ -614,6 +690,7 @@ void charge(oracle_state& s) {
         s.eta_o.assign(nc, 0.0); s.eta_h.assign(nc, 0.0); s.eta_a.assign(nc, 0.0);
         s.zd.assign(nc * N, 0.0); s.gamma_d.assign(nc * N, 0.0); s.chg_iters.assign(nc, 0);
     }
+    if (g.chg_mode & SHARK_CHARGE_ANALYTICAL) { analytical_charge(s); return; }
 #pragma omp parallel
     {
         ChargeCell c;
@@ -1895,6 +1972,7 @@ int32_t oracle_apply_boundaries(oracle_state* s) { if (!s) return SHARK_ERR_INVA
 int32_t oracle_charge(oracle_state* s, const double* seed, int32_t* iters) {
     if (!s || s->ndust == 0) return SHARK_ERR_INVALID_ARG;
     if (seed) s->chg_seed.assign(seed, seed + s->ncells);
+    ctoprim(*s);
     charge(*s);
     s->chg_seed.clear();
     if (iters) std::memcpy(iters, s->chg_iters.data(), s->chg_iters.size() * sizeof(int32_t));

@@ -227,6 +227,88 @@ __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
     if (threadIdx.x == 0 && s_iter) atomicAdd(&p.hist[CHARGE_HIST + 1], s_iter);
 }
 
+// Fujii et al. (2011) analytical charging (ionisation.f90:809-922, functions_NR.f90:15-128,
+// newton_raphson.f90:7-97): per cell and species, Newton on the grain charge Z from -1 until
+// |f| < 1e-14 or 1e5 iterations, FP64 in both precisions.  f is the small difference of two
+// large, nearly equal terms, so its rounding stays above 1e-14 and the reference's loop runs its
+// full 1e5 iterations; restated as written.  n_i, n_e are those of the last species (the
+// reference overwrites them in its species loop).
+__device__ __forceinline__ double fujii_f_d(double y, double zeta, double rho, double m_d, double rho_d, double s_d,
+                                            double T, double mu_gas, double mu_ions, double* fp) {
+    const double mH = chg::mH, kB = 1.38e-16, e = chg::e_el, pi = chg::pi;
+    const double m_i = mu_ions * mH, m_e = chg::m_el;
+    const double k_e = pi * (s_d * s_d) * sqrt(8 * kB * T / (pi * m_e)) * exp((e * e) * y / (s_d * kB * T));
+    const double k_i = pi * (s_d * s_d) * sqrt(8 * kB * T / (pi * m_i)) * (1 - (e * e) * y / (s_d * kB * T));
+    const double a = m_d * rho / (rho_d * mu_gas * mH);
+    const double f = mu_gas * mH * zeta / rho * (a * a) * ((1 / k_i) - (1 / k_e)) - y;
+    if (fp) {
+        const double kp_e = pi * s_d * sqrt(8 * kB * T / pi / m_e) * (e * e) / kB / T * exp((e * e) * (y) / s_d / kB / T);
+        const double kp_i = -pi * s_d * sqrt(8 * kB * T / pi / m_i) * (e * e) / kB / T;
+        const double b = m_d * rho / rho_d / mu_gas / mH;
+        *fp = mu_gas * mH * zeta / rho * (b * b) * (kp_e / (k_e * k_e) - kp_i / (k_i * k_i)) - 1;
+    }
+    return f;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_charge_fujii(ChargeParams<R> p, double smallr, double mu_gas, double ul) {
+    const int N = p.ndust;
+    const long long ncell = (long long)p.nx_max * p.ny_max;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    __shared__ unsigned int s_hist[CHARGE_HIST + 1];
+    __shared__ unsigned long long s_iter;
+    for (int b = threadIdx.x; b <= CHARGE_HIST; b += blockDim.x) s_hist[b] = 0u;
+    if (threadIdx.x == 0) s_iter = 0ull;
+    __syncthreads();
+    if (t < ncell) {
+        const int iy = (int)(t / p.nx_max), ix = (int)(t - (long long)iy * p.nx_max);
+        const long long c = (long long)iy * p.pitch + ix;
+        const int row = p.t_per_col ? ix : 0;
+        const double T = p.trow[(size_t)row * 8];
+        const double hs = p.hs ? p.hs[ix] : 1.0;
+        const double u0 = (double)p.u[c];
+        double x = p.x0;
+        if (p.sig_att > 0.0) x = p.x0 * exp(-(u0 * p.ud * p.ul) / p.sig_att);
+        const double rho = (u0 > smallr ? u0 : smallr) / hs * p.ud;
+        int total = 0;
+        unsigned int nconv = 0;
+        double ni = 0.0, ne = 0.0;
+        for (int k = 0; k < N; ++k) {
+            const double m_d = p.mkum[k];
+            const double rho_d = (double)p.u[(long long)(5 + k) * p.plane + c] / hs * p.ud;
+            const double s_d = sqrt(p.l2[k]);
+            double y = -1.0;
+            int it;
+            bool conv = false;
+            for (it = 1; it <= 100000; ++it) {
+                double fp;
+                const double fy = fujii_f_d(y, x, rho, m_d, rho_d, s_d, T, mu_gas, p.mu_ions, &fp);
+                if (fabs(fy) < 1.e-14) { conv = true; break; }
+                y = y - fy / fp;
+            }
+            if (!conv) conv = fabs(fujii_f_d(y, x, rho, m_d, rho_d, s_d, T, mu_gas, p.mu_ions, nullptr)) <= 1.e-14;
+            if (!conv) ++nconv;
+            total += it - 1;
+            p.zd[(long long)k * p.plane + c] = R(y);
+            const double mH = chg::mH, kB = 1.38e-16, e = chg::e_el, pi = chg::pi;
+            const double k_e = pi * (s_d * s_d) * sqrt(8 * kB * T / (pi * chg::m_el)) * exp((e * e) * y / (s_d * kB * T));
+            const double k_i = pi * (s_d * s_d) * sqrt(8 * kB * T / (pi * (p.mu_ions * mH))) * (1 - (e * e) * y / (s_d * kB * T));
+            ni = x * rho * m_d / (k_i * mu_gas * mH * rho_d);
+            ne = x * rho * m_d / (k_e * mu_gas * mH * rho_d);
+        }
+        p.ni[c] = R(ni);
+        p.ne[c] = R(ne);
+        p.iters[c] = total;
+        atomicAdd(&s_hist[total < CHARGE_HIST - 1 ? total : CHARGE_HIST - 1], 1u);
+        if (nconv) atomicAdd(&s_hist[CHARGE_HIST], nconv);
+        atomicAdd(&s_iter, (unsigned long long)total);
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b <= CHARGE_HIST; b += blockDim.x)
+        if (s_hist[b]) atomicAdd(&p.hist[b], (unsigned long long)s_hist[b]);
+    if (threadIdx.x == 0 && s_iter) atomicAdd(&p.hist[CHARGE_HIST + 1], s_iter);
+}
+
 // Network features of the cells (SHARK_MLP_NFEAT floats per cell, plane layout [plane][F]):
 // log10 nH, log10 T, log10 zeta, log10 of the grain cross-section, radius and number per H
 // (sum_k n_k pi a_k^2 / nH, sum_k n_k a_k / nH, sum_k n_k / nH).  The same state -> input map as

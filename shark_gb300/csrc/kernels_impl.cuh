@@ -253,7 +253,8 @@ cudaError_t launch_charge(const DeviceView& v) {
     cudaError_t e = cudaMemsetAsync(c.hist, 0, (CHARGE_HIST + 2) * sizeof(unsigned long long), v.stream);
     if (e != cudaSuccess) return e;
     const long long n = (long long)v.nx_max * v.ny_max;
-    k_charge<R><<<(unsigned)((n + 127) / 128), 128, 0, v.stream>>>(q);
+    if (c.analytical) k_charge_fujii<R><<<(unsigned)((n + 127) / 128), 128, 0, v.stream>>>(q, c.smallr, c.mu_gas, c.ul);
+    else k_charge<R><<<(unsigned)((n + 127) / 128), 128, 0, v.stream>>>(q);
     return cudaGetLastError();
 }
 

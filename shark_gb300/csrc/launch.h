@@ -13,6 +13,8 @@ namespace shark {
 struct ChargeView {
     bool on;
     int res, use_seed, t_per_col;
+    int analytical;                         // Fujii et al. per-species Newton instead of Marchand
+    double smallr, mu_gas;
     const double *hs, *trow, *tau, *alpha, *l2, *mkum, *ak;
     double unH, ud, ul, x0, sig_att, thetai, th2, th3, psi0, eps, B0, mu_ions;
     int nitermax;

@@ -297,8 +297,8 @@ int32_t validate(const shark_gpu_config* c) {
         if (c->ndust < 1) return fail(SHARK_ERR_INVALID_ARG, "charging needs dust species");
         if (c->setup != SHARK_SETUP_DISK_POLAR && c->setup != SHARK_SETUP_DUSTYTURB)
             return fail(SHARK_ERR_UNSUPPORTED, "charging needs the cgs map of the polar disk or dustyTurb setup");
-        if (c->chg_mode & SHARK_CHARGE_ANALYTICAL)
-            return fail(SHARK_ERR_UNSUPPORTED, "analytical (Fujii) charging is not built");
+        if ((c->chg_mode & SHARK_CHARGE_ANALYTICAL) && (c->chg_mode & SHARK_CHARGE_MLP_SEED))
+            return fail(SHARK_ERR_INVALID_ARG, "the network seeds the Marchand iteration, not the analytical one");
         if (!(c->chg_x > 0.0) || !(c->chg_mu_ions > 0.0) || !(c->chg_stick_el > 0.0) || !(c->chg_eps > 0.0) ||
             c->chg_nitermax < 1 || !(c->mu_gas > 0.0) || !(c->rhograin > 0.0))
             return fail(SHARK_ERR_INVALID_ARG, "charging parameters must be positive");
@@ -427,7 +427,10 @@ void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_m
         h[off[6] + k] = std::sqrt(kPi * c.gamma / 8.0) * (c.rhograin * ud) * (lk);
     }
     cv.t_per_col = disk ? 1 : 0;
-    cv.res = (c.chg_mode & SHARK_CHARGE_RESISTIVITIES) ? 1 : 0;
+    cv.analytical = (c.chg_mode & SHARK_CHARGE_ANALYTICAL) ? 1 : 0;
+    cv.smallr = c.smallr;
+    cv.mu_gas = c.mu_gas;
+    cv.res = (c.chg_mode & SHARK_CHARGE_RESISTIVITIES) && !(c.chg_mode & SHARK_CHARGE_ANALYTICAL) ? 1 : 0;
     cv.use_seed = 0;
     cv.unH = ud / (c.mu_gas * kMH);
     cv.ud = ud;

@@ -112,3 +112,24 @@ def test_charge_reset_restarts_cold():
         _, _, again = g.charge_stats()
     assert again == cold
     assert warm < cold / 5
+
+
+def test_analytical_charge_fp64():
+    """Fujii et al. mode: Z_k per species, n_i and n_e of the last species; the reference's loop
+    runs its 1e5 iterations (the 1e-14 residual is below f's rounding), on GPU and oracle alike."""
+    cfg, u0 = _noisy_turb(n=10, ndust=3)
+    cfg.chg_mode |= K.CHARGE_ANALYTICAL
+    o = Oracle(cfg)
+    o.set_u(u0)
+    o.apply_boundaries()
+    it_o = o.charge()
+    co = o.get_charge()
+    with Shark(cfg) as g:
+        g.upload(u0)
+        g.charge()
+        cg = g.download_charge()
+    # a cell whose rounding noise happens to dip below 1e-14 stops early on one side only
+    assert abs(cg["iters"].mean() / it_o.mean() - 1.0) <= 0.02
+    for key in ("ni", "ne"):
+        assert _rel(cg[key], co[key]) <= 1e-10, key
+    assert _rel(cg["zd"], co["zd"]) <= 1e-10
