@@ -52,7 +52,8 @@ def lib():
                             ("oracle_charge", [D, C.POINTER(C.c_int32)]),
                             ("oracle_get_charge", [D, D, D, D, D, D]),
                             ("oracle_reset_charge", []), ("oracle_charge_psi0", [D]),
-                            ("oracle_growth", [C.POINTER(C.c_int32)]), ("oracle_growth_grid", [D, D, D])]:
+                            ("oracle_growth", [C.POINTER(C.c_int32)]), ("oracle_growth_grid", [D, D, D]),
+                            ("oracle_turb_kick", []), ("oracle_turb_coef", [D, D, C.POINTER(C.c_int32)])]:
             f = getattr(L, name)
             f.restype = C.c_int32
             f.argtypes = [P] + extra
@@ -212,6 +213,17 @@ class Oracle:
         mk, rd = np.zeros(N), np.zeros(N * N)
         self._chk(lib().oracle_growth_grid(self._h, _dptr(z), _dptr(mk), _dptr(rd)), "oracle_growth_grid")
         return z, mk, rd.reshape(N, N)
+
+    def turb_kick(self):
+        self._chk(lib().oracle_turb_kick(self._h), "oracle_turb_kick")
+
+    def turb_coef(self):
+        """(modes (nm, 3): kx', ky', |k'|; coefficients (nm, 2))."""
+        nm = C.c_int32(0)
+        self._chk(lib().oracle_turb_coef(self._h, None, None, C.byref(nm)), "oracle_turb_coef")
+        m, c = np.zeros(3 * nm.value), np.zeros(2 * nm.value)
+        self._chk(lib().oracle_turb_coef(self._h, _dptr(m), _dptr(c), C.byref(nm)), "oracle_turb_coef")
+        return m.reshape(-1, 3), c.reshape(-1, 2)
 
     def fargo(self):
         """fargo_scheme alone on the current state with the dt last set (FARGO configs)."""

@@ -57,6 +57,9 @@ struct oracle_state {
     std::vector<double> psi_old, ni, ne, eta_o, eta_h, eta_a, zd, gamma_d;
     std::vector<int32_t> chg_iters;
     std::vector<double> chg_seed;   // optional Newton start per cell (0 = none)
+    // dustyTurb Ornstein-Uhlenbeck forcing: modes (kx', ky', |k'|) and coefficients (a_m, b_m)
+    std::vector<double> ou_modes, ou_coef;
+    int64_t ou_step = 0;
     double dt = 0.0, time = 0.0;
 
     // setup-derived scalars
@@ -943,6 +946,82 @@ void dust_growth(oracle_state& s) {
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Driven turbulence of the dustyTurb box, 2D (the reference drives 1D modes only:
+// src/turb/turb.f90:227-324 and solve.f90:129-146).  Solenoidal acceleration
+//   a(x) = sum_m e_m [a_m cos(k_m.x) + b_m sin(k_m.x)],  e_m = (k_y, -k_x)/|k|,
+// over the integer wave vectors kmin <= |k| L/(2 pi) <= kmax of one half plane; the coefficients
+// follow an Ornstein-Uhlenbeck process with correlation time tcorr, advanced exactly each step,
+//   c <- f c + s sqrt(1 - f^2) xi,  f = exp(-dt/tcorr),  xi ~ N(0,1),
+// from the stationary law at t = 0; s = mach^(3/2) cs^2/(L sqrt(Nm)) (energy injection of the
+// order of the dissipation (mach cs)^3/L at tcorr = L/cs).  Normal deviates by Box-Muller from
+// the counter-based uniform of the ICs, counter ((step Nm + m) 2 + component) 2 + {0, 1}.  The
+// kick is the reference's: gas momentum += rho a dt on the active cells, after dust growth.
+// ---------------------------------------------------------------------------------------------
+inline double hash_uniform(uint64_t seed, uint64_t counter);
+
+void turb_modes(const shark_gpu_config& c, std::vector<double>& modes) {
+    modes.clear();
+    const int kmax = c.turb_kmax, kmin = c.turb_kmin;
+    for (int kx = 0; kx <= kmax; ++kx)
+        for (int ky = -kmax; ky <= kmax; ++ky) {
+            if (kx == 0 && ky <= 0) continue;
+            const double kk = std::sqrt((double)(kx * kx + ky * ky));
+            if (kk < kmin || kk > kmax) continue;
+            const double kxp = 2.0 * pi * kx / c.box_l, kyp = 2.0 * pi * ky / c.box_l_y;
+            modes.push_back(kxp);
+            modes.push_back(kyp);
+            modes.push_back(std::sqrt(kxp * kxp + kyp * kyp));
+        }
+}
+
+double ou_normal(uint64_t seed, uint64_t counter) {
+    const double u1 = hash_uniform(seed, 2 * counter), u2 = hash_uniform(seed, 2 * counter + 1);
+    return std::sqrt(-2.0 * std::log(1.0 - u1)) * std::cos(2.0 * pi * u2);
+}
+
+double ou_sigma(const shark_gpu_config& c, int nm) {
+    return std::pow(c.turb_mach, 1.5) * (c.cs0 * c.cs0) / c.box_l / std::sqrt((double)nm);
+}
+
+void turb_init(oracle_state& s) {
+    turb_modes(s.cfg, s.ou_modes);
+    const int nm = (int)s.ou_modes.size() / 3;
+    const double sg = ou_sigma(s.cfg, nm);
+    s.ou_coef.assign(2 * nm, 0.0);
+    for (int m = 0; m < nm; ++m)
+        for (int q = 0; q < 2; ++q) s.ou_coef[2 * m + q] = sg * ou_normal(s.cfg.turb_seed, (uint64_t)(m * 2 + q));
+    s.ou_step = 0;
+}
+
+void turb_kick(oracle_state& s) {
+    const int nm = (int)s.ou_modes.size() / 3;
+    if (nm == 0) return;
+    s.ou_step = s.ou_step + 1;
+    const double f = std::exp(-s.dt / s.cfg.turb_tcorr);
+    const double sg = ou_sigma(s.cfg, nm) * std::sqrt(1.0 - f * f);
+    for (int m = 0; m < nm; ++m)
+        for (int q = 0; q < 2; ++q)
+            s.ou_coef[2 * m + q] = f * s.ou_coef[2 * m + q] +
+                                   sg * ou_normal(s.cfg.turb_seed, (uint64_t)((s.ou_step * nm + m) * 2 + q));
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        const double x = s.POS(i, 0), y = s.POS(i, 1);
+        double ax = 0.0, ay = 0.0;
+        for (int m = 0; m < nm; ++m) {
+            const double kxp = s.ou_modes[3 * m], kyp = s.ou_modes[3 * m + 1], kk = s.ou_modes[3 * m + 2];
+            const double ph = kxp * x + kyp * y;
+            const double w = s.ou_coef[2 * m] * std::cos(ph) + s.ou_coef[2 * m + 1] * std::sin(ph);
+            ax = ax + kyp / kk * w;
+            ay = ay - kxp / kk * w;
+        }
+        const double rho = s.U(i, s.irho);
+        s.U(i, s.ivx) = s.U(i, s.ivx) + rho * ax * s.dt;
+        s.U(i, s.ivy) = s.U(i, s.ivy) + rho * ay * s.dt;
+    }
+}
+
 // update_force_setup of disk_polar (disk_polar/setup.f90:364-398) without planet/self-gravity:
 // point-mass gravity -Mstar/r^2 on gas and dust.
 void disk_force(oracle_state& s) {
@@ -1643,6 +1722,7 @@ void solve(oracle_state& s) {
     if (s.flag(SHARK_FLAG_FARGO)) fargo_scheme(s);
     if (s.ndust > 0 && s.flag(SHARK_FLAG_DRAG)) dust_drag(s, 1.0);
     if (s.ndust > 0 && s.flag(SHARK_FLAG_GROWTH)) dust_growth(s);
+    if (s.cfg.setup == SHARK_SETUP_DUSTYTURB && s.cfg.turb_mach > 0.0) turb_kick(s);
     setup_inloop(s);
 }
 
@@ -1856,6 +1936,7 @@ oracle_state* oracle_create(const shark_gpu_config* cfg) {
     s->fargo_v.assign(nc, 0.0);
     if (cfg->iso_cs == 1)
         for (size_t i = 0; i < nc; ++i) s->cs[i] = cfg->cs0;
+    if (cfg->setup == SHARK_SETUP_DUSTYTURB && cfg->turb_mach > 0.0) turb_init(*s);
     if (cfg->setup == SHARK_SETUP_DISK_POLAR) {
         for (size_t i = 0; i < nc; ++i) {
             const double rr = s->radii_c[i];
@@ -2018,6 +2099,18 @@ int32_t oracle_growth_grid(const oracle_state* s, double* zeta_eta_massmin, doub
     if (zeta_eta_massmin) { zeta_eta_massmin[0] = G.zeta; zeta_eta_massmin[1] = G.eta; zeta_eta_massmin[2] = G.massmin; }
     if (mk) std::memcpy(mk, G.mk.data(), G.mk.size() * sizeof(double));
     if (redis) std::memcpy(redis, G.redis.data(), G.redis.size() * sizeof(double));
+    return SHARK_OK;
+}
+int32_t oracle_turb_kick(oracle_state* s) {
+    if (!s || s->ou_modes.empty()) return SHARK_ERR_INVALID_ARG;
+    turb_kick(*s);
+    return SHARK_OK;
+}
+int32_t oracle_turb_coef(const oracle_state* s, double* modes, double* coef, int32_t* nm) {
+    if (!s) return SHARK_ERR_INVALID_ARG;
+    if (nm) *nm = (int32_t)(s->ou_modes.size() / 3);
+    if (modes) std::memcpy(modes, s->ou_modes.data(), s->ou_modes.size() * sizeof(double));
+    if (coef) std::memcpy(coef, s->ou_coef.data(), s->ou_coef.size() * sizeof(double));
     return SHARK_OK;
 }
 int32_t oracle_fargo(oracle_state* s) {

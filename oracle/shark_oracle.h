@@ -72,6 +72,10 @@ int32_t oracle_charge_psi0(const oracle_state* s, double* psi0);
  * and compute_tstop first); substeps (ncells, nullable) receives the sub-steps per cell. */
 int32_t oracle_growth(oracle_state* s, int32_t* substeps);
 int32_t oracle_growth_grid(const oracle_state* s, double* zeta_eta_massmin, double* mk, double* redis);
+/* dustyTurb forcing: one Ornstein-Uhlenbeck update and gas kick with the dt last set; the
+ * modes (3 nm: kx', ky', |k'|) and coefficients (2 nm) */
+int32_t oracle_turb_kick(oracle_state* s);
+int32_t oracle_turb_coef(const oracle_state* s, double* modes, double* coef, int32_t* nm);
 
 int32_t oracle_set_threads(int32_t nthreads);
 

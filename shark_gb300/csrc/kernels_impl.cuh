@@ -32,6 +32,10 @@ static KParams<R> make_params(const DeviceView& v) {
     p.fgravd = v.md[5]; p.treld = v.md[6]; p.hsd = v.md[7]; p.vkd = v.md[8];
     p.u_init = (const R*)v.u_init;
     p.gw = v.gw;
+    p.ou_nm = v.ou_nm;
+    p.ou = v.ou;
+    p.ou_modes = v.ou_modes;
+    p.box_l_y = c.box_l_y;
     p.chg_eta = (const R*)v.chg.eta;
     p.chg_gamma_d = (const R*)v.chg.gamma_d;
     p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize; p.dstokes = v.dstokes; p.turb_rho0 = c.turb_rho0;
@@ -166,6 +170,8 @@ cudaError_t launch_step(const DeviceView& v, int slot) {
                                                       (p.setup == SHARK_SETUP_SI && std::is_same<R, float>::value) ? 1 : 0,
                                                       p.coef);
     if (v.chg.on && (e = launch_charge<R>(v)) != cudaSuccess) return e;   // charge: solve.f90:36-42
+    if (v.ou_nm > 0)   // this step's forcing coefficients, from the dt on the device
+        k_ou_update<<<1, 2 * v.ou_nm, 0, v.stream>>>(v.ou, v.ou_nm, p.dt, v.ou_sigma, v.ou_tcorr, v.ou_seed, v.step);
     if (v.time_kernels) cudaEventRecord(v.ev[1], v.stream);
     e = (v.ndim == 2) ? strip_launch<R>(v, p) : flux_launch<R, 1>(p, v.stream);
     if (e != cudaSuccess) return e;

@@ -55,6 +55,13 @@ struct DeviceView {
     bool time_kernels;
     ChargeView chg;
     GrowthDev gw;               // dust growth (gw.on = 0: off)
+    // dustyTurb Ornstein-Uhlenbeck forcing (ou_nm = 0: off)
+    int ou_nm;
+    double* ou;                 // [2 nm] coefficients (a_m, b_m)
+    const double* ou_modes;     // [3 nm] k_x', k_y', |k'|
+    double ou_sigma, ou_tcorr;
+    unsigned long long ou_seed;
+    long long step;             // 1-based number of the step being launched
 };
 
 // Record `msg` as this thread's shark_gpu_last_error text and return `code`.

@@ -97,6 +97,8 @@ struct shark_gpu_ctx {
     float* chg_seed = nullptr;       // network start points (plane layout)
     int32_t* chg_iters = nullptr;    // Newton iterations per cell (plane layout)
     double* grw_d = nullptr;         // dust growth tables (FP64)
+    double* ou_d = nullptr;          // forcing: modes [3 nm] | coefficients [2 nm]
+    std::vector<double> ou_init;     // initial coefficients (stationary law, seeded)
     int32_t* grw_i = nullptr;        // dust growth target bins
     bool chg_cold = true;            // psi_old is zero everywhere (no charging call since reset)
     // charging network
@@ -305,6 +307,11 @@ int32_t validate(const shark_gpu_config* c) {
         if (c->setup == SHARK_SETUP_DUSTYTURB && !(c->T_cloud > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "T_cloud must be > 0");
         for (int k = 0; k < c->ndust; ++k)
             if (!(c->dust_size[k] > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "dust_size[%d] must be > 0", k);
+    }
+    if (c->setup == SHARK_SETUP_DUSTYTURB && c->turb_mach > 0.0) {
+        if (c->ny < 4) return fail(SHARK_ERR_UNSUPPORTED, "the 2D turbulence forcing needs a 2D box");
+        if (!(c->turb_tcorr > 0.0) || c->turb_kmin < 1 || c->turb_kmax < c->turb_kmin || c->turb_kmax > 8 || !(c->cs0 > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "forcing needs turb_tcorr > 0, 1 <= turb_kmin <= turb_kmax <= 8, cs0 > 0");
     }
     if (c->setup == SHARK_SETUP_DUSTYTURB) {
         if (c->geom != 0) return fail(SHARK_ERR_UNSUPPORTED, "dustyTurb is Cartesian");
@@ -549,6 +556,38 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     g.dust_ratio_min = c.dust_ratio_min;
 }
 
+// ---- dustyTurb Ornstein-Uhlenbeck forcing (the oracle's turb_modes / turb_init, same operations) --
+double hash_uniform_h(uint64_t seed, uint64_t counter) {
+    uint64_t z = seed * 0x9E3779B97F4A7C15ull + counter + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+void build_forcing(const shark_gpu_config& c, std::vector<double>& modes, std::vector<double>& coef, double& sigma) {
+    modes.clear();
+    for (int kx = 0; kx <= c.turb_kmax; ++kx)
+        for (int ky = -c.turb_kmax; ky <= c.turb_kmax; ++ky) {
+            if (kx == 0 && ky <= 0) continue;
+            const double kk = std::sqrt((double)(kx * kx + ky * ky));
+            if (kk < c.turb_kmin || kk > c.turb_kmax) continue;
+            const double kxp = 2.0 * kPi * kx / c.box_l, kyp = 2.0 * kPi * ky / c.box_l_y;
+            modes.push_back(kxp);
+            modes.push_back(kyp);
+            modes.push_back(std::sqrt(kxp * kxp + kyp * kyp));
+        }
+    const int nm = (int)modes.size() / 3;
+    sigma = std::pow(c.turb_mach, 1.5) * (c.cs0 * c.cs0) / c.box_l / std::sqrt((double)nm);
+    coef.assign(2 * nm, 0.0);
+    for (int m = 0; m < nm; ++m)
+        for (int q = 0; q < 2; ++q) {
+            const uint64_t cnt = (uint64_t)(m * 2 + q);
+            const double u1 = hash_uniform_h(c.turb_seed, 2 * cnt), u2 = hash_uniform_h(c.turb_seed, 2 * cnt + 1);
+            coef[2 * m + q] = sigma * (std::sqrt(-2.0 * std::log(1.0 - u1)) * std::cos(2.0 * kPi * u2));
+        }
+}
+
 template <typename T>
 void upload_cols(std::vector<T>& dst, const Columns& col) {
     const std::vector<double>* src[13] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
@@ -579,6 +618,7 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->chg_seed) cudaFree(c->chg_seed);
     if (c->chg_iters) cudaFree(c->chg_iters);
     if (c->grw_d) cudaFree(c->grw_d);
+    if (c->ou_d) cudaFree(c->ou_d);
     if (c->grw_i) cudaFree(c->grw_i);
     for (void* p : {(void*)c->mlp_blob, (void*)c->mlp_packed, (void*)c->mlp_grad, (void*)c->mlp_adam,
                     (void*)c->mlp_feat, (void*)c->mlp_train, (void*)c->mlp_count, (void*)c->mlp_perm,
@@ -894,6 +934,24 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         v.chg.iters = c->chg_iters;
         v.chg.on = true;
     }
+    v.ou_nm = 0;
+    v.ou = nullptr;
+    v.ou_modes = nullptr;
+    if (cfg->setup == SHARK_SETUP_DUSTYTURB && cfg->turb_mach > 0.0) {
+        std::vector<double> modes;
+        double sigma;
+        build_forcing(*cfg, modes, c->ou_init, sigma);
+        const int nm = (int)modes.size() / 3;
+        INIT_TRY(cudaMalloc(&c->ou_d, (size_t)5 * nm * sizeof(double)));
+        INIT_TRY(cudaMemcpy(c->ou_d, modes.data(), modes.size() * sizeof(double), cudaMemcpyHostToDevice));
+        INIT_TRY(cudaMemcpy(c->ou_d + 3 * nm, c->ou_init.data(), c->ou_init.size() * sizeof(double), cudaMemcpyHostToDevice));
+        v.ou_nm = nm;
+        v.ou_modes = c->ou_d;
+        v.ou = c->ou_d + 3 * nm;
+        v.ou_sigma = sigma;
+        v.ou_tcorr = cfg->turb_tcorr;
+        v.ou_seed = (unsigned long long)cfg->turb_seed;
+    }
     v.gw = shark::GrowthDev{};
     if (cfg->flags & SHARK_FLAG_GROWTH) {
         std::vector<double> hd;
@@ -949,6 +1007,9 @@ int32_t shark_gpu_upload(shark_gpu_ctx* c, const double* u_prim, int64_t ncells,
     }
     CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
     c->status_seen = 0;
+    if (c->v.ou_nm > 0)   // the forcing restarts from its initial coefficients with the state
+        CUDA_TRY(cudaMemcpyAsync(c->v.ou, c->ou_init.data(), c->ou_init.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                 c->stream));
     // apply_boundaries of the first step on every buffer (fixed SOD ghosts are only ever set here)
     for (int b = 0; b < c->v.nbuf; ++b) {
         c->v.cur = b;
@@ -984,6 +1045,7 @@ int32_t shark_gpu_step(shark_gpu_ctx* c, double* dt_out, int32_t* status_out) {
         int32_t rs = seed_charges(c);
         if (rs) return rs;
     }
+    c->v.step = c->nstep + 1;
     cudaError_t e = do_step(c, slot);
     if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
     c->chg_cold = false;

@@ -41,6 +41,10 @@ struct KParams {
     const double *fgravd, *treld, *hsd, *vkd;
     const R* u_init;                   // polar disk relaxation reference state
     GrowthDev gw;                      // dust growth tables and constants
+    int ou_nm;                         // dustyTurb forcing modes (0: no forcing)
+    const double* ou;                  // [2 nm] this step's coefficients
+    const double* ou_modes;            // [3 nm]
+    double box_l_y;
     const R* chg_eta;                  // charging outputs: eta (3 planes), gamma_d (N planes)
     const R* chg_gamma_d;
     // per-species constants
@@ -327,6 +331,29 @@ __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int
     return ok ? 0u : (unsigned)SHARK_STATUS_GROWTH;
 }
 
+// Driven-turbulence kick of the dustyTurb box (turb.f90:227-324 in 2D): the gas momentum gains
+// rho a dt with the solenoidal Ornstein-Uhlenbeck acceleration of this step at the cell centre.
+// C = double follows the oracle's operations; C = float is the mixed-precision form.
+template <typename C, typename R>
+__device__ __forceinline__ void turb_kick_cell(const KParams<R>& p, R* u, int gx, int gy, double dt) {
+    const C x = C(p.xposd[gx]);
+    const C y = C(((double)(float)(gy - p.ng) + 0.5) * p.box_l_y / (double)(float)p.ny);
+    C ax = C(0), ay = C(0);
+    for (int m = 0; m < p.ou_nm; ++m) {
+        const C kxp = C(p.ou_modes[3 * m]), kyp = C(p.ou_modes[3 * m + 1]), kk = C(p.ou_modes[3 * m + 2]);
+        const C ph = kxp * x + kyp * y;
+        C sn, cs;
+        if constexpr (sizeof(C) == 8) sincos(ph, &sn, &cs);
+        else sincosf(ph, &sn, &cs);
+        const C w = C(p.ou[2 * m]) * cs + C(p.ou[2 * m + 1]) * sn;
+        ax = ax + kyp / kk * w;
+        ay = ay - kxp / kk * w;
+    }
+    const C rho = C(u[uidx(p, 0, gy, gx)]);
+    u[uidx(p, 1, gy, gx)] = R(C(u[uidx(p, 1, gy, gx)]) + rho * ax * C(dt));
+    u[uidx(p, 2, gy, gx)] = R(C(u[uidx(p, 2, gy, gx)]) + rho * ay * C(dt));
+}
+
 template <typename R, int NS, int MODE, bool GROW = false>
 __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
@@ -397,6 +424,11 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
             }
         }
         if (GROW && MODE == 0) st |= grow_in_finalize(p, u, gx, gy, dt);   // dust_growth (solve.f90:113)
+        if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)
+            turb_kick_cell<double>(p, u, gx, gy, dt);
+            px = (double)u[uidx(p, 1, gy, gx)];
+            py = (double)u[uidx(p, 2, gy, gx)];
+        }
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
             const double om = p.si_om, qsh = p.si_q;
@@ -567,6 +599,11 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
             }
         }
         if (GROW && MODE == 0) st |= grow_in_finalize(p, u, gx, gy, dt);   // dust_growth (solve.f90:113)
+        if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)
+            turb_kick_cell<float>(p, u, gx, gy, dt);
+            px = u[uidx(p, 1, gy, gx)];
+            py = u[uidx(p, 2, gy, gx)];
+        }
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
             const float om = (float)p.si_om, qsh = (float)p.si_q;
@@ -658,6 +695,28 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
 // Per-step preparation, one small block before the flux kernels: reset the next-dt slot and,
 // when the stopping times are per-species constants (SI box), compute the stiff drag
 // coefficients 1/(1+a_k) and a_k/(1+a_k), a_k = dt/t_k, once in FP64 (dust_drag.f90:29-46).
+__device__ __forceinline__ double hash_uniform_d(unsigned long long seed, unsigned long long counter) {
+    unsigned long long z = seed * 0x9E3779B97F4A7C15ull + counter + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// Ornstein-Uhlenbeck update of the forcing coefficients for step `step` (one thread each):
+// c <- f c + sigma sqrt(1 - f^2) xi with f = exp(-dt/tcorr) and a Box-Muller normal deviate.
+static __global__ void k_ou_update(double* ou, int nm, const double* dt, double sigma, double tcorr,
+                                   unsigned long long seed, long long step) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * nm) return;
+    const double f = exp(-(*dt) / tcorr);
+    const double sg = sigma * sqrt(1.0 - f * f);
+    const unsigned long long cnt = (unsigned long long)(step * nm + q / 2) * 2 + (q & 1);
+    const double u1 = hash_uniform_d(seed, 2 * cnt), u2 = hash_uniform_d(seed, 2 * cnt + 1);
+    const double xi = sqrt(-2.0 * log(1.0 - u1)) * cos(2.0 * 3.141592653589793238462643383279 * u2);
+    ou[q] = f * ou[q] + sg * xi;
+}
+
 static __global__ void k_prepare_step(unsigned long long* dt_next, const double* dt, const double* dtstop, int ndust,
                                       int const_ts, float* coef) {
     const int k = threadIdx.x;
