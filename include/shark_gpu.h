@@ -177,7 +177,10 @@ typedef struct shark_gpu_config {
     double grw_gamma_grains, grw_estar_grains;
     int32_t grw_kernel;                /* 0 physical, 1 constant, 2 additive (kernel_type)     */
     int32_t grw_mode;                  /* SHARK_GROWTH_* bits                                   */
-    double reserved[12];
+    /* viscosity (SHARK_FLAG_VISCOSITY, source_terms.f90:99-118): the polar disk's
+     * eta_visc = disk_alpha_visc H cs (disk_polar/setup.f90:67) */
+    double disk_alpha_visc;
+    double reserved[11];
 
     /* Optional grid metrics from the caller (Fortran dx(ncells,ndim), surf(ncells,ndim),
      * vol(ncells), radii_c(ncells), position(ncells,ndim), cs(ncells)).  NULL: the library

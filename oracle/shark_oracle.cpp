@@ -59,6 +59,7 @@ struct oracle_state {
     std::vector<double> chg_seed;   // optional Newton start per cell (0 = none)
     // dustyTurb Ornstein-Uhlenbeck forcing: modes (kx', ky', |k'|) and coefficients (a_m, b_m)
     std::vector<double> ou_modes, ou_coef;
+    std::vector<double> eta_visc;   // kinematic viscosity per cell (disk: alpha H cs)
     int64_t ou_step = 0;
     double dt = 0.0, time = 0.0;
 
@@ -1604,7 +1605,30 @@ void source_terms(oracle_state& s) {
                               dt * (s.Q(i, s.ivz) * (s.Q(i, s.ivz) - s.Q(i, s.ivdz[k]))) / ts;
             }
         }
-        // viscosity (source_terms.f90:99-118) is rejected at create time (not used by any config).
+        if (visc && s.ndim == 2) {   // viscosity (source_terms.f90:99-118)
+            const int ix = (int)(i % s.nx_max), iy = (int)(i / s.nx_max);
+            const int64_t il = s.icell(ix - 1, iy), ir = s.icell(ix + 1, iy);
+            const double eta = s.eta_visc[i], rho = s.Q(i, s.irho), dx = s.DX(i, 0);
+            if (!polar) {
+                const int64_t jd = s.icell(ix, iy - 1), ju = s.icell(ix, iy + 1);
+                const double dy = s.DX(i, 1);
+                const double lap_x_u = (s.Q(ir, s.ivx) + s.Q(il, s.ivx) - 2.0 * s.Q(i, s.ivx)) / (dx * dx);
+                SU(i, s.ivx) = SU(i, s.ivx) + rho * dt * eta * lap_x_u;
+                const double lap_y_u = (s.Q(ju, s.ivx) + s.Q(jd, s.ivx) - 2.0 * s.Q(i, s.ivx)) / (dy * dy);
+                SU(i, s.ivx) = SU(i, s.ivx) + rho * dt * eta * lap_y_u;
+                const double lap_x_v = (s.Q(ir, s.ivy) + s.Q(il, s.ivy) - 2.0 * s.Q(i, s.ivy)) / (dx * dx);
+                const double lap_y_v = (s.Q(ju, s.ivy) + s.Q(jd, s.ivy) - 2.0 * s.Q(i, s.ivy)) / (dy * dy);
+                SU(i, s.ivy) = SU(i, s.ivy) + rho * dt * eta * (lap_x_v + lap_y_v);
+            } else {
+                const double rc = s.radii_c[i];
+                const double lap_x_u = (s.Q(ir, s.ivx) + s.Q(il, s.ivx) - 2.0 * s.Q(i, s.ivx)) / (dx * dx) +
+                                       (s.Q(ir, s.ivx) + s.Q(il, s.ivx)) / rc / dx / 2.0 - s.Q(i, s.ivx) / rc / rc;
+                SU(i, s.ivx) = SU(i, s.ivx) + rho * dt * eta * lap_x_u;
+                const double lap_x_v = (s.Q(ir, s.ivy) + s.Q(il, s.ivy) - 2.0 * s.Q(i, s.ivy)) / (dx * dx) -
+                                       s.Q(i, s.ivy) / (rc * rc) + (s.Q(ir, s.ivy) + s.Q(il, s.ivy)) / rc / dx / 2.0;
+                SU(i, s.ivy) = SU(i, s.ivy) + rho * dt * eta * lap_x_v;
+            }
+        }
     }
     for (size_t j = 0; j < S.size(); ++j) s.u[j] = s.u[j] + S[j];
 }
@@ -1885,7 +1909,6 @@ oracle_state* oracle_create(const shark_gpu_config* cfg) {
     if (cfg->slope_type < 0 || cfg->slope_type > 3) return nullptr;
     if (cfg->geom != 0 && cfg->geom != 2) return nullptr;
     if (cfg->geom == 2 && cfg->ny == 1) return nullptr;
-    if (cfg->flags & SHARK_FLAG_VISCOSITY) return nullptr;
     oracle_state* s = new oracle_state();
     s->cfg = *cfg;
     s->nx = cfg->nx; s->ny = cfg->ny; s->nghost = cfg->nghost; s->ndust = cfg->ndust;
@@ -1937,10 +1960,12 @@ oracle_state* oracle_create(const shark_gpu_config* cfg) {
     if (cfg->iso_cs == 1)
         for (size_t i = 0; i < nc; ++i) s->cs[i] = cfg->cs0;
     if (cfg->setup == SHARK_SETUP_DUSTYTURB && cfg->turb_mach > 0.0) turb_init(*s);
+    s->eta_visc.assign(nc, 0.0);
     if (cfg->setup == SHARK_SETUP_DISK_POLAR) {
         for (size_t i = 0; i < nc; ++i) {
             const double rr = s->radii_c[i];
             s->cs[i] = disk_cs(*cfg, rr);
+            s->eta_visc[i] = cfg->disk_alpha_visc * (disk_h(*cfg, rr) * rr) * s->cs[i];   // setup.f90:67
             if (cfg->flags & SHARK_FLAG_FARGO) s->fargo_v[i] = -std::sqrt(cfg->disk_mstar / powi(rr, 3)) * rr;
         }
     }

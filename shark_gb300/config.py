@@ -82,7 +82,8 @@ class SharkConfig(C.Structure):
         ("grw_eps_thr", _D), ("grw_eps_thr_frag", _D), ("grw_dtcontrol", _D), ("grw_delta_vambi", _D),
         ("grw_alpha_turb", _D), ("grw_size_mono", _D), ("grw_slope_mono", _D), ("grw_Abr", _D),
         ("grw_gamma_grains", _D), ("grw_estar_grains", _D), ("grw_kernel", _I), ("grw_mode", _I),
-        ("reserved", _D * 12),
+        ("disk_alpha_visc", _D),
+        ("reserved", _D * 11),
         ("dx", _P), ("surf", _P), ("vol", _P), ("radii_c", _P), ("position", _P), ("cs", _P),
     ]
 
@@ -157,4 +158,5 @@ def default_config():
     c.grw_Abr = 2.8e3
     c.grw_gamma_grains = 25.0
     c.grw_estar_grains = 2.8e11
+    c.disk_alpha_visc = 1e-2                  # disk_polar/setup_commons.f90:21
     return c

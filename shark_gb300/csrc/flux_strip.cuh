@@ -305,6 +305,12 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 gb[0] = d.rho; gb[2] = d.mn; gb[1] = d.mt; gb[3] = d.mz;
             }
         }
+        // radial neighbours of row P-1's old velocities for the viscous term (all lanes shuffle)
+        R vxl = R(0), vxr = R(0), vyl = R(0), vyr = R(0);
+        if (IS_GAS && p.visc) {
+            vxl = shfl_up1(q0[1]); vxr = shfl_dn1(q0[1]);
+            vyl = shfl_up1(q0[2]); vyr = shfl_dn1(q0[2]);
+        }
         // ---- finish row P-1: y-flux part, then the polar sources on its OLD q (= q0) ---------------
         if (row > ay0 && finish_upd) {
             R un[NV];
@@ -313,7 +319,31 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 if constexpr (FAST) un[k] = t_prev[k] + (g_prev[k] - gb[k]) * s2 * (dt * rvol);
                 else un[k] = t_prev[k] + (g_prev[k] * s2 - gb[k] * s2) / vol * dt;
             }
-            if (polar) {   // Source_terms GEOM==2 (source_terms.f90:37-47)
+            if (polar && IS_GAS && p.visc) {
+                // Source_terms GEOM==2 (source_terms.f90:37-47) plus the viscous term
+                // (source_terms.f90:110-115), accumulated in S_U before the update as there
+                const R qr = q0[0], qvx = q0[1], qvy = q0[2];
+                const R eta = p.etav[gxc];
+                R S1, S2;
+                if constexpr (FAST) {
+                    const R dtr = dt * irp, idx2 = R(1) / (dx1 * dx1);
+                    S1 = (qr * sq(qvy) + q0[4]) * dtr;
+                    S2 = -(qr * qvy * qvx * dtr);
+                    const R lu = (vxr + vxl - R(2) * qvx) * idx2 + (vxr + vxl) * irp / dx1 * half - qvx * irp * irp;
+                    const R lv = (vyr + vyl - R(2) * qvy) * idx2 - qvy * irp * irp + (vyr + vyl) * irp / dx1 * half;
+                    S1 = S1 + qr * dt * eta * lu;
+                    S2 = S2 + qr * dt * eta * lv;
+                } else {
+                    S1 = dt * (qr * sq(qvy) + q0[4]) / radc;
+                    S2 = R(0) - dt * (qr * qvy * qvx / radc);
+                    const R lu = (vxr + vxl - R(2) * qvx) / (dx1 * dx1) + (vxr + vxl) / radc / dx1 / R(2) - qvx / radc / radc;
+                    S1 = S1 + qr * dt * eta * lu;
+                    const R lv = (vyr + vyl - R(2) * qvy) / (dx1 * dx1) - qvy / (radc * radc) + (vyr + vyl) / radc / dx1 / R(2);
+                    S2 = S2 + qr * dt * eta * lv;
+                }
+                un[1] = un[1] + S1;
+                un[2] = un[2] + S2;
+            } else if (polar) {   // Source_terms GEOM==2 (source_terms.f90:37-47)
                 const R qr = q0[0], qvx = q0[1], qvy = q0[2];
                 if constexpr (FAST) {
                     const R dtr = dt * irp;

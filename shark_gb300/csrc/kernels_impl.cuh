@@ -28,6 +28,8 @@ static KParams<R> make_params(const DeviceView& v) {
     p.vol = (const R*)v.m[4]; p.radc = (const R*)v.m[5]; p.xpos = (const R*)v.m[6]; p.cs = (const R*)v.m[7];
     p.sfx = (const R*)v.m[8]; p.sfy = (const R*)v.m[9]; p.irp = (const R*)v.m[10]; p.rvol = (const R*)v.m[11];
     p.fgrav = (const R*)v.m[12];
+    p.etav = (const R*)v.m[13];
+    p.visc = (c.flags & SHARK_FLAG_VISCOSITY) ? 1 : 0;
     p.dx1d = v.md[0]; p.dx2d = v.md[1]; p.radcd = v.md[2]; p.xposd = v.md[3]; p.csd = v.md[4];
     p.fgravd = v.md[5]; p.treld = v.md[6]; p.hsd = v.md[7]; p.vkd = v.md[8];
     p.u_init = (const R*)v.u_init;

@@ -35,9 +35,9 @@ struct DeviceView {
     int nbuf;                   // buffers in rotation
     int cur;                    // index of the current state
     const void* u_init;         // relaxation reference state (polar disk), state precision
-    const void* m[13];          // dx1, dx2, surf1, surf2, vol, radc, xpos, cs, sfx, sfy, irp, rvol,
-                                // fgrav (state precision; sfx..rvol are derived tables, fgrav the
-                                // radial point-mass gravity of the polar disk)
+    const void* m[14];          // dx1, dx2, surf1, surf2, vol, radc, xpos, cs, sfx, sfy, irp, rvol,
+                                // fgrav, etav (state precision; sfx..rvol are derived tables, fgrav
+                                // the radial point-mass gravity of the polar disk, etav its viscosity)
     const double* md[9];        // dx1, dx2, radc, xpos, cs, fgrav, trel, hs, vk (FP64): trel the
                                 // disk relaxation time (0 outside r_relax), hs = sqrt(2 pi) H,
                                 // vk the FARGO orbital velocity

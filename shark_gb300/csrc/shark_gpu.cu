@@ -130,7 +130,7 @@ struct Columns {
     std::vector<double> dx1, dx2, surf1, surf2, vol, radc, xpos, cs;
     // polar disk (disk_polar/setup.f90): point-mass gravity -Mstar/r^2, relaxation time t_rel
     // inside r_relax (0 elsewhere), sqrt(2 pi) H for the midplane density, FARGO velocity -Omega r
-    std::vector<double> fgrav, trel, hs, vk;
+    std::vector<double> fgrav, trel, hs, vk, etav;
     // derived tables used by the mixed-precision kernels (division-free slopes and update):
     // sfx[i] = 2/(dx1[i]+dx1[i-1]), sfy[i] = 1/(dx2[i]*r_i), irp[i] = 1/r_i, rvol[i] = 1/vol[i]
     std::vector<double> sfx, sfy, irp, rvol;
@@ -234,7 +234,7 @@ int32_t build_columns(const shark_gpu_config& c, int nx_max, int ny_max, Columns
         }
     }
     col.fgrav.assign(nx_max, 0.0); col.trel.assign(nx_max, 0.0);
-    col.hs.assign(nx_max, 0.0); col.vk.assign(nx_max, 0.0);
+    col.hs.assign(nx_max, 0.0); col.vk.assign(nx_max, 0.0); col.etav.assign(nx_max, 0.0);
     if (c.setup == SHARK_SETUP_DISK_POLAR) {
         const double M = c.disk_mstar, tw = c.disk_n_rel * 2.0 * kPi;
         for (int ix = 0; ix < nx_max; ++ix) {
@@ -244,6 +244,7 @@ int32_t build_columns(const shark_gpu_config& c, int nx_max, int ny_max, Columns
             col.cs[ix] = std::sqrt(M / (r * r * r)) * H;                          // Omega H
             col.fgrav[ix] = -M / (r * r);                                         // setup.f90:362
             col.hs[ix] = std::sqrt(2.0 * kPi) * H;
+            col.etav[ix] = c.disk_alpha_visc * H * col.cs[ix];                     // setup.f90:67
             if (c.flags & SHARK_FLAG_FARGO) col.vk[ix] = -std::sqrt(M / powi(r, 3)) * r;   // setup.f90:33-36
             const bool act = ix >= ng && ix < ng + nx;
             if (act && r < c.disk_r_relax)                                        // setup.f90:226
@@ -277,7 +278,8 @@ int32_t validate(const shark_gpu_config* c) {
     if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_DUSTYTURB)
         return fail(SHARK_ERR_UNSUPPORTED, "setup %d has no device hooks in this build", c->setup);
     const int f = c->flags;
-    if (f & SHARK_FLAG_VISCOSITY) return fail(SHARK_ERR_UNSUPPORTED, "viscosity is not built");
+    if ((f & SHARK_FLAG_VISCOSITY) && c->setup != SHARK_SETUP_DISK_POLAR)
+        return fail(SHARK_ERR_UNSUPPORTED, "viscosity: only the polar disk defines eta_visc (disk_polar/setup.f90:67)");
     if (f & SHARK_FLAG_GROWTH) {
         if (c->ndust < 1) return fail(SHARK_ERR_INVALID_ARG, "growth needs dust species");
         if (c->setup != SHARK_SETUP_DISK_POLAR && c->setup != SHARK_SETUP_DUSTYTURB)
@@ -340,12 +342,8 @@ int32_t validate(const shark_gpu_config* c) {
         if (ring > 200 * 1024)
             return fail(SHARK_ERR_UNSUPPORTED, "FARGO ring of %d cells exceeds one CTA's shared memory", c->ny);
     }
-    if (c->ndust > 0 && (f & SHARK_FLAG_BACK_REACTION) && c->iso_cs < 1)
-        return fail(SHARK_ERR_UNSUPPORTED, "adiabatic drag heating (source_terms.f90:88-97) is not built");
     if (c->setup == SHARK_SETUP_SI && c->ndust > 0 && !(f & SHARK_FLAG_DRAG) && (f & SHARK_FLAG_FORCE_KICK))
         return fail(SHARK_ERR_UNSUPPORTED, "SI explicit drag forces (drag=.false.) are not built");
-    if (c->setup == SHARK_SETUP_SOD && c->ndust > 0 && c->iso_cs != 1 && (f & SHARK_FLAG_DRAG))
-        return fail(SHARK_ERR_UNSUPPORTED, "Epstein drag needs an isothermal sound speed in this build");
     if (!(c->gamma > 1.0) || !(c->cfl > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "gamma > 1 and cfl > 0 required");
     for (int k = 0; k < c->ndust; ++k) {
         if (c->setup == SHARK_SETUP_SI && (f & SHARK_FLAG_DRAG) && !(c->dust_tstop[k] > 0.0))
@@ -590,11 +588,12 @@ void build_forcing(const shark_gpu_config& c, std::vector<double>& modes, std::v
 
 template <typename T>
 void upload_cols(std::vector<T>& dst, const Columns& col) {
-    const std::vector<double>* src[13] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
-                                          &col.xpos, &col.cs, &col.sfx, &col.sfy, &col.irp, &col.rvol, &col.fgrav};
+    const std::vector<double>* src[14] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol, &col.radc,
+                                          &col.xpos, &col.cs, &col.sfx, &col.sfy, &col.irp, &col.rvol, &col.fgrav,
+                                          &col.etav};
     const size_t n = col.dx1.size();
-    dst.resize(13 * n);
-    for (int a = 0; a < 13; ++a)
+    dst.resize(14 * n);
+    for (int a = 0; a < 14; ++a)
         for (size_t i = 0; i < n; ++i) dst[a * n + i] = (T)(*src[a])[i];
 }
 
@@ -788,6 +787,7 @@ int32_t shark_gpu_config_defaults(shark_gpu_config* cfg) {
     cfg->grw_Abr = 2.8e3;
     cfg->grw_gamma_grains = 25.0;
     cfg->grw_estar_grains = 2.8e11;
+    cfg->disk_alpha_visc = 1e-2;        // disk_polar/setup_commons.f90:21
     return SHARK_OK;
 }
 
@@ -866,7 +866,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     }
     v.u_init = c->uinit;
     const size_t ncol = (size_t)v.nx_max;
-    INIT_TRY(cudaMalloc(&c->metrics, 13 * ncol * c->elem));
+    INIT_TRY(cudaMalloc(&c->metrics, 14 * ncol * c->elem));
     INIT_TRY(cudaMalloc(&c->metrics_d, 9 * ncol * sizeof(double)));
     if (is_mixed(c)) {
         std::vector<float> h;
@@ -877,7 +877,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         upload_cols(h, col);
         INIT_TRY(cudaMemcpy(c->metrics, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
-    for (int a = 0; a < 13; ++a) v.m[a] = (const char*)c->metrics + a * ncol * c->elem;
+    for (int a = 0; a < 14; ++a) v.m[a] = (const char*)c->metrics + a * ncol * c->elem;
     {
         std::vector<double> hd(9 * ncol);
         const std::vector<double>* src[9] = {&col.dx1, &col.dx2, &col.radc, &col.xpos, &col.cs,

@@ -34,6 +34,8 @@ struct KParams {
     const R *dx1, *dx2, *surf1, *surf2, *vol, *radc, *xpos, *cs;
     const R *sfx, *sfy, *irp, *rvol;   // division-free tables (mixed path)
     const R* fgrav;                    // polar disk: -Mstar/r^2 (0 for the other setups)
+    const R* etav;                     // polar disk: kinematic viscosity alpha H cs
+    int visc;                          // viscosity source term on
     // per-column metrics in FP64 (courant, drag)
     const double *dx1d, *dx2d, *radcd, *xposd, *csd;
     // polar disk per-column FP64 tables: gravity, relaxation time (0 = no relaxation),
@@ -253,6 +255,21 @@ __device__ __forceinline__ void block_reduce_dt(double dtc, unsigned int st, uns
     }
 }
 
+// Sound speed of the cell at the start of the step: the isothermal column value, or ctoprim's
+// sqrt(gamma P / max(rho, smallr)) of the adiabatic state (solve.f90:205-233).
+template <typename R>
+__device__ __forceinline__ double cs_start(const KParams<R>& p, int gx, int gy) {
+    if (p.iso == 1) return p.csd[gx];
+    const double rho = (double)p.u_cur[uidx(p, 0, gy, gx)];
+    const double vx = (double)p.u_cur[uidx(p, 1, gy, gx)] / rho, vy = (double)p.u_cur[uidx(p, 2, gy, gx)] / rho;
+    const double vz = (double)p.u_cur[uidx(p, 3, gy, gx)] / rho;
+    const double ekin = 0.5 * rho * (vx * vx) + 0.5 * rho * (vy * vy) + 0.5 * rho * (vz * vz);
+    double P = (p.gamma - 1.0) * ((double)p.u_cur[uidx(p, 4, gy, gx)] - ekin - 0.0);
+    P = P > p.smallp ? P : p.smallp;
+    const double qr = rho > p.smallr ? rho : p.smallr;
+    return sqrt(p.gamma * P / qr);
+}
+
 // Stopping time of species k at cell (gx, gy) from the state at the start of the step
 // (compute_tstop runs before the update, solve.f90:34-35); qrho_old = max(rho_old, smallr).
 template <typename R>
@@ -267,8 +284,29 @@ __device__ __forceinline__ double tstop_cell(const KParams<R>& p, int k, double 
         return p.dstokes[k] * p.box_l * p.turb_rho0 / p.csd[gx] / qrho_old;
     if (p.setup == SHARK_SETUP_DISK_POLAR)   // Epstein on the midplane density Sigma/(sqrt(2 pi) H)
         return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old / p.hsd[gx] * p.csd[gx]);
-    // Epstein (SOD/setup.f90:179-185); isothermal cs only (checked at init)
-    return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old * p.csd[gx]);
+    // Epstein (SOD/setup.f90:179-185) with the cell's sound speed
+    return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old * cs_start(p, gx, gy));
+}
+
+// Drag heating of an adiabatic gas with back reaction (source_terms.f90:88-97): the energy
+// gains sum_k dt v.(v - v_k)/t_k with the velocities and stopping times at the start of the step.
+template <typename R>
+__device__ __forceinline__ double drag_heating(const KParams<R>& p, int gx, int gy, double dt) {
+    const int N = p.ndust;
+    const double rho = (double)p.u_cur[uidx(p, 0, gy, gx)];
+    const double qrho = rho > p.smallr ? rho : p.smallr;
+    const double vx = (double)p.u_cur[uidx(p, 1, gy, gx)] / rho, vy = (double)p.u_cur[uidx(p, 2, gy, gx)] / rho;
+    const double vz = (double)p.u_cur[uidx(p, 3, gy, gx)] / rho;
+    double S = 0.0;
+    for (int k = 0; k < N; ++k) {
+        const double ts = tstop_cell(p, k, qrho, gx, gy);
+        const double rd = (double)p.u_cur[uidx(p, 5 + k, gy, gx)];
+        const double vdx = (double)p.u_cur[uidx(p, 5 + N + k, gy, gx)] / rd;
+        const double vdy = (double)p.u_cur[uidx(p, 5 + 2 * N + k, gy, gx)] / rd;
+        const double vdz = (double)p.u_cur[uidx(p, 5 + 3 * N + k, gy, gx)] / rd;
+        S = S + dt * (vx * (vx - vdx)) / ts + dt * (vy * (vy - vdy)) / ts + dt * (vz * (vz - vdz)) / ts;
+    }
+    return S;
 }
 
 // setup_inloop of the polar disk (disk_polar/setup.f90:206-284) for one active cell, FP64 or
@@ -422,6 +460,10 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
                 const double fl = rho * p.dust_ratio_min;
                 if (fl > rd) u[ir] = R(fl);
             }
+        }
+        if (MODE == 0 && N > 0 && br && p.iso < 1) {   // drag heating, part of S_U (source_terms.f90:88-97)
+            const long long ie = uidx(p, 4, gy, gx);
+            u[ie] = R((double)u[ie] + drag_heating(p, gx, gy, dt));
         }
         if (GROW && MODE == 0) st |= grow_in_finalize(p, u, gx, gy, dt);   // dust_growth (solve.f90:113)
         if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)
@@ -597,6 +639,10 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
                 const long long ir = uidx(p, 5 + k, gy, gx);
                 if (fl > u[ir]) u[ir] = fl;
             }
+        }
+        if (MODE == 0 && N > 0 && (p.flags & SHARK_FLAG_BACK_REACTION) && p.iso < 1) {   // drag heating
+            const long long ie = uidx(p, 4, gy, gx);
+            u[ie] = (float)((double)u[ie] + drag_heating(p, gx, gy, dt));
         }
         if (GROW && MODE == 0) st |= grow_in_finalize(p, u, gx, gy, dt);   // dust_growth (solve.f90:113)
         if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)

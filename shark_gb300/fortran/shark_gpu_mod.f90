@@ -40,7 +40,8 @@ module shark_gpu
     real(c_double) :: grw_eps_thr_frag, grw_dtcontrol, grw_delta_vambi, grw_alpha_turb, grw_size_mono
     real(c_double) :: grw_slope_mono, grw_Abr, grw_gamma_grains, grw_estar_grains
     integer(c_int32_t) :: grw_kernel, grw_mode
-    real(c_double) :: reserved(12)
+    real(c_double) :: disk_alpha_visc
+    real(c_double) :: reserved(11)
     type(c_ptr) :: dx, surf, vol, radii_c, position, cs
   end type shark_gpu_config
 

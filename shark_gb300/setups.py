@@ -125,14 +125,22 @@ def si_boundaries(cfg, u):
 # SOD
 # ---------------------------------------------------------------------------------------------
 def sod(nx=1000, ny=1, gamma=1.4, cfl=0.5, slope_type=1, solver=2, precision=PREC_FP64,
-        rho_l=1.0, rho_r=0.125, P_l=1.0, P_r=0.1):
-    """1D Sod shock tube (src/setups/SOD/setup.f90:1-46, boundaries.f90:49-77)."""
+        rho_l=1.0, rho_r=0.125, P_l=1.0, P_r=0.1, ndust=0, dust2gas=1.0, sizes=(1e-3, 1e-1),
+        rhograin=1.0):
+    """1D Sod shock tube (src/setups/SOD/setup.f90:1-46, boundaries.f90:49-77).  With ndust > 0 a
+    dusty shock tube: each species carries dust2gas/ndust of the gas density, at rest, with grain
+    radii log-spaced over `sizes` (Epstein drag on the adiabatic sound speed, back reaction and
+    drag heating, SOD/setup.f90:179-185 and source_terms.f90:88-97)."""
     cfg = default_config()
-    cfg.nx, cfg.ny, cfg.ndust = nx, ny, 0
+    cfg.nx, cfg.ny, cfg.ndust = nx, ny, ndust
     cfg.gamma, cfg.cfl, cfg.slope_type, cfg.solver = gamma, cfl, slope_type, solver
     cfg.precision = precision
     cfg.setup = SETUP_SOD
-    cfg.flags = 0
+    cfg.flags = (FLAG_DRAG | FLAG_BACK_REACTION) if ndust > 0 else 0
+    cfg.rhograin = rhograin
+    for k in range(ndust):
+        cfg.dust_size[k] = sizes[0] * (sizes[1] / sizes[0]) ** (k / max(ndust - 1, 1))
+        cfg.dust_eps[k] = dust2gas / ndust
     cfg.sod_rho_l, cfg.sod_rho_r, cfg.sod_P_l, cfg.sod_P_r = rho_l, rho_r, P_l, P_r
     cfg.sod_direction = 0
     pos = positions(cfg)
@@ -140,6 +148,8 @@ def sod(nx=1000, ny=1, gamma=1.4, cfl=0.5, slope_type=1, solver=2, precision=PRE
     right = pos[:, 0] > 0.5
     q[0] = np.where(right, rho_r, rho_l)
     q[4] = np.where(right, P_r, P_l)
+    for k in range(ndust):
+        q[5 + k] = cfg.dust_eps[k] * q[0]
     u = primtoc(cfg, q).reshape(-1)
     return cfg, u
 
