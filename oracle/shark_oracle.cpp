@@ -544,6 +544,7 @@ int charge_cell(const shark_gpu_config& g, const ChargeCell& c, double psi0, dou
             2.0 * n_i * vi / (x * nH) * (et2 + et) *
                 ((dni / n_i + (D) * (2.0 * et + 1.0) / (eps_psi * (1.0 + et))) * (S4) + ((D) * S5)) +
             n_i * vi / (x * nH) * (dni / n_i * (1.0 - psi) - 1.0) * (S6);
+        const double prev = psi;
         psi = psi - fpsi / dfdpsi;
         if (psi < psi0) {
             psi = psi0 * 0.9999999;
@@ -553,6 +554,9 @@ int charge_cell(const shark_gpu_config& g, const ChargeCell& c, double psi0, dou
         }
         conv = std::fabs(fpsi);   // the reference's interim values of conv are overwritten here
         niter = niter + 1;
+        // an update that leaves psi unchanged with the residual above the tolerance repeats
+        // itself until nitermax (e.g. the psi0 clamp): go there directly, same final state
+        if (psi == prev && conv > g.chg_eps) niter = g.chg_nitermax;
     }
     eps_psi = (1.0 - psi) / thetai * std::exp(-psi);
     if (lowT > 0) eps_psi = epsone;

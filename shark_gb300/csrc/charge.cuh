@@ -117,7 +117,12 @@ __device__ __forceinline__ void charge_newton(const ChargeParams<R>& p, const do
         }
         conv = fabs(fpsi);
         niter = niter + 1;
-        if (stall && psi == prev) break;
+        if (psi == prev) {
+            if (stall) break;   // FP32 phase: no further progress in FP32
+            // an unchanged psi with the residual above the tolerance repeats itself until
+            // nitermax (e.g. the psi0 clamp): go there directly, same final state
+            if (conv > tol) niter = p.nitermax;
+        }
     }
 }
 

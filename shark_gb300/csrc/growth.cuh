@@ -19,9 +19,13 @@
 
 namespace shark {
 
+// largest species count of the growth kernel: the per-cell pair table lives in local memory
+constexpr int GROWTH_MAX_DUST = 32;
+
 struct GrowthDev {
     int on, kernel, mode, t_per_col;
     const double* pA;        // [N*N] (clustered^2 pi)(s_k + s_j)^2
+    const double* pK;        // [N*N] rate factor of the mixed path: pA/m_k/m_j, 1/m_k/m_j, (m_k+m_j)/m_k/m_j
     const double* pS;        // [N*N] m_k unit_m + m_j unit_m
     const double* pD;        // [N*N] m_k m_j unit_m^2
     const int32_t* pic;      // [N*N*2] target bins ic1, ic2 (1-based) without fragmentation
@@ -88,7 +92,11 @@ __device__ __forceinline__ double growth_dv_d(const GrowthDev& g, int N, int k, 
 
 // Sub-cycled growth of one cell: rd[N] in/out (dust densities after the drag), rho_gas the
 // conserved gas density, rho_q the floored gas density at the start of the step (q(irho)).
+// The pair velocities depend only on the start of the step, so they are formed once per cell
+// (the values the oracle re-forms every sub-step).  FAST (mixed path): the pair rate is
+// pK dv rho_k rho_j / hs with a host-tabulated pK instead of the oracle's two divisions.
 // Returns false if the sub-step cap was reached.
+template <bool FAST>
 static __device__ bool growth_cell_d(const GrowthDev& g, int N, int ix, double dt, double rho_gas, double rho_q, double hs,
                               double* rd, const double* ts, const double* vx, const double* vy, const double* vz,
                               const double* gam, double eta_a) {
@@ -104,18 +112,22 @@ static __device__ bool growth_cell_d(const GrowthDev& g, int N, int ix, double d
     const double t_eta = t_L / sqrt(Re);
     const double rm = pow(Re, -0.5);
     const bool frag = (g.mode & SHARK_GROWTH_FRAGMENTATION) != 0;
-    double drhodt[SHARK_MAX_DUST];
+    double dvp[GROWTH_MAX_DUST * (GROWTH_MAX_DUST + 1) / 2];
+    for (int k = 0, q = 0; k < N; ++k)
+        for (int j = 0; j <= k; ++j, ++q)
+            dvp[q] = g.kernel == 0 ? growth_dv_d(g, N, k, j, T, cs_v, t_L, t_eta, rm, vambi, ts, vx, vy, vz, gam) : 0.0;
+    const double ihs = 1.0 / hs;
+    double drhodt[GROWTH_MAX_DUST];
     double time_growth = 0.0;
     int niter = 0;
     while (time_growth < dt && niter < grw::MAX_SUB) {
         for (int k = 0; k < N; ++k) drhodt[k] = 0.0;
         niter = niter + 1;
-        for (int k = 0; k < N; ++k) {
+        for (int k = 0, q = 0; k < N; ++k) {
             const double m1 = g.mk[k];
-            for (int j = 0; j <= k; ++j) {
+            for (int j = 0; j <= k; ++j, ++q) {
                 const double m2 = g.mk[j];
-                const double dv = g.kernel == 0 ? growth_dv_d(g, N, k, j, T, cs_v, t_L, t_eta, rm, vambi, ts, vx, vy, vz, gam)
-                                                : 0.0;
+                const double dv = dvp[q];
                 double f_frag = 0.0, p_coag = 1.0;
                 if (frag) {
                     const double Ecol = 0.5 * (m1 * m2) / (m1 + m2) * (dv * dv);
@@ -125,11 +137,16 @@ static __device__ bool growth_cell_d(const GrowthDev& g, int N, int ix, double d
                     f_frag = lo > 0.0 ? lo : 0.0;
                 }
                 double dndt;
-                if (g.kernel == 1) dndt = rd[k] * rd[j] / m1 / m2;
-                else if (g.kernel == 2) dndt = (m1 + m2) * rd[k] * rd[j] / m1 / m2;
-                else dndt = g.pA[k * N + j] * dv * rd[k] * rd[j] / m1 / m2;
-                dndt = dndt / hs;
-                if (k == j) dndt = dndt / 2.0;
+                if constexpr (FAST) {
+                    dndt = g.pK[k * N + j] * (g.kernel == 0 ? dv : 1.0) * rd[k] * rd[j] * ihs;
+                    if (k == j) dndt = dndt * 0.5;
+                } else {
+                    if (g.kernel == 1) dndt = rd[k] * rd[j] / m1 / m2;
+                    else if (g.kernel == 2) dndt = (m1 + m2) * rd[k] * rd[j] / m1 / m2;
+                    else dndt = g.pA[k * N + j] * dv * rd[k] * rd[j] / m1 / m2;
+                    dndt = dndt / hs;
+                    if (k == j) dndt = dndt / 2.0;
+                }
                 if (g.kernel == 0) {
                     if (g.eps_thr > 0.0 && (rd[k] < g.eps_thr * rho_gas)) p_coag = 0.0;
                     if (g.eps_thr > 0.0 && (rd[j] < g.eps_thr * rho_gas)) p_coag = 0.0;

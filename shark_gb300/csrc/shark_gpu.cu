@@ -282,6 +282,7 @@ int32_t validate(const shark_gpu_config* c) {
         return fail(SHARK_ERR_UNSUPPORTED, "viscosity: only the polar disk defines eta_visc (disk_polar/setup.f90:67)");
     if (f & SHARK_FLAG_GROWTH) {
         if (c->ndust < 1) return fail(SHARK_ERR_INVALID_ARG, "growth needs dust species");
+        if (c->ndust > 32) return fail(SHARK_ERR_UNSUPPORTED, "growth is built for at most 32 dust species");
         if (c->setup != SHARK_SETUP_DISK_POLAR && c->setup != SHARK_SETUP_DUSTYTURB)
             return fail(SHARK_ERR_UNSUPPORTED, "growth needs the temperature of the polar disk or dustyTurb setup");
         if (c->grw_kernel < 0 || c->grw_kernel > 2) return fail(SHARK_ERR_INVALID_ARG, "grw_kernel must be 0, 1 or 2");
@@ -455,7 +456,7 @@ void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_m
 // ---- dust growth tables (src/dust/dust_growth.f90:3-256, dust_init.f90:11-45) --------------------
 // The operations follow the CPU oracle's growth_grid so the tables are bit-identical to it.
 void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_max, std::vector<double>& hd,
-                         std::vector<int32_t>& hi, shark::GrowthDev& g, size_t off[8]) {
+                         std::vector<int32_t>& hi, shark::GrowthDev& g, size_t off[9]) {
     const int N = c.ndust;
     const double ul = unit1(c.unit_l), ud = unit1(c.unit_d), ut = unit1(c.unit_t);
     const double um = ul * ul * ul * ud, uv = ul / ut;
@@ -472,7 +473,8 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     off[5] = off[4] + N;         // sk
     off[6] = off[5] + N;         // redis
     off[7] = off[6] + NN;        // col
-    hd.assign(off[7] + (size_t)rows * 4, 0.0);
+    off[8] = off[7] + (size_t)rows * 4;   // pK
+    hd.assign(off[8] + NN, 0.0);
     hi.assign(NN * 2, 1);
     const double zeta = std::pow(c.grw_smax / c.grw_smin, 1.0 / N);
     const double eta = zeta * zeta * zeta;
@@ -502,6 +504,8 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
             const size_t q = (size_t)k * N + j;
             const double sk = c.dust_size[k], sj = c.dust_size[j];
             hd[off[0] + q] = (cl * cl) * kPi * ((sk + sj) * (sk + sj));
+            const double rate = c.grw_kernel == 1 ? 1.0 : c.grw_kernel == 2 ? (mk[k] + mk[j]) : hd[off[0] + q];
+            hd[off[8] + q] = rate / mk[k] / mk[j];
             hd[off[1] + q] = mk[k] * um + mk[j] * um;
             hd[off[2] + q] = mk[k] * mk[j] * (um * um);
             const double mc = (1.0 - 0.0) * (mk[k] + mk[j]);
@@ -956,7 +960,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     if (cfg->flags & SHARK_FLAG_GROWTH) {
         std::vector<double> hd;
         std::vector<int32_t> hi;
-        size_t off[8];
+        size_t off[9];
         build_growth_tables(*cfg, col, v.nx_max, hd, hi, v.gw, off);
         INIT_TRY(cudaMalloc(&c->grw_d, hd.size() * sizeof(double)));
         INIT_TRY(cudaMemcpy(c->grw_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
@@ -965,6 +969,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         v.gw.pA = c->grw_d + off[0]; v.gw.pS = c->grw_d + off[1]; v.gw.pD = c->grw_d + off[2];
         v.gw.peps = c->grw_d + off[3]; v.gw.mk = c->grw_d + off[4]; v.gw.sk = c->grw_d + off[5];
         v.gw.redis = c->grw_d + off[6]; v.gw.col = c->grw_d + off[7]; v.gw.pic = c->grw_i;
+        v.gw.pK = c->grw_d + off[8];
     }
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
     std::memset(c->host_ring, 0, 4 * sizeof(double));

@@ -346,8 +346,8 @@ __device__ __forceinline__ bool disk_inloop_cell(const KParams<R>& p, R* u, int 
 template <typename R>
 __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int gx, int gy, double dt) {
     const int N = p.ndust;
-    double rd[SHARK_MAX_DUST], ts[SHARK_MAX_DUST], vx[SHARK_MAX_DUST], vy[SHARK_MAX_DUST], vz[SHARK_MAX_DUST];
-    double gam[SHARK_MAX_DUST];
+    double rd[GROWTH_MAX_DUST], ts[GROWTH_MAX_DUST], vx[GROWTH_MAX_DUST], vy[GROWTH_MAX_DUST], vz[GROWTH_MAX_DUST];
+    double gam[GROWTH_MAX_DUST];
     const double rho_old = (double)p.u_cur[uidx(p, 0, gy, gx)];
     const double qrho_old = rho_old > p.smallr ? rho_old : p.smallr;
     const bool ambi = (p.gw.mode & SHARK_GROWTH_AMBIPOLAR) && p.chg_gamma_d;
@@ -364,7 +364,8 @@ __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int
     const double eta_a = ambi ? (double)p.chg_eta[2 * p.plane + c] : 0.0;
     const double hs = p.setup == SHARK_SETUP_DISK_POLAR ? p.hsd[gx] : 1.0;
     const double rho_gas = (double)u[uidx(p, 0, gy, gx)];
-    const bool ok = growth_cell_d(p.gw, N, gx, dt, rho_gas, qrho_old, hs, rd, ts, vx, vy, vz, ambi ? gam : nullptr, eta_a);
+    constexpr bool FAST = sizeof(R) == 4;
+    const bool ok = growth_cell_d<FAST>(p.gw, N, gx, dt, rho_gas, qrho_old, hs, rd, ts, vx, vy, vz, ambi ? gam : nullptr, eta_a);
     for (int k = 0; k < N; ++k) u[uidx(p, 5 + k, gy, gx)] = R(rd[k]);
     return ok ? 0u : (unsigned)SHARK_STATUS_GROWTH;
 }
