@@ -90,6 +90,136 @@ __device__ __forceinline__ double growth_dv_d(const GrowthDev& g, int N, int k, 
     return dv;
 }
 
+// Mixed-precision form of the cell update: the same algorithm with the relative velocities,
+// rates, mass bookkeeping and sub-steps in FP32 (the state is FP32 on this path), the elapsed
+// growth time in FP64.  Without fragmentation the target bins and splits come from the tables.
+static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int ix, double dt, float rho_gas, float rho_q,
+                                           float hs, double* rdd, const double* tsd, const double* vxd,
+                                           const double* vyd, const double* vzd, const double* gamd, float eta_a) {
+    const int row = g.t_per_col ? ix : 0;
+    const double* cc = g.col + (size_t)row * 4;
+    const float T = (float)cc[0], cs_T = (float)cc[1], cs_v = (float)cc[2];
+    const float pi = (float)grw::pi;
+    const float rho_cgs = rho_q / hs * (float)g.ud;
+    const float tff = sqrtf(3.f * pi / (32.f * (float)grw::grav * rho_cgs));
+    const float lambJ = tff * cs_T;
+    const float vambi = (float)g.delta_vambi * (float)(grw::clight * grw::clight) * eta_a / lambJ / (4.f * pi);
+    const float Re = 6.2e7f * sqrtf(rho_cgs / ((float)g.mu_gas * (float)grw::mH) / 1e5f) * sqrtf(T / 10.f);
+    const float t_L = g.t_per_col ? (float)cc[3] : tff / (float)g.ut;
+    const float t_eta = t_L / sqrtf(Re);
+    const float rm = rsqrtf(Re);
+    const bool frag = (g.mode & SHARK_GROWTH_FRAGMENTATION) != 0;
+    float rd[GROWTH_MAX_DUST], ts[GROWTH_MAX_DUST], gm[GROWTH_MAX_DUST];
+    for (int k = 0; k < N; ++k) {
+        rd[k] = (float)rdd[k];
+        ts[k] = (float)tsd[k];
+        gm[k] = gamd ? fabsf((float)gamd[k]) * rsqrtf(1.f + (float)gamd[k] * (float)gamd[k]) : 0.f;
+    }
+    // pair rate constants pK dv / hs (and the fragmented fraction), once per cell
+    float kp[GROWTH_MAX_DUST * (GROWTH_MAX_DUST + 1) / 2], fp[GROWTH_MAX_DUST * (GROWTH_MAX_DUST + 1) / 2];
+    const float ihs = 1.f / hs, a = (float)g.alpha_turb;
+    for (int k = 0, q = 0; k < N; ++k)
+        for (int j = 0; j <= k; ++j, ++q) {
+            float dv = 1.f;
+            if (g.kernel == 0) {
+                dv = 0.f;
+                if (g.mode & SHARK_GROWTH_TURB) {
+                    const float x = ts[j] / ts[k];
+                    const float fS = 3.2f - 1.f - x + 2.f / (1.f + x) * (1.f / 2.6f + x * x * x / (1.6f + x));
+                    const float St1 = ts[k] / t_L, St2 = ts[j] / t_L;
+                    float vt = a * cs_v * sqrtf(fS * St1);
+                    if (ts[k] < t_eta)
+                        vt = a * cs_v * sqrtf((St1 - St2) / (St1 + St2)) * sqrtf(St1 * St1 / (St1 + rm) - St2 * St2 / (St2 + rm));
+                    if (ts[k] > t_L) vt = a * cs_v * sqrtf(1.f / (1.f + St1) + 1.f / (1.f + St2));
+                    dv = vt;
+                }
+                if (g.mode & SHARK_GROWTH_BROWNIAN) {
+                    const float X = (float)((8.0 * grw::kB * (double)T / grw::pi) * g.pS[k * N + j] / g.pD[k * N + j] / g.uv2);
+                    dv = sqrtf(dv * dv + X);
+                }
+                if (g.mode & SHARK_GROWTH_DRIFT) {
+                    const float dx = (float)(vxd[k] - vxd[j]), dy = (float)(vyd[k] - vyd[j]), dz = (float)(vzd[k] - vzd[j]);
+                    dv = sqrtf(dv * dv + dx * dx + dy * dy + dz * dz);
+                }
+                if ((g.mode & SHARK_GROWTH_AMBIPOLAR) && gamd) {
+                    const float d = vambi / (float)g.uv * (gm[k] - gm[j]);
+                    dv = sqrtf(dv * dv + d * d);
+                }
+            }
+            const float m1 = (float)g.mk[k], m2 = (float)g.mk[j];
+            float ff = 0.f;
+            if (frag) {
+                const double Ecol = 0.5 * (g.mk[k] * g.mk[j]) / (g.mk[k] + g.mk[j]) * ((double)dv * dv);
+                const double Ebr = (g.mk[k] + g.mk[j]) / g.m_mono * g.Ebr_mono;
+                ff = (float)fmin(fmax((Ecol - 0.1 * Ebr) / (4.9 * Ebr), 0.0), 1.0);
+            }
+            (void)m1; (void)m2;
+            kp[q] = (float)g.pK[k * N + j] * dv * ihs * (k == j ? 0.5f : 1.f);
+            fp[q] = ff;
+        }
+    float drhodt[GROWTH_MAX_DUST];
+    double time_growth = 0.0;
+    int niter = 0;
+    const float st = (float)g.sticking;
+    while (time_growth < dt && niter < grw::MAX_SUB) {
+        for (int k = 0; k < N; ++k) drhodt[k] = 0.f;
+        niter = niter + 1;
+        for (int k = 0, q = 0; k < N; ++k) {
+            const float m1 = (float)g.mk[k];
+            for (int j = 0; j <= k; ++j, ++q) {
+                const float m2 = (float)g.mk[j];
+                float f_frag = fp[q], p_coag = 1.f;
+                const float dndt = kp[q] * rd[k] * rd[j];
+                if (g.kernel == 0) {
+                    if (g.eps_thr > 0.0 && (rd[k] < (float)g.eps_thr * rho_gas)) p_coag = 0.f;
+                    if (g.eps_thr > 0.0 && (rd[j] < (float)g.eps_thr * rho_gas)) p_coag = 0.f;
+                    if (g.eps_thr_frag > 0.0 && (rd[k] < (float)g.eps_thr_frag * rho_gas)) f_frag = 0.f;
+                    if (g.eps_thr_frag > 0.0 && (rd[j] < (float)g.eps_thr_frag * rho_gas)) f_frag = 0.f;
+                }
+                int ic1, ic2;
+                float eps_m;
+                if (f_frag == 0.f) {
+                    ic1 = g.pic[(k * N + j) * 2];
+                    ic2 = g.pic[(k * N + j) * 2 + 1];
+                    eps_m = (float)g.peps[k * N + j];
+                } else {
+                    const double mc = (1.0 - f_frag) * (g.mk[k] + g.mk[j]);
+                    ic1 = growth_bin_d(mc, g.massmin, g.eta, 0, N);
+                    ic2 = growth_bin_d(mc, g.massmin, g.eta, 1, N);
+                    eps_m = 1.f;
+                    if (ic1 < ic2) eps_m = fminf((float)((g.mk[ic2 - 1] - mc) / (g.mk[ic2 - 1] - g.mk[ic1 - 1])), 1.f);
+                }
+                const float pc = p_coag * dndt, one_f = 1.f - f_frag;
+                drhodt[k] -= pc * m1 * (one_f * st + f_frag);
+                drhodt[j] -= pc * m2 * (one_f * st + f_frag);
+                if (f_frag < 1.f) {
+                    const float add = pc * one_f * (m1 + m2) * st;
+                    drhodt[ic1 - 1] += eps_m * add;
+                    drhodt[ic2 - 1] += (1.f - eps_m) * add;
+                }
+                if (frag && f_frag > 0.f && p_coag > 0.f) {
+                    const int b = (int)floor(log(0.1 * f_frag * (g.mk[k] + g.mk[j]) / g.massmin) / log(g.eta) + 1);
+                    const int ifrag2 = max(min(b, ic1), 1);
+                    const float add = pc * f_frag * (m1 + m2);
+                    for (int kd = 0; kd < ifrag2; ++kd) drhodt[kd] += add * (float)g.redis[(ifrag2 - 1) * N + kd];
+                }
+            }
+        }
+        float dtg = 1e30f;
+        for (int k = 0; k < N; ++k)
+            if (drhodt[k] != 0.f) dtg = fminf(dtg, rd[k] / fabsf(drhodt[k]) * (float)g.cfl);
+        double dtgd = (double)dtg;
+        const double rest = dt - time_growth;
+        dtgd = dtgd < rest ? dtgd : rest;
+        if (g.dtctl > 0.0) dtgd = g.dtctl < rest ? g.dtctl : rest;
+        const float dtf = (float)dtgd, fl = rho_gas * (float)g.dust_ratio_min;
+        for (int k = 0; k < N; ++k) rd[k] = fmaxf(rd[k] + drhodt[k] * dtf, fl);
+        time_growth = time_growth + dtgd;
+    }
+    for (int k = 0; k < N; ++k) rdd[k] = (double)rd[k];
+    return time_growth >= dt;
+}
+
 // Sub-cycled growth of one cell: rd[N] in/out (dust densities after the drag), rho_gas the
 // conserved gas density, rho_q the floored gas density at the start of the step (q(irho)).
 // The pair velocities depend only on the start of the step, so they are formed once per cell

@@ -364,8 +364,12 @@ __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int
     const double eta_a = ambi ? (double)p.chg_eta[2 * p.plane + c] : 0.0;
     const double hs = p.setup == SHARK_SETUP_DISK_POLAR ? p.hsd[gx] : 1.0;
     const double rho_gas = (double)u[uidx(p, 0, gy, gx)];
-    constexpr bool FAST = sizeof(R) == 4;
-    const bool ok = growth_cell_d<FAST>(p.gw, N, gx, dt, rho_gas, qrho_old, hs, rd, ts, vx, vy, vz, ambi ? gam : nullptr, eta_a);
+    bool ok;
+    if constexpr (sizeof(R) == 4)
+        ok = growth_cell_f(p.gw, N, gx, dt, (float)rho_gas, (float)qrho_old, (float)hs, rd, ts, vx, vy, vz,
+                           ambi ? gam : nullptr, (float)eta_a);
+    else
+        ok = growth_cell_d<false>(p.gw, N, gx, dt, rho_gas, qrho_old, hs, rd, ts, vx, vy, vz, ambi ? gam : nullptr, eta_a);
     for (int k = 0; k < N; ++k) u[uidx(p, 5 + k, gy, gx)] = R(rd[k]);
     return ok ? 0u : (unsigned)SHARK_STATUS_GROWTH;
 }
