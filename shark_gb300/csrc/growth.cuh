@@ -26,6 +26,8 @@ struct GrowthDev {
     int on, kernel, mode, t_per_col;
     const double* pA;        // [N*N] (clustered^2 pi)(s_k + s_j)^2
     const double* pK;        // [N*N] rate factor of the mixed path: pA/m_k/m_j, 1/m_k/m_j, (m_k+m_j)/m_k/m_j
+    const int32_t* pnb;      // [N*N*4] mixed path without fragmentation: bins touched by a pair (-1: none)
+    const float* pnc;        // [N*N*4] their net mass change per collision (FP64-formed, then rounded)
     const double* pS;        // [N*N] m_k unit_m + m_j unit_m
     const double* pD;        // [N*N] m_k m_j unit_m^2
     const int32_t* pic;      // [N*N*2] target bins ic1, ic2 (1-based) without fragmentation
@@ -35,6 +37,8 @@ struct GrowthDev {
     const double* redis;     // [N*N] fragment shares: redis[ifrag * N + k]
     const double* col;       // [rows][4]: T, cs_T (cgs), cs_v (code), t_L (disk; 0 otherwise)
     double massmin, eta, m_mono, Ebr_mono, uv, uv2, ud, ut, mu_gas, dtctl, cfl, sticking, eps_thr, eps_thr_frag;
+    double mref;             // mass unit of the FP32 path (the smallest grain mass): pK is pre-multiplied
+                             // and pnc pre-divided by it, so code-unit masses (1e-45 in AU/Msun) stay in range
     double delta_vambi, alpha_turb, dust_ratio_min;
 };
 
@@ -93,6 +97,8 @@ __device__ __forceinline__ double growth_dv_d(const GrowthDev& g, int N, int k, 
 // Mixed-precision form of the cell update: the same algorithm with the relative velocities,
 // rates, mass bookkeeping and sub-steps in FP32 (the state is FP32 on this path), the elapsed
 // growth time in FP64.  Without fragmentation the target bins and splits come from the tables.
+// Masses are counted in units of the smallest grain mass and rates in grains of that mass, so the
+// bookkeeping stays in FP32 range whatever the code units.
 static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int ix, double dt, float rho_gas, float rho_q,
                                            float hs, double* rdd, const double* tsd, const double* vxd,
                                            const double* vyd, const double* vzd, const double* gamd, float eta_a) {
@@ -146,15 +152,13 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
                     dv = sqrtf(dv * dv + d * d);
                 }
             }
-            const float m1 = (float)g.mk[k], m2 = (float)g.mk[j];
             float ff = 0.f;
             if (frag) {
                 const double Ecol = 0.5 * (g.mk[k] * g.mk[j]) / (g.mk[k] + g.mk[j]) * ((double)dv * dv);
                 const double Ebr = (g.mk[k] + g.mk[j]) / g.m_mono * g.Ebr_mono;
                 ff = (float)fmin(fmax((Ecol - 0.1 * Ebr) / (4.9 * Ebr), 0.0), 1.0);
             }
-            (void)m1; (void)m2;
-            kp[q] = (float)g.pK[k * N + j] * dv * ihs * (k == j ? 0.5f : 1.f);
+            kp[q] = (float)(g.pK[k * N + j] * (double)dv * (double)ihs) * (k == j ? 0.5f : 1.f);
             fp[q] = ff;
         }
     float drhodt[GROWTH_MAX_DUST];
@@ -165,9 +169,9 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
         for (int k = 0; k < N; ++k) drhodt[k] = 0.f;
         niter = niter + 1;
         for (int k = 0, q = 0; k < N; ++k) {
-            const float m1 = (float)g.mk[k];
+            const float m1 = (float)(g.mk[k] / g.mref);
             for (int j = 0; j <= k; ++j, ++q) {
-                const float m2 = (float)g.mk[j];
+                const float m2 = (float)(g.mk[j] / g.mref);
                 float f_frag = fp[q], p_coag = 1.f;
                 const float dndt = kp[q] * rd[k] * rd[j];
                 if (g.kernel == 0) {
@@ -190,6 +194,17 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
                     if (ic1 < ic2) eps_m = fminf((float)((g.mk[ic2 - 1] - mc) / (g.mk[ic2 - 1] - g.mk[ic1 - 1])), 1.f);
                 }
                 const float pc = p_coag * dndt, one_f = 1.f - f_frag;
+                if (!frag) {
+                    // net transfers of the pair, formed in FP64 on the host: in FP32, m_k + m_j
+                    // rounds to m_k for mass ratios below 6e-8 and would drop the small grain
+                    const int32_t* b = g.pnb + (size_t)(k * N + j) * 4;
+                    const float* cf = g.pnc + (size_t)(k * N + j) * 4;
+                    const float w = pc * st;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (b[e] >= 0) drhodt[b[e]] += w * cf[e];
+                    continue;
+                }
                 drhodt[k] -= pc * m1 * (one_f * st + f_frag);
                 drhodt[j] -= pc * m2 * (one_f * st + f_frag);
                 if (f_frag < 1.f) {

@@ -99,7 +99,8 @@ struct shark_gpu_ctx {
     double* grw_d = nullptr;         // dust growth tables (FP64)
     double* ou_d = nullptr;          // forcing: modes [3 nm] | coefficients [2 nm]
     std::vector<double> ou_init;     // initial coefficients (stationary law, seeded)
-    int32_t* grw_i = nullptr;        // dust growth target bins
+    int32_t* grw_i = nullptr;        // dust growth target bins | net-transfer bins
+    float* grw_f = nullptr;          // dust growth net-transfer coefficients (mixed path)
     bool chg_cold = true;            // psi_old is zero everywhere (no charging call since reset)
     // charging network
     float* mlp_blob = nullptr;       // SHARK_MLP_NBLOB FP32
@@ -456,7 +457,7 @@ void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_m
 // ---- dust growth tables (src/dust/dust_growth.f90:3-256, dust_init.f90:11-45) --------------------
 // The operations follow the CPU oracle's growth_grid so the tables are bit-identical to it.
 void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_max, std::vector<double>& hd,
-                         std::vector<int32_t>& hi, shark::GrowthDev& g, size_t off[9]) {
+                         std::vector<int32_t>& hi, std::vector<float>& hf, shark::GrowthDev& g, size_t off[9]) {
     const int N = c.ndust;
     const double ul = unit1(c.unit_l), ud = unit1(c.unit_d), ut = unit1(c.unit_t);
     const double um = ul * ul * ul * ud, uv = ul / ut;
@@ -475,7 +476,8 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     off[7] = off[6] + NN;        // col
     off[8] = off[7] + (size_t)rows * 4;   // pK
     hd.assign(off[8] + NN, 0.0);
-    hi.assign(NN * 2, 1);
+    hi.assign(NN * 2 + NN * 4, -1);
+    hf.assign(NN * 4, 0.0f);
     const double zeta = std::pow(c.grw_smax / c.grw_smin, 1.0 / N);
     const double eta = zeta * zeta * zeta;
     const double massmin = (c.grw_kernel == 0) ? f43 * kPi * rg_cgs * (c.grw_smin * c.grw_smin * c.grw_smin) / um
@@ -505,7 +507,7 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
             const double sk = c.dust_size[k], sj = c.dust_size[j];
             hd[off[0] + q] = (cl * cl) * kPi * ((sk + sj) * (sk + sj));
             const double rate = c.grw_kernel == 1 ? 1.0 : c.grw_kernel == 2 ? (mk[k] + mk[j]) : hd[off[0] + q];
-            hd[off[8] + q] = rate / mk[k] / mk[j];
+            hd[off[8] + q] = rate / mk[k] / mk[j] * mk[0];   // in grains of the smallest mass
             hd[off[1] + q] = mk[k] * um + mk[j] * um;
             hd[off[2] + q] = mk[k] * mk[j] * (um * um);
             const double mc = (1.0 - 0.0) * (mk[k] + mk[j]);
@@ -519,6 +521,41 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
                 e = v < 1.0 ? v : 1.0;
             }
             hd[off[3] + q] = e;
+            // net mass change of each bin per collision (times dndt and the sticking efficiency).
+            // The share of ic2 is formed directly, (M - m_ic1)/(m_ic2 - m_ic1) M, and where ic1 is
+            // bin k itself its net m_j - share is formed without m_k, so nothing cancels.
+            const double M = mk[k] + mk[j];
+            double sh2 = 0.0;
+            if (ic1 < ic2) {
+                const double frac = (M - mk[ic1 - 1]) / (mk[ic2 - 1] - mk[ic1 - 1]);
+                sh2 = (e < 1.0 ? frac : 0.0) * M;
+            }
+            double cf[4] = {0, 0, 0, 0};
+            int32_t bn[4] = {-1, -1, -1, -1};
+            int nb = 0;
+            auto add = [&](int bin, double v) {
+                for (int t = 0; t < nb; ++t)
+                    if (bn[t] == bin) { cf[t] += v; return; }
+                bn[nb] = bin;
+                cf[nb++] = v;
+            };
+            if (ic1 - 1 == k && k != j) {
+                add(k, mk[j] - sh2);          // -m_k + (M - sh2)
+                add(j, -mk[j]);
+                if (sh2 != 0.0) add(ic2 - 1, sh2);
+            } else if (ic1 - 1 == k && k == j) {
+                add(k, -sh2);                 // -2 m_k + (M - sh2), M = 2 m_k
+                if (sh2 != 0.0) add(ic2 - 1, sh2);
+            } else {
+                add(k, -mk[k]);
+                add(j, -mk[j]);
+                add(ic1 - 1, M - sh2);
+                if (sh2 != 0.0) add(ic2 - 1, sh2);
+            }
+            for (int t = 0; t < 4; ++t) {
+                hi[NN * 2 + q * 4 + t] = t < nb ? bn[t] : -1;
+                hf[q * 4 + t] = t < nb ? (float)(cf[t] / mk[0]) : 0.0f;   // in units of the smallest mass
+            }
         }
     for (int r = 0; r < rows; ++r) {
         double T = c.T_cloud;
@@ -539,6 +576,7 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     g.t_per_col = disk ? 1 : 0;
     g.massmin = massmin;
     g.eta = eta;
+    g.mref = mk[0];
     const double a_mu = c.grw_size_mono / 2.0;
     g.Ebr_mono = c.grw_Abr * std::pow(c.grw_gamma_grains, 5.0 / 3.0) * std::pow(a_mu, 4.0 / 3.0) /
                  std::pow(c.grw_estar_grains, 2.0 / 3.0) / (uv * uv * um);
@@ -623,6 +661,7 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->grw_d) cudaFree(c->grw_d);
     if (c->ou_d) cudaFree(c->ou_d);
     if (c->grw_i) cudaFree(c->grw_i);
+    if (c->grw_f) cudaFree(c->grw_f);
     for (void* p : {(void*)c->mlp_blob, (void*)c->mlp_packed, (void*)c->mlp_grad, (void*)c->mlp_adam,
                     (void*)c->mlp_feat, (void*)c->mlp_train, (void*)c->mlp_count, (void*)c->mlp_perm,
                     (void*)c->mlp_scratch, (void*)c->mlp_err})
@@ -960,8 +999,11 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     if (cfg->flags & SHARK_FLAG_GROWTH) {
         std::vector<double> hd;
         std::vector<int32_t> hi;
+        std::vector<float> hf;
         size_t off[9];
-        build_growth_tables(*cfg, col, v.nx_max, hd, hi, v.gw, off);
+        build_growth_tables(*cfg, col, v.nx_max, hd, hi, hf, v.gw, off);
+        INIT_TRY(cudaMalloc(&c->grw_f, hf.size() * sizeof(float)));
+        INIT_TRY(cudaMemcpy(c->grw_f, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
         INIT_TRY(cudaMalloc(&c->grw_d, hd.size() * sizeof(double)));
         INIT_TRY(cudaMemcpy(c->grw_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
         INIT_TRY(cudaMalloc(&c->grw_i, hi.size() * sizeof(int32_t)));
@@ -970,6 +1012,8 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         v.gw.peps = c->grw_d + off[3]; v.gw.mk = c->grw_d + off[4]; v.gw.sk = c->grw_d + off[5];
         v.gw.redis = c->grw_d + off[6]; v.gw.col = c->grw_d + off[7]; v.gw.pic = c->grw_i;
         v.gw.pK = c->grw_d + off[8];
+        v.gw.pnb = c->grw_i + (size_t)cfg->ndust * cfg->ndust * 2;
+        v.gw.pnc = c->grw_f;
     }
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
     std::memset(c->host_ring, 0, 4 * sizeof(double));
