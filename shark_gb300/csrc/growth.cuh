@@ -134,8 +134,14 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
                     const float fS = 3.2f - 1.f - x + 2.f / (1.f + x) * (1.f / 2.6f + x * x * x / (1.6f + x));
                     const float St1 = ts[k] / t_L, St2 = ts[j] / t_L;
                     float vt = a * cs_v * sqrtf(fS * St1);
-                    if (ts[k] < t_eta)
-                        vt = a * cs_v * sqrtf((St1 - St2) / (St1 + St2)) * sqrtf(St1 * St1 / (St1 + rm) - St2 * St2 / (St2 + rm));
+                    if (ts[k] < t_eta) {
+                        // both radicands are >= 0 in exact arithmetic and 0 for k == j; with
+                        // contracted, reciprocal-based division the second can round to -1 ulp,
+                        // whose square root (NaN) would floor every bin it touches
+                        const float r1 = fmaxf((St1 - St2) / (St1 + St2), 0.f);
+                        const float r2 = fmaxf(St1 * St1 / (St1 + rm) - St2 * St2 / (St2 + rm), 0.f);
+                        vt = a * cs_v * sqrtf(r1) * sqrtf(r2);
+                    }
                     if (ts[k] > t_L) vt = a * cs_v * sqrtf(1.f / (1.f + St1) + 1.f / (1.f + St2));
                     dv = vt;
                 }

@@ -82,3 +82,19 @@ def test_growth_mixed_polar_disk_code_units():
     mg = active(cfg, ug)[5:5 + N].sum()
     mo = active(cfg, uo)[5:5 + N].sum()
     assert abs(mg / mo - 1.0) <= 1e-5
+
+
+def test_growth_mixed_mrn_32_species_turbulent_pairs():
+    """32 species over five decades of size: the smallest pairs sit in the inertial-range branch of
+    the turbulent velocity, where equal stopping times give a radicand of exactly zero; the FP32
+    path must keep it at zero (a NaN rate would floor the small bins and drop their mass)."""
+    cfg, u0 = setups.dusty_turb(n=16, ndust=32, growth=True, precision=K.PREC_MIXED)
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 1)
+    assert st == 0
+    N = cfg.ndust
+    ga, oa = active(cfg, ug), active(cfg, uo)
+    assert np.isfinite(ga).all()
+    assert (ga[5:5 + N] / ga[0]).min() > 1e3 * cfg.dust_ratio_min
+    err = rel_l1(cfg, ug, uo)
+    assert err.max() <= GROWTH_MIXED_TOL, err
+    assert abs(ga[5:5 + N].sum() / oa[5:5 + N].sum() - 1.0) <= 1e-5
