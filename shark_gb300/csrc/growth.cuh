@@ -7,9 +7,10 @@
 // (q velocities, stopping times) exactly as the CPU oracle (oracle/shark_oracle.cpp, growth_*)
 // forms it; per-pair constants that involve no state -- the collision cross-section factor, the
 // Brownian mass factor, and without fragmentation the target bins and their mass split -- are
-// tabulated on the host with the oracle's operations.  Arithmetic: FP64 in both precisions (the
-// densities are read from and written to the state in its precision).  A cell needing more than
-// 100000 sub-steps stops there and raises SHARK_STATUS_GROWTH.
+// tabulated on the host with the oracle's operations.  The FP64 path follows the oracle's
+// operations; the mixed path integrates in FP32 (growth_dv_f, growth_cell_f and the warp-per-cell
+// form in the mixed K2).  A cell needing more than 100000 sub-steps stops there and raises
+// SHARK_STATUS_GROWTH.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -19,15 +20,23 @@
 
 namespace shark {
 
-// largest species count of the growth kernel: the per-cell pair table lives in local memory
+// largest species count of the growth kernels: one bin per lane of a warp in the mixed path, and
+// per-cell pair tables in local memory in the FP64 path
 constexpr int GROWTH_MAX_DUST = 32;
+constexpr int GROWTH_MAX_PAIRS = GROWTH_MAX_DUST * (GROWTH_MAX_DUST + 1) / 2;
 
 struct GrowthDev {
     int on, kernel, mode, t_per_col;
     const double* pA;        // [N*N] (clustered^2 pi)(s_k + s_j)^2
     const double* pK;        // [N*N] rate factor of the mixed path: pA/m_k/m_j, 1/m_k/m_j, (m_k+m_j)/m_k/m_j
-    const int32_t* pnb;      // [N*N*4] mixed path without fragmentation: bins touched by a pair (-1: none)
-    const float* pnc;        // [N*N*4] their net mass change per collision (FP64-formed, then rounded)
+    // FP32 path.  Pairs are numbered q = k (k + 1) / 2 + j, j <= k.
+    const int32_t* pair;     // [npair] k << 8 | j
+    const float* pKf;        // [npair] pK in FP32
+    const float* pBf;        // [npair] (8 kB / pi) (m_k + m_j) / (m_k m_j) / uv^2, masses in g: Brownian dv^2 / T
+    const int32_t* gq;       // [gL * 32] without fragmentation, entry t of bin b at t * 32 + b: a pair
+    const float* gc;         //           and the net mass it moves into bin b per collision, in units of
+                             //           mref (formed in FP64; 0 pads the short rows)
+    int npair, gL;
     const double* pS;        // [N*N] m_k unit_m + m_j unit_m
     const double* pD;        // [N*N] m_k m_j unit_m^2
     const int32_t* pic;      // [N*N*2] target bins ic1, ic2 (1-based) without fragmentation
@@ -37,8 +46,8 @@ struct GrowthDev {
     const double* redis;     // [N*N] fragment shares: redis[ifrag * N + k]
     const double* col;       // [rows][4]: T, cs_T (cgs), cs_v (code), t_L (disk; 0 otherwise)
     double massmin, eta, m_mono, Ebr_mono, uv, uv2, ud, ut, mu_gas, dtctl, cfl, sticking, eps_thr, eps_thr_frag;
-    double mref;             // mass unit of the FP32 path (the smallest grain mass): pK is pre-multiplied
-                             // and pnc pre-divided by it, so code-unit masses (1e-45 in AU/Msun) stay in range
+    double mref;             // mass unit of the FP32 path (the smallest grain mass): pK/pKf are pre-multiplied
+                             // and gc pre-divided by it, so code-unit masses (1e-45 in AU/Msun) stay in range
     double delta_vambi, alpha_turb, dust_ratio_min;
 };
 
@@ -94,26 +103,71 @@ __device__ __forceinline__ double growth_dv_d(const GrowthDev& g, int N, int k, 
     return dv;
 }
 
-// Mixed-precision form of the cell update: the same algorithm with the relative velocities,
-// rates, mass bookkeeping and sub-steps in FP32 (the state is FP32 on this path), the elapsed
-// growth time in FP64.  Without fragmentation the target bins and splits come from the tables.
-// Masses are counted in units of the smallest grain mass and rates in grains of that mass, so the
-// bookkeeping stays in FP32 range whatever the code units.
-static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int ix, double dt, float rho_gas, float rho_q,
-                                           float hs, double* rdd, const double* tsd, const double* vxd,
-                                           const double* vyd, const double* vzd, const double* gamd, float eta_a) {
+// FP32 cell constants of the pair relative velocity (dust_growth.f90:60-87).
+struct GrowthCellF {
+    float T, cs_v, t_L, t_eta, rm, vambi;
+};
+
+__device__ __forceinline__ GrowthCellF growth_cell_consts_f(const GrowthDev& g, int ix, float rho_q, float hs, float eta_a) {
     const int row = g.t_per_col ? ix : 0;
     const double* cc = g.col + (size_t)row * 4;
-    const float T = (float)cc[0], cs_T = (float)cc[1], cs_v = (float)cc[2];
+    GrowthCellF c;
+    c.T = (float)cc[0];
+    const float cs_T = (float)cc[1];
+    c.cs_v = (float)cc[2];
     const float pi = (float)grw::pi;
     const float rho_cgs = rho_q / hs * (float)g.ud;
     const float tff = sqrtf(3.f * pi / (32.f * (float)grw::grav * rho_cgs));
     const float lambJ = tff * cs_T;
-    const float vambi = (float)g.delta_vambi * (float)(grw::clight * grw::clight) * eta_a / lambJ / (4.f * pi);
-    const float Re = 6.2e7f * sqrtf(rho_cgs / ((float)g.mu_gas * (float)grw::mH) / 1e5f) * sqrtf(T / 10.f);
-    const float t_L = g.t_per_col ? (float)cc[3] : tff / (float)g.ut;
-    const float t_eta = t_L / sqrtf(Re);
-    const float rm = rsqrtf(Re);
+    c.vambi = (float)g.delta_vambi * (float)(grw::clight * grw::clight) * eta_a / lambJ / (4.f * pi);
+    const float Re = 6.2e7f * sqrtf(rho_cgs / ((float)g.mu_gas * (float)grw::mH) / 1e5f) * sqrtf(c.T / 10.f);
+    c.t_L = g.t_per_col ? (float)cc[3] : tff / (float)g.ut;
+    c.t_eta = c.t_L / sqrtf(Re);
+    c.rm = rsqrtf(Re);
+    return c;
+}
+
+// FP32 relative velocity of a pair k >= j (dust_growth.f90:88-114): stopping times tk, tj, the
+// Brownian term X = T pBf, the drift (dx, dy, dz) = v_k - v_j and dg = |G_k| - |G_j| of the
+// ambipolar term, G = gamma / sqrt(1 + gamma^2).
+__device__ __forceinline__ float growth_dv_f(const GrowthDev& g, const GrowthCellF& c, float tk, float tj, float X,
+                                             float dx, float dy, float dz, float dg, bool ambi) {
+    float dv = 0.f;
+    if (g.mode & SHARK_GROWTH_TURB) {
+        const float a = (float)g.alpha_turb;
+        const float x = tj / tk;
+        const float fS = 3.2f - 1.f - x + 2.f / (1.f + x) * (1.f / 2.6f + x * x * x / (1.6f + x));
+        const float St1 = tk / c.t_L, St2 = tj / c.t_L;
+        float vt = a * c.cs_v * sqrtf(fS * St1);
+        if (tk < c.t_eta) {
+            // both radicands are >= 0 in exact arithmetic and 0 for k == j; with contracted,
+            // reciprocal-based division the second can round to -1 ulp, whose square root (NaN)
+            // would floor every bin the pair touches
+            const float r1 = fmaxf((St1 - St2) / (St1 + St2), 0.f);
+            const float r2 = fmaxf(St1 * St1 / (St1 + c.rm) - St2 * St2 / (St2 + c.rm), 0.f);
+            vt = a * c.cs_v * sqrtf(r1) * sqrtf(r2);
+        }
+        if (tk > c.t_L) vt = a * c.cs_v * sqrtf(1.f / (1.f + St1) + 1.f / (1.f + St2));
+        dv = vt;
+    }
+    if (g.mode & SHARK_GROWTH_BROWNIAN) dv = sqrtf(dv * dv + X);
+    if (g.mode & SHARK_GROWTH_DRIFT) dv = sqrtf(dv * dv + dx * dx + dy * dy + dz * dz);
+    if ((g.mode & SHARK_GROWTH_AMBIPOLAR) && ambi) {
+        const float d = c.vambi / (float)g.uv * dg;
+        dv = sqrtf(dv * dv + d * d);
+    }
+    return dv;
+}
+
+// Mixed-precision form of the cell update with fragmentation, one thread per cell (without
+// fragmentation the warp-per-cell form in the mixed K2 runs instead): the same algorithm with the
+// relative velocities, rates, mass bookkeeping and sub-steps in FP32 (the state is FP32 on this
+// path), the elapsed growth time in FP64.  Masses are counted in units of the smallest grain mass
+// and rates in grains of that mass, so the bookkeeping stays in FP32 range whatever the code units.
+static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int ix, double dt, float rho_gas, float rho_q,
+                                           float hs, double* rdd, const double* tsd, const double* vxd,
+                                           const double* vyd, const double* vzd, const double* gamd, float eta_a) {
+    const GrowthCellF cc = growth_cell_consts_f(g, ix, rho_q, hs, eta_a);
     const bool frag = (g.mode & SHARK_GROWTH_FRAGMENTATION) != 0;
     float rd[GROWTH_MAX_DUST], ts[GROWTH_MAX_DUST], gm[GROWTH_MAX_DUST];
     for (int k = 0; k < N; ++k) {
@@ -123,48 +177,20 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
     }
     // pair rate constants pK dv / hs (and the fragmented fraction), once per cell
     float kp[GROWTH_MAX_DUST * (GROWTH_MAX_DUST + 1) / 2], fp[GROWTH_MAX_DUST * (GROWTH_MAX_DUST + 1) / 2];
-    const float ihs = 1.f / hs, a = (float)g.alpha_turb;
+    const float ihs = 1.f / hs;
     for (int k = 0, q = 0; k < N; ++k)
         for (int j = 0; j <= k; ++j, ++q) {
             float dv = 1.f;
-            if (g.kernel == 0) {
-                dv = 0.f;
-                if (g.mode & SHARK_GROWTH_TURB) {
-                    const float x = ts[j] / ts[k];
-                    const float fS = 3.2f - 1.f - x + 2.f / (1.f + x) * (1.f / 2.6f + x * x * x / (1.6f + x));
-                    const float St1 = ts[k] / t_L, St2 = ts[j] / t_L;
-                    float vt = a * cs_v * sqrtf(fS * St1);
-                    if (ts[k] < t_eta) {
-                        // both radicands are >= 0 in exact arithmetic and 0 for k == j; with
-                        // contracted, reciprocal-based division the second can round to -1 ulp,
-                        // whose square root (NaN) would floor every bin it touches
-                        const float r1 = fmaxf((St1 - St2) / (St1 + St2), 0.f);
-                        const float r2 = fmaxf(St1 * St1 / (St1 + rm) - St2 * St2 / (St2 + rm), 0.f);
-                        vt = a * cs_v * sqrtf(r1) * sqrtf(r2);
-                    }
-                    if (ts[k] > t_L) vt = a * cs_v * sqrtf(1.f / (1.f + St1) + 1.f / (1.f + St2));
-                    dv = vt;
-                }
-                if (g.mode & SHARK_GROWTH_BROWNIAN) {
-                    const float X = (float)((8.0 * grw::kB * (double)T / grw::pi) * g.pS[k * N + j] / g.pD[k * N + j] / g.uv2);
-                    dv = sqrtf(dv * dv + X);
-                }
-                if (g.mode & SHARK_GROWTH_DRIFT) {
-                    const float dx = (float)(vxd[k] - vxd[j]), dy = (float)(vyd[k] - vyd[j]), dz = (float)(vzd[k] - vzd[j]);
-                    dv = sqrtf(dv * dv + dx * dx + dy * dy + dz * dz);
-                }
-                if ((g.mode & SHARK_GROWTH_AMBIPOLAR) && gamd) {
-                    const float d = vambi / (float)g.uv * (gm[k] - gm[j]);
-                    dv = sqrtf(dv * dv + d * d);
-                }
-            }
+            if (g.kernel == 0)
+                dv = growth_dv_f(g, cc, ts[k], ts[j], cc.T * g.pBf[q], (float)(vxd[k] - vxd[j]), (float)(vyd[k] - vyd[j]),
+                                 (float)(vzd[k] - vzd[j]), gm[k] - gm[j], gamd != nullptr);
             float ff = 0.f;
             if (frag) {
                 const double Ecol = 0.5 * (g.mk[k] * g.mk[j]) / (g.mk[k] + g.mk[j]) * ((double)dv * dv);
                 const double Ebr = (g.mk[k] + g.mk[j]) / g.m_mono * g.Ebr_mono;
                 ff = (float)fmin(fmax((Ecol - 0.1 * Ebr) / (4.9 * Ebr), 0.0), 1.0);
             }
-            kp[q] = (float)(g.pK[k * N + j] * (double)dv * (double)ihs) * (k == j ? 0.5f : 1.f);
+            kp[q] = g.pKf[q] * dv * ihs * (k == j ? 0.5f : 1.f);
             fp[q] = ff;
         }
     float drhodt[GROWTH_MAX_DUST];
@@ -200,17 +226,6 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
                     if (ic1 < ic2) eps_m = fminf((float)((g.mk[ic2 - 1] - mc) / (g.mk[ic2 - 1] - g.mk[ic1 - 1])), 1.f);
                 }
                 const float pc = p_coag * dndt, one_f = 1.f - f_frag;
-                if (!frag) {
-                    // net transfers of the pair, formed in FP64 on the host: in FP32, m_k + m_j
-                    // rounds to m_k for mass ratios below 6e-8 and would drop the small grain
-                    const int32_t* b = g.pnb + (size_t)(k * N + j) * 4;
-                    const float* cf = g.pnc + (size_t)(k * N + j) * 4;
-                    const float w = pc * st;
-#pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        if (b[e] >= 0) drhodt[b[e]] += w * cf[e];
-                    continue;
-                }
                 drhodt[k] -= pc * m1 * (one_f * st + f_frag);
                 drhodt[j] -= pc * m2 * (one_f * st + f_frag);
                 if (f_frag < 1.f) {
@@ -244,10 +259,7 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
 // Sub-cycled growth of one cell: rd[N] in/out (dust densities after the drag), rho_gas the
 // conserved gas density, rho_q the floored gas density at the start of the step (q(irho)).
 // The pair velocities depend only on the start of the step, so they are formed once per cell
-// (the values the oracle re-forms every sub-step).  FAST (mixed path): the pair rate is
-// pK dv rho_k rho_j / hs with a host-tabulated pK instead of the oracle's two divisions.
-// Returns false if the sub-step cap was reached.
-template <bool FAST>
+// (the values the oracle re-forms every sub-step).  Returns false if the sub-step cap was reached.
 static __device__ bool growth_cell_d(const GrowthDev& g, int N, int ix, double dt, double rho_gas, double rho_q, double hs,
                               double* rd, const double* ts, const double* vx, const double* vy, const double* vz,
                               const double* gam, double eta_a) {
@@ -267,7 +279,6 @@ static __device__ bool growth_cell_d(const GrowthDev& g, int N, int ix, double d
     for (int k = 0, q = 0; k < N; ++k)
         for (int j = 0; j <= k; ++j, ++q)
             dvp[q] = g.kernel == 0 ? growth_dv_d(g, N, k, j, T, cs_v, t_L, t_eta, rm, vambi, ts, vx, vy, vz, gam) : 0.0;
-    const double ihs = 1.0 / hs;
     double drhodt[GROWTH_MAX_DUST];
     double time_growth = 0.0;
     int niter = 0;
@@ -288,16 +299,11 @@ static __device__ bool growth_cell_d(const GrowthDev& g, int N, int ix, double d
                     f_frag = lo > 0.0 ? lo : 0.0;
                 }
                 double dndt;
-                if constexpr (FAST) {
-                    dndt = g.pK[k * N + j] * (g.kernel == 0 ? dv : 1.0) * rd[k] * rd[j] * ihs;
-                    if (k == j) dndt = dndt * 0.5;
-                } else {
-                    if (g.kernel == 1) dndt = rd[k] * rd[j] / m1 / m2;
-                    else if (g.kernel == 2) dndt = (m1 + m2) * rd[k] * rd[j] / m1 / m2;
-                    else dndt = g.pA[k * N + j] * dv * rd[k] * rd[j] / m1 / m2;
-                    dndt = dndt / hs;
-                    if (k == j) dndt = dndt / 2.0;
-                }
+                if (g.kernel == 1) dndt = rd[k] * rd[j] / m1 / m2;
+                else if (g.kernel == 2) dndt = (m1 + m2) * rd[k] * rd[j] / m1 / m2;
+                else dndt = g.pA[k * N + j] * dv * rd[k] * rd[j] / m1 / m2;
+                dndt = dndt / hs;
+                if (k == j) dndt = dndt / 2.0;
                 if (g.kernel == 0) {
                     if (g.eps_thr > 0.0 && (rd[k] < g.eps_thr * rho_gas)) p_coag = 0.0;
                     if (g.eps_thr > 0.0 && (rd[j] < g.eps_thr * rho_gas)) p_coag = 0.0;

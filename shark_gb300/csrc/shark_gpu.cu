@@ -476,8 +476,11 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     off[7] = off[6] + NN;        // col
     off[8] = off[7] + (size_t)rows * 4;   // pK
     hd.assign(off[8] + NN, 0.0);
-    hi.assign(NN * 2 + NN * 4, -1);
-    hf.assign(NN * 4, 0.0f);
+    hi.assign(NN * 2, 1);
+    const int P = N * (N + 1) / 2;
+    std::vector<int32_t> pair(P);
+    std::vector<float> pKf(P), pBf(P);
+    std::vector<std::vector<std::pair<int32_t, float>>> gat(N);   // gather rows of the net transfers
     const double zeta = std::pow(c.grw_smax / c.grw_smin, 1.0 / N);
     const double eta = zeta * zeta * zeta;
     const double massmin = (c.grw_kernel == 0) ? f43 * kPi * rg_cgs * (c.grw_smin * c.grw_smin * c.grw_smin) / um
@@ -552,10 +555,11 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
                 add(ic1 - 1, M - sh2);
                 if (sh2 != 0.0) add(ic2 - 1, sh2);
             }
-            for (int t = 0; t < 4; ++t) {
-                hi[NN * 2 + q * 4 + t] = t < nb ? bn[t] : -1;
-                hf[q * 4 + t] = t < nb ? (float)(cf[t] / mk[0]) : 0.0f;   // in units of the smallest mass
-            }
+            const int pq = k * (k + 1) / 2 + j;
+            pair[pq] = (k << 8) | j;
+            pKf[pq] = (float)hd[off[8] + q];
+            pBf[pq] = (float)((8.0 * kKB / kPi) * hd[off[1] + q] / hd[off[2] + q] / (uv * uv));
+            for (int t = 0; t < nb; ++t) gat[bn[t]].emplace_back(pq, (float)(cf[t] / mk[0]));   // in units of m_0
         }
     for (int r = 0; r < rows; ++r) {
         double T = c.T_cloud;
@@ -577,6 +581,23 @@ void build_growth_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     g.massmin = massmin;
     g.eta = eta;
     g.mref = mk[0];
+    // FP32 tables: [pair | gq] in hi after the target bins, [pKf | pBf | gc] in hf; the gather
+    // table is transposed (entry t of bin b at t * 32 + b) so a warp reads it in one line per t
+    size_t L = 1;
+    for (const auto& r : gat) L = std::max(L, r.size());
+    hi.insert(hi.end(), pair.begin(), pair.end());
+    const size_t gq0 = hi.size();
+    hi.resize(gq0 + L * 32, 0);
+    hf.assign((size_t)2 * P + L * 32, 0.0f);
+    std::copy(pKf.begin(), pKf.end(), hf.begin());
+    std::copy(pBf.begin(), pBf.end(), hf.begin() + P);
+    for (int b = 0; b < N; ++b)
+        for (size_t t = 0; t < gat[b].size(); ++t) {
+            hi[gq0 + t * 32 + b] = gat[b][t].first;
+            hf[(size_t)2 * P + t * 32 + b] = gat[b][t].second;
+        }
+    g.npair = P;
+    g.gL = (int)L;
     const double a_mu = c.grw_size_mono / 2.0;
     g.Ebr_mono = c.grw_Abr * std::pow(c.grw_gamma_grains, 5.0 / 3.0) * std::pow(a_mu, 4.0 / 3.0) /
                  std::pow(c.grw_estar_grains, 2.0 / 3.0) / (uv * uv * um);
@@ -1012,8 +1033,14 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         v.gw.peps = c->grw_d + off[3]; v.gw.mk = c->grw_d + off[4]; v.gw.sk = c->grw_d + off[5];
         v.gw.redis = c->grw_d + off[6]; v.gw.col = c->grw_d + off[7]; v.gw.pic = c->grw_i;
         v.gw.pK = c->grw_d + off[8];
-        v.gw.pnb = c->grw_i + (size_t)cfg->ndust * cfg->ndust * 2;
-        v.gw.pnc = c->grw_f;
+        {
+            const size_t NN = (size_t)cfg->ndust * cfg->ndust, P = (size_t)v.gw.npair;
+            v.gw.pair = c->grw_i + NN * 2;
+            v.gw.gq = c->grw_i + NN * 2 + P;
+            v.gw.pKf = c->grw_f;
+            v.gw.pBf = c->grw_f + P;
+            v.gw.gc = c->grw_f + 2 * P;
+        }
     }
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
     std::memset(c->host_ring, 0, 4 * sizeof(double));

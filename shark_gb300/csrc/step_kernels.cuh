@@ -369,9 +369,112 @@ __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int
         ok = growth_cell_f(p.gw, N, gx, dt, (float)rho_gas, (float)qrho_old, (float)hs, rd, ts, vx, vy, vz,
                            ambi ? gam : nullptr, (float)eta_a);
     else
-        ok = growth_cell_d<false>(p.gw, N, gx, dt, rho_gas, qrho_old, hs, rd, ts, vx, vy, vz, ambi ? gam : nullptr, eta_a);
+        ok = growth_cell_d(p.gw, N, gx, dt, rho_gas, qrho_old, hs, rd, ts, vx, vy, vz, ambi ? gam : nullptr, eta_a);
     for (int k = 0; k < N; ++k) u[uidx(p, 5 + k, gy, gx)] = R(rd[k]);
     return ok ? 0u : (unsigned)SHARK_STATUS_GROWTH;
+}
+
+// Dust growth of the mixed path without fragmentation (dust_growth.f90:3-256), one warp per cell
+// for the 256 cells of a K2 block (warp w takes cells 32 w .. 32 w + 31 in turn).  Lane b holds
+// bin b's density.  Once per cell the lanes form the pair rates pK dv / hs of pairs
+// q = lane, lane + 32, ... from the start-of-step stopping times and velocities (exchanged by
+// shuffles).  Every sub-step each lane writes the collision rate w_q = rate_q rho_k rho_j (times
+// the sticking efficiency) of its pairs to shared memory, and lane b gathers
+// drho_b/dt = sum_t gc[t][b] w[gq[t][b]] from the host-built table of net transfers; the sub-step
+// is the warp minimum of CFL_growth rho_b/|drho_b/dt|.  The lanes of a warp take the same
+// sub-steps, so a warp costs the sub-steps of its own cell rather than those of the slowest of 32
+// cells, and nothing leaves registers and shared memory.  Called by every thread of the block.
+constexpr int GROWTH_PAIR_SLOTS = (GROWTH_MAX_PAIRS + 31) / 32;
+
+static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p, int gx_block, int gy, double dt) {
+    __shared__ float sw[8][GROWTH_MAX_PAIRS];
+    const GrowthDev& g = p.gw;
+    const int N = p.ndust, P = g.npair;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float* w = sw[wid];
+    float* u = p.u_next;
+    const unsigned FULL = 0xffffffffu;
+    const bool ambi = (g.mode & SHARK_GROWTH_AMBIPOLAR) && p.chg_gamma_d;
+    const bool on = lane < N;
+    const int b = on ? lane : 0;
+    const bool thr_on = g.kernel == 0 && g.eps_thr > 0.0;
+    unsigned st = 0;
+    for (int c = 0; c < 32; ++c) {
+        const int gx = gx_block + wid * 32 + c;
+        if (gx >= p.ng + p.nx) break;
+        const double rho_old = (double)p.u_cur[uidx(p, 0, gy, gx)];
+        const double qrho_old = rho_old > p.smallr ? rho_old : p.smallr;
+        float rd = u[uidx(p, 5 + b, gy, gx)];
+        const float ts = (float)tstop_cell(p, b, qrho_old, gx, gy);
+        const float r0 = p.u_cur[uidx(p, 5 + b, gy, gx)];
+        const float vx = p.u_cur[uidx(p, 5 + N + b, gy, gx)] / r0;
+        const float vy = p.u_cur[uidx(p, 5 + 2 * N + b, gy, gx)] / r0;
+        const float vz = p.u_cur[uidx(p, 5 + 3 * N + b, gy, gx)] / r0;
+        const long long cidx = (long long)gy * p.pitch + gx;
+        float gm = 0.f, eta_a = 0.f;
+        if (ambi) {
+            const float ga = p.chg_gamma_d[(long long)b * p.plane + cidx];
+            gm = fabsf(ga) * rsqrtf(1.f + ga * ga);
+            eta_a = p.chg_eta[2 * p.plane + cidx];
+        }
+        const float hs = p.setup == SHARK_SETUP_DISK_POLAR ? (float)p.hsd[gx] : 1.f;
+        const float rho_gas = u[uidx(p, 0, gy, gx)];
+        const GrowthCellF cc = growth_cell_consts_f(g, gx, (float)qrho_old, hs, eta_a);
+        const float ihs = 1.f / hs;
+        float kp[GROWTH_PAIR_SLOTS];
+        int kj[GROWTH_PAIR_SLOTS];
+#pragma unroll
+        for (int i = 0; i < GROWTH_PAIR_SLOTS; ++i) {
+            kp[i] = 0.f;
+            kj[i] = 0;
+            if (32 * i >= P) continue;                      // uniform over the warp
+            const int q = lane + 32 * i;
+            const bool has = q < P;
+            const int pr = has ? __ldg(g.pair + q) : 0;
+            const int k = pr >> 8, j = pr & 255;
+            kj[i] = pr;
+            const float tk = __shfl_sync(FULL, ts, k), tj = __shfl_sync(FULL, ts, j);
+            const float dx = __shfl_sync(FULL, vx, k) - __shfl_sync(FULL, vx, j);
+            const float dy = __shfl_sync(FULL, vy, k) - __shfl_sync(FULL, vy, j);
+            const float dz = __shfl_sync(FULL, vz, k) - __shfl_sync(FULL, vz, j);
+            const float dg = __shfl_sync(FULL, gm, k) - __shfl_sync(FULL, gm, j);
+            if (!has) continue;
+            float dv = 1.f;
+            if (g.kernel == 0) dv = growth_dv_f(g, cc, tk, tj, cc.T * __ldg(g.pBf + q), dx, dy, dz, dg, ambi);
+            kp[i] = __ldg(g.pKf + q) * dv * ihs * (k == j ? 0.5f : 1.f);
+        }
+        const float stick = (float)g.sticking, cflg = (float)g.cfl;
+        const float thr = (float)g.eps_thr * rho_gas, fl = rho_gas * (float)g.dust_ratio_min;
+        double time_growth = 0.0;
+        int niter = 0;
+        while (time_growth < dt && niter < grw::MAX_SUB) {
+            niter = niter + 1;
+#pragma unroll
+            for (int i = 0; i < GROWTH_PAIR_SLOTS; ++i) {
+                if (32 * i >= P) continue;
+                const int q = lane + 32 * i;
+                const float rk = __shfl_sync(FULL, rd, kj[i] >> 8), rj = __shfl_sync(FULL, rd, kj[i] & 255);
+                float pc = kp[i] * rk * rj;
+                if (thr_on && (rk < thr || rj < thr)) pc = 0.f;
+                if (q < P) w[q] = pc * stick;
+            }
+            __syncwarp();
+            float d = 0.f;
+            for (int t = 0; t < g.gL; ++t) d += __ldg(g.gc + t * 32 + lane) * w[__ldg(g.gq + t * 32 + lane)];
+            __syncwarp();
+            float cand = (on && d != 0.f) ? rd / fabsf(d) * cflg : 1e30f;
+            for (int o = 16; o > 0; o >>= 1) cand = fminf(cand, __shfl_xor_sync(FULL, cand, o));
+            double dtg = (double)cand;
+            const double rest = dt - time_growth;
+            dtg = dtg < rest ? dtg : rest;
+            if (g.dtctl > 0.0) dtg = g.dtctl < rest ? g.dtctl : rest;
+            rd = fmaxf(rd + d * (float)dtg, fl);
+            time_growth = time_growth + dtg;
+        }
+        if (on) u[uidx(p, 5 + b, gy, gx)] = rd;
+        if (!(time_growth >= dt)) st |= (unsigned)SHARK_STATUS_GROWTH;
+    }
+    return st;
 }
 
 // Driven-turbulence kick of the dustyTurb box (turb.f90:227-324 in 2D): the gas momentum gains
@@ -599,10 +702,12 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
     const int gy = (p.ndim == 2) ? blockIdx.y + p.ng : 0;
     float dtc = 2e38f;
     unsigned int st = 0;
-    if (gx < p.ng + p.nx) {
-        float* u = p.u_next;
-        float rho = u[uidx(p, 0, gy, gx)];
-        float px = u[uidx(p, 1, gy, gx)], py = u[uidx(p, 2, gy, gx)], pz = u[uidx(p, 3, gy, gx)];
+    const bool act = gx < p.ng + p.nx;
+    float* u = p.u_next;
+    float rho = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+    if (act) {
+        rho = u[uidx(p, 0, gy, gx)];
+        px = u[uidx(p, 1, gy, gx)]; py = u[uidx(p, 2, gy, gx)]; pz = u[uidx(p, 3, gy, gx)];
         if (drag) {
             float rk[NMAX], wk[NMAX];
             float rhon = rho, pnx = px, pny = py, pnz = pz;
@@ -649,7 +754,17 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
             const long long ie = uidx(p, 4, gy, gx);
             u[ie] = (float)((double)u[ie] + drag_heating(p, gx, gy, dt));
         }
-        if (GROW && MODE == 0) st |= grow_in_finalize(p, u, gx, gy, dt);   // dust_growth (solve.f90:113)
+    }
+    if constexpr (GROW && MODE == 0) {   // dust_growth (solve.f90:113)
+        if (p.gw.mode & SHARK_GROWTH_FRAGMENTATION) {
+            if (act) st |= grow_in_finalize(p, u, gx, gy, dt);
+        } else {
+            __syncthreads();             // the block's cells after the drag
+            st |= grow_block_warps(p, blockIdx.x * blockDim.x + p.ng, gy, dt);
+            __syncthreads();
+        }
+    }
+    if (act) {
         if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)
             turb_kick_cell<float>(p, u, gx, gy, dt);
             px = u[uidx(p, 1, gy, gx)];
