@@ -39,6 +39,10 @@ struct ChargeParams {
     const double* l2;            // [N] grain radius^2 (cm^2)
     const double* mkum;          // [N] grain mass (g)
     const double* ak;            // [N] sqrt(pi gamma/8) rhograin_cgs l_k (stopping-time numerator)
+    const double* rtau;          // [rows][N] 1/tau_k        (mixed path)
+    const double* nfac;          // [N] unit_d / m_k (g)     (mixed path: n_k = rho_k / hs * nfac_k)
+    const double* rmk;           // [N] 1/m_k (g)            (mixed path)
+    const double* pl2;           // [N] pi l_k^2             (mixed path)
     double unH, ud, ul, x0, sig_att;
     double thetai, th2, th3, psi0, eps, B0, mu_ions;
     int nitermax;
@@ -126,6 +130,128 @@ __device__ __forceinline__ void charge_newton(const ChargeParams<R>& p, const do
     }
 }
 
+// 1/x for the mixed path: the FP32 reciprocal refined by one FP64 Newton step, relative error
+// ~1e-14, for x within FP32 range.
+__device__ __forceinline__ double rcp_refined(double x) {
+    const double r = (double)(1.0f / (float)x);
+    return r * (2.0 - x * r);
+}
+
+// FP64 phase of the mixed path: the iteration of charge_newton with the residual f in FP64 and
+// the divisions of its species loop replaced by tabulated reciprocals and a refined reciprocal of
+// the denominator 1 + et a_k + et^2.  The derivative's species factors are FP32 (Newton needs
+// f' to a few digits only), accumulated against n_k in FP64 so no FP32 product leaves range.
+// The stopping test |f| < chg_eps is the reference's.  `uk` points at species 0 of the cell.
+template <typename R>
+__device__ __forceinline__ void charge_newton_mix(const ChargeParams<R>& p, const double* tau, const double* alp,
+                                                  const double* rtau, const R* uk, double ihs, double nH, double x,
+                                                  double sigmav_ie, double vi, double& psi, int& niter, int& lowT,
+                                                  double& conv) {
+    const int N = p.ndust;
+    const double thetai = p.thetai, psi0 = p.psi0;
+    const float thf = (float)p.thetai, th2f = (float)p.th2, th3f = (float)p.th3;
+    const double rxnH = 1.0 / (x * nH);
+    while (conv > p.eps && niter < p.nitermax) {
+        const double eps_psi = (1.0 - psi) / thetai * exp(-psi);
+        const double et = eps_psi * thetai;
+        const double et2 = et * et, et21 = et2 + et, om = 1.0 - eps_psi, rom = 1.0 / om;
+        const double D = (-eps_psi * (2.0 - psi) / (1.0 - psi));
+        const float ef = (float)eps_psi, et2f = (float)et2;
+        const float c2a = -(et2f * et2f), c2b = ef * ef;
+        double n_i = 0.0, S1 = 0.0, S2 = 0.0, S3 = 0.0, S4 = 0.0, S5 = 0.0, S6 = 0.0;
+        for (int k = 0; k < N; ++k) {
+            const double n = (double)uk[(long long)k * p.plane] * ihs * p.nfac[k];
+            const double tk = tau[k], ak = alp[k], rtk = rtau[k];
+            const double den = 1.0 + et * ak + et2;
+            const double r = rcp_refined(den);
+            n_i = n_i - (psi * tk + (1.0 - et2) * r) * n * rom;
+            const double npl = n * p.pl2[k];
+            S1 = S1 + npl * ((1.0 - psi) + (2.0 * rtk) * et21 * r);
+            const float akf = (float)ak, rf = (float)r, rtkf = (float)rtk, pl2f = (float)p.pl2[k];
+            const float f2 = (c2a + (4.f * th2f - th3f * akf) * c2b + (2.f * thf * akf - 4.f * th2f) * ef + 1.f - thf * akf) * (rf * rf);
+            const float f4 = pl2f * rtkf * rf;
+            const float f5 = pl2f * (2.f * ef * th2f + thf * akf) * rtkf * (rf * rf);
+            S2 = S2 + n * (double)f2;
+            S3 = S3 + n * tk;
+            S4 = S4 + n * (double)f4;
+            S5 = S5 + n * (double)f5;
+            S6 = S6 + npl;
+        }
+        const double fpsi = sigmav_ie * eps_psi * (n_i * n_i) * rxnH + n_i * vi * rxnH * S1 - 1.0;
+        const double dni = -(rom * rom) * D * S2 - (psi * rom * D + 1.0) * S3 * rom;
+        const double dfdpsi = sigmav_ie * n_i * rxnH * (n_i * D + 2.0 * eps_psi * dni) +
+                              2.0 * n_i * vi * rxnH * et21 *
+                                  ((dni / n_i + D * (2.0 * et + 1.0) / (eps_psi * (1.0 + et))) * S4 + D * S5) +
+                              n_i * vi * rxnH * (dni / n_i * (1.0 - psi) - 1.0) * S6;
+        const double prev = psi;
+        psi = psi - fpsi / dfdpsi;
+        if (psi < psi0) {
+            psi = psi0 * 0.9999999;
+            lowT = 1;
+        } else if (psi > 0.0) {
+            psi = -1e-5;
+        }
+        conv = fabs(fpsi);
+        niter = niter + 1;
+        if (psi == prev && conv > p.eps) niter = p.nitermax;
+    }
+}
+
+// Outputs of the mixed path (ionisation.f90:137-206): Z_k, n_i, n_e, psi_old and, with the
+// resistivities, eta_o/H/a and gamma_d, in FP64 with the tabulated reciprocals, stored in FP32.
+template <typename R>
+__device__ __forceinline__ void charge_outputs_mix(const ChargeParams<R>& p, const double* tau, const double* alp,
+                                                   long long c, double ihs, double rho, double nH, double x,
+                                                   double sigmav_ie, const double* tr, double psi, double eps_psi,
+                                                   int lowT) {
+    const int N = p.ndust;
+    const double e2t = (eps_psi * eps_psi) * p.th2, et1 = eps_psi * p.thetai, r1e = 1.0 / (1.0 - eps_psi);
+    const R* uk = p.u + 5 * p.plane + c;
+    double nsum = 0.0;
+    for (int k = 0; k < N; ++k) {
+        const double n = (double)uk[(long long)k * p.plane] * ihs * p.nfac[k];
+        const double z = psi * tau[k] + (1.0 - e2t) * rcp_refined(1.0 + et1 * alp[k] + e2t);
+        p.zd[(long long)k * p.plane + c] = R(z);
+        nsum = nsum - z * n * r1e;
+    }
+    if (lowT > 0 && N > 0) nsum = sqrt(eps_psi * x * nH / sigmav_ie);
+    p.ni[c] = R(nsum);
+    p.ne[c] = R(eps_psi * nsum);
+    p.psi_old[c] = lowT > 0 ? p.psi0 : psi;
+    if (!p.res) return;
+    const double e = chg::e_el, cl = chg::clight, mel = chg::m_el, mi = p.mu_ions * chg::mH;
+    const double B = p.B0 * sqrt(nH / 1e4);
+    const double rnH = 1.0 / nH;
+    const double t_sel = tr[4] * rnH, t_sions = tr[5] * rnH;
+    const double irc = 1.0 / (rho * p.ud * tr[3]);
+    const double sig_el = (eps_psi * nsum) * (e * e) * t_sel / mel;
+    const double sig_i = (nsum) * (e * e) * t_sions / mi;
+    const double om_el = -e * B / cl / mel;
+    const double om_i = e * B / cl / mi;
+    const double eBc = e * B / cl;
+    double so = 0.0, sp = 0.0, sh = 0.0;
+    for (int k = 0; k < N; ++k) {
+        const double n = (double)uk[(long long)k * p.plane] * ihs * p.nfac[k];
+        const double z = psi * tau[k] + (1.0 - e2t) * rcp_refined(1.0 + et1 * alp[k] + e2t);
+        const double t_sd = p.ak[k] * irc;
+        const double sd = n * ((z * e) * (z * e)) * t_sd * p.rmk[k];
+        const double omd = z * eBc * p.rmk[k];
+        const double wt = omd * t_sd;
+        const double q = 1.0 / (1.0 + wt * wt);
+        so = so + sd;
+        sp = sp + sd * q;
+        sh = sh + sd * wt * q;
+        p.gamma_d[(long long)k * p.plane + c] = R(t_sd * omd);
+    }
+    const double wi = om_i * t_sions, we = om_el * t_sel;
+    const double sigma_o = so + sig_i + sig_el;
+    const double sigma_p = sig_i / (1.0 + wi * wi) + sig_el / (1.0 + we * we) + sp;
+    const double sigma_h = -sig_i * (wi) / (1.0 + wi * wi) - sig_el * (we) / (1.0 + we * we) - sh;
+    p.eta[c] = R(1.0 / sigma_o);
+    p.eta[p.plane + c] = R(sigma_h / (sigma_p * 2.0 + sigma_h * sigma_h));
+    p.eta[2 * p.plane + c] = R(sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - 1.0 / sigma_o);
+}
+
 // K5.  R = double: the reference loop in FP64 (parity path).  R = float (mixed precision): from a
 // cold or network start, FP32 Newton steps until |f| < 1e-3 or psi stops moving in FP32, then FP64
 // steps to the reference tolerance chg_eps; a warm start (psi_old, FP64) goes to FP64 directly.
@@ -167,59 +293,68 @@ __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
             const float sd = p.seed[c];
             if (sd < 0.0f) { psi = (double)sd; cold = true; }
         }
+        const double ihs = 1.0 / hs;
         if (sizeof(R) == 4 && cold) {
             float psif = (float)psi, convf = 1e4f;
-            auto nk32 = [&](int k) -> float { return (float)nk64(k); };
+            auto nk32 = [&](int k) -> float { return (float)((double)p.u[(long long)(5 + k) * p.plane + c] * ihs * p.nfac[k]); };
             charge_newton<float>(p, tau, alp, nk32, (float)nH, (float)x, (float)sigmav_ie, (float)vi,
                                  fmaxf((float)p.eps, 1e-3f), true, psif, niter, lowT, convf);
             psi = (double)psif;
             conv = 1e4;   // the FP64 phase re-evaluates the residual
         }
-        charge_newton<double>(p, tau, alp, nk64, nH, x, sigmav_ie, vi, p.eps, false, psi, niter, lowT, conv);
+        if constexpr (sizeof(R) == 4)
+            charge_newton_mix(p, tau, alp, p.rtau + (size_t)row * N, p.u + 5 * p.plane + c, ihs, nH, x, sigmav_ie, vi, psi,
+                              niter, lowT, conv);
+        else
+            charge_newton<double>(p, tau, alp, nk64, nH, x, sigmav_ie, vi, p.eps, false, psi, niter, lowT, conv);
         double eps_psi = (1.0 - psi) / thetai * exp(-psi);
         if (lowT > 0) eps_psi = 0.99999;
-        double nsum = 0.0;
-        for (int k = 0; k < N; ++k) {
-            const double tk = tau[k], ak = alp[k];
-            const double z = psi * tk + (1.0 - (eps_psi * eps_psi) * th2) / (1.0 + eps_psi * thetai * ak + (eps_psi * eps_psi) * th2);
-            p.zd[(long long)k * p.plane + c] = R(z);
-            nsum = nsum - z * nk64(k) / (1.0 - eps_psi);
-        }
-        if (lowT > 0 && N > 0) nsum = sqrt(eps_psi * x * nH / sigmav_ie);
-        p.ni[c] = R(nsum);
-        p.ne[c] = R(eps_psi * nsum);
-        p.psi_old[c] = lowT > 0 ? p.psi0 : psi;
-        if (p.res) {
-            // resistivities (ionisation.f90:163-206)
-            const double e = chg::e_el, cl = chg::clight, mel = chg::m_el, mi = p.mu_ions * chg::mH;
-            const double B = p.B0 * sqrt(nH / 1e4);
-            const double cs_T = tr[3];
-            const double t_sel = tr[4] / nH, t_sions = tr[5] / nH;
-            const double rho_cgs = rho * p.ud;
-            const double sig_el = (eps_psi * nsum) * (e * e) * t_sel / mel;
-            const double sig_i = (nsum) * (e * e) * t_sions / mi;
-            const double om_el = -e * B / cl / mel;
-            const double om_i = e * B / cl / mi;
-            double so = 0.0, sp = 0.0, sh = 0.0;
+        if constexpr (sizeof(R) == 4)
+            charge_outputs_mix(p, tau, alp, c, ihs, rho, nH, x, sigmav_ie, tr, psi, eps_psi, lowT);
+        else {
+            double nsum = 0.0;
             for (int k = 0; k < N; ++k) {
                 const double tk = tau[k], ak = alp[k];
                 const double z = psi * tk + (1.0 - (eps_psi * eps_psi) * th2) / (1.0 + eps_psi * thetai * ak + (eps_psi * eps_psi) * th2);
-                const double t_sd = p.ak[k] / (rho_cgs * cs_T);
-                const double sd = nk64(k) * ((z * e) * (z * e)) * t_sd / p.mkum[k];
-                const double omd = z * e * B / cl / p.mkum[k];
-                const double wt = omd * t_sd;
-                so = so + sd;
-                sp = sp + sd / (1.0 + wt * wt);
-                sh = sh + sd * wt / (1.0 + wt * wt);
-                p.gamma_d[(long long)k * p.plane + c] = R(t_sd * omd);
+                p.zd[(long long)k * p.plane + c] = R(z);
+                nsum = nsum - z * nk64(k) / (1.0 - eps_psi);
             }
-            const double wi = om_i * t_sions, we = om_el * t_sel;
-            const double sigma_o = so + sig_i + sig_el;
-            const double sigma_p = sig_i / (1.0 + wi * wi) + sig_el / (1.0 + we * we) + sp;
-            const double sigma_h = -sig_i * (wi) / (1.0 + wi * wi) - sig_el * (we) / (1.0 + we * we) - sh;
-            p.eta[c] = R(1.0 / sigma_o);
-            p.eta[p.plane + c] = R(sigma_h / (sigma_p * 2.0 + sigma_h * sigma_h));
-            p.eta[2 * p.plane + c] = R(sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - 1.0 / sigma_o);
+            if (lowT > 0 && N > 0) nsum = sqrt(eps_psi * x * nH / sigmav_ie);
+            p.ni[c] = R(nsum);
+            p.ne[c] = R(eps_psi * nsum);
+            p.psi_old[c] = lowT > 0 ? p.psi0 : psi;
+            if (p.res) {
+                // resistivities (ionisation.f90:163-206)
+                const double e = chg::e_el, cl = chg::clight, mel = chg::m_el, mi = p.mu_ions * chg::mH;
+                const double B = p.B0 * sqrt(nH / 1e4);
+                const double cs_T = tr[3];
+                const double t_sel = tr[4] / nH, t_sions = tr[5] / nH;
+                const double rho_cgs = rho * p.ud;
+                const double sig_el = (eps_psi * nsum) * (e * e) * t_sel / mel;
+                const double sig_i = (nsum) * (e * e) * t_sions / mi;
+                const double om_el = -e * B / cl / mel;
+                const double om_i = e * B / cl / mi;
+                double so = 0.0, sp = 0.0, sh = 0.0;
+                for (int k = 0; k < N; ++k) {
+                    const double tk = tau[k], ak = alp[k];
+                    const double z = psi * tk + (1.0 - (eps_psi * eps_psi) * th2) / (1.0 + eps_psi * thetai * ak + (eps_psi * eps_psi) * th2);
+                    const double t_sd = p.ak[k] / (rho_cgs * cs_T);
+                    const double sd = nk64(k) * ((z * e) * (z * e)) * t_sd / p.mkum[k];
+                    const double omd = z * e * B / cl / p.mkum[k];
+                    const double wt = omd * t_sd;
+                    so = so + sd;
+                    sp = sp + sd / (1.0 + wt * wt);
+                    sh = sh + sd * wt / (1.0 + wt * wt);
+                    p.gamma_d[(long long)k * p.plane + c] = R(t_sd * omd);
+                }
+                const double wi = om_i * t_sions, we = om_el * t_sel;
+                const double sigma_o = so + sig_i + sig_el;
+                const double sigma_p = sig_i / (1.0 + wi * wi) + sig_el / (1.0 + we * we) + sp;
+                const double sigma_h = -sig_i * (wi) / (1.0 + wi * wi) - sig_el * (we) / (1.0 + we * we) - sh;
+                p.eta[c] = R(1.0 / sigma_o);
+                p.eta[p.plane + c] = R(sigma_h / (sigma_p * 2.0 + sigma_h * sigma_h));
+                p.eta[2 * p.plane + c] = R(sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - 1.0 / sigma_o);
+            }
         }
         p.iters[c] = niter;
         atomicAdd(&s_hist[niter < CHARGE_HIST - 1 ? niter : CHARGE_HIST - 1], 1u);

@@ -383,7 +383,7 @@ double charge_psi0(double thetai) {
 // constants of the view.  Temperature rows: one per column for the polar disk (T from the
 // isothermal cs through cs_eos), one row (T_cloud) for dustyTurb.
 void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_max, std::vector<double>& h,
-                         shark::ChargeView& cv, size_t off[7]) {
+                         shark::ChargeView& cv, size_t off[11]) {
     const int N = c.ndust;
     const double ul = unit1(c.unit_l), ud = unit1(c.unit_d), ut = unit1(c.unit_t);
     const double um = ul * ul * ul * ud, uv = ul / ut;
@@ -396,7 +396,11 @@ void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_m
     off[4] = off[3] + (size_t)rows * N;       // l2
     off[5] = off[4] + N;                      // mkum
     off[6] = off[5] + N;                      // ak
-    h.assign(off[6] + N, 0.0);
+    off[7] = off[6] + N;                      // rtau: 1/tau (mixed path)
+    off[8] = off[7] + (size_t)rows * N;       // nfac: unit_d / m_k (g), grain number per unit of rho_k
+    off[9] = off[8] + N;                      // rmk: 1/m_k (g)
+    off[10] = off[9] + N;                     // pl2: pi l_k^2
+    h.assign(off[10] + N, 0.0);
     for (int ix = 0; ix < nx_max; ++ix) h[off[0] + ix] = disk ? col.hs[ix] : 1.0;
     const double mu = c.chg_mu_ions;
     const double as_He_ions = (double)1.14f, as_He_el = (double)1.16f;   // REAL*4 literals
@@ -424,6 +428,7 @@ void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_m
             const double tau = lk * kKB * T / (kEl * kEl);
             h[off[2] + (size_t)r * N + k] = tau;
             h[off[3] + (size_t)r * N + k] = std::sqrt(8.0 / (kPi * tau));
+            h[off[7] + (size_t)r * N + k] = 1.0 / tau;
         }
     }
     const double f43 = (double)(4.0f / 3.0f);   // Fortran 4./3. is a default-REAL quotient
@@ -432,6 +437,9 @@ void build_charge_tables(const shark_gpu_config& c, const Columns& col, int nx_m
         h[off[4] + k] = lk * lk;
         h[off[5] + k] = (f43 * kPi * c.rhograin * (sk * sk * sk)) * um;
         h[off[6] + k] = std::sqrt(kPi * c.gamma / 8.0) * (c.rhograin * ud) * (lk);
+        h[off[8] + k] = ud / h[off[5] + k];
+        h[off[9] + k] = 1.0 / h[off[5] + k];
+        h[off[10] + k] = kPi * h[off[4] + k];
     }
     cv.t_per_col = disk ? 1 : 0;
     cv.analytical = (c.chg_mode & SHARK_CHARGE_ANALYTICAL) ? 1 : 0;
@@ -970,13 +978,15 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     v.chg = shark::ChargeView{};
     if (cfg->flags & SHARK_FLAG_CHARGING) {
         std::vector<double> h;
-        size_t off[7];
+        size_t off[11];
         build_charge_tables(*cfg, col, v.nx_max, h, v.chg, off);
         INIT_TRY(cudaMalloc(&c->chg_tables, h.size() * sizeof(double)));
         INIT_TRY(cudaMemcpy(c->chg_tables, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
         v.chg.hs = c->chg_tables + off[0]; v.chg.trow = c->chg_tables + off[1]; v.chg.tau = c->chg_tables + off[2];
         v.chg.alpha = c->chg_tables + off[3]; v.chg.l2 = c->chg_tables + off[4]; v.chg.mkum = c->chg_tables + off[5];
         v.chg.ak = c->chg_tables + off[6];
+        v.chg.rtau = c->chg_tables + off[7]; v.chg.nfac = c->chg_tables + off[8];
+        v.chg.rmk = c->chg_tables + off[9]; v.chg.pl2 = c->chg_tables + off[10];
         const size_t pl = (size_t)v.plane;
         INIT_TRY(cudaMalloc(&c->chg_psi, pl * sizeof(double)));
         INIT_TRY(cudaMemsetAsync(c->chg_psi, 0, pl * sizeof(double), c->stream));

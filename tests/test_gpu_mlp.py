@@ -14,6 +14,7 @@ import pytest
 from shark_gb300 import config as K, setups
 from shark_gb300.solver import Shark
 from oracle import mlp_oracle as M
+from oracle.oracle import Oracle
 from tests.test_charge_cpu import _noisy_turb
 from tests.test_mlp_cpu import _blob
 
@@ -91,6 +92,7 @@ def _train_on_varied_states(g, cfg, u0, factors, seeds):
 def test_trained_network_cuts_cold_start_newton_iterations():
     factors = [0.03, 0.1, 0.3, 1.0, 3.0, 10.0, 30.0]
     cfg, u0, g = _ctx(n=48, ndust=8)
+    psi0 = Oracle(cfg).charge_psi0()
     with g:
         n, loss = _train_on_varied_states(g, cfg, u0, factors, seeds=[11, 12])
         blob = g.mlp_save()
@@ -115,9 +117,16 @@ def test_trained_network_cuts_cold_start_newton_iterations():
                 _, nc_mlp, it_mlp = s.charge_stats()
                 got = s.download_charge()
             conv = ref["iters"] < cfg.chg_nitermax
-            # same converged tolerance: the same cells converge, to the same potential
+            # same converged tolerance: the same cells converge, to the same potential.  A Newton
+            # step below psi0 latches the reference's low-temperature branch (ionisation.f90:
+            # psi = psi0, eps = 0.99999 in the outputs) for the rest of the call, so where the root
+            # lies within ~1e-3 of psi0 the outcome depends on the start point; such cells (psi
+            # reported as psi0 exactly) are few and left out of the comparison
             assert nc_mlp == nc_ref
-            assert np.max(np.abs(got["psi"][conv] - ref["psi"][conv]) / np.abs(ref["psi"][conv])) < 1e-5
+            latched = np.isclose(got["psi"], psi0, rtol=1e-12, atol=0) | np.isclose(ref["psi"], psi0, rtol=1e-12, atol=0)
+            assert latched.mean() <= 0.01, latched.sum()
+            cmp = conv & ~latched
+            assert np.max(np.abs(got["psi"][cmp] - ref["psi"][cmp]) / np.abs(ref["psi"][cmp])) < 1e-5
             res.append((it_ref, it_mlp))
     ratio = sum(r for r, _ in res) / sum(m for _, m in res)
     assert ratio >= 3.0, res
