@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include "../../include/shark_gpu.h"
+#include "physics.cuh"
 
 namespace shark {
 
@@ -128,13 +129,6 @@ __device__ __forceinline__ void charge_newton(const ChargeParams<R>& p, const do
             if (conv > tol) niter = p.nitermax;
         }
     }
-}
-
-// 1/x for the mixed path: the FP32 reciprocal refined by one FP64 Newton step, relative error
-// ~1e-14, for x within FP32 range.
-__device__ __forceinline__ double rcp_refined(double x) {
-    const double r = (double)(1.0f / (float)x);
-    return r * (2.0 - x * r);
 }
 
 // FP64 phase of the mixed path: the iteration of charge_newton with the residual f in FP64 and

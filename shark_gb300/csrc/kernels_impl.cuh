@@ -40,7 +40,8 @@ static KParams<R> make_params(const DeviceView& v) {
     p.box_l_y = c.box_l_y;
     p.chg_eta = (const R*)v.chg.eta;
     p.chg_gamma_d = (const R*)v.chg.gamma_d;
-    p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize; p.dstokes = v.dstokes; p.turb_rho0 = c.turb_rho0;
+    p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize; p.dstokes = v.dstokes; p.dinvts = v.dinvts;
+    p.turb_rho0 = c.turb_rho0;
     p.dt = nullptr; p.dt_next = nullptr; p.status = v.status; p.coef = v.coef;
     p.u_cur = (const R*)v.u[v.cur];
     p.u_next = (R*)v.u[(v.cur + 1) % v.nbuf];

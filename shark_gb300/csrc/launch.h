@@ -46,6 +46,7 @@ struct DeviceView {
     const double* dtstop;
     const double* dsize;
     const double* dstokes;
+    const double* dinvts;       // 1/C_k with t_k = C_k / (cell factor) for the per-cell stopping times
     double* dt_slots;           // [2] dt of step n lives in slot n % 2
     unsigned int* status;       // OR of SHARK_STATUS_* bits
     float* coef;                // [2*SHARK_MAX_DUST] per-step drag coefficients (mixed path)

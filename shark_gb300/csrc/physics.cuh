@@ -13,6 +13,13 @@
 
 namespace shark {
 
+// 1/x for the mixed path: the FP32 reciprocal refined by one FP64 Newton step, relative error
+// ~1e-14, for x within FP32 range (a handful of FP64 operations instead of a division).
+__device__ __forceinline__ double rcp_refined(double x) {
+    const double r = (double)(1.0f / (float)x);
+    return r * (2.0 - x * r);
+}
+
 template <typename R> __device__ __forceinline__ R sq(R x) { return x * x; }
 // gfortran MAX/MIN on non-NaN operands
 template <typename R> __device__ __forceinline__ R fmax2(R a, R b) { return a > b ? a : b; }

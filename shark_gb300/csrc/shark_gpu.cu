@@ -76,7 +76,7 @@ struct shark_gpu_ctx {
     bool have_uinit = false;
     void* metrics = nullptr;         // 13 arrays x nx_max in state precision
     double* metrics_d = nullptr;     // 9 arrays x nx_max FP64
-    double* species = nullptr;       // dK | dtstop | dsize | dstokes (4 x SHARK_MAX_DUST)
+    double* species = nullptr;       // dK | dtstop | dsize | dstokes | dinvts (5 x SHARK_MAX_DUST)
     double* dt_slots = nullptr;      // [2]
     unsigned int* status = nullptr;
     float* coef = nullptr;           // per-step drag coefficients
@@ -958,7 +958,20 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         INIT_TRY(cudaMemcpy(c->metrics_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
         for (int a = 0; a < 9; ++a) v.md[a] = c->metrics_d + a * ncol;
     }
-    INIT_TRY(cudaMalloc(&c->species, 4 * SHARK_MAX_DUST * sizeof(double)));
+    INIT_TRY(cudaMalloc(&c->species, 5 * SHARK_MAX_DUST * sizeof(double)));
+    {
+        // 1/C_k of the stopping times t_k = C_k / F_cell that K2's mixed path multiplies out:
+        // dustyTurb C_k = St_0,k L rho_0 (F = c_s rho), Epstein C_k = sqrt(pi gamma/8) rho_grain s_k
+        // (F = rho c_s, the polar disk's rho/hs c_s)
+        double inv[SHARK_MAX_DUST] = {0};
+        for (int k = 0; k < cfg->ndust; ++k) {
+            const double C = cfg->setup == SHARK_SETUP_DUSTYTURB
+                                 ? cfg->dust_stokes[k] * cfg->box_l * cfg->turb_rho0
+                                 : std::sqrt(kPi * cfg->gamma / 8.0) * cfg->rhograin * cfg->dust_size[k];
+            inv[k] = C != 0.0 ? 1.0 / C : 0.0;
+        }
+        INIT_TRY(cudaMemcpy(c->species + 4 * SHARK_MAX_DUST, inv, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
+    }
     INIT_TRY(cudaMemcpy(c->species + 3 * SHARK_MAX_DUST, cfg->dust_stokes, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
     INIT_TRY(cudaMemcpy(c->species, cfg->dust_K, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
     INIT_TRY(cudaMemcpy(c->species + SHARK_MAX_DUST, cfg->dust_tstop, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
@@ -967,6 +980,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     v.dtstop = c->species + SHARK_MAX_DUST;
     v.dsize = c->species + 2 * SHARK_MAX_DUST;
     v.dstokes = c->species + 3 * SHARK_MAX_DUST;
+    v.dinvts = c->species + 4 * SHARK_MAX_DUST;
     INIT_TRY(cudaMalloc(&c->dt_slots, 2 * sizeof(double)));
     INIT_TRY(cudaMalloc(&c->status, sizeof(unsigned int)));
     INIT_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));

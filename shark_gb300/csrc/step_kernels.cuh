@@ -51,6 +51,7 @@ struct KParams {
     const R* chg_gamma_d;
     // per-species constants
     const double *dK, *dtstop, *dsize, *dstokes;
+    const double* dinvts;             // 1/C_k, t_k = C_k / F_cell (dustyTurb, Epstein, polar disk)
     double turb_rho0;
     // time step bookkeeping
     const double* dt;                 // dt of the current step
@@ -380,16 +381,24 @@ __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int
 // q = lane, lane + 32, ... from the start-of-step stopping times and velocities (exchanged by
 // shuffles).  Every sub-step each lane writes the collision rate w_q = rate_q rho_k rho_j (times
 // the sticking efficiency) of its pairs to shared memory, and lane b gathers
-// drho_b/dt = sum_t gc[t][b] w[gq[t][b]] from the host-built table of net transfers; the sub-step
-// is the warp minimum of CFL_growth rho_b/|drho_b/dt|.  The lanes of a warp take the same
-// sub-steps, so a warp costs the sub-steps of its own cell rather than those of the slowest of 32
-// cells, and nothing leaves registers and shared memory.  Called by every thread of the block.
+// drho_b/dt = sum_t gc[t][b] w[gq[t][b]] from the host-built table of net transfers (staged in
+// shared memory); the sub-step is the warp minimum of CFL_growth rho_b/|drho_b/dt|, and the part
+// of dt still to integrate is kept as an FP32 fraction (the last sub-step takes all of it).  The
+// lanes of a warp take the same sub-steps, so a warp costs the sub-steps of its own cell rather
+// than those of the slowest of 32 cells.  Called by every thread of the block.
 constexpr int GROWTH_PAIR_SLOTS = (GROWTH_MAX_PAIRS + 31) / 32;
+constexpr int GROWTH_SMEM_ROWS = 80;        // gather rows staged in shared memory (64 at 32 species)
 
 static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p, int gx_block, int gy, double dt) {
     __shared__ float sw[8][GROWTH_MAX_PAIRS];
+    __shared__ int2 sg[GROWTH_SMEM_ROWS * 32];
     const GrowthDev& g = p.gw;
-    const int N = p.ndust, P = g.npair;
+    const int N = p.ndust, P = g.npair, L = g.gL;
+    const bool staged = L <= GROWTH_SMEM_ROWS;
+    if (staged)
+        for (int e = threadIdx.x; e < L * 32; e += blockDim.x)
+            sg[e] = make_int2(__ldg(g.gq + e), __float_as_int(__ldg(g.gc + e)));
+    __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float* w = sw[wid];
     float* u = p.u_next;
@@ -398,6 +407,9 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
     const bool on = lane < N;
     const int b = on ? lane : 0;
     const bool thr_on = g.kernel == 0 && g.eps_thr > 0.0;
+    const float dtf = (float)dt, idtf = 1.f / dtf;
+    const float fctl = g.dtctl > 0.0 ? (float)(g.dtctl / dt) : 0.f, dtctl = (float)g.dtctl;
+    const float stick = (float)g.sticking, cflg = (float)g.cfl;
     unsigned st = 0;
     for (int c = 0; c < 32; ++c) {
         const int gx = gx_block + wid * 32 + c;
@@ -443,11 +455,10 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
             if (g.kernel == 0) dv = growth_dv_f(g, cc, tk, tj, cc.T * __ldg(g.pBf + q), dx, dy, dz, dg, ambi);
             kp[i] = __ldg(g.pKf + q) * dv * ihs * (k == j ? 0.5f : 1.f);
         }
-        const float stick = (float)g.sticking, cflg = (float)g.cfl;
         const float thr = (float)g.eps_thr * rho_gas, fl = rho_gas * (float)g.dust_ratio_min;
-        double time_growth = 0.0;
+        float rem = 1.f;                                    // part of dt still to integrate
         int niter = 0;
-        while (time_growth < dt && niter < grw::MAX_SUB) {
+        while (rem > 0.f && niter < grw::MAX_SUB) {
             niter = niter + 1;
 #pragma unroll
             for (int i = 0; i < GROWTH_PAIR_SLOTS; ++i) {
@@ -460,19 +471,27 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
             }
             __syncwarp();
             float d = 0.f;
-            for (int t = 0; t < g.gL; ++t) d += __ldg(g.gc + t * 32 + lane) * w[__ldg(g.gq + t * 32 + lane)];
+            if (staged) {
+#pragma unroll 4
+                for (int t = 0; t < L; ++t) {
+                    const int2 e = sg[t * 32 + lane];
+                    d += __int_as_float(e.y) * w[e.x];
+                }
+            } else {
+                for (int t = 0; t < L; ++t) d += __ldg(g.gc + t * 32 + lane) * w[__ldg(g.gq + t * 32 + lane)];
+            }
             __syncwarp();
             float cand = (on && d != 0.f) ? rd / fabsf(d) * cflg : 1e30f;
             for (int o = 16; o > 0; o >>= 1) cand = fminf(cand, __shfl_xor_sync(FULL, cand, o));
-            double dtg = (double)cand;
-            const double rest = dt - time_growth;
-            dtg = dtg < rest ? dtg : rest;
-            if (g.dtctl > 0.0) dtg = g.dtctl < rest ? g.dtctl : rest;
-            rd = fmaxf(rd + d * (float)dtg, fl);
-            time_growth = time_growth + dtg;
+            const float dtg0 = fctl > 0.f ? dtctl : cand;
+            const float frac = fctl > 0.f ? fctl : cand * idtf;
+            float dtg;
+            if (frac >= rem) { dtg = rem * dtf; rem = 0.f; }
+            else { dtg = dtg0; rem = rem - frac; }
+            rd = fmaxf(rd + d * dtg, fl);
         }
         if (on) u[uidx(p, 5 + b, gy, gx)] = rd;
-        if (!(time_growth >= dt)) st |= (unsigned)SHARK_STATUS_GROWTH;
+        if (rem > 0.f) st |= (unsigned)SHARK_STATUS_GROWTH;
     }
     return st;
 }
@@ -687,8 +706,28 @@ __device__ __forceinline__ void drag_coeffs(double a, float& r, float& w) {
     w = (float)(a / d);
 }
 
+// a_k = dt/t_k of the mixed path for the per-cell stopping times t_k = C_k / F_cell: dt F_cell
+// times the tabulated 1/C_k, and the coefficients with a refined reciprocal (FP64 throughout; the
+// divisions cost most of K2's FP64 work at 32 species)
+__device__ __forceinline__ double drag_cell_factor(const KParams<float>& p, double dt, double qrho_old, int gx, int gy) {
+    if (p.setup == SHARK_SETUP_DUSTYTURB) return dt * (p.csd[gx] * qrho_old);
+    if (p.setup == SHARK_SETUP_DISK_POLAR) return dt * (qrho_old / p.hsd[gx] * p.csd[gx]);
+    return dt * (qrho_old * cs_start(p, gx, gy));
+}
+
+__device__ __forceinline__ void drag_coeffs_mix(double a, float& r, float& w) {
+    const double d = 1.0 + a;
+    if (d < 1e30) {
+        const double q = rcp_refined(d);
+        r = (float)q;
+        w = (float)(a * q);
+    } else {
+        drag_coeffs(a, r, w);
+    }
+}
+
 template <int NS, int MODE, bool GROW = false>
-__global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
+__global__ void __launch_bounds__(256, GROW ? 3 : 1) k_finalize_mixed(KParams<float> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;
     const bool drag = MODE == 0 && N > 0 && (p.flags & SHARK_FLAG_DRAG);
@@ -713,10 +752,13 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
             float rhon = rho, pnx = px, pny = py, pnz = pz;
             const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
             const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
+            const bool direct = p.setup == SHARK_SETUP_DUSTYWAVE;   // t_k from the species density
+            const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx, gy);
             for (int k = 0; k < N; ++k) {
                 float r, w;
                 if (const_ts) { r = cr[k]; w = cw[k]; }
-                else drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
+                else if (direct) drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
+                else drag_coeffs_mix(Fc * p.dinvts[k], r, w);
                 if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
                 pnx += w * u[uidx(p, 5 + N + k, gy, gx)];
                 pny += w * u[uidx(p, 5 + 2 * N + k, gy, gx)];
@@ -729,7 +771,8 @@ __global__ void __launch_bounds__(256) k_finalize_mixed(KParams<float> p) {
                 float r, w;
                 if (NS > 0) { r = rk[k < NMAX ? k : 0]; w = wk[k < NMAX ? k : 0]; }
                 else if (const_ts) { r = cr[k]; w = cw[k]; }
-                else drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
+                else if (direct) drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
+                else drag_coeffs_mix(Fc * p.dinvts[k], r, w);
                 const float rd = u[uidx(p, 5 + k, gy, gx)];
                 const long long ixx = uidx(p, 5 + N + k, gy, gx), iyy = uidx(p, 5 + 2 * N + k, gy, gx),
                                 izz = uidx(p, 5 + 3 * N + k, gy, gx);
