@@ -44,6 +44,8 @@ struct ChargeParams {
     const double* nfac;          // [N] unit_d / m_k (g)     (mixed path: n_k = rho_k / hs * nfac_k)
     const double* rmk;           // [N] 1/m_k (g)            (mixed path)
     const double* pl2;           // [N] pi l_k^2             (mixed path)
+    const float4* tf;            // [rows][N][2] (alpha, 1/tau, pi l^2/tau, tau), (unit_d/m, pi l^2, 1/m,
+                                 // sqrt(pi gamma/8) rhograin l) in FP32 (mixed path)
     double unH, ud, ul, x0, sig_att;
     double thetai, th2, th3, psi0, eps, B0, mu_ions;
     int nitermax;
@@ -131,14 +133,26 @@ __device__ __forceinline__ void charge_newton(const ChargeParams<R>& p, const do
     }
 }
 
-// FP64 phase of the mixed path: the iteration of charge_newton with the residual f in FP64 and
-// the divisions of its species loop replaced by tabulated reciprocals and a refined reciprocal of
-// the denominator 1 + et a_k + et^2.  The derivative's species factors are FP32 (Newton needs
-// f' to a few digits only), accumulated against n_k in FP64 so no FP32 product leaves range.
-// The stopping test |f| < chg_eps is the reference's.  `uk` points at species 0 of the cell.
+// Compensated FP32 sum (Kahan): s + c carries the sum of the added terms to ~1 ulp.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// FP64 phase of the mixed path: the iteration of charge_newton with the residual f accurate to
+// ~1e-8.  Its species sums split into psi-independent parts, formed once per cell in FP64,
+//   T1 = sum n_k tau_k,  T3 = sum n_k pi l_k^2,
+// and psi-dependent corrections of a few per cent, formed per iteration in compensated FP32,
+//   T2 = sum n_k r_k,  T4 = sum n_k pi l_k^2 r_k / tau_k,   r_k = 1/(1 + et alpha_k + et^2):
+//   n_i = -(psi T1 + (1 - et^2) T2)/(1 - eps),   S1 = (1 - psi) T3 + 2 (et^2 + et) T4.
+// The derivative's species sums are FP32 (Newton needs f' to a few digits).  n_k = rho_k/hs
+// unit_d/m_k; the FP32 sums run on rho_k unit_d/m_k and take 1/hs afterwards.  The stopping test
+// |f| < chg_eps is the reference's.  `uk` points at species 0 of the cell, `tf` at the cell's row.
 template <typename R>
-__device__ __forceinline__ void charge_newton_mix(const ChargeParams<R>& p, const double* tau, const double* alp,
-                                                  const double* rtau, const R* uk, double ihs, double nH, double x,
+__device__ __forceinline__ void charge_newton_mix(const ChargeParams<R>& p, const float4* tf, const R* uk,
+                                                  double T1, double T3, double ihs, double nH, double x,
                                                   double sigmav_ie, double vi, double& psi, int& niter, int& lowT,
                                                   double& conv) {
     const int N = p.ndust;
@@ -150,33 +164,30 @@ __device__ __forceinline__ void charge_newton_mix(const ChargeParams<R>& p, cons
         const double et = eps_psi * thetai;
         const double et2 = et * et, et21 = et2 + et, om = 1.0 - eps_psi, rom = 1.0 / om;
         const double D = (-eps_psi * (2.0 - psi) / (1.0 - psi));
-        const float ef = (float)eps_psi, et2f = (float)et2;
-        const float c2a = -(et2f * et2f), c2b = ef * ef;
-        double n_i = 0.0, S1 = 0.0, S2 = 0.0, S3 = 0.0, S4 = 0.0, S5 = 0.0, S6 = 0.0;
+        const float ef = (float)eps_psi, etf = (float)et, et2f = (float)et2;
+        const float c2a = -(et2f * et2f), c2b = ef * ef, c5 = 2.f * ef * th2f;
+        float T2 = 0.f, k2 = 0.f, T4 = 0.f, k4 = 0.f, S2 = 0.f, S5 = 0.f;
         for (int k = 0; k < N; ++k) {
-            const double n = (double)uk[(long long)k * p.plane] * ihs * p.nfac[k];
-            const double tk = tau[k], ak = alp[k], rtk = rtau[k];
-            const double den = 1.0 + et * ak + et2;
-            const double r = rcp_refined(den);
-            n_i = n_i - (psi * tk + (1.0 - et2) * r) * n * rom;
-            const double npl = n * p.pl2[k];
-            S1 = S1 + npl * ((1.0 - psi) + (2.0 * rtk) * et21 * r);
-            const float akf = (float)ak, rf = (float)r, rtkf = (float)rtk, pl2f = (float)p.pl2[k];
-            const float f2 = (c2a + (4.f * th2f - th3f * akf) * c2b + (2.f * thf * akf - 4.f * th2f) * ef + 1.f - thf * akf) * (rf * rf);
-            const float f4 = pl2f * rtkf * rf;
-            const float f5 = pl2f * (2.f * ef * th2f + thf * akf) * rtkf * (rf * rf);
-            S2 = S2 + n * (double)f2;
-            S3 = S3 + n * tk;
-            S4 = S4 + n * (double)f4;
-            S5 = S5 + n * (double)f5;
-            S6 = S6 + npl;
+            const float4 a = tf[2 * k], b = tf[2 * k + 1];   // (alpha, 1/tau, pi l^2/tau, tau), (unit_d/m, ...)
+            const float nf = (float)uk[(long long)k * p.plane] * b.x;
+            const float r = 1.f / (1.f + etf * a.x + et2f);
+            const float nr = nf * r;
+            kahan_add(T2, k2, nr);
+            kahan_add(T4, k4, nr * a.z);
+            const float f2 = (c2a + (4.f * th2f - th3f * a.x) * c2b + (2.f * thf * a.x - 4.f * th2f) * ef + 1.f - thf * a.x) * r;
+            S2 = S2 + nr * f2;
+            S5 = S5 + nr * a.z * (c5 + thf * a.x) * r;
         }
+        const double T2d = ihs * (double)T2, T4d = ihs * (double)T4;
+        const double n_i = -(psi * T1 + (1.0 - et2) * T2d) * rom;
+        const double S1 = (1.0 - psi) * T3 + 2.0 * et21 * T4d;
         const double fpsi = sigmav_ie * eps_psi * (n_i * n_i) * rxnH + n_i * vi * rxnH * S1 - 1.0;
-        const double dni = -(rom * rom) * D * S2 - (psi * rom * D + 1.0) * S3 * rom;
+        const double S2d = ihs * (double)S2, S4d = T4d, S5d = ihs * (double)S5;
+        const double dni = -(rom * rom) * D * S2d - (psi * rom * D + 1.0) * T1 * rom;
         const double dfdpsi = sigmav_ie * n_i * rxnH * (n_i * D + 2.0 * eps_psi * dni) +
                               2.0 * n_i * vi * rxnH * et21 *
-                                  ((dni / n_i + D * (2.0 * et + 1.0) / (eps_psi * (1.0 + et))) * S4 + D * S5) +
-                              n_i * vi * rxnH * (dni / n_i * (1.0 - psi) - 1.0) * S6;
+                                  ((dni / n_i + D * (2.0 * et + 1.0) / (eps_psi * (1.0 + et))) * S4d + D * S5d) +
+                              n_i * vi * rxnH * (dni / n_i * (1.0 - psi) - 1.0) * T3;
         const double prev = psi;
         psi = psi - fpsi / dfdpsi;
         if (psi < psi0) {
@@ -192,22 +203,23 @@ __device__ __forceinline__ void charge_newton_mix(const ChargeParams<R>& p, cons
 }
 
 // Outputs of the mixed path (ionisation.f90:137-206): Z_k, n_i, n_e, psi_old and, with the
-// resistivities, eta_o/H/a and gamma_d, in FP64 with the tabulated reciprocals, stored in FP32.
+// resistivities, eta_o/H/a and gamma_d.  The per-species terms are FP32 (the outputs are stored
+// in FP32) with compensated sums; the cell-level electron and ion terms are FP64.
 template <typename R>
-__device__ __forceinline__ void charge_outputs_mix(const ChargeParams<R>& p, const double* tau, const double* alp,
-                                                   long long c, double ihs, double rho, double nH, double x,
-                                                   double sigmav_ie, const double* tr, double psi, double eps_psi,
-                                                   int lowT) {
+__device__ __forceinline__ void charge_outputs_mix(const ChargeParams<R>& p, const float4* tf, long long c, double ihs,
+                                                   double rho, double nH, double x, double sigmav_ie, const double* tr,
+                                                   double psi, double eps_psi, int lowT) {
     const int N = p.ndust;
-    const double e2t = (eps_psi * eps_psi) * p.th2, et1 = eps_psi * p.thetai, r1e = 1.0 / (1.0 - eps_psi);
     const R* uk = p.u + 5 * p.plane + c;
-    double nsum = 0.0;
+    const float psif = (float)psi, e2t = (float)((eps_psi * eps_psi) * p.th2), et1 = (float)(eps_psi * p.thetai);
+    float zs = 0.f, kz = 0.f;
     for (int k = 0; k < N; ++k) {
-        const double n = (double)uk[(long long)k * p.plane] * ihs * p.nfac[k];
-        const double z = psi * tau[k] + (1.0 - e2t) * rcp_refined(1.0 + et1 * alp[k] + e2t);
+        const float4 a = tf[2 * k], b = tf[2 * k + 1];
+        const float z = psif * a.w + (1.f - e2t) / (1.f + et1 * a.x + e2t);
         p.zd[(long long)k * p.plane + c] = R(z);
-        nsum = nsum - z * n * r1e;
+        kahan_add(zs, kz, z * ((float)uk[(long long)k * p.plane] * b.x));
     }
+    double nsum = -(ihs * (double)zs) / (1.0 - eps_psi);
     if (lowT > 0 && N > 0) nsum = sqrt(eps_psi * x * nH / sigmav_ie);
     p.ni[c] = R(nsum);
     p.ne[c] = R(eps_psi * nsum);
@@ -217,30 +229,32 @@ __device__ __forceinline__ void charge_outputs_mix(const ChargeParams<R>& p, con
     const double B = p.B0 * sqrt(nH / 1e4);
     const double rnH = 1.0 / nH;
     const double t_sel = tr[4] * rnH, t_sions = tr[5] * rnH;
-    const double irc = 1.0 / (rho * p.ud * tr[3]);
+    const double irc = 1.0 / (rho * p.ud * tr[3]);      // t_sd = sqrt(pi gamma/8) rhograin l / (rho_cgs cs_T)
     const double sig_el = (eps_psi * nsum) * (e * e) * t_sel / mel;
     const double sig_i = (nsum) * (e * e) * t_sions / mi;
     const double om_el = -e * B / cl / mel;
     const double om_i = e * B / cl / mi;
-    const double eBc = e * B / cl;
-    double so = 0.0, sp = 0.0, sh = 0.0;
+    const float ircf = (float)irc, eBc = (float)(e * B / cl), ef = (float)e;
+    float so = 0.f, ko = 0.f, sp = 0.f, kp = 0.f, sh = 0.f, kh = 0.f;
     for (int k = 0; k < N; ++k) {
-        const double n = (double)uk[(long long)k * p.plane] * ihs * p.nfac[k];
-        const double z = psi * tau[k] + (1.0 - e2t) * rcp_refined(1.0 + et1 * alp[k] + e2t);
-        const double t_sd = p.ak[k] * irc;
-        const double sd = n * ((z * e) * (z * e)) * t_sd * p.rmk[k];
-        const double omd = z * eBc * p.rmk[k];
-        const double wt = omd * t_sd;
-        const double q = 1.0 / (1.0 + wt * wt);
-        so = so + sd;
-        sp = sp + sd * q;
-        sh = sh + sd * wt * q;
-        p.gamma_d[(long long)k * p.plane + c] = R(t_sd * omd);
+        const float4 a = tf[2 * k], b = tf[2 * k + 1];
+        const float z = psif * a.w + (1.f - e2t) / (1.f + et1 * a.x + e2t);
+        const float t_sd = b.w * ircf;
+        const float ze = z * ef;
+        const float sd = ((float)uk[(long long)k * p.plane] * b.x) * b.z * (ze * ze) * t_sd;   // times 1/hs below
+        const float omd = z * eBc * b.z;
+        const float wt = omd * t_sd;
+        const float q = 1.f / (1.f + wt * wt);
+        const float h = fabsf(wt) > 1e18f ? 1.f / wt : wt * q;   // wt / (1 + wt^2) without overflow
+        kahan_add(so, ko, sd);
+        kahan_add(sp, kp, sd * q);
+        kahan_add(sh, kh, sd * h);
+        p.gamma_d[(long long)k * p.plane + c] = R(wt);
     }
     const double wi = om_i * t_sions, we = om_el * t_sel;
-    const double sigma_o = so + sig_i + sig_el;
-    const double sigma_p = sig_i / (1.0 + wi * wi) + sig_el / (1.0 + we * we) + sp;
-    const double sigma_h = -sig_i * (wi) / (1.0 + wi * wi) - sig_el * (we) / (1.0 + we * we) - sh;
+    const double sigma_o = ihs * (double)so + sig_i + sig_el;
+    const double sigma_p = sig_i / (1.0 + wi * wi) + sig_el / (1.0 + we * we) + ihs * (double)sp;
+    const double sigma_h = -sig_i * (wi) / (1.0 + wi * wi) - sig_el * (we) / (1.0 + we * we) - ihs * (double)sh;
     p.eta[c] = R(1.0 / sigma_o);
     p.eta[p.plane + c] = R(sigma_h / (sigma_p * 2.0 + sigma_h * sigma_h));
     p.eta[2 * p.plane + c] = R(sigma_p / (sigma_p * sigma_p + sigma_h * sigma_h) - 1.0 / sigma_o);
@@ -296,15 +310,21 @@ __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
             psi = (double)psif;
             conv = 1e4;   // the FP64 phase re-evaluates the residual
         }
-        if constexpr (sizeof(R) == 4)
-            charge_newton_mix(p, tau, alp, p.rtau + (size_t)row * N, p.u + 5 * p.plane + c, ihs, nH, x, sigmav_ie, vi, psi,
-                              niter, lowT, conv);
-        else
+        if constexpr (sizeof(R) == 4) {
+            double T1 = 0.0, T3 = 0.0;                 // psi-independent sums of the mixed iteration
+            for (int k = 0; k < N; ++k) {
+                const double n = (double)p.u[(long long)(5 + k) * p.plane + c] * ihs * p.nfac[k];
+                T1 = T1 + n * tau[k];
+                T3 = T3 + n * p.pl2[k];
+            }
+            charge_newton_mix(p, p.tf + (size_t)row * N * 2, p.u + 5 * p.plane + c, T1, T3, ihs, nH, x, sigmav_ie, vi,
+                              psi, niter, lowT, conv);
+        } else
             charge_newton<double>(p, tau, alp, nk64, nH, x, sigmav_ie, vi, p.eps, false, psi, niter, lowT, conv);
         double eps_psi = (1.0 - psi) / thetai * exp(-psi);
         if (lowT > 0) eps_psi = 0.99999;
         if constexpr (sizeof(R) == 4)
-            charge_outputs_mix(p, tau, alp, c, ihs, rho, nH, x, sigmav_ie, tr, psi, eps_psi, lowT);
+            charge_outputs_mix(p, p.tf + (size_t)row * N * 2, c, ihs, rho, nH, x, sigmav_ie, tr, psi, eps_psi, lowT);
         else {
             double nsum = 0.0;
             for (int k = 0; k < N; ++k) {

@@ -247,7 +247,7 @@ static ChargeParams<R> charge_params(const DeviceView& v) {
     q.ndust = v.ndust; q.nvar = v.nvar;
     q.t_per_col = c.t_per_col; q.res = c.res; q.use_seed = c.use_seed;
     q.hs = c.hs; q.trow = c.trow; q.tau = c.tau; q.alpha = c.alpha; q.l2 = c.l2; q.mkum = c.mkum; q.ak = c.ak;
-    q.rtau = c.rtau; q.nfac = c.nfac; q.rmk = c.rmk; q.pl2 = c.pl2;
+    q.rtau = c.rtau; q.nfac = c.nfac; q.rmk = c.rmk; q.pl2 = c.pl2; q.tf = c.tf;
     q.unH = c.unH; q.ud = c.ud; q.ul = c.ul; q.x0 = c.x0; q.sig_att = c.sig_att;
     q.thetai = c.thetai; q.th2 = c.th2; q.th3 = c.th3; q.psi0 = c.psi0; q.eps = c.eps; q.B0 = c.B0;
     q.mu_ions = c.mu_ions; q.nitermax = c.nitermax;

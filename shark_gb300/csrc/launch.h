@@ -17,6 +17,7 @@ struct ChargeView {
     double smallr, mu_gas;
     const double *hs, *trow, *tau, *alpha, *l2, *mkum, *ak;
     const double *rtau, *nfac, *rmk, *pl2;  // mixed path: 1/tau [rows][N], unit_d/m_k, 1/m_k, pi l_k^2
+    const float4* tf;                       // mixed path: [rows][N][2] FP32 species table
     double unH, ud, ul, x0, sig_att, thetai, th2, th3, psi0, eps, B0, mu_ions;
     int nitermax;
     double* psi_old;                        // FP64 [plane]

@@ -91,6 +91,7 @@ struct shark_gpu_ctx {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // charging: tables (FP64) and outputs
     double* chg_tables = nullptr;
+    float* chg_tf = nullptr;         // charging: FP32 per-row species table of the mixed path
     double* chg_psi = nullptr;
     void* chg_out = nullptr;         // zd | ni | ne | eta | gamma_d in state precision
     unsigned long long* chg_hist = nullptr;
@@ -682,6 +683,7 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->chg_tables) cudaFree(c->chg_tables);
+    if (c->chg_tf) cudaFree(c->chg_tf);
     if (c->chg_psi) cudaFree(c->chg_psi);
     if (c->chg_out) cudaFree(c->chg_out);
     if (c->chg_hist) cudaFree(c->chg_hist);
@@ -1001,6 +1003,28 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         v.chg.ak = c->chg_tables + off[6];
         v.chg.rtau = c->chg_tables + off[7]; v.chg.nfac = c->chg_tables + off[8];
         v.chg.rmk = c->chg_tables + off[9]; v.chg.pl2 = c->chg_tables + off[10];
+        {
+            // FP32 copy for the mixed path, per temperature row and species: (alpha, 1/tau,
+            // pi l^2/tau, tau), (unit_d/m, pi l^2, 1/m, sqrt(pi gamma/8) rhograin l)
+            const int N = cfg->ndust, rows = v.chg.t_per_col ? v.nx_max : 1;
+            std::vector<float> tf((size_t)rows * N * 8);
+            for (int r = 0; r < rows; ++r)
+                for (int k = 0; k < N; ++k) {
+                    float* e = &tf[((size_t)r * N + k) * 8];
+                    const double tau = h[off[2] + (size_t)r * N + k];
+                    e[0] = (float)h[off[3] + (size_t)r * N + k];
+                    e[1] = (float)h[off[7] + (size_t)r * N + k];
+                    e[2] = (float)(h[off[10] + k] / tau);
+                    e[3] = (float)tau;
+                    e[4] = (float)h[off[8] + k];
+                    e[5] = (float)h[off[10] + k];
+                    e[6] = (float)h[off[9] + k];
+                    e[7] = (float)h[off[6] + k];
+                }
+            INIT_TRY(cudaMalloc(&c->chg_tf, tf.size() * sizeof(float)));
+            INIT_TRY(cudaMemcpy(c->chg_tf, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice));
+            v.chg.tf = reinterpret_cast<const float4*>(c->chg_tf);
+        }
         const size_t pl = (size_t)v.plane;
         INIT_TRY(cudaMalloc(&c->chg_psi, pl * sizeof(double)));
         INIT_TRY(cudaMemsetAsync(c->chg_psi, 0, pl * sizeof(double), c->stream));
