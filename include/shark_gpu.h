@@ -252,9 +252,11 @@ int32_t shark_gpu_totals(shark_gpu_ctx* ctx, double* out);
  * (CUDA events on the context's stream; waits for the step). */
 int32_t shark_gpu_last_step_ms(shark_gpu_ctx* ctx, float* ms_out);
 
-/* Benchmark helper: synchronize, record a CUDA event on the context's stream, run nsteps steps
- * exactly as shark_gpu_run does (per-step dt readback included), record a second event,
- * synchronize.  *ms_out = device time between the events; *time_io is advanced by the dts. */
+/* Benchmark helper: synchronize, record a CUDA event on the context's stream, queue nsteps steps
+ * back to back (the same kernels as shark_gpu_step, with each step's dt copied to pinned host
+ * memory instead of waited on), record a second event, synchronize.  *ms_out = device time
+ * between the events; *time_io is advanced by the dts.  No host wait sits inside the timed
+ * region, so a stalled host thread cannot show up as GPU time. */
 int32_t shark_gpu_timed_run(shark_gpu_ctx* ctx, int64_t nsteps, double* time_io, float* ms_out);
 
 /* Benchmark helper: run nsteps steps with CUDA events around every kernel on the context's

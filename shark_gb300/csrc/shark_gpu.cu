@@ -963,8 +963,8 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     INIT_TRY(cudaMalloc(&c->species, 5 * SHARK_MAX_DUST * sizeof(double)));
     {
         // 1/C_k of the stopping times t_k = C_k / F_cell that K2's mixed path multiplies out:
-        // dustyTurb C_k = St_0,k L rho_0 (F = c_s rho), Epstein C_k = sqrt(pi gamma/8) rho_grain s_k
-        // (F = rho c_s, the polar disk's rho/hs c_s)
+        // dustyTurb C_k = St_0,k L rho_0 (F = c_s rho), polar disk (Epstein on the midplane density)
+        // C_k = sqrt(pi gamma/8) rho_grain s_k (F = rho/hs c_s)
         double inv[SHARK_MAX_DUST] = {0};
         for (int k = 0; k < cfg->ndust; ++k) {
             const double C = cfg->setup == SHARK_SETUP_DUSTYTURB
@@ -1273,29 +1273,67 @@ int32_t shark_gpu_last_step_ms(shark_gpu_ctx* c, float* ms_out) {
 int32_t shark_gpu_timed_run(shark_gpu_ctx* c, int64_t nsteps, double* time_io, float* ms_out) {
     if (!c || !time_io || !ms_out) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
     if (!c->uploaded) return fail(SHARK_ERR_STATE, "timed run before upload");
-    cudaEvent_t e0, e1;
-    CUDA_TRY(cudaEventCreate(&e0));
-    CUDA_TRY(cudaEventCreate(&e1));
-    CUDA_TRY(cudaStreamSynchronize(c->stream));
+    if (nsteps < 0) return fail(SHARK_ERR_INVALID_ARG, "nsteps < 0");
+    // The steps are queued back to back with no host wait between them (the dt of every step
+    // lives on the device; a copy of it per step lands in pinned memory and is summed
+    // afterwards), so host-side stalls cannot leave the GPU idle inside the timed region.
+    const bool is_static = (c->cfg.flags & SHARK_FLAG_STATIC) != 0;
+    double* dts = nullptr;
+    CUDA_TRY(cudaHostAlloc(&dts, (size_t)(nsteps > 0 ? nsteps : 1) * sizeof(double), cudaHostAllocDefault));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int32_t rc = SHARK_OK;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e != cudaSuccess) rc = fail(SHARK_ERR_CUDA, "timed run: %s", cudaGetErrorString(e));
+    double time = *time_io;
+    const int slot0 = (int)(c->nstep & 1);
+    double dt_first = 0.0;
+    if (rc == SHARK_OK) {
+        unsigned st0;
+        rc = wait_readback(c, slot0, &dt_first, &st0);   // the readback the next step would wait on
+    }
+    if (rc == SHARK_OK && c->v.chg.on) rc = seed_charges(c);
+    if (rc == SHARK_OK) {
+        if ((e = cudaStreamSynchronize(c->stream)) != cudaSuccess) rc = fail(SHARK_ERR_CUDA, "timed run: %s", cudaGetErrorString(e));
+    }
     const bool tk = c->v.time_kernels;
     c->v.time_kernels = false;
-    CUDA_TRY(cudaEventRecord(e0, c->stream));
-    double time = *time_io;
-    int32_t rc = SHARK_OK;
+    if (rc == SHARK_OK) cudaEventRecord(e0, c->stream);
     for (int64_t n = 0; n < nsteps && rc == SHARK_OK; ++n) {
-        double dt;
-        rc = shark_gpu_step(c, &dt, nullptr);
-        time = time + dt;
+        const int slot = (int)(c->nstep & 1);
+        if (!is_static) {
+            c->v.step = c->nstep + 1;
+            if ((e = do_step(c, slot)) != cudaSuccess) { rc = fail(SHARK_ERR_CUDA, "step launch: %s", cudaGetErrorString(e)); break; }
+            c->chg_cold = false;
+            c->v.cur = shark::next_cur(c->v);
+        }
+        if ((e = cudaMemcpyAsync(dts + n, c->dt_slots + slot, sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) {
+            rc = fail(SHARK_ERR_CUDA, "timed run: %s", cudaGetErrorString(e));
+            break;
+        }
+        if (!is_static) c->nstep++;   // a static step keeps its dt slot, as shark_gpu_step does
     }
     c->v.time_kernels = tk;
     if (rc == SHARK_OK) {
         cudaEventRecord(e1, c->stream);
-        cudaError_t e = cudaEventSynchronize(e1);
+        rc = queue_readback(c, (int)(c->nstep & 1));   // what the next step waits on
+    }
+    if (rc == SHARK_OK) {
+        e = cudaEventSynchronize(e1);
         if (e == cudaSuccess) e = cudaEventElapsedTime(ms_out, e0, e1);
         if (e != cudaSuccess) rc = fail(SHARK_ERR_CUDA, "timed run: %s", cudaGetErrorString(e));
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    if (rc == SHARK_OK) {
+        for (int64_t n = 0; n < nsteps; ++n) time = time + dts[n];
+        unsigned int st = 0;
+        if ((e = cudaMemcpy(&st, c->status, sizeof st, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            rc = fail(SHARK_ERR_CUDA, "timed run: %s", cudaGetErrorString(e));
+        c->status_seen |= st;
+    }
+    (void)dt_first;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFreeHost(dts);
     *time_io = time;
     return rc;
 }

@@ -706,13 +706,13 @@ __device__ __forceinline__ void drag_coeffs(double a, float& r, float& w) {
     w = (float)(a / d);
 }
 
-// a_k = dt/t_k of the mixed path for the per-cell stopping times t_k = C_k / F_cell: dt F_cell
-// times the tabulated 1/C_k, and the coefficients with a refined reciprocal (FP64 throughout; the
-// divisions cost most of K2's FP64 work at 32 species)
-__device__ __forceinline__ double drag_cell_factor(const KParams<float>& p, double dt, double qrho_old, int gx, int gy) {
+// a_k = dt/t_k of the mixed path where the per-cell stopping time factors as t_k = C_k / F_cell
+// (dustyTurb C_k = St_0,k L rho_0, F = c_s rho; polar disk Epstein F = rho/hs c_s): dt F_cell times
+// the tabulated 1/C_k, and the coefficients with a refined reciprocal (FP64 throughout; the
+// divisions cost most of K2's FP64 work at 32 species).  Other setups divide directly.
+__device__ __forceinline__ double drag_cell_factor(const KParams<float>& p, double dt, double qrho_old, int gx) {
     if (p.setup == SHARK_SETUP_DUSTYTURB) return dt * (p.csd[gx] * qrho_old);
-    if (p.setup == SHARK_SETUP_DISK_POLAR) return dt * (qrho_old / p.hsd[gx] * p.csd[gx]);
-    return dt * (qrho_old * cs_start(p, gx, gy));
+    return dt * (qrho_old / p.hsd[gx] * p.csd[gx]);
 }
 
 __device__ __forceinline__ void drag_coeffs_mix(double a, float& r, float& w) {
@@ -727,7 +727,7 @@ __device__ __forceinline__ void drag_coeffs_mix(double a, float& r, float& w) {
 }
 
 template <int NS, int MODE, bool GROW = false>
-__global__ void __launch_bounds__(256, GROW ? 3 : 1) k_finalize_mixed(KParams<float> p) {
+__global__ void __launch_bounds__(256, 3) k_finalize_mixed(KParams<float> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;
     const bool drag = MODE == 0 && N > 0 && (p.flags & SHARK_FLAG_DRAG);
@@ -744,7 +744,9 @@ __global__ void __launch_bounds__(256, GROW ? 3 : 1) k_finalize_mixed(KParams<fl
     const bool act = gx < p.ng + p.nx;
     float* u = p.u_next;
     float rho = 0.f, px = 0.f, py = 0.f, pz = 0.f;
-    if (act) {
+    // part 1: drag, floor, drag heating; part 2: kick, setup_inloop, CFL.  With growth in between
+    // (a block-wide phase) the two parts are separate; otherwise they form one block of code.
+    auto part1 = [&]() {
         rho = u[uidx(p, 0, gy, gx)];
         px = u[uidx(p, 1, gy, gx)]; py = u[uidx(p, 2, gy, gx)]; pz = u[uidx(p, 3, gy, gx)];
         if (drag) {
@@ -752,13 +754,12 @@ __global__ void __launch_bounds__(256, GROW ? 3 : 1) k_finalize_mixed(KParams<fl
             float rhon = rho, pnx = px, pny = py, pnz = pz;
             const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
             const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
-            const bool direct = p.setup == SHARK_SETUP_DUSTYWAVE;   // t_k from the species density
-            const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx, gy);
+            const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
+            const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
             for (int k = 0; k < N; ++k) {
                 float r, w;
                 if (const_ts) { r = cr[k]; w = cw[k]; }
-                else if (direct) drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
-                else drag_coeffs_mix(Fc * p.dinvts[k], r, w);
+                else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], r, w);
                 if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
                 pnx += w * u[uidx(p, 5 + N + k, gy, gx)];
                 pny += w * u[uidx(p, 5 + 2 * N + k, gy, gx)];
@@ -771,8 +772,7 @@ __global__ void __launch_bounds__(256, GROW ? 3 : 1) k_finalize_mixed(KParams<fl
                 float r, w;
                 if (NS > 0) { r = rk[k < NMAX ? k : 0]; w = wk[k < NMAX ? k : 0]; }
                 else if (const_ts) { r = cr[k]; w = cw[k]; }
-                else if (direct) drag_coeffs(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
-                else drag_coeffs_mix(Fc * p.dinvts[k], r, w);
+                else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], r, w);
                 const float rd = u[uidx(p, 5 + k, gy, gx)];
                 const long long ixx = uidx(p, 5 + N + k, gy, gx), iyy = uidx(p, 5 + 2 * N + k, gy, gx),
                                 izz = uidx(p, 5 + 3 * N + k, gy, gx);
@@ -797,17 +797,8 @@ __global__ void __launch_bounds__(256, GROW ? 3 : 1) k_finalize_mixed(KParams<fl
             const long long ie = uidx(p, 4, gy, gx);
             u[ie] = (float)((double)u[ie] + drag_heating(p, gx, gy, dt));
         }
-    }
-    if constexpr (GROW && MODE == 0) {   // dust_growth (solve.f90:113)
-        if (p.gw.mode & SHARK_GROWTH_FRAGMENTATION) {
-            if (act) st |= grow_in_finalize(p, u, gx, gy, dt);
-        } else {
-            __syncthreads();             // the block's cells after the drag
-            st |= grow_block_warps(p, blockIdx.x * blockDim.x + p.ng, gy, dt);
-            __syncthreads();
-        }
-    }
-    if (act) {
+    };
+    auto part2 = [&]() {
         if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)
             turb_kick_cell<float>(p, u, gx, gy, dt);
             px = u[uidx(p, 1, gy, gx)];
@@ -896,6 +887,20 @@ __global__ void __launch_bounds__(256, GROW ? 3 : 1) k_finalize_mixed(KParams<fl
         if (!(rho > 0.f)) st |= SHARK_STATUS_NEG_DENSITY;
         if (!isfinite(vx) || !isfinite(vy) || !isfinite(vz)) st |= SHARK_STATUS_NAN;
         if (!(dtc > 0.f) || !isfinite(dtc)) { st |= SHARK_STATUS_DT_UNDERFLOW; dtc = 2e38f; }
+    };
+    if constexpr (GROW && MODE == 0) {   // dust_growth (solve.f90:113) between the two parts
+        if (act) part1();
+        if (p.gw.mode & SHARK_GROWTH_FRAGMENTATION) {
+            if (act) st |= grow_in_finalize(p, u, gx, gy, dt);
+        } else {
+            __syncthreads();             // the block's cells after the drag
+            st |= grow_block_warps(p, blockIdx.x * blockDim.x + p.ng, gy, dt);
+            __syncthreads();
+        }
+        if (act) part2();
+    } else if (act) {
+        part1();
+        part2();
     }
     block_reduce_dt(dtc >= 2e38f ? 2e44 : (double)dtc, st, p.dt_next, p.status);
     if (MODE == 0 && gx < p.ng + p.nx) fill_ghost_images(p, p.u_next, gx, gy);

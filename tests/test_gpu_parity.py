@@ -187,6 +187,28 @@ def test_static_flag_leaves_state_untouched():
         assert np.array_equal(active(cfg, g.download()), active(cfg, u0))
 
 
+def test_timed_run_matches_stepping():
+    """The benchmark helper queues its steps without host waits: the same states and times as
+    stepping one solve() at a time, and ordinary steps carry on after it."""
+    cfg, u0 = setups.si(n=64, ndust=4)
+    with Shark(cfg) as a, Shark(cfg) as b:
+        a.upload(u0)
+        b.upload(u0)
+        a.solve()
+        b.solve()
+        t = 0.0
+        for _ in range(7):
+            t = t + a.solve()
+        t0 = b.time
+        ms = b.timed_run(7)
+        assert ms > 0.0
+        assert b.time - t0 == pytest.approx(t, rel=1e-15)
+        assert np.array_equal(a.download(), b.download())
+        assert a.solve() == b.solve()
+        assert np.array_equal(a.download(), b.download())
+        assert a.sync() == b.sync() == 0
+
+
 def test_unsupported_options_fail_loudly():
     cfg, _ = setups.si(n=32, ndust=2)
     cfg.flags |= K.FLAG_GROWTH
