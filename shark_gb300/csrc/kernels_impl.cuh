@@ -123,6 +123,27 @@ static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
     const int nbx = (p.nx + STRIP_UX - 1) / STRIP_UX;
     const int nstrips = (p.ny + STRIP_H - 1) / STRIP_H;
     dim3 grid(nbx, (nstrips + STRIP_WARPS - 1) / STRIP_WARPS, 1);
+    if constexpr (std::is_same<R, float>::value) {
+        if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0) {
+            // mixed path, Cartesian, Huang & Bai dust: gas and dust strips in one launch
+            const int nbx_g = (p.nx + STRIP_UX - 1) / STRIP_UX, nbx_d = (p.nx + STRIP2_UX - 1) / STRIP2_UX;
+            const int nby = (int)grid.y;
+            const long long nblk = (long long)nbx_g * nby + (long long)nbx_d * nby * p.ndust;
+            const dim3 g1((unsigned)nblk, 1, 1), b1(32 * STRIP_WARPS, 1, 1);
+            const int gs = p.solver == 0 ? 0 : p.solver == 1 ? 1 : 2;
+            switch (p.slope_type * 3 + gs) {
+#define SHARK_K1M(ST, GS) \
+    case ST * 3 + GS: k_flux_strip_mixed<ST, GS><<<g1, b1, 0, v.stream>>>(p, nbx_g, nbx_d, nby); break;
+                SHARK_K1M(0, 0) SHARK_K1M(0, 1) SHARK_K1M(0, 2)
+                SHARK_K1M(1, 0) SHARK_K1M(1, 1) SHARK_K1M(1, 2)
+                SHARK_K1M(2, 0) SHARK_K1M(2, 1) SHARK_K1M(2, 2)
+                SHARK_K1M(3, 0) SHARK_K1M(3, 1)
+                default: k_flux_strip_mixed<3, 2><<<g1, b1, 0, v.stream>>>(p, nbx_g, nbx_d, nby); break;
+#undef SHARK_K1M
+            }
+            return cudaGetLastError();
+        }
+    }
     if (p.ndust > 0) {
         cudaEventRecord(v.fork, v.stream);
         cudaStreamWaitEvent(v.stream2, v.fork, 0);

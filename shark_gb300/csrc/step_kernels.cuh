@@ -147,6 +147,7 @@ __global__ void k_boundaries(KParams<R> p, R* u) {
 
 #include "flux_tile.cuh"
 #include "flux_strip.cuh"
+#include "flux_strip2.cuh"
 
 namespace shark {
 
