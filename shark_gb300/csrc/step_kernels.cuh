@@ -728,7 +728,7 @@ __device__ __forceinline__ void drag_coeffs_mix(double a, float& r, float& w) {
 }
 
 template <int NS, int MODE, bool GROW = false>
-__global__ void __launch_bounds__(256, 3) k_finalize_mixed(KParams<float> p) {
+__global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KParams<float> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;
     const bool drag = MODE == 0 && N > 0 && (p.flags & SHARK_FLAG_DRAG);
@@ -745,12 +745,62 @@ __global__ void __launch_bounds__(256, 3) k_finalize_mixed(KParams<float> p) {
     const bool act = gx < p.ng + p.nx;
     float* u = p.u_next;
     float rho = 0.f, px = 0.f, py = 0.f, pz = 0.f;
+    // compile-time species count: the cell's dust state is loaded once into registers (all loads
+    // in flight together) and the CFL loop reads it there unless a setup hook rewrote it
+    float dr[NMAX], dmx[NMAX], dmy[NMAX], dmz[NMAX];
+    bool in_regs = false;
     // part 1: drag, floor, drag heating; part 2: kick, setup_inloop, CFL.  With growth in between
     // (a block-wide phase) the two parts are separate; otherwise they form one block of code.
     auto part1 = [&]() {
         rho = u[uidx(p, 0, gy, gx)];
         px = u[uidx(p, 1, gy, gx)]; py = u[uidx(p, 2, gy, gx)]; pz = u[uidx(p, 3, gy, gx)];
-        if (drag) {
+        if constexpr (NS > 0) {
+            if (drag) {
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    dr[k] = u[uidx(p, 5 + k, gy, gx)];
+                    dmx[k] = u[uidx(p, 5 + N + k, gy, gx)];
+                    dmy[k] = u[uidx(p, 5 + 2 * N + k, gy, gx)];
+                    dmz[k] = u[uidx(p, 5 + 3 * N + k, gy, gx)];
+                }
+                float rk[NMAX], wk[NMAX];
+                const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
+                const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
+                const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
+                const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
+                float rhon = rho, pnx = px, pny = py, pnz = pz;
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    if (const_ts) { rk[k] = cr[k]; wk[k] = cw[k]; }
+                    else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], rk[k], wk[k]);
+                    pnx += wk[k] * dmx[k];
+                    pny += wk[k] * dmy[k];
+                    pnz += wk[k] * dmz[k];
+                    rhon += wk[k] * dr[k];
+                }
+                const float irhon = 1.0f / rhon;
+                const float vbx = pnx * irhon, vby = pny * irhon, vbz = pnz * irhon;
+                const float fl = rho * (float)p.dust_ratio_min;   // floor (dust_drag.f90:63-73)
+#pragma unroll
+                for (int k = 0; k < NS; ++k) {
+                    const float wr = wk[k] * dr[k];
+                    dmx[k] = dmx[k] * rk[k] + wr * vbx;
+                    dmy[k] = dmy[k] * rk[k] + wr * vby;
+                    dmz[k] = dmz[k] * rk[k] + wr * vbz;
+                    u[uidx(p, 5 + N + k, gy, gx)] = dmx[k];
+                    u[uidx(p, 5 + 2 * N + k, gy, gx)] = dmy[k];
+                    u[uidx(p, 5 + 3 * N + k, gy, gx)] = dmz[k];
+                    if (fl > dr[k]) { dr[k] = fl; u[uidx(p, 5 + k, gy, gx)] = fl; }
+                }
+                if (p.flags & SHARK_FLAG_BACK_REACTION) {
+                    px = vbx * rho; py = vby * rho; pz = vbz * rho;
+                    u[uidx(p, 1, gy, gx)] = px;
+                    u[uidx(p, 2, gy, gx)] = py;
+                    u[uidx(p, 3, gy, gx)] = pz;
+                }
+                in_regs = true;
+            }
+        } else if (drag) {
             float rk[NMAX], wk[NMAX];
             float rhon = rho, pnx = px, pny = py, pnz = pz;
             const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
@@ -807,6 +857,7 @@ __global__ void __launch_bounds__(256, 3) k_finalize_mixed(KParams<float> p) {
         }
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
+            in_regs = false;
             const float om = (float)p.si_om, qsh = (float)p.si_q;
             const float Ohmdt = (float)(p.si_om * dt), O2 = Ohmdt * Ohmdt, inv = 1.0f / (1.0f + O2);
             const float xc = p.xpos[gx] - 0.5f * (float)p.box_l;
@@ -828,6 +879,7 @@ __global__ void __launch_bounds__(256, 3) k_finalize_mixed(KParams<float> p) {
             }
         }
         if (MODE == 0 && p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<float, float>(p, u, gx, gy, dt)) {
+            in_regs = false;
             rho = u[uidx(p, 0, gy, gx)];
             px = u[uidx(p, 1, gy, gx)];
             py = u[uidx(p, 2, gy, gx)];
@@ -864,12 +916,21 @@ __global__ void __launch_bounds__(256, 3) k_finalize_mixed(KParams<float> p) {
         } else if (fk) {
             fmx = fabsf(p.fgrav[gx]);   // polar disk: the point-mass force, the same on gas and dust
         }
+#pragma unroll
         for (int k = 0; k < N; ++k) {
-            const float rd = u[uidx(p, 5 + k, gy, gx)];
+            float rd, mx, my, mz;
+            if (NS > 0 && in_regs) {
+                rd = dr[k < NMAX ? k : 0]; mx = dmx[k < NMAX ? k : 0]; my = dmy[k < NMAX ? k : 0]; mz = dmz[k < NMAX ? k : 0];
+            } else {
+                rd = u[uidx(p, 5 + k, gy, gx)];
+                mx = u[uidx(p, 5 + N + k, gy, gx)];
+                my = u[uidx(p, 5 + 2 * N + k, gy, gx)];
+                mz = u[uidx(p, 5 + 3 * N + k, gy, gx)];
+            }
             const float ird = 1.0f / rd;
-            const float vdx = u[uidx(p, 5 + N + k, gy, gx)] * ird;
-            const float vdy = u[uidx(p, 5 + 2 * N + k, gy, gx)] * ird;
-            const float vdz = u[uidx(p, 5 + 3 * N + k, gy, gx)] * ird;
+            const float vdx = mx * ird;
+            const float vdy = my * ird;
+            const float vdz = mz * ird;
             vv = fabsf(vdx) + fabsf(vdy) + fabsf(vdz);
             vmax = fmaxf(vmax, vv);
             if (fk_si) {
