@@ -744,6 +744,11 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
     unsigned int st = 0;
     const bool act = gx < p.ng + p.nx;
     float* u = p.u_next;
+    // this cell's element of plane 0; variable v sits v planes further (32-bit plane offsets: the
+    // context guarantees nvar * plane < 2^31)
+    float* const uc = u + ((long long)gy * p.pitch + gx);
+    const float* const ucur = p.u_cur + ((long long)gy * p.pitch + gx);
+    const int pl = (int)p.plane;
     float rho = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     // compile-time species count: the cell's dust state is loaded once into registers (all loads
     // in flight together) and the CFL loop reads it there unless a setup hook rewrote it
@@ -752,19 +757,19 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
     // part 1: drag, floor, drag heating; part 2: kick, setup_inloop, CFL.  With growth in between
     // (a block-wide phase) the two parts are separate; otherwise they form one block of code.
     auto part1 = [&]() {
-        rho = u[uidx(p, 0, gy, gx)];
-        px = u[uidx(p, 1, gy, gx)]; py = u[uidx(p, 2, gy, gx)]; pz = u[uidx(p, 3, gy, gx)];
+        rho = uc[(0) * pl];
+        px = uc[(1) * pl]; py = uc[(2) * pl]; pz = uc[(3) * pl];
         if constexpr (NS > 0) {
             if (drag) {
 #pragma unroll
                 for (int k = 0; k < NS; ++k) {
-                    dr[k] = u[uidx(p, 5 + k, gy, gx)];
-                    dmx[k] = u[uidx(p, 5 + N + k, gy, gx)];
-                    dmy[k] = u[uidx(p, 5 + 2 * N + k, gy, gx)];
-                    dmz[k] = u[uidx(p, 5 + 3 * N + k, gy, gx)];
+                    dr[k] = uc[(5 + k) * pl];
+                    dmx[k] = uc[(5 + N + k) * pl];
+                    dmy[k] = uc[(5 + 2 * N + k) * pl];
+                    dmz[k] = uc[(5 + 3 * N + k) * pl];
                 }
                 float rk[NMAX], wk[NMAX];
-                const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
+                const float rho_old = ucur[(0) * pl];
                 const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
                 const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
                 const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
@@ -787,23 +792,23 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                     dmx[k] = dmx[k] * rk[k] + wr * vbx;
                     dmy[k] = dmy[k] * rk[k] + wr * vby;
                     dmz[k] = dmz[k] * rk[k] + wr * vbz;
-                    u[uidx(p, 5 + N + k, gy, gx)] = dmx[k];
-                    u[uidx(p, 5 + 2 * N + k, gy, gx)] = dmy[k];
-                    u[uidx(p, 5 + 3 * N + k, gy, gx)] = dmz[k];
-                    if (fl > dr[k]) { dr[k] = fl; u[uidx(p, 5 + k, gy, gx)] = fl; }
+                    uc[(5 + N + k) * pl] = dmx[k];
+                    uc[(5 + 2 * N + k) * pl] = dmy[k];
+                    uc[(5 + 3 * N + k) * pl] = dmz[k];
+                    if (fl > dr[k]) { dr[k] = fl; uc[(5 + k) * pl] = fl; }
                 }
                 if (p.flags & SHARK_FLAG_BACK_REACTION) {
                     px = vbx * rho; py = vby * rho; pz = vbz * rho;
-                    u[uidx(p, 1, gy, gx)] = px;
-                    u[uidx(p, 2, gy, gx)] = py;
-                    u[uidx(p, 3, gy, gx)] = pz;
+                    uc[(1) * pl] = px;
+                    uc[(2) * pl] = py;
+                    uc[(3) * pl] = pz;
                 }
                 in_regs = true;
             }
         } else if (drag) {
             float rk[NMAX], wk[NMAX];
             float rhon = rho, pnx = px, pny = py, pnz = pz;
-            const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
+            const float rho_old = ucur[(0) * pl];
             const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
             const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
             const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
@@ -812,10 +817,10 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                 if (const_ts) { r = cr[k]; w = cw[k]; }
                 else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], r, w);
                 if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
-                pnx += w * u[uidx(p, 5 + N + k, gy, gx)];
-                pny += w * u[uidx(p, 5 + 2 * N + k, gy, gx)];
-                pnz += w * u[uidx(p, 5 + 3 * N + k, gy, gx)];
-                rhon += w * u[uidx(p, 5 + k, gy, gx)];
+                pnx += w * uc[(5 + N + k) * pl];
+                pny += w * uc[(5 + 2 * N + k) * pl];
+                pnz += w * uc[(5 + 3 * N + k) * pl];
+                rhon += w * uc[(5 + k) * pl];
             }
             const float irhon = 1.0f / rhon;
             const float vbx = pnx * irhon, vby = pny * irhon, vbz = pnz * irhon;
@@ -824,7 +829,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                 if (NS > 0) { r = rk[k < NMAX ? k : 0]; w = wk[k < NMAX ? k : 0]; }
                 else if (const_ts) { r = cr[k]; w = cw[k]; }
                 else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], r, w);
-                const float rd = u[uidx(p, 5 + k, gy, gx)];
+                const float rd = uc[(5 + k) * pl];
                 const long long ixx = uidx(p, 5 + N + k, gy, gx), iyy = uidx(p, 5 + 2 * N + k, gy, gx),
                                 izz = uidx(p, 5 + 3 * N + k, gy, gx);
                 const float wr = w * rd;
@@ -834,9 +839,9 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
             }
             if (p.flags & SHARK_FLAG_BACK_REACTION) {
                 px = vbx * rho; py = vby * rho; pz = vbz * rho;
-                u[uidx(p, 1, gy, gx)] = px;
-                u[uidx(p, 2, gy, gx)] = py;
-                u[uidx(p, 3, gy, gx)] = pz;
+                uc[(1) * pl] = px;
+                uc[(2) * pl] = py;
+                uc[(3) * pl] = pz;
             }
             const float fl = rho * (float)p.dust_ratio_min;   // floor (dust_drag.f90:63-73)
             for (int k = 0; k < N; ++k) {
@@ -852,8 +857,8 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
     auto part2 = [&]() {
         if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)
             turb_kick_cell<float>(p, u, gx, gy, dt);
-            px = u[uidx(p, 1, gy, gx)];
-            py = u[uidx(p, 2, gy, gx)];
+            px = uc[(1) * pl];
+            py = uc[(2) * pl];
         }
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
@@ -866,13 +871,13 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                 const float uz = pz / rho, vx = px / rho;
                 pz = rho * (uz * (1.f - O2) + 2.f * vx * Ohmdt + AA * O2) * inv;
                 px = rho * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
-                u[uidx(p, 3, gy, gx)] = pz;
-                u[uidx(p, 1, gy, gx)] = px;
+                uc[(3) * pl] = pz;
+                uc[(1) * pl] = px;
             }
             AA = 2.0f * qsh * om * xc;
             for (int k = 0; k < N; ++k) {
                 const long long iz = uidx(p, 5 + 3 * N + k, gy, gx), ixx = uidx(p, 5 + N + k, gy, gx);
-                const float d = u[uidx(p, 5 + k, gy, gx)];
+                const float d = uc[(5 + k) * pl];
                 const float uz = u[iz] / d, vx = u[ixx] / d;
                 u[iz] = d * (uz * (1.f - O2) + 2.f * vx * Ohmdt + AA * O2) * inv;
                 u[ixx] = d * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
@@ -880,10 +885,10 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         }
         if (MODE == 0 && p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<float, float>(p, u, gx, gy, dt)) {
             in_regs = false;
-            rho = u[uidx(p, 0, gy, gx)];
-            px = u[uidx(p, 1, gy, gx)];
-            py = u[uidx(p, 2, gy, gx)];
-            pz = u[uidx(p, 3, gy, gx)];
+            rho = uc[(0) * pl];
+            px = uc[(1) * pl];
+            py = uc[(2) * pl];
+            pz = uc[(3) * pl];
         }
         // ---- courant on the final state (src/solver/courant.f90:11-124), FP32 ----------------------
         const float cfl = (float)p.cfl;
@@ -892,7 +897,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         float cs;
         if (p.iso == 1) cs = p.cs[gx];
         else {
-            const float E = u[uidx(p, 4, gy, gx)];
+            const float E = uc[(4) * pl];
             const float ekin = 0.5f * rho * (vx * vx) + 0.5f * rho * (vy * vy) + 0.5f * rho * (vz * vz);
             const float P = fmaxf((float)(p.gamma - 1.0) * (E - ekin), (float)p.smallp);
             cs = sqrtf((float)p.gamma * P / fmaxf(rho, (float)p.smallr));
@@ -909,10 +914,11 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         const bool fk = fk_si || ((p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_DISK_POLAR);
         const float om = (float)p.si_om, qsh = (float)p.si_q;
         const float xc = p.xpos[gx] - 0.5f * (float)p.box_l;
+        float fmx2 = 0.f;                 // SI: the largest |f|^2, one square root after the loop
         if (fk_si) {
             const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vz - 2.0f * (float)p.si_r0 * om * (float)p.si_eta;
             const float f3 = 2.0f * om * vx;
-            fmx = sqrtf(f1 * f1 + f3 * f3);
+            fmx2 = f1 * f1 + f3 * f3;
         } else if (fk) {
             fmx = fabsf(p.fgrav[gx]);   // polar disk: the point-mass force, the same on gas and dust
         }
@@ -922,10 +928,10 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
             if (NS > 0 && in_regs) {
                 rd = dr[k < NMAX ? k : 0]; mx = dmx[k < NMAX ? k : 0]; my = dmy[k < NMAX ? k : 0]; mz = dmz[k < NMAX ? k : 0];
             } else {
-                rd = u[uidx(p, 5 + k, gy, gx)];
-                mx = u[uidx(p, 5 + N + k, gy, gx)];
-                my = u[uidx(p, 5 + 2 * N + k, gy, gx)];
-                mz = u[uidx(p, 5 + 3 * N + k, gy, gx)];
+                rd = uc[(5 + k) * pl];
+                mx = uc[(5 + N + k) * pl];
+                my = uc[(5 + 2 * N + k) * pl];
+                mz = uc[(5 + 3 * N + k) * pl];
             }
             const float ird = 1.0f / rd;
             const float vdx = mx * ird;
@@ -936,11 +942,12 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
             if (fk_si) {
                 const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vdz;
                 const float f3 = 2.0f * om * vdx;
-                fmx = fmaxf(fmx, sqrtf(f1 * f1 + f3 * f3));
+                fmx2 = fmaxf(fmx2, f1 * f1 + f3 * f3);
             }
             if (!(rd > 0.f)) st |= SHARK_STATUS_NEG_DENSITY;
             if (!isfinite(vv)) st |= SHARK_STATUS_NAN;
         }
+        if (fk_si) fmx = sqrtf(fmx2);
         dtc = cfl * dxx / fabsf(vmax);
         if (fk && vv != 0.f) {
             const float fratio = fmaxf(fmx * dxx / (vv * vv), 1e-3f);
