@@ -1104,6 +1104,18 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     return SHARK_OK;
 }
 
+// Pinned or registered host memory (cudaHostAlloc / cudaHostRegister) is read and written by the
+// conversion kernels directly over the host link, which moves the bytes no slower than a copy
+// engine and saves the staging pass; any other pointer goes through the FP64 staging buffer.
+static const void* pinned_device_alias(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int32_t shark_gpu_upload(shark_gpu_ctx* c, const double* u_prim, int64_t ncells, int32_t nvar) {
     if (!c || !u_prim) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
     const shark::DeviceView& v = c->v;
@@ -1114,19 +1126,24 @@ int32_t shark_gpu_upload(shark_gpu_ctx* c, const double* u_prim, int64_t ncells,
     // drain any readbacks still in flight: the new state starts a new dt sequence
     for (int s = 0; s < 2; ++s) if (c->pending_read[s]) { cudaEventSynchronize(c->ev_read[s]); c->pending_read[s] = false; }
     const size_t bytes = (size_t)ncells * nvar * sizeof(double);
-    if (!c->staging) CUDA_TRY(cudaMalloc(&c->staging, bytes));
-    CUDA_TRY(cudaMemcpyAsync(c->staging, u_prim, bytes, cudaMemcpyHostToDevice, c->stream));
+    const double* src = static_cast<const double*>(pinned_device_alias(u_prim));
+    if (!src) {
+        if (!c->staging) CUDA_TRY(cudaMalloc(&c->staging, bytes));
+        CUDA_TRY(cudaMemcpyAsync(c->staging, u_prim, bytes, cudaMemcpyHostToDevice, c->stream));
+        src = c->staging;
+    }
     c->v.cur = 0;
-    for (int b = 0; b < c->v.nbuf; ++b) {
-        cudaError_t e = is_mixed(c) ? shark::launch_from_fortran<float>(c->v, c->staging, c->ubuf[b])
-                                    : shark::launch_from_fortran<double>(c->v, c->staging, c->ubuf[b]);
+    {
+        cudaError_t e = is_mixed(c) ? shark::launch_from_fortran<float>(c->v, src, c->ubuf[0])
+                                    : shark::launch_from_fortran<double>(c->v, src, c->ubuf[0]);
         if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "upload conversion: %s", cudaGetErrorString(e));
     }
+    const size_t sbytes = c->state_bytes;
+    for (int b = 1; b < c->v.nbuf; ++b)
+        CUDA_TRY(cudaMemcpyAsync(c->ubuf[b], c->ubuf[0], sbytes, cudaMemcpyDeviceToDevice, c->stream));
     if (c->uinit && !c->have_uinit) {
         // the first state uploaded is the disk's initial state (uprim_condinit, setup.f90:79-83)
-        cudaError_t e = is_mixed(c) ? shark::launch_from_fortran<float>(c->v, c->staging, c->uinit)
-                                    : shark::launch_from_fortran<double>(c->v, c->staging, c->uinit);
-        if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "upload conversion: %s", cudaGetErrorString(e));
+        CUDA_TRY(cudaMemcpyAsync(c->uinit, c->ubuf[0], sbytes, cudaMemcpyDeviceToDevice, c->stream));
         c->have_uinit = true;
     }
     CUDA_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
@@ -1219,12 +1236,17 @@ int32_t shark_gpu_download(shark_gpu_ctx* c, double* u_prim, double* q) {
     if (!c->uploaded) return fail(SHARK_ERR_STATE, "download before upload");
     const shark::DeviceView& v = c->v;
     const size_t n = (size_t)v.nx_max * v.ny_max * v.nvar;
-    if (!c->staging) CUDA_TRY(cudaMalloc(&c->staging, n * sizeof(double)));
     if (u_prim) {
-        cudaError_t e = is_mixed(c) ? shark::launch_to_fortran<float>(v, v.u[v.cur], c->staging)
-                                    : shark::launch_to_fortran<double>(v, v.u[v.cur], c->staging);
+        double* dst = static_cast<double*>(const_cast<void*>(pinned_device_alias(u_prim)));
+        if (!dst) {
+            if (!c->staging) CUDA_TRY(cudaMalloc(&c->staging, n * sizeof(double)));
+            dst = c->staging;
+        }
+        cudaError_t e = is_mixed(c) ? shark::launch_to_fortran<float>(v, v.u[v.cur], dst)
+                                    : shark::launch_to_fortran<double>(v, v.u[v.cur], dst);
         if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "download conversion: %s", cudaGetErrorString(e));
-        CUDA_TRY(cudaMemcpyAsync(u_prim, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        if (dst == c->staging)
+            CUDA_TRY(cudaMemcpyAsync(u_prim, c->staging, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         CUDA_TRY(cudaStreamSynchronize(c->stream));
     }
     if (q) return shark_gpu_ctoprim(c, q, nullptr);

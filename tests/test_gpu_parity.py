@@ -209,6 +209,34 @@ def test_timed_run_matches_stepping():
         assert a.sync() == b.sync() == 0
 
 
+@pytest.mark.parametrize("make", ["si_mixed", "si_fp64", "disk_mixed"])
+def test_pinned_host_buffers_match_pageable(make):
+    """Pinned host buffers are read and written by the conversion kernels directly; pageable ones go
+    through the staging copy.  Both give the same states, the polar disk's relaxation reference
+    (the first upload) included."""
+    torch = pytest.importorskip("torch")
+    if make == "disk_mixed":
+        cfg, u0 = setups.disk_polar(nr=40, nphi=32, ndust=2, noise=1e-2, seed=3, fargo=True, precision=K.PREC_MIXED)
+    else:
+        cfg, u0 = setups.si(n=64, ndust=4, precision=K.PREC_MIXED if make == "si_mixed" else K.PREC_FP64)
+    pin = torch.empty(u0.size, dtype=torch.float64).pin_memory()
+    pin.numpy()[:] = u0
+    with Shark(cfg) as a, Shark(cfg) as b:
+        a.upload(u0)
+        b.upload_ptr(pin.data_ptr())
+        for _ in range(4):
+            assert a.solve() == b.solve()
+        ua = a.download()
+        pin.numpy()[:] = 0.0
+        b.download_ptr(pin.data_ptr())
+        assert np.array_equal(ua, pin.numpy())
+        a.upload(ua)
+        b.upload_ptr(pin.data_ptr())
+        for _ in range(2):
+            assert a.solve() == b.solve()
+        assert np.array_equal(a.download(), b.download())
+
+
 def test_unsupported_options_fail_loudly():
     cfg, _ = setups.si(n=32, ndust=2)
     cfg.flags |= K.FLAG_GROWTH
