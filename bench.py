@@ -16,6 +16,14 @@ one species (gas counts as one) x one step, so one step is 1024^2 x 9 = 9,437,18
   cpu_baseline the C++ FP64 OpenMP oracle (a restatement of the Fortran, "port") on the host cores,
               a bounded sample of the same workload.
 
+  workloads   (default SI run) the polar disk with FARGO, growth and charging (512 x 1024, 16
+              species) and the driven dusty turbulence with charging and growth (2048^2, 32
+              species): mixed and FP64 ms/step, their L1 distance, charging iterations.
+  charging_mlp (default SI run) the charging network trained on the GPU on (state, converged psi)
+              pairs of dusty boxes, then the cold-start Newton iterations on the 2048^2 box with
+              and without its seed, at the same residual tolerance.
+
+`--workload disk|turb` prints the same line for one of those two configurations instead.
 `--impl reference` times that CPU implementation alone on the host cores (rank 0 only).
 Multi-GPU (torchrun): independent replicas, one per GPU; value = total updates / max time.
 """
@@ -40,10 +48,37 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
-def workload(args, precision):
+def workload(args, precision, name=None):
     from shark_gb300 import setups
-    cfg, u0 = setups.si(n=args.n, ndust=args.ndust, precision=precision, noise=1e-3, seed=1)
-    return cfg, u0
+    name = name or args.workload
+    if name == "disk":   # polar disk 1-100 AU, FARGO, growth, charging (MLP-seedable Newton)
+        return setups.disk_polar_au(growth=True, precision=precision)
+    if name == "turb":   # driven dusty turbulence, charging and growth every step
+        return setups.dusty_turb(n=2048, ndust=32, forcing=True, charging=True, growth=True, precision=precision)
+    return setups.si(n=args.n, ndust=args.ndust, precision=precision, noise=1e-3, seed=1)
+
+
+def describe(args, cfg):
+    if args.workload == "disk":
+        return (f"polar disk {cfg.nx}x{cfg.ny} (log r 1-100 AU x phi), {cfg.ndust} dust species 1 um-1 cm, FARGO, "
+                f"growth, charging, mixed precision")
+    if args.workload == "turb":
+        return (f"driven dusty turbulence {cfg.nx}x{cfg.ny}, {cfg.ndust} dust species 0.01 um-1 mm, OU forcing, "
+                f"charging and growth every step, mixed precision")
+    return f"SI shearing box {cfg.nx}x{cfg.ny} active cells, {cfg.ndust} dust species, mixed precision"
+
+
+def launches_per_step(cfg):
+    """Kernels of one mixed-precision step: k_prepare_step, charging, forcing update, K1 (one launch
+    on Cartesian grids with the Huang & Bai dust solver, gas and dust launches otherwise), FARGO, K2."""
+    from shark_gb300 import config as K
+    n = 2
+    n += 1 if cfg.flags & K.FLAG_CHARGING else 0
+    n += 1 if getattr(cfg, "turb_mach", 0.0) > 0.0 else 0
+    cart_hb = cfg.geom != 2 and cfg.solverdust == 0 and cfg.ndust > 0
+    n += 1 if (cart_hb or cfg.ndust == 0) else 2
+    n += 1 if cfg.flags & K.FLAG_FARGO else 0
+    return n
 
 
 def peaks():
@@ -132,8 +167,17 @@ def cpu_oracle_rate(args, max_seconds=25.0, n_small=None):
     from oracle.oracle import Oracle
     from shark_gb300 import config as K
     cores = os.cpu_count() or 1
-    cfg, u0 = workload(args, K.PREC_FP64)
-    sample = f"SI {args.n}x{args.n}, {args.ndust} species"
+    if args.workload == "turb":
+        from shark_gb300 import setups
+        cfg, u0 = setups.dusty_turb(n=128, ndust=32, forcing=True, charging=True, growth=True)
+        sample = "driven dusty turbulence 128x128 (sub-box of the 2048^2 case), 32 species, charging and growth"
+    elif args.workload == "disk":
+        from shark_gb300 import setups
+        cfg, u0 = setups.disk_polar_au(nr=128, nphi=256, growth=True)
+        sample = "polar disk 128x256 (coarser grid of the 512x1024 case), 16 species, FARGO, growth, charging"
+    else:
+        cfg, u0 = workload(args, K.PREC_FP64)
+        sample = f"SI {args.n}x{args.n}, {args.ndust} species"
     if n_small:
         from shark_gb300 import setups
         cfg, u0 = setups.si(n=n_small, ndust=args.ndust, noise=1e-3, seed=1)
@@ -216,11 +260,11 @@ def run_gpu(args):
         if world > 1:
             torch.distributed.barrier()
 
-    zs_step = args.n * args.n * (args.ndust + 1)
-
     # ---- mixed path, state resident -----------------------------------------------------------
     cfg_m, u0 = workload(args, K.PREC_MIXED)
     cfg_m.device = local_rank
+    zs_step = cfg_m.nx * cfg_m.ny * (cfg_m.ndust + 1)
+    fp64_steps = args.steps if args.workload == "si" else min(args.steps, 3)
     gm = Shark(cfg_m)
     gm.upload(u0)
     for _ in range(args.warmup):
@@ -249,10 +293,10 @@ def run_gpu(args):
     gd.upload(u0)
     for _ in range(args.warmup):
         gd.solve()
-    ms_d = gd.timed_run(args.steps)
-    gd.run_steps(steps_done_m - args.warmup - args.steps)
+    ms_d = gd.timed_run(fp64_steps)
+    gd.run_steps(steps_done_m - args.warmup - fp64_steps)
     u_fp64 = gd.download()
-    value_fp64 = zs_step * args.steps / (ms_d * 1e-3)
+    value_fp64 = zs_step * fp64_steps / (ms_d * 1e-3)
     l1 = rel_l1_max(cfg_m, u_mixed, u_fp64)
     kt_d = gd.kernel_times(3)
     gd.close()
@@ -291,13 +335,14 @@ def run_gpu(args):
     # ---- roofline of the flux/update kernel ---------------------------------------------------
     hbm, peak_kind = peaks()
     nvar = cfg_m.nvar
-    alg_bytes_k1 = 2 * 4 * nvar * args.n * args.n            # read + write each conserved value once
+    ncell = cfg_m.nx * cfg_m.ny
+    alg_bytes_k1 = 2 * 4 * nvar * ncell                      # read + write each conserved value once
     k1_s = kt[1] * 1e-3
     achieved = alg_bytes_k1 / k1_s / 1e9
-    alg_bytes_k2 = 4 * (7 * (args.ndust + 1) + args.ndust) * args.n * args.n
+    alg_bytes_k2 = 4 * (7 * (cfg_m.ndust + 1) + cfg_m.ndust) * ncell
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "k_flux_traffic.txt")
-    if os.path.exists(tfile) and args.n == 1024 and args.ndust == 8:
+    if os.path.exists(tfile) and args.workload == "si" and args.n == 1024 and args.ndust == 8:
         with open(tfile) as f:
             for line in f:
                 if line.startswith("bytes_per_launch_full_size:"):
@@ -316,11 +361,11 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (flux/update) + f64 (drag, dt)",
         "data": "synthetic",
-        "config": {"workload": f"SI shearing box {args.n}x{args.n} active cells, {args.ndust} dust species, "
-                               f"mixed precision", "zone_species_per_step": zs_step,
+        "config": {"workload": describe(args, cfg_m), "zone_species_per_step": zs_step,
                    "parallelism": "replicas only" if world > 1 else "single GPU",
-                   "l2": "state (2 x 160 MB ping-pong, FP32) larger than the 129 MB L2; no flush"},
-        "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": ms_d / args.steps,
+                   "l2": f"state (2 x {cfg_m.ncells * nvar * 4 / 1e6:.0f} MB ping-pong, FP32) larger than the "
+                         f"129 MB L2; no flush"},
+        "fp64": {"value": value_fp64, "unit": UNIT, "ms_per_step": ms_d / fp64_steps, "steps": fp64_steps,
                  "mixed_over_fp64": value / world / value_fp64,
                  "l1_mixed_vs_fp64": l1, "l1_note": f"max relative L1 over the {nvar} conserved fields after "
                                                     f"{steps_done_m} steps from the same state",
@@ -337,12 +382,139 @@ def run_gpu(args):
                 "resident_value": zs_step * e2e_steps / el_res,
                 "resident_note": "state kept on the device, per step shark_gpu_step with its 12-byte dt/status readback"},
         "cpu_baseline": cpu,
-        "gpu_launches": 4 * args.steps,
-        "gpu_launches_note": "per step: k_reset_dt, k_flux_strip (gas, side stream), k_flux_strip (dust), k_finalize",
+        "gpu_launches": launches_per_step(cfg_m) * args.steps,
+        "gpu_launches_note": launches_note(cfg_m),
         "status": st,
         "clocks": clocks.summary(),
     }
+    if args.workload == "si" and world == 1 and not args.no_extra:
+        line["workloads"] = {name: config_leg(args, name, local_rank) for name in ("disk", "turb")}
+        line["charging_mlp"] = mlp_leg(local_rank)
     print(json.dumps(line), flush=True)
+
+
+def launches_note(cfg):
+    from shark_gb300 import config as K
+    parts = ["k_prepare_step"]
+    if cfg.flags & K.FLAG_CHARGING:
+        parts.append("k_charge")
+    if getattr(cfg, "turb_mach", 0.0) > 0.0:
+        parts.append("k_ou_update")
+    if cfg.geom != 2 and cfg.solverdust == 0 and cfg.ndust > 0:
+        parts.append("k_flux_strip_mixed (gas and dust strips)")
+    else:
+        parts.append("k_flux_strip (gas, side stream) + k_flux_strip (dust)")
+    if cfg.flags & K.FLAG_FARGO:
+        parts.append("k_fargo")
+    parts.append("k_finalize_mixed")
+    return "per step: " + ", ".join(parts)
+
+
+def config_leg(args, name, device, mixed_steps=5, fp64_steps=2):
+    """Mixed and FP64 timing of one of the two larger configurations, their L1 distance after the
+    same number of steps from the same state, and the charging iterations of the last step."""
+    from shark_gb300 import config as K
+    from shark_gb300.solver import Shark
+    out = {}
+    ctx = {}
+    for prec, ns in ((K.PREC_MIXED, mixed_steps), (K.PREC_FP64, fp64_steps)):
+        cfg, u0 = workload(args, prec, name)
+        cfg.device = device
+        g = Shark(cfg)
+        g.upload(u0)
+        for _ in range(2):
+            g.solve()
+        ms = g.timed_run(ns)
+        kt = g.kernel_times(2)
+        st = g.sync()
+        zs = cfg.nx * cfg.ny * (cfg.ndust + 1)
+        _, nonconv, tot = g.charge_stats()
+        out["mixed" if prec == K.PREC_MIXED else "fp64"] = {
+            "value": zs * ns / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / ns, "steps": ns,
+            "kernel_ms": {"charge_forcing": kt[0], "flux_update": kt[1], "drag_growth_dt": kt[2], "step": kt[3]},
+            "status": st, "charging_nonconverged_cells": nonconv, "charging_iterations_per_cell": tot / (cfg.nx * cfg.ny)}
+        ctx[prec] = (cfg, g)
+        del u0
+    (cm, gm), (cd, gd) = ctx[K.PREC_MIXED], ctx[K.PREC_FP64]
+    nm = 2 + mixed_steps + 2
+    gd.run_steps(nm - (2 + fp64_steps + 2))
+    gd.sync()
+    out["l1_mixed_vs_fp64"] = rel_l1_max(cm, gm.download(), gd.download())
+    out["l1_note"] = f"max relative L1 over the {cm.nvar} conserved fields after {nm} steps from the same state"
+    out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    out["workload"] = describe(argparse.Namespace(workload=name), cm)
+    gm.close()
+    gd.close()
+    return out
+
+
+def noisy_box(cfg, u, seed, amp=0.5):
+    """Lognormal density structure on a dusty box (gas and each species independently, momenta
+    scaled alike): states spanning the charging network's input range."""
+    from shark_gb300 import setups
+    rng = np.random.default_rng(seed)
+    g = u.reshape(cfg.nvar, -1)
+    f = np.exp(amp * rng.standard_normal(cfg.ncells))
+    g[:5] *= f
+    N = cfg.ndust
+    for k in range(N):
+        fk = f * np.exp(amp * rng.standard_normal(cfg.ncells))
+        for c in range(4):
+            g[5 + c * N + k] *= fk
+    setups.periodic_boundaries(cfg, u)
+    return u
+
+
+def mlp_leg(device):
+    """Train the charging network on the GPU (forward/backward kernels, Adam) on (state, converged
+    psi) pairs that the charging solver produces on dusty boxes over a range of densities, then
+    charge the 2048^2, 32-species box from a cold start with and without the network's seed."""
+    from shark_gb300 import config as K, setups
+    from shark_gb300.solver import Shark
+    t0 = time.perf_counter()
+    cfg, u0 = setups.dusty_turb(n=128, ndust=32, charging=True)
+    cfg.device = device
+    n = 0
+    with Shark(cfg) as g:
+        for f in (0.03, 0.1, 0.3, 1.0, 3.0, 10.0, 30.0):
+            for seed in (11, 12):
+                c, u = setups.dusty_turb(n=128, ndust=32, charging=True)
+                g.upload(noisy_box(c, u, seed) * f)
+                n = g.mlp_collect(capacity=1 << 20)
+        loss1 = g.mlp_train(3000, batch=2048, lr=2e-3, seed=7)
+        loss2 = g.mlp_train(3000, batch=2048, lr=3e-4, seed=8)
+        blob = g.mlp_save()
+    t_train = time.perf_counter() - t0
+    res = {}
+    for mode in ("cold", "seeded"):
+        c, u = setups.dusty_turb(n=2048, ndust=32, forcing=True, charging=True, growth=True, precision=K.PREC_MIXED)
+        u = noisy_box(c, u, 99)                      # held out: a seed the training did not see
+        c.device = device
+        if mode == "seeded":
+            c.chg_mode |= K.CHARGE_MLP_SEED
+        with Shark(c) as g:
+            if mode == "seeded":
+                g.mlp_load(blob)
+            g.upload(u)
+            g.charge_reset()
+            g.charge()
+            hist, nonconv, tot = g.charge_stats()
+            ch = g.download_charge()
+        res[mode] = (tot, nonconv, ch["psi"], ch["iters"])
+        del u
+    cells = 2048 * 2048
+    conv = res["cold"][3] < c.chg_nitermax          # cells the cold start converges
+    dpsi = float(np.max(np.abs(res["seeded"][2][conv] - res["cold"][2][conv]) / np.abs(res["cold"][2][conv])))
+    return {"training_pairs": int(n), "train_seconds": t_train,
+            "loss_first_50": float(np.mean(loss1[:50])), "loss_last_200": float(np.mean(loss2[-200:])),
+            "newton_iterations_per_cell_cold": res["cold"][0] / cells,
+            "newton_iterations_per_cell_seeded": res["seeded"][0] / cells,
+            "iteration_ratio": res["cold"][0] / max(res["seeded"][0], 1),
+            "nonconverged_cells_cold": int(res["cold"][1]), "nonconverged_cells_seeded": int(res["seeded"][1]),
+            "max_rel_psi_difference": dpsi,
+            "note": "2048^2 dusty box, 32 species, lognormal density structure (held-out seed), mixed precision, "
+                    "cold start from psi0 vs the network's seed, residual tolerance chg_eps in both; training on "
+                    "128^2 boxes at 7 density factors x 2 seeds"}
 
 
 def main():
@@ -354,7 +526,11 @@ def main():
     ap.add_argument("--n", type=int, default=1024)
     ap.add_argument("--ndust", type=int, default=8)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true", help="skip the disk/turbulence and network legs")
+    ap.add_argument("--workload", default="si", choices=["si", "disk", "turb"])
     args = ap.parse_args()
+    if args.workload != "si" and "--steps" not in sys.argv:
+        args.steps = 5
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
