@@ -53,8 +53,9 @@ def workload(args, precision, name=None):
     name = name or args.workload
     if name == "disk":   # polar disk 1-100 AU, FARGO, growth, charging (MLP-seedable Newton)
         return setups.disk_polar_au(growth=True, precision=precision)
-    if name == "turb":   # driven dusty turbulence, charging and growth every step
-        return setups.dusty_turb(n=2048, ndust=32, forcing=True, charging=True, growth=True, precision=precision)
+    if name == "turb":   # driven dusty turbulence, charging and growth every step (--n: smaller boxes)
+        n = args.n if (name == args.workload and getattr(args, "n_given", False)) else 2048
+        return setups.dusty_turb(n=n, ndust=32, forcing=True, charging=True, growth=True, precision=precision)
     return setups.si(n=args.n, ndust=args.ndust, precision=precision, noise=1e-3, seed=1)
 
 
@@ -531,6 +532,7 @@ def main():
     args = ap.parse_args()
     if args.workload != "si" and "--steps" not in sys.argv:
         args.steps = 5
+    args.n_given = "--n" in sys.argv
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -257,6 +257,34 @@ __device__ __forceinline__ void block_reduce_dt(double dtc, unsigned int st, uns
     }
 }
 
+// FP32 form for the mixed path, whose CFL candidates are FP32: the min runs in FP32 (the FP64
+// pipe is narrow) and the block's result is widened once for the atomic.  No candidate: 2e38f.
+__device__ __forceinline__ void block_reduce_dt_f(float dtc, unsigned int st, unsigned long long* dt_next,
+                                                  unsigned int* status) {
+    for (int o = 16; o > 0; o >>= 1) {
+        dtc = fminf(dtc, __shfl_xor_sync(0xffffffffu, dtc, o));
+        st |= __shfl_xor_sync(0xffffffffu, st, o);
+    }
+    __shared__ float wminf[32];
+    __shared__ unsigned int wstf[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { wminf[wid] = dtc; wstf[wid] = st; }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        dtc = lane < nw ? wminf[lane] : 2e38f;
+        st = lane < nw ? wstf[lane] : 0u;
+        for (int o = 16; o > 0; o >>= 1) {
+            dtc = fminf(dtc, __shfl_xor_sync(0xffffffffu, dtc, o));
+            st |= __shfl_xor_sync(0xffffffffu, st, o);
+        }
+        if (lane == 0) {
+            atomic_min_dt(dt_next, dtc >= 2e38f ? 2e44 : (double)dtc);
+            if (st) atomicOr(status, st);
+        }
+    }
+}
+
 // Sound speed of the cell at the start of the step: the isothermal column value, or ctoprim's
 // sqrt(gamma P / max(rho, smallr)) of the adiabatic state (solve.f90:205-233).
 template <typename R>
@@ -971,7 +999,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         part1();
         part2();
     }
-    block_reduce_dt(dtc >= 2e38f ? 2e44 : (double)dtc, st, p.dt_next, p.status);
+    block_reduce_dt_f(dtc, st, p.dt_next, p.status);
     if (MODE == 0 && gx < p.ng + p.nx) fill_ghost_images(p, p.u_next, gx, gy);
 }
 
