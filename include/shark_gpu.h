@@ -242,6 +242,26 @@ int32_t shark_gpu_download(shark_gpu_ctx* ctx, double* u_prim, double* q);
  * cs (ncells, nullable). */
 int32_t shark_gpu_ctoprim(shark_gpu_ctx* ctx, double* q, double* cs);
 
+/* output(iout) -- replaces src/commons/write_output.f90:2-300 (called from shark.f90:114 and by
+ * solve when outputing): writes the directory  prefix + "output_" + five digits of iout  with
+ * info.dat (the reference's labels, I11 / E23.15) and one raw FP64 stream file per field, the
+ * active cells in cell order, unit-scaled as the reference scales them: x, rho, v, y (2D), vy,
+ * vz, P; with dust rhod_tot, rhod, sd, vd, vdy, vdz (species-major); with charging eta_a,
+ * eta_o, eta_h, ni, ne, zd.  The primitives come from ctoprim of the current device state
+ * (the final dump's `call ctoprim; call output(iout)`), packed on the device; `time` is the
+ * run time to record.  prefix may be "" (current directory) or end in '/'.  Not written: the
+ * MHD, NDUSTPSCAL and 1D-turbulence rms files (MHD = NDUSTPSCAL = TURB = 0 here). */
+int32_t shark_gpu_output(shark_gpu_ctx* ctx, int32_t iout, double time, const char* prefix);
+
+/* Restart from an output directory written by shark_gpu_output (or by the reference's output
+ * for the same configuration) -- the reference's read_output (src/commons/read_output.f90) is an
+ * empty stub, so this has no reference counterpart to replace.  Checks info.dat against the
+ * context (nvar, ndust, NX, NY, GEOM), divides out the units, rebuilds the conserved state with
+ * primtoc's operations (solve.f90:265-302) and uploads it (ghost cells from the boundaries, as
+ * shark_gpu_upload does).  *time_out (nullable) receives the recorded time.  The energy of an
+ * isothermal run is rebuilt from P = rho cs^2; it does not enter the isothermal update. */
+int32_t shark_gpu_read_output(shark_gpu_ctx* ctx, const char* dir, double* time_out);
+
 /* Compensated (Kahan) FP64 totals over the active cells, for each species s = 0..N (gas
  * first): out[4*s+0] = sum rho, out[4*s+1..3] = sum of the three momenta.  out has 4*(N+1)
  * doubles.  Deterministic: fixed reduction tree. */

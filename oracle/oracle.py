@@ -53,6 +53,7 @@ def lib():
                             ("oracle_get_charge", [D, D, D, D, D, D]),
                             ("oracle_reset_charge", []), ("oracle_charge_psi0", [D]),
                             ("oracle_growth", [C.POINTER(C.c_int32)]), ("oracle_growth_grid", [D, D, D]),
+                            ("oracle_output", [C.c_int32, C.c_double, C.c_char_p]),
                             ("oracle_turb_kick", []), ("oracle_turb_coef", [D, D, C.POINTER(C.c_int32)])]:
             f = getattr(L, name)
             f.restype = C.c_int32
@@ -205,6 +206,10 @@ class Oracle:
         it = np.zeros(self.ncells, dtype=np.int32)
         self._chk(lib().oracle_growth(self._h, it.ctypes.data_as(C.POINTER(C.c_int32))), "oracle_growth")
         return it
+
+    def output(self, iout, time, prefix=""):
+        """output (write_output.f90:2-300) of the current state into prefix + "output_%05d"."""
+        self._chk(lib().oracle_output(self._h, int(iout), float(time), prefix.encode()), "oracle_output")
 
     def growth_grid(self):
         """(zeta, eta, massmin), bin masses m_k, fragment shares redis[ifrag][k]."""

@@ -11,6 +11,10 @@
 #include "shark_oracle.h"
 
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+#include <sys/stat.h>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -2172,3 +2176,132 @@ int32_t oracle_set_threads(int32_t n) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// output (src/commons/write_output.f90:2-300): the run's raw stream files, restated for the
+// checks of the library's writer.  `prefix` + "output_" + five digits (title, iout) holds
+// info.dat (formatted, the reference's labels and edit descriptors I11 / E23.15) and one
+// unformatted stream file per field, active cells in cell order, unit-scaled: x (position(:,1)
+// or radii_c for GEOM 2), rho (unit_d, or unit_dcol = unit_d unit_l for GEOM 2), v, y (2D:
+// position(:,2)), vy, vz (unit_v), P (unit_P = unit_v^2 of the five setups, times unit_l for
+// GEOM 2), and with dust rhod_tot, rhod, sd (unit_l), vd, vdy, vdz (species-major), with charging
+// eta_a, eta_o, eta_h, ni, ne, zd.  MHD, NDUSTPSCAL and the 1D-turbulence rms files are not part
+// of any configuration here (MHD = NDUSTPSCAL = TURB = 0).  ctoprim runs first (the final dump of
+// time_loop, shark.f90:114-118).
+// ---------------------------------------------------------------------------------------------
+namespace {
+std::string fortran_i11(long long v) {
+    char b[64];
+    std::snprintf(b, sizeof b, "%11lld", v);
+    return b;
+}
+// Fortran E23.15: [sign]0.ddddddddddddddd E+ee (the E dropped for three-digit exponents),
+// right-justified in 23 characters.
+std::string fortran_e23_15(double v) {
+    char m[64];
+    std::string body;
+    if (v == 0.0) {
+        body = std::string(std::signbit(v) ? "-" : "") + "0.000000000000000E+00";
+    } else {
+        std::snprintf(m, sizeof m, "%.14E", v);   // d.dddddddddddddddE+ee, 15 significant digits
+        std::string s(m);
+        const bool neg = s[0] == '-';
+        if (neg) s = s.substr(1);
+        const size_t epos = s.find('E');
+        const std::string digits = s.substr(0, 1) + s.substr(2, epos - 2);
+        const int e = std::atoi(s.c_str() + epos + 1) + 1;
+        char ex[16];
+        if (std::abs(e) <= 99) std::snprintf(ex, sizeof ex, "E%c%02d", e < 0 ? '-' : '+', std::abs(e));
+        else std::snprintf(ex, sizeof ex, "%c%03d", e < 0 ? '-' : '+', std::abs(e));
+        body = std::string(neg ? "-" : "") + "0." + digits + ex;
+    }
+    return std::string(body.size() < 23 ? 23 - body.size() : 0, ' ') + body;
+}
+bool write_stream(const std::string& path, const std::vector<double>& v) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const bool ok = std::fwrite(v.data(), sizeof(double), v.size(), f) == v.size();
+    return std::fclose(f) == 0 && ok;
+}
+}  // namespace
+
+int32_t oracle_output(oracle_state* s, int32_t iout, double time, const char* prefix) {
+    if (!s || !prefix || iout < 0 || iout > 99999) return SHARK_ERR_INVALID_ARG;
+    ctoprim(*s);
+    const auto& g = s->cfg;
+    const double ul = unit_or_1(g.unit_l), ud = unit_or_1(g.unit_d), ut = unit_or_1(g.unit_t);
+    const double uv = ul / ut, uP = uv * uv, udcol = ud * ul;
+    const bool polar = g.geom == 2;
+    char nchar[8];
+    std::snprintf(nchar, sizeof nchar, "%05d", iout);
+    const std::string dir = std::string(prefix) + "output_" + nchar;
+    mkdir(dir.c_str(), 0755);
+    const bool charging = (g.flags & SHARK_FLAG_CHARGING) != 0;
+    {
+        FILE* f = std::fopen((dir + "/info.dat").c_str(), "w");
+        if (!f) return SHARK_ERR_INVALID_ARG;
+        std::fprintf(f, "nvar        =%s\n", fortran_i11(s->nvar).c_str());
+        std::fprintf(f, "ndust        =%s\n", fortran_i11(s->ndust).c_str());
+        std::fprintf(f, "ndustpscal   =%s\n", fortran_i11(0).c_str());
+        std::fprintf(f, "NX        =%s\n", fortran_i11(s->nx).c_str());
+        std::fprintf(f, "NY        =%s\n", fortran_i11(s->ny).c_str());
+        std::fprintf(f, "MHD        =%s\n", fortran_i11(0).c_str());
+        std::fprintf(f, "GEOM        =%s\n", fortran_i11(g.geom).c_str());
+        std::fprintf(f, "TURB        =%s\n", fortran_i11(0).c_str());
+        std::fprintf(f, "GRIDSPACE       =%s\n", fortran_i11(g.gridspace).c_str());
+        std::fprintf(f, "time        =%s\n", fortran_e23_15(time).c_str());
+        std::fprintf(f, "unit_t        =%s\n", fortran_e23_15(ut).c_str());
+        std::fprintf(f, "unit_d        =%s\n", fortran_e23_15(ud).c_str());
+        std::fprintf(f, "unit_l        =%s\n", fortran_e23_15(ul).c_str());
+        std::fprintf(f, "unit_v        =%s\n", fortran_e23_15(uv).c_str());
+        std::fprintf(f, "unit_p        =%s\n", fortran_e23_15(uP).c_str());
+        std::fprintf(f, "charging       =%s\n", fortran_i11(charging ? 1 : 0).c_str());
+        std::fclose(f);
+    }
+    std::vector<int64_t> act;
+    for (int64_t i = 0; i < s->ncells; ++i)
+        if (s->active[i]) act.push_back(i);
+    std::vector<double> buf;
+    auto field = [&](const char* name, auto value) -> bool {
+        buf.clear();
+        for (int64_t i : act) buf.push_back(value(i));
+        return write_stream(dir + "/" + name, buf);
+    };
+    auto species = [&](const char* name, auto value) -> bool {
+        buf.clear();
+        for (int k = 0; k < s->ndust; ++k)
+            for (int64_t i : act) buf.push_back(value(i, k));
+        return write_stream(dir + "/" + name, buf);
+    };
+    const double urho = polar ? udcol : ud;
+    bool ok = field("x", [&](int64_t i) { return polar ? s->radii_c[i] : s->POS(i, 0); });
+    ok = ok && field("rho", [&](int64_t i) { return s->Q(i, s->irho) * urho; });
+    ok = ok && field("v", [&](int64_t i) { return s->Q(i, s->ivx) * uv; });
+    if (s->ndim == 2) ok = ok && field("y", [&](int64_t i) { return s->POS(i, 1); });
+    ok = ok && field("vy", [&](int64_t i) { return s->Q(i, s->ivy) * uv; });
+    ok = ok && field("vz", [&](int64_t i) { return s->Q(i, s->ivz) * uv; });
+    ok = ok && field("P", [&](int64_t i) { return polar ? s->Q(i, s->iP) * uP * ul : s->Q(i, s->iP) * uP; });
+    if (s->ndust > 0) {
+        ok = ok && field("rhod_tot", [&](int64_t i) {
+            double t = 0.0;
+            for (int k = 0; k < s->ndust; ++k) t = t + s->Q(i, s->irhod[k]) * urho;
+            return t;
+        });
+        ok = ok && species("rhod", [&](int64_t i, int k) { return s->Q(i, s->irhod[k]) * urho; });
+        ok = ok && species("sd", [&](int64_t i, int k) { return s->SDUST(i, k) * ul; });
+        ok = ok && species("vd", [&](int64_t i, int k) { return s->Q(i, s->ivdx[k]) * uv; });
+        ok = ok && species("vdy", [&](int64_t i, int k) { return s->Q(i, s->ivdy[k]) * uv; });
+        ok = ok && species("vdz", [&](int64_t i, int k) { return s->Q(i, s->ivdz[k]) * uv; });
+    }
+    if (charging) {   // before the first charging call the reference's arrays hold zeros
+        const bool have = !s->psi_old.empty();
+        ok = ok && field("eta_a", [&](int64_t i) { return have ? s->eta_a[i] : 0.0; });
+        ok = ok && field("eta_o", [&](int64_t i) { return have ? s->eta_o[i] : 0.0; });
+        ok = ok && field("eta_h", [&](int64_t i) { return have ? s->eta_h[i] : 0.0; });
+        ok = ok && field("ni", [&](int64_t i) { return have ? s->ni[i] : 0.0; });
+        ok = ok && field("ne", [&](int64_t i) { return have ? s->ne[i] : 0.0; });
+        if (s->ndust > 0)
+            ok = ok && species("zd", [&](int64_t i, int k) { return have ? s->zd[(size_t)k * s->ncells + i] : 0.0; });
+    }
+    return ok ? SHARK_OK : SHARK_ERR_INVALID_ARG;
+}

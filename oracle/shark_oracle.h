@@ -77,6 +77,10 @@ int32_t oracle_growth_grid(const oracle_state* s, double* zeta_eta_massmin, doub
 int32_t oracle_turb_kick(oracle_state* s);
 int32_t oracle_turb_coef(const oracle_state* s, double* modes, double* coef, int32_t* nm);
 
+/* output (src/commons/write_output.f90:2-300) of the current state after ctoprim: writes
+ * prefix + "output_" + five digits (iout) with info.dat and the raw stream field files. */
+int32_t oracle_output(oracle_state* s, int32_t iout, double time, const char* prefix);
+
 int32_t oracle_set_threads(int32_t nthreads);
 
 #ifdef __cplusplus

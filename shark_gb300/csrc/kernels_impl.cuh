@@ -304,6 +304,59 @@ cudaError_t launch_charge_collect(const DeviceView& v, const float* feat, float*
     return cudaGetLastError();
 }
 
+// Output streams (write_output.f90:46-296) of the active cells from ctoprim's FP64 q (Fortran
+// order) and the charging outputs, in file order, each stream nact long, dust streams
+// species-major: rho, v, vy, vz, P, [rhod_tot, rhod(N), sd(N), vd(N), vdy(N), vdz(N)],
+// [eta_a, eta_o, eta_h, ni, ne, zd(N)].  One thread per active cell.
+template <typename R>
+__global__ void k_output_pack(const double* __restrict__ q, long long ncells, int nx_max, int ng, int nx, int ndim,
+                              long long nact, int N, OutScale sc, const double* __restrict__ dsize, int chg,
+                              const R* __restrict__ zd, const R* __restrict__ ni, const R* __restrict__ ne,
+                              const R* __restrict__ eta, long long plane, int pitch, double* __restrict__ out) {
+    const long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (a >= nact) return;
+    const int ix = ng + (ndim == 2 ? (int)(a % nx) : (int)a);
+    const int iy = ndim == 2 ? ng + (int)(a / nx) : 0;
+    const long long c = (long long)iy * nx_max + ix;
+    auto Q = [&](int v) { return q[(long long)v * ncells + c]; };
+    long long s = 0;
+    auto put = [&](double x) { out[s * nact + a] = x; ++s; };
+    put(Q(0) * sc.urho);
+    put(Q(1) * sc.uv);
+    put(Q(2) * sc.uv);
+    put(Q(3) * sc.uv);
+    put(Q(4) * sc.uP);
+    if (N > 0) {
+        double t = 0.0;
+        for (int k = 0; k < N; ++k) t = t + Q(5 + k) * sc.urho;
+        put(t);
+        for (int k = 0; k < N; ++k) put(Q(5 + k) * sc.urho);
+        for (int k = 0; k < N; ++k) put(dsize[k] * sc.ul);
+        for (int k = 0; k < N; ++k) put(Q(5 + N + k) * sc.uv);
+        for (int k = 0; k < N; ++k) put(Q(5 + 2 * N + k) * sc.uv);
+        for (int k = 0; k < N; ++k) put(Q(5 + 3 * N + k) * sc.uv);
+    }
+    if (chg) {
+        const long long pc = (long long)iy * pitch + ix;
+        put((double)eta[2 * plane + pc]);
+        put((double)eta[pc]);
+        put((double)eta[plane + pc]);
+        put((double)ni[pc]);
+        put((double)ne[pc]);
+        for (int k = 0; k < N; ++k) put((double)zd[(long long)k * plane + pc]);
+    }
+}
+
+template <typename R>
+cudaError_t launch_output_pack(const DeviceView& v, const double* q, OutScale sc, double* out) {
+    const long long nact = (long long)v.nx * (v.ndim == 2 ? v.ny : 1);
+    const ChargeView& c = v.chg;
+    k_output_pack<R><<<(unsigned)((nact + 255) / 256), 256, 0, v.stream>>>(
+        q, (long long)v.nx_max * v.ny_max, v.nx_max, v.ng, v.nx, v.ndim, nact, v.ndust, sc, v.dsize, c.on ? 1 : 0,
+        (const R*)c.zd, (const R*)c.ni, (const R*)c.ne, (const R*)c.eta, v.plane, v.pitch, out);
+    return cudaGetLastError();
+}
+
 template <typename R>
 cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int count, double* dst_dev) {
     const long long n = (long long)v.nx_max * v.ny_max * count;
@@ -323,6 +376,7 @@ cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int c
     template cudaError_t launch_charge<R>(const DeviceView&);                                      \
     template cudaError_t launch_charge_features<R>(const DeviceView&, float*);                     \
     template cudaError_t launch_charge_collect<R>(const DeviceView&, const float*, float*, unsigned long long*, long long); \
-    template cudaError_t launch_planes_to_fortran<R>(const DeviceView&, const void*, int, double*);
+    template cudaError_t launch_planes_to_fortran<R>(const DeviceView&, const void*, int, double*);                  \
+    template cudaError_t launch_output_pack<R>(const DeviceView&, const double*, OutScale, double*);
 
 }  // namespace shark

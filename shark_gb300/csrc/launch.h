@@ -93,5 +93,11 @@ template <typename R>
 cudaError_t launch_charge_collect(const DeviceView& v, const float* feat, float* out, unsigned long long* count, long long cap);
 // plane-layout array of `count` planes -> Fortran-order FP64 (ncells per plane)
 template <typename R> cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int count, double* dst_dev);
+// unit factors of the output streams: rho / rhod, velocities, pressure (unit_P, times unit_l for
+// GEOM 2), grain sizes
+struct OutScale {
+    double urho, uv, uP, ul;
+};
+template <typename R> cudaError_t launch_output_pack(const DeviceView& v, const double* q, OutScale sc, double* out);
 
 }  // namespace shark

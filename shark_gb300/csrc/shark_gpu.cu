@@ -14,6 +14,10 @@
 #include <new>
 #include <string>
 #include <vector>
+#include <cerrno>
+#include <cstdlib>
+#include <sys/stat.h>
+#include <map>
 
 #include "../../include/shark_gpu.h"
 #include "launch.h"
@@ -100,6 +104,7 @@ struct shark_gpu_ctx {
     double* grw_d = nullptr;         // dust growth tables (FP64)
     double* ou_d = nullptr;          // forcing: modes [3 nm] | coefficients [2 nm]
     std::vector<double> ou_init;     // initial coefficients (stationary law, seeded)
+    std::vector<double> out_x, out_y;   // output positions of the active cells (x / radius, y)
     int32_t* grw_i = nullptr;        // dust growth target bins | net-transfer bins
     float* grw_f = nullptr;          // dust growth net-transfer coefficients (mixed path)
     bool chg_cold = true;            // psi_old is zero everywhere (no charging call since reset)
@@ -148,6 +153,36 @@ void derive_tables(const shark_gpu_config& c, Columns& col) {
         col.irp[i] = 1.0 / rp;
         col.rvol[i] = col.vol[i] != 0.0 ? 1.0 / col.vol[i] : 0.0;
     }
+}
+
+// Positions written by the output routine (write_output.f90:46-96): position(:,1) (radii_c for
+// GEOM 2) and in 2D position(:,2), active cells in cell order, with gridinit's operations
+// (grid.f90:104-240): right cell edges in 1D, cell centres in 2D Cartesian, r (cos phi, sin phi)
+// on the polar grids; the caller's arrays when it passed its own grid.
+void output_positions(const shark_gpu_config& c, const Columns& col, int nx_max, int ny_max, std::vector<double>& x,
+                      std::vector<double>& y) {
+    const int ng = c.nghost, nx = c.nx, ny = c.ny;
+    const bool one_d = ny <= 1;
+    const long long ncells = (long long)nx_max * ny_max;
+    x.clear();
+    y.clear();
+    for (int iy = one_d ? 0 : ng; iy < (one_d ? 1 : ng + ny); ++iy)
+        for (int ix = ng; ix < ng + nx; ++ix) {
+            const long long i = (long long)iy * nx_max + ix;
+            if (c.position) {
+                x.push_back(c.geom == 2 && c.radii_c ? c.radii_c[i] : c.position[i]);
+                if (!one_d) y.push_back(c.position[ncells + i]);
+                continue;
+            }
+            x.push_back(c.geom == 2 ? col.radc[ix] : col.xpos[ix]);
+            if (one_d) continue;
+            if (c.geom == 2) {
+                const double phi = ((double)(float)(iy - ng) + 0.5) * 2.0 * kPi / (double)(float)ny;
+                y.push_back(col.radc[ix] * std::sin(phi));
+            } else {
+                y.push_back(((double)(float)(iy - ng) + 0.5) * c.box_l_y / (double)(float)ny);
+            }
+        }
 }
 
 int32_t build_columns(const shark_gpu_config& c, int nx_max, int ny_max, Columns& col) {
@@ -905,6 +940,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
 
     Columns col;
     if ((rc = build_columns(*cfg, v.nx_max, v.ny_max, col))) { release(c); return rc; }
+    output_positions(*cfg, col, v.nx_max, v.ny_max, c->out_x, c->out_y);
     derive_tables(*cfg, col);
 
 #define INIT_TRY(call)                                                                            \
@@ -1268,6 +1304,222 @@ int32_t shark_gpu_ctoprim(shark_gpu_ctx* c, double* q, double* cs) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     cudaFree(tmp);
     if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "ctoprim copy: %s", cudaGetErrorString(e));
+    return SHARK_OK;
+}
+
+// ---- output / restart (write_output.f90:2-300; the reference's read_output is a stub) --------
+namespace {
+std::string f_i11(long long v) {
+    char b[64];
+    std::snprintf(b, sizeof b, "%11lld", v);
+    return b;
+}
+// Fortran E23.15: [sign]0.d1..d15 and E+ee (a signed three-digit exponent without the E),
+// right-justified in 23 characters
+std::string f_e23_15(double v) {
+    std::string body;
+    if (v == 0.0) {
+        body = std::string(std::signbit(v) ? "-" : "") + "0.000000000000000E+00";
+    } else {
+        char m[64];
+        std::snprintf(m, sizeof m, "%.14E", std::fabs(v));
+        const std::string t(m);
+        const size_t ep = t.find('E');
+        const int e = std::atoi(t.c_str() + ep + 1) + 1;
+        char ex[16];
+        if (std::abs(e) <= 99) std::snprintf(ex, sizeof ex, "E%c%02d", e < 0 ? '-' : '+', std::abs(e));
+        else std::snprintf(ex, sizeof ex, "%c%03d", e < 0 ? '-' : '+', std::abs(e));
+        body = std::string(v < 0 ? "-" : "") + "0." + t.substr(0, 1) + t.substr(2, ep - 2) + ex;
+    }
+    return std::string(body.size() < 23 ? 23 - body.size() : 0, ' ') + body;
+}
+struct OutUnits {
+    double ul, ud, ut, uv, uP, urho, uPe;
+};
+OutUnits out_units(const shark_gpu_config& c) {
+    OutUnits u;
+    u.ul = unit1(c.unit_l);
+    u.ud = unit1(c.unit_d);
+    u.ut = unit1(c.unit_t);
+    u.uv = u.ul / u.ut;
+    u.uP = u.uv * u.uv;                                   // unit_P = unit_v**2 (disk_polar/units.f90)
+    u.urho = c.geom == 2 ? u.ud * u.ul : u.ud;            // unit_dcol for GEOM 2
+    u.uPe = c.geom == 2 ? u.uP * u.ul : u.uP;
+    return u;
+}
+bool write_raw(const std::string& path, const double* p, size_t n) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) return false;
+    const bool ok = std::fwrite(p, sizeof(double), n, f) == n;
+    return (std::fclose(f) == 0) && ok;
+}
+bool read_raw(const std::string& path, std::vector<double>& v, size_t n) {
+    FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    v.resize(n);
+    const bool ok = std::fread(v.data(), sizeof(double), n, f) == n && std::fgetc(f) == EOF;
+    std::fclose(f);
+    return ok;
+}
+}  // namespace
+
+int32_t shark_gpu_output(shark_gpu_ctx* c, int32_t iout, double time, const char* prefix) {
+    if (!c || !prefix) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    if (iout < 0 || iout > 99999) return fail(SHARK_ERR_INVALID_ARG, "iout %d outside 0..99999", iout);
+    if (!c->uploaded) return fail(SHARK_ERR_STATE, "output before upload");
+    const shark::DeviceView& v = c->v;
+    const shark_gpu_config& cf = c->cfg;
+    const OutUnits u = out_units(cf);
+    const int N = v.ndust;
+    const bool chg = v.chg.on;
+    const size_t nact = (size_t)v.nx * (v.ndim == 2 ? v.ny : 1);
+    const size_t nstreams = 5 + (N > 0 ? 1 + 5 * (size_t)N : 0) + (chg ? 5 + (size_t)N : 0);
+    char nchar[8];
+    std::snprintf(nchar, sizeof nchar, "%05d", iout);
+    const std::string dir = std::string(prefix) + "output_" + nchar;
+    if (mkdir(dir.c_str(), 0755) != 0 && errno != EEXIST) return fail(SHARK_ERR_INVALID_ARG, "cannot create %s", dir.c_str());
+    // fields: ctoprim on the device, then the active cells packed into the streams' file order
+    const size_t ncells = (size_t)v.nx_max * v.ny_max;
+    double* q = nullptr;
+    double* packed = nullptr;
+    CUDA_TRY(cudaMalloc(&q, ncells * v.nvar * sizeof(double)));
+    cudaError_t e = cudaMalloc(&packed, nstreams * nact * sizeof(double));
+    if (e == cudaSuccess) e = is_mixed(c) ? shark::launch_ctoprim<float>(v, q, nullptr) : shark::launch_ctoprim<double>(v, q, nullptr);
+    const shark::OutScale sc{u.urho, u.uv, u.uPe, u.ul};
+    if (e == cudaSuccess)
+        e = is_mixed(c) ? shark::launch_output_pack<float>(v, q, sc, packed) : shark::launch_output_pack<double>(v, q, sc, packed);
+    std::vector<double> h(nstreams * nact);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), packed, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(q);
+    cudaFree(packed);
+    if (e != cudaSuccess) return fail(SHARK_ERR_CUDA, "output: %s", cudaGetErrorString(e));
+    {
+        FILE* f = std::fopen((dir + "/info.dat").c_str(), "w");
+        if (!f) return fail(SHARK_ERR_INVALID_ARG, "cannot write %s/info.dat", dir.c_str());
+        std::fprintf(f, "nvar        =%s\n", f_i11(v.nvar).c_str());
+        std::fprintf(f, "ndust        =%s\n", f_i11(N).c_str());
+        std::fprintf(f, "ndustpscal   =%s\n", f_i11(0).c_str());
+        std::fprintf(f, "NX        =%s\n", f_i11(cf.nx).c_str());
+        std::fprintf(f, "NY        =%s\n", f_i11(cf.ny).c_str());
+        std::fprintf(f, "MHD        =%s\n", f_i11(0).c_str());
+        std::fprintf(f, "GEOM        =%s\n", f_i11(cf.geom).c_str());
+        std::fprintf(f, "TURB        =%s\n", f_i11(0).c_str());
+        std::fprintf(f, "GRIDSPACE       =%s\n", f_i11(cf.gridspace).c_str());
+        std::fprintf(f, "time        =%s\n", f_e23_15(time).c_str());
+        std::fprintf(f, "unit_t        =%s\n", f_e23_15(u.ut).c_str());
+        std::fprintf(f, "unit_d        =%s\n", f_e23_15(u.ud).c_str());
+        std::fprintf(f, "unit_l        =%s\n", f_e23_15(u.ul).c_str());
+        std::fprintf(f, "unit_v        =%s\n", f_e23_15(u.uv).c_str());
+        std::fprintf(f, "unit_p        =%s\n", f_e23_15(u.uP).c_str());
+        std::fprintf(f, "charging       =%s\n", f_i11(chg ? 1 : 0).c_str());
+        if (std::fclose(f) != 0) return fail(SHARK_ERR_INVALID_ARG, "cannot write %s/info.dat", dir.c_str());
+    }
+    const double* p = h.data();
+    auto W = [&](const char* name, const double* src, size_t n) { return write_raw(dir + "/" + name, src, n); };
+    bool ok = W("x", c->out_x.data(), nact);
+    ok = ok && W("rho", p, nact);
+    ok = ok && W("v", p + nact, nact);
+    if (v.ndim == 2) ok = ok && W("y", c->out_y.data(), nact);
+    ok = ok && W("vy", p + 2 * nact, nact);
+    ok = ok && W("vz", p + 3 * nact, nact);
+    ok = ok && W("P", p + 4 * nact, nact);
+    size_t s = 5;
+    if (N > 0) {
+        ok = ok && W("rhod_tot", p + s * nact, nact); s += 1;
+        for (const char* name : {"rhod", "sd", "vd", "vdy", "vdz"}) { ok = ok && W(name, p + s * nact, (size_t)N * nact); s += N; }
+    }
+    if (chg) {
+        for (const char* name : {"eta_a", "eta_o", "eta_h", "ni", "ne"}) { ok = ok && W(name, p + s * nact, nact); s += 1; }
+        if (N > 0) ok = ok && W("zd", p + s * nact, (size_t)N * nact);
+    }
+    if (!ok) return fail(SHARK_ERR_INVALID_ARG, "cannot write the field files of %s", dir.c_str());
+    return SHARK_OK;
+}
+
+int32_t shark_gpu_read_output(shark_gpu_ctx* c, const char* dir, double* time_out) {
+    if (!c || !dir) return fail(SHARK_ERR_INVALID_ARG, "NULL argument");
+    const shark::DeviceView& v = c->v;
+    const shark_gpu_config& cf = c->cfg;
+    const std::string d(dir);
+    FILE* f = std::fopen((d + "/info.dat").c_str(), "r");
+    if (!f) return fail(SHARK_ERR_INVALID_ARG, "cannot open %s/info.dat", dir);
+    std::map<std::string, std::string> info;
+    char line[256];
+    while (std::fgets(line, sizeof line, f)) {
+        std::string t(line);
+        const size_t eq = t.find('=');
+        if (eq == std::string::npos) continue;
+        std::string k = t.substr(0, eq);
+        k.erase(k.find_last_not_of(' ') + 1);
+        info[k] = t.substr(eq + 1);
+    }
+    std::fclose(f);
+    auto geti = [&](const char* k, long long& x) {
+        auto it = info.find(k);
+        if (it == info.end()) return false;
+        x = std::atoll(it->second.c_str());
+        return true;
+    };
+    // E23.15 values: a three-digit exponent has no E; insert it for strtod
+    auto getd = [&](const char* k, double& x) {
+        auto it = info.find(k);
+        if (it == info.end()) return false;
+        std::string t = it->second;
+        t.erase(0, t.find_first_not_of(' '));
+        t.erase(t.find_last_not_of(" \n\r") + 1);
+        if (t.find('E') == std::string::npos) {
+            const size_t pm = t.find_last_of("+-");
+            if (pm != std::string::npos && pm > 0) t.insert(pm, "E");
+        }
+        x = std::strtod(t.c_str(), nullptr);
+        return true;
+    };
+    long long nvar = 0, ndust = 0, nx = 0, ny = 0, geom = 0;
+    double time = 0.0, ud = 0.0, ul = 0.0, uv = 0.0, up = 0.0;
+    if (!(geti("nvar", nvar) && geti("ndust", ndust) && geti("NX", nx) && geti("NY", ny) && geti("GEOM", geom) &&
+          getd("time", time) && getd("unit_d", ud) && getd("unit_l", ul) && getd("unit_v", uv) && getd("unit_p", up)))
+        return fail(SHARK_ERR_INVALID_ARG, "%s/info.dat lacks a field", dir);
+    if (nvar != v.nvar || ndust != v.ndust || nx != cf.nx || ny != cf.ny || geom != cf.geom)
+        return fail(SHARK_ERR_INVALID_ARG, "%s holds nvar %lld ndust %lld %lldx%lld geom %lld, the context %dx%d", dir, nvar,
+                    ndust, nx, ny, geom, cf.nx, cf.ny);
+    const int N = v.ndust;
+    const size_t nact = (size_t)v.nx * (v.ndim == 2 ? v.ny : 1);
+    std::vector<double> rho, vx, vy, vz, P, rd, vdx, vdy, vdz;
+    bool ok = read_raw(d + "/rho", rho, nact) && read_raw(d + "/v", vx, nact) && read_raw(d + "/vy", vy, nact) &&
+              read_raw(d + "/vz", vz, nact) && read_raw(d + "/P", P, nact);
+    if (N > 0)
+        ok = ok && read_raw(d + "/rhod", rd, (size_t)N * nact) && read_raw(d + "/vd", vdx, (size_t)N * nact) &&
+             read_raw(d + "/vdy", vdy, (size_t)N * nact) && read_raw(d + "/vdz", vdz, (size_t)N * nact);
+    if (!ok) return fail(SHARK_ERR_INVALID_ARG, "%s: a field file is missing or has the wrong size", dir);
+    const double urho = geom == 2 ? ud * ul : ud, uPe = geom == 2 ? up * ul : up;
+    // primitives -> conserved with primtoc's operations (solve.f90:265-302); ghost cells are filled
+    // by the upload's boundaries
+    const size_t ncells = (size_t)v.nx_max * v.ny_max;
+    std::vector<double> U(ncells * v.nvar, 0.0);
+    const double g1 = cf.gamma - 1.0;
+    for (size_t a = 0; a < nact; ++a) {
+        const int ix = v.ng + (v.ndim == 2 ? (int)(a % v.nx) : (int)a);
+        const int iy = v.ndim == 2 ? v.ng + (int)(a / v.nx) : 0;
+        const size_t i = (size_t)iy * v.nx_max + ix;
+        const double r = rho[a] / urho, ux = vx[a] / uv, uy = vy[a] / uv, uz = vz[a] / uv, p = P[a] / uPe;
+        U[0 * ncells + i] = r;
+        U[1 * ncells + i] = r * ux;
+        U[2 * ncells + i] = r * uy;
+        U[3 * ncells + i] = r * uz;
+        U[4 * ncells + i] = p / g1 + 0.5 * r * (ux * ux) + 0.5 * r * (uy * uy) + 0.5 * r * (uz * uz);
+        for (int k = 0; k < N; ++k) {
+            const size_t j = (size_t)k * nact + a;
+            const double d_k = rd[j] / urho;
+            U[(5 + k) * ncells + i] = d_k;
+            U[(5 + N + k) * ncells + i] = d_k * (vdx[j] / uv);
+            U[(5 + 2 * N + k) * ncells + i] = d_k * (vdy[j] / uv);
+            U[(5 + 3 * N + k) * ncells + i] = d_k * (vdz[j] / uv);
+        }
+    }
+    int32_t rc = shark_gpu_upload(c, U.data(), (int64_t)ncells, v.nvar);
+    if (rc) return rc;
+    if (time_out) *time_out = time;
     return SHARK_OK;
 }
 

@@ -84,6 +84,21 @@ module shark_gpu
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: out(*)
     end function
+    ! output(iout) from the device (write_output.f90:2-300); prefix and dir are C strings
+    ! (terminate them with c_null_char)
+    integer(c_int32_t) function shark_gpu_output(ctx, iout, time, prefix) bind(C, name="shark_gpu_output")
+      import :: c_int32_t, c_ptr, c_double, c_char
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: iout
+      real(c_double), value :: time
+      character(kind=c_char), intent(in) :: prefix(*)
+    end function
+    integer(c_int32_t) function shark_gpu_read_output(ctx, dir, time) bind(C, name="shark_gpu_read_output")
+      import :: c_int32_t, c_ptr, c_double, c_char
+      type(c_ptr), value :: ctx
+      character(kind=c_char), intent(in) :: dir(*)
+      real(c_double), intent(out) :: time
+    end function
     integer(c_int32_t) function shark_gpu_free(ctx) bind(C, name="shark_gpu_free")
       import :: c_int32_t, c_ptr
       type(c_ptr), value :: ctx

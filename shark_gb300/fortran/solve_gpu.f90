@@ -137,3 +137,20 @@ subroutine primtoc
 #endif
   end do
 end subroutine primtoc
+
+! output_gpu : output(iout) written from the device state (shark_gpu_output) into
+!              output_XXXXX/ of the working directory, the same files as write_output.f90's
+!              output for MHD = NDUSTPSCAL = TURB = 0; call it where shark.f90 calls output once
+!              the GPU owns the state.
+subroutine output_gpu(iout)
+  use commons
+  use shark_gpu
+  implicit none
+  integer :: iout
+  integer(c_int32_t) :: rc
+  rc = shark_gpu_output(gpu_ctx, int(iout, c_int32_t), time, c_null_char)
+  if (rc /= 0) then
+    print *, 'shark_gpu_output failed: ', rc
+    stop
+  end if
+end subroutine output_gpu

@@ -25,7 +25,7 @@ EXPORTS = [
     "shark_gpu_totals_noalloc", "shark_gpu_last_error", "shark_gpu_free",
     "shark_gpu_charge", "shark_gpu_charge_reset", "shark_gpu_charge_stats", "shark_gpu_download_charge",
     "shark_gpu_mlp_collect", "shark_gpu_mlp_train", "shark_gpu_mlp_save", "shark_gpu_mlp_load",
-    "shark_gpu_mlp_eval", "shark_gpu_mlp_features",
+    "shark_gpu_mlp_eval", "shark_gpu_mlp_features", "shark_gpu_output", "shark_gpu_read_output",
 ]
 MLP_NFEAT, MLP_NPARAM, MLP_NBLOB = 6, 5313, 5327
 CHARGE_HIST = 64   # SHARK_CHARGE_HIST
@@ -90,7 +90,9 @@ def load_library(path=None):
                        ("shark_gpu_mlp_train", [P, I32, I32, C.c_float, C.c_uint64, FP]),
                        ("shark_gpu_mlp_save", [P, FP, C.c_int64]), ("shark_gpu_mlp_load", [P, FP, C.c_int64]),
                        ("shark_gpu_mlp_eval", [P, FP, FP, C.c_int64, FP, FP, FP]),
-                       ("shark_gpu_mlp_features", [P, FP])]:
+                       ("shark_gpu_mlp_features", [P, FP]),
+                       ("shark_gpu_output", [P, I32, C.c_double, C.c_char_p]),
+                       ("shark_gpu_read_output", [P, C.c_char_p, D])]:
         f = getattr(L, name)
         f.restype = I32
         f.argtypes = args
@@ -173,6 +175,21 @@ class Shark:
                "shark_gpu_download")
 
     u_prim = property(download)
+
+    # -- output / restart (src/commons/write_output.f90:2-300) ----------------------------------
+    def output(self, iout, time=None, prefix=""):
+        """Write prefix + "output_%05d" (info.dat and the raw field streams) of the current state."""
+        t = self.time if time is None else float(time)
+        _check(load_library().shark_gpu_output(self._h, int(iout), t, prefix.encode()), "shark_gpu_output")
+        return os.path.join(prefix, "output_%05d" % int(iout)) if prefix else "output_%05d" % int(iout)
+
+    def read_output(self, directory):
+        """Restart from an output directory: upload its state; returns (and keeps) its time."""
+        t = C.c_double(0.0)
+        _check(load_library().shark_gpu_read_output(self._h, str(directory).encode(), C.byref(t)),
+               "shark_gpu_read_output")
+        self.time = t.value
+        return t.value
 
     def ctoprim(self):
         """(q, cs) of the current device state (src/solver/solve.f90:195-253)."""
