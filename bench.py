@@ -433,7 +433,10 @@ def config_leg(args, name, device, mixed_steps=5, fp64_steps=2):
         out["mixed" if prec == K.PREC_MIXED else "fp64"] = {
             "value": zs * ns / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms / ns, "steps": ns,
             "kernel_ms": {"charge_forcing": kt[0], "flux_update": kt[1], "drag_growth_dt": kt[2], "step": kt[3]},
-            "status": st, "charging_nonconverged_cells": nonconv, "charging_iterations_per_cell": tot / (cfg.nx * cfg.ny)}
+            "status": st, "charging_nonconverged_cells": nonconv, "charging_iterations_per_cell": tot / (cfg.nx * cfg.ny),
+            "status_note": "bits: 1 NaN, 2 negative density, 4 dt underflow, 8 a charging Newton ended above its "
+                           "tolerance (the polar disk's outer cells stall at psi0 in the reference's loop too), "
+                           "16 growth sub-step cap"}
         ctx[prec] = (cfg, g)
         del u0
     (cm, gm), (cd, gd) = ctx[K.PREC_MIXED], ctx[K.PREC_FP64]

@@ -58,6 +58,7 @@ struct ChargeParams {
     const float* seed;           // [plane] network start points (nullptr: none)
     int32_t* iters;              // [plane] Newton iterations of the last call
     unsigned long long* hist;    // [CHARGE_HIST + 2]: histogram, non-converged cells, total iterations
+    unsigned int* status;        // the step's status word: SHARK_STATUS_NEWTON if a cell did not converge
 };
 
 namespace chg {
@@ -379,6 +380,7 @@ __global__ void __launch_bounds__(128) k_charge(ChargeParams<R> p) {
     for (int b = threadIdx.x; b <= CHARGE_HIST; b += blockDim.x)
         if (s_hist[b]) atomicAdd(&p.hist[b], (unsigned long long)s_hist[b]);
     if (threadIdx.x == 0 && s_iter) atomicAdd(&p.hist[CHARGE_HIST + 1], s_iter);
+    if (threadIdx.x == 0 && s_hist[CHARGE_HIST] && p.status) atomicOr(p.status, (unsigned)SHARK_STATUS_NEWTON);
 }
 
 // Fujii et al. (2011) analytical charging (ionisation.f90:809-922, functions_NR.f90:15-128,
@@ -461,6 +463,7 @@ __global__ void __launch_bounds__(128) k_charge_fujii(ChargeParams<R> p, double 
     for (int b = threadIdx.x; b <= CHARGE_HIST; b += blockDim.x)
         if (s_hist[b]) atomicAdd(&p.hist[b], (unsigned long long)s_hist[b]);
     if (threadIdx.x == 0 && s_iter) atomicAdd(&p.hist[CHARGE_HIST + 1], s_iter);
+    if (threadIdx.x == 0 && s_hist[CHARGE_HIST] && p.status) atomicOr(p.status, (unsigned)SHARK_STATUS_NEWTON);
 }
 
 // Network features of the cells (SHARK_MLP_NFEAT floats per cell, plane layout [plane][F]):

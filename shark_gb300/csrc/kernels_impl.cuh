@@ -274,6 +274,7 @@ static ChargeParams<R> charge_params(const DeviceView& v) {
     q.mu_ions = c.mu_ions; q.nitermax = c.nitermax;
     q.psi_old = c.psi_old; q.zd = (R*)c.zd; q.ni = (R*)c.ni; q.ne = (R*)c.ne; q.eta = (R*)c.eta;
     q.gamma_d = (R*)c.gamma_d; q.seed = c.seed; q.hist = c.hist; q.iters = c.iters;
+    q.status = v.status;
     return q;
 }
 

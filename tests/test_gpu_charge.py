@@ -133,3 +133,25 @@ def test_analytical_charge_fp64():
     for key in ("ni", "ne"):
         assert _rel(cg[key], co[key]) <= 1e-10, key
     assert _rel(cg["zd"], co["zd"]) <= 1e-10
+
+
+def test_newton_cap_surfaces_in_status_and_context_stays_usable():
+    """Fault injection on the host: a Newton cap of 2 iterations leaves cells above the
+    tolerance; the step's status word carries SHARK_STATUS_NEWTON, the statistics count the
+    cells, and the context keeps stepping.  With the reference's cap the same state is clean."""
+    cfg, u0 = _noisy_turb(n=16, ndust=4)
+    cfg.chg_nitermax = 2
+    with Shark(cfg) as g:
+        g.upload(u0)
+        g.solve()
+        assert g.sync() & K.STATUS_NEWTON
+        _, nonconv, _ = g.charge_stats()
+        assert nonconv > 0
+        for _ in range(2):
+            g.solve()
+        assert np.isfinite(g.download()).all()
+    cfg.chg_nitermax = 1000
+    with Shark(cfg) as g:
+        g.upload(u0)
+        g.solve()
+        assert g.sync() & K.STATUS_NEWTON == 0
