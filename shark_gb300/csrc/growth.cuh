@@ -103,25 +103,43 @@ __device__ __forceinline__ double growth_dv_d(const GrowthDev& g, int N, int k, 
     return dv;
 }
 
-// FP32 cell constants of the pair relative velocity (dust_growth.f90:60-87).
+// FP32 constants of the pair relative velocity (dust_growth.f90:60-87): those of the run, formed
+// once per thread (each is a conversion on the narrow FP64 pipe), and those of one cell.
+struct GrowthRunF {
+    float ud, mu_mH, ut, dvambi, alpha, inv_uv;
+};
+__device__ __forceinline__ GrowthRunF growth_run_consts_f(const GrowthDev& g) {
+    GrowthRunF r;
+    r.ud = (float)g.ud;
+    r.mu_mH = (float)g.mu_gas * (float)grw::mH;
+    r.ut = (float)g.ut;
+    r.dvambi = (float)g.delta_vambi;
+    r.alpha = (float)g.alpha_turb;
+    r.inv_uv = 1.f / (float)g.uv;
+    return r;
+}
 struct GrowthCellF {
     float T, cs_v, t_L, t_eta, rm, vambi;
 };
+// the temperature row's T, cs_T (cgs), cs_v (code), t_L (disk) in FP32
+__device__ __forceinline__ float4 growth_row_f(const GrowthDev& g, int ix) {
+    const double* cc = g.col + (size_t)(g.t_per_col ? ix : 0) * 4;
+    return make_float4((float)cc[0], (float)cc[1], (float)cc[2], (float)cc[3]);
+}
 
-__device__ __forceinline__ GrowthCellF growth_cell_consts_f(const GrowthDev& g, int ix, float rho_q, float hs, float eta_a) {
-    const int row = g.t_per_col ? ix : 0;
-    const double* cc = g.col + (size_t)row * 4;
+__device__ __forceinline__ GrowthCellF growth_cell_consts_f(const GrowthDev& g, const GrowthRunF& r, float4 row,
+                                                            float rho_q, float hs, float eta_a) {
     GrowthCellF c;
-    c.T = (float)cc[0];
-    const float cs_T = (float)cc[1];
-    c.cs_v = (float)cc[2];
+    c.T = row.x;
+    const float cs_T = row.y;
+    c.cs_v = row.z;
     const float pi = (float)grw::pi;
-    const float rho_cgs = rho_q / hs * (float)g.ud;
+    const float rho_cgs = rho_q / hs * r.ud;
     const float tff = sqrtf(3.f * pi / (32.f * (float)grw::grav * rho_cgs));
     const float lambJ = tff * cs_T;
-    c.vambi = (float)g.delta_vambi * (float)(grw::clight * grw::clight) * eta_a / lambJ / (4.f * pi);
-    const float Re = 6.2e7f * sqrtf(rho_cgs / ((float)g.mu_gas * (float)grw::mH) / 1e5f) * sqrtf(c.T / 10.f);
-    c.t_L = g.t_per_col ? (float)cc[3] : tff / (float)g.ut;
+    c.vambi = r.dvambi * (float)(grw::clight * grw::clight) * eta_a / lambJ / (4.f * pi) * r.inv_uv;
+    const float Re = 6.2e7f * sqrtf(rho_cgs / r.mu_mH / 1e5f) * sqrtf(c.T / 10.f);
+    c.t_L = g.t_per_col ? row.w : tff / r.ut;
     c.t_eta = c.t_L / sqrtf(Re);
     c.rm = rsqrtf(Re);
     return c;
@@ -130,11 +148,11 @@ __device__ __forceinline__ GrowthCellF growth_cell_consts_f(const GrowthDev& g, 
 // FP32 relative velocity of a pair k >= j (dust_growth.f90:88-114): stopping times tk, tj, the
 // Brownian term X = T pBf, the drift (dx, dy, dz) = v_k - v_j and dg = |G_k| - |G_j| of the
 // ambipolar term, G = gamma / sqrt(1 + gamma^2).
-__device__ __forceinline__ float growth_dv_f(const GrowthDev& g, const GrowthCellF& c, float tk, float tj, float X,
-                                             float dx, float dy, float dz, float dg, bool ambi) {
+__device__ __forceinline__ float growth_dv_f(const GrowthDev& g, const GrowthRunF& r, const GrowthCellF& c, float tk,
+                                             float tj, float X, float dx, float dy, float dz, float dg, bool ambi) {
     float dv = 0.f;
     if (g.mode & SHARK_GROWTH_TURB) {
-        const float a = (float)g.alpha_turb;
+        const float a = r.alpha;
         const float x = tj / tk;
         const float fS = 3.2f - 1.f - x + 2.f / (1.f + x) * (1.f / 2.6f + x * x * x / (1.6f + x));
         const float St1 = tk / c.t_L, St2 = tj / c.t_L;
@@ -153,7 +171,7 @@ __device__ __forceinline__ float growth_dv_f(const GrowthDev& g, const GrowthCel
     if (g.mode & SHARK_GROWTH_BROWNIAN) dv = sqrtf(dv * dv + X);
     if (g.mode & SHARK_GROWTH_DRIFT) dv = sqrtf(dv * dv + dx * dx + dy * dy + dz * dz);
     if ((g.mode & SHARK_GROWTH_AMBIPOLAR) && ambi) {
-        const float d = c.vambi / (float)g.uv * dg;
+        const float d = c.vambi * dg;                 // vambi carries 1/unit_v
         dv = sqrtf(dv * dv + d * d);
     }
     return dv;
@@ -167,7 +185,8 @@ __device__ __forceinline__ float growth_dv_f(const GrowthDev& g, const GrowthCel
 static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int ix, double dt, float rho_gas, float rho_q,
                                            float hs, double* rdd, const double* tsd, const double* vxd,
                                            const double* vyd, const double* vzd, const double* gamd, float eta_a) {
-    const GrowthCellF cc = growth_cell_consts_f(g, ix, rho_q, hs, eta_a);
+    const GrowthRunF rf = growth_run_consts_f(g);
+    const GrowthCellF cc = growth_cell_consts_f(g, rf, growth_row_f(g, ix), rho_q, hs, eta_a);
     const bool frag = (g.mode & SHARK_GROWTH_FRAGMENTATION) != 0;
     float rd[GROWTH_MAX_DUST], ts[GROWTH_MAX_DUST], gm[GROWTH_MAX_DUST];
     for (int k = 0; k < N; ++k) {
@@ -182,7 +201,7 @@ static __device__ __noinline__ bool growth_cell_f(const GrowthDev& g, int N, int
         for (int j = 0; j <= k; ++j, ++q) {
             float dv = 1.f;
             if (g.kernel == 0)
-                dv = growth_dv_f(g, cc, ts[k], ts[j], cc.T * g.pBf[q], (float)(vxd[k] - vxd[j]), (float)(vyd[k] - vyd[j]),
+                dv = growth_dv_f(g, rf, cc, ts[k], ts[j], cc.T * g.pBf[q], (float)(vxd[k] - vxd[j]), (float)(vyd[k] - vyd[j]),
                                  (float)(vzd[k] - vzd[j]), gm[k] - gm[j], gamd != nullptr);
             float ff = 0.f;
             if (frag) {

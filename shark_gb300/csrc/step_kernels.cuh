@@ -439,14 +439,27 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
     const float dtf = (float)dt, idtf = 1.f / dtf;
     const float fctl = g.dtctl > 0.0 ? (float)(g.dtctl / dt) : 0.f, dtctl = (float)g.dtctl;
     const float stick = (float)g.sticking, cflg = (float)g.cfl;
+    const float eps_thr = (float)g.eps_thr, rmin = (float)g.dust_ratio_min, smallr = (float)p.smallr;
+    // stopping times for the pair velocities (FP32): t_k = C_k / F_cell with the tabulated 1/C_k
+    // (dustyTurb F = c_s rho, polar disk F = rho/hs c_s); other setups through tstop_cell
+    const bool ts_tab = p.setup == SHARK_SETUP_DUSTYTURB || p.setup == SHARK_SETUP_DISK_POLAR;
+    const float invc = (float)p.dinvts[b];
+    const GrowthRunF rf = growth_run_consts_f(g);
+    const float4 row0 = growth_row_f(g, 0);        // the one temperature row (dustyTurb)
     unsigned st = 0;
     for (int c = 0; c < 32; ++c) {
         const int gx = gx_block + wid * 32 + c;
         if (gx >= p.ng + p.nx) break;
-        const double rho_old = (double)p.u_cur[uidx(p, 0, gy, gx)];
-        const double qrho_old = rho_old > p.smallr ? rho_old : p.smallr;
+        const float rho_old = p.u_cur[uidx(p, 0, gy, gx)];
+        const float qrho_old = rho_old > smallr ? rho_old : smallr;
         float rd = u[uidx(p, 5 + b, gy, gx)];
-        const float ts = (float)tstop_cell(p, b, qrho_old, gx, gy);
+        float ts;
+        if (ts_tab) {
+            const float F = p.setup == SHARK_SETUP_DUSTYTURB ? p.cs[gx] * qrho_old : qrho_old / (float)p.hsd[gx] * p.cs[gx];
+            ts = 1.f / (invc * F);
+        } else {
+            ts = (float)tstop_cell(p, b, (double)qrho_old, gx, gy);
+        }
         const float r0 = p.u_cur[uidx(p, 5 + b, gy, gx)];
         const float vx = p.u_cur[uidx(p, 5 + N + b, gy, gx)] / r0;
         const float vy = p.u_cur[uidx(p, 5 + 2 * N + b, gy, gx)] / r0;
@@ -460,7 +473,7 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
         }
         const float hs = p.setup == SHARK_SETUP_DISK_POLAR ? (float)p.hsd[gx] : 1.f;
         const float rho_gas = u[uidx(p, 0, gy, gx)];
-        const GrowthCellF cc = growth_cell_consts_f(g, gx, (float)qrho_old, hs, eta_a);
+        const GrowthCellF cc = growth_cell_consts_f(g, rf, g.t_per_col ? growth_row_f(g, gx) : row0, qrho_old, hs, eta_a);
         const float ihs = 1.f / hs;
         float kp[GROWTH_PAIR_SLOTS];
         int kj[GROWTH_PAIR_SLOTS];
@@ -481,10 +494,10 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
             const float dg = __shfl_sync(FULL, gm, k) - __shfl_sync(FULL, gm, j);
             if (!has) continue;
             float dv = 1.f;
-            if (g.kernel == 0) dv = growth_dv_f(g, cc, tk, tj, cc.T * __ldg(g.pBf + q), dx, dy, dz, dg, ambi);
+            if (g.kernel == 0) dv = growth_dv_f(g, rf, cc, tk, tj, cc.T * __ldg(g.pBf + q), dx, dy, dz, dg, ambi);
             kp[i] = __ldg(g.pKf + q) * dv * ihs * (k == j ? 0.5f : 1.f);
         }
-        const float thr = (float)g.eps_thr * rho_gas, fl = rho_gas * (float)g.dust_ratio_min;
+        const float thr = eps_thr * rho_gas, fl = rho_gas * rmin;
         float rem = 1.f;                                    // part of dt still to integrate
         int niter = 0;
         while (rem > 0.f && niter < grw::MAX_SUB) {
