@@ -28,10 +28,10 @@ constexpr int GROWTH_MAX_PAIRS = GROWTH_MAX_DUST * (GROWTH_MAX_DUST + 1) / 2;
 struct GrowthDev {
     int on, kernel, mode, t_per_col;
     const double* pA;        // [N*N] (clustered^2 pi)(s_k + s_j)^2
-    const double* pK;        // [N*N] rate factor of the mixed path: pA/m_k/m_j, 1/m_k/m_j, (m_k+m_j)/m_k/m_j
     // FP32 path.  Pairs are numbered q = k (k + 1) / 2 + j, j <= k.
     const int32_t* pair;     // [npair] k << 8 | j
-    const float* pKf;        // [npair] pK in FP32
+    const float* pKf;        // [npair] pair rate factor pA/m_k/m_j (constant kernel 1/m_k/m_j, additive
+                             // (m_k+m_j)/m_k/m_j) times mref, formed in FP64 on the host
     const float* pBf;        // [npair] (8 kB / pi) (m_k + m_j) / (m_k m_j) / uv^2, masses in g: Brownian dv^2 / T
     const int32_t* gq;       // [gL * 32] without fragmentation, entry t of bin b at t * 32 + b: a pair
     const float* gc;         //           and the net mass it moves into bin b per collision, in units of
@@ -46,7 +46,7 @@ struct GrowthDev {
     const double* redis;     // [N*N] fragment shares: redis[ifrag * N + k]
     const double* col;       // [rows][4]: T, cs_T (cgs), cs_v (code), t_L (disk; 0 otherwise)
     double massmin, eta, m_mono, Ebr_mono, uv, uv2, ud, ut, mu_gas, dtctl, cfl, sticking, eps_thr, eps_thr_frag;
-    double mref;             // mass unit of the FP32 path (the smallest grain mass): pK/pKf are pre-multiplied
+    double mref;             // mass unit of the FP32 path (the smallest grain mass): pKf is pre-multiplied
                              // and gc pre-divided by it, so code-unit masses (1e-45 in AU/Msun) stay in range
     double delta_vambi, alpha_turb, dust_ratio_min;
 };

@@ -1116,7 +1116,6 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         v.gw.pA = c->grw_d + off[0]; v.gw.pS = c->grw_d + off[1]; v.gw.pD = c->grw_d + off[2];
         v.gw.peps = c->grw_d + off[3]; v.gw.mk = c->grw_d + off[4]; v.gw.sk = c->grw_d + off[5];
         v.gw.redis = c->grw_d + off[6]; v.gw.col = c->grw_d + off[7]; v.gw.pic = c->grw_i;
-        v.gw.pK = c->grw_d + off[8];
         {
             const size_t NN = (size_t)cfg->ndust * cfg->ndust, P = (size_t)v.gw.npair;
             v.gw.pair = c->grw_i + NN * 2;
