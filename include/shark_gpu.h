@@ -59,6 +59,8 @@ extern "C" {
 #define SHARK_SETUP_SI          3   /* shearing box                     SI/setup.f90, SI/boundaries.f90 */
 #define SHARK_SETUP_DISK_POLAR  4   /* polar disk (FARGO)               disk_polar/                 */
 #define SHARK_SETUP_DUSTYTURB   5   /* periodic driven turbulence       dustyTurb/                  */
+#define SHARK_SETUP_KH          6   /* periodic shear layer, Epstein    KH/setup.f90, KH/units.f90  */
+#define SHARK_SETUP_SEDOV       7   /* periodic blast wave, gas only    sedov/setup.f90             */
 
 /* ---- run-time switches (the reference's namelist logicals) -------------------------------- */
 #define SHARK_FLAG_DRAG           0x1   /* drag               src/dust/dust_commons.f90:5        */
@@ -180,7 +182,12 @@ typedef struct shark_gpu_config {
     /* viscosity (SHARK_FLAG_VISCOSITY, source_terms.f90:99-118): the polar disk's
      * eta_visc = disk_alpha_visc H cs (disk_polar/setup.f90:67) */
     double disk_alpha_visc;
-    double reserved[11];
+    /* KH (KH/setup_commons.f90): dense and band densities (g cm^-3), temperature (K), Mach number
+     * of the shear, amplitude vy0 and wavenumber kx of the vy seed; code units from unit_l/d/t */
+    double kh_rho_dense, kh_rho_diffuse, kh_T_dense, kh_mach, kh_vy0, kh_kx;
+    /* sedov (sedov/setup_commons.f90): ambient density and pressure, blast overpressure, radius */
+    double sedov_rho_ext, sedov_P_ext, sedov_P_cen, sedov_r_expl;
+    double reserved[1];
 
     /* Optional grid metrics from the caller (Fortran dx(ncells,ndim), surf(ncells,ndim),
      * vol(ncells), radii_c(ncells), position(ncells,ndim), cs(ncells)).  NULL: the library

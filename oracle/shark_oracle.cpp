@@ -389,7 +389,7 @@ void apply_boundaries(oracle_state& s) {
         case SHARK_SETUP_SOD: sod_boundaries(s); break;
         case SHARK_SETUP_SI: si_boundaries(s); break;
         case SHARK_SETUP_DISK_POLAR: disk_boundaries(s); break;
-        default: periodic_boundaries(s); break;   // DUSTYWAVE (DUSTYWAVE/boundaries.f90), dustyTurb
+        default: periodic_boundaries(s); break;   // DUSTYWAVE, dustyTurb, KH, sedov (*/boundaries.f90)
     }
 }
 
@@ -418,7 +418,7 @@ void compute_tstop(oracle_state& s) {
                          (s.Q(i, s.irho) / (std::sqrt(2.0 * pi) * H) * s.cs[i]);
                     break;
                 }
-                default:                      // SOD/setup.f90:179-185, Epstein
+                default:                      // SOD/setup.f90:179-185, KH/setup.f90:218-239, Epstein
                     ts = std::sqrt(pi * s.cfg.gamma / 8.0) * (s.cfg.rhograin) * s.SDUST(i, k) /
                          (s.Q(i, s.irho) * s.cs[i]);
                     break;
@@ -1814,6 +1814,63 @@ void setup_dustywave(oracle_state& s) {
     primtoc(s);
 }
 
+// KH setup (src/setups/KH/setup.f90:1-51, KH/eos.f90 cs_eos, KH/units.f90): a band |y - L_y/2| <
+// L_y/4 of density rho_diffuse moving at -Mach cs/2 inside gas of density rho_dense moving at
+// +Mach cs/2, vy seeded with vy0 Mach cs cos(2 kx pi x'/L) over the whole box, one pressure
+// rho_dense cs^2, cs = cs_eos(T_dense); cgs inputs divided by unit_d, unit_v, unit_P = unit_d
+// unit_v^2.  Dust: epsilondust = dust_eps[k] (distribution_dust, or 0.01 for one species), at rest.
+void setup_kh(oracle_state& s) {
+    const shark_gpu_config& c = s.cfg;
+    const double ul = unit_or_1(c.unit_l), ud = unit_or_1(c.unit_d), ut = unit_or_1(c.unit_t);
+    const double uv = ul / ut, uP = ud * (uv * uv);
+    constexpr double mH = 1.67e-24, kB = 1.38e-16;                      // phys_const.f90:8-9
+    const double cs = std::sqrt(c.gamma * kB * c.kh_T_dense / (c.mu_gas * mH));   // KH/eos.f90
+    std::fill(s.q.begin(), s.q.end(), 0.0);
+    for (int iy = 0; iy < s.ny_max; ++iy)
+        for (int ix = 0; ix < s.nx_max; ++ix) {
+            const int64_t i = s.icell(ix, iy);
+            const double xx = s.POS(i, 0) - half * s.box_l;
+            const double yy = s.POS(i, 1) - half * s.box_l_y;
+            s.Q(i, s.irho) = c.kh_rho_dense / ud;
+            s.Q(i, s.ivx) = cs * c.kh_mach / uv * half;
+            s.Q(i, s.ivy) = (c.kh_vy0 * cs * c.kh_mach * std::cos(xx * 2.0 * c.kh_kx * pi / s.box_l)) / uv;
+            s.Q(i, s.iP) = c.kh_rho_dense * (cs * cs) / uP;
+            if (std::fabs(yy / s.box_l_y) < 0.25) {
+                s.Q(i, s.irho) = c.kh_rho_diffuse / ud;
+                s.Q(i, s.ivx) = -(cs * c.kh_mach / uv / 2.0);
+                s.Q(i, s.iP) = c.kh_rho_dense * (cs * cs) / uP;
+            }
+        }
+    for (int64_t i = 0; i < s.ncells; ++i)
+        for (int k = 0; k < s.ndust; ++k) {
+            s.EPSD(i, k) = c.dust_eps[k];
+            s.Q(i, s.irhod[k]) = s.EPSD(i, k) * s.Q(i, s.irho);
+        }
+    apply_boundaries(s);
+    primtoc(s);
+    ctoprim(s);
+}
+
+// sedov setup (src/setups/sedov/setup.f90:1-34): gas at rest, density rho_ext, pressure P_ext,
+// plus P_cen inside the disc |x - L/2|^2 + |y - L/2|^2 < r_expl^2 of the active cells; the ghost
+// cells stay zero until the boundaries fill them.
+void setup_sedov(oracle_state& s) {
+    const shark_gpu_config& c = s.cfg;
+    std::fill(s.q.begin(), s.q.end(), 0.0);
+    for (int iy = 0; iy < s.ny_max; ++iy)
+        for (int ix = 0; ix < s.nx_max; ++ix) {
+            const int64_t i = s.icell(ix, iy);
+            if (!s.active[i]) continue;
+            s.Q(i, s.irho) = c.sedov_rho_ext;
+            s.Q(i, s.iP) = c.sedov_P_ext;
+            const double xn = std::fabs(s.POS(i, 0) - half * s.box_l);
+            const double yn = std::fabs(s.POS(i, 1) - half * s.box_l_y);
+            if (xn * xn + yn * yn < c.sedov_r_expl * c.sedov_r_expl) s.Q(i, s.iP) = c.sedov_P_ext + c.sedov_P_cen;
+        }
+    apply_boundaries(s);
+    primtoc(s);
+}
+
 // SI setup (src/setups/SI/setup.f90:1-117): dust2gas_species = dust_eps[k], Stokes_species =
 // dust_stokes[k] (the host computes both, e.g. from the MRN bins of distribution_dust).  Noise:
 // uniform in [-noise_amp, noise_amp] on the three dust velocity components from a counter-based
@@ -1991,6 +2048,8 @@ int32_t oracle_setup_ic(oracle_state* s, double noise_amp, uint64_t seed) {
         case SHARK_SETUP_DUSTYWAVE: setup_dustywave(*s); break;
         case SHARK_SETUP_SI: setup_si(*s, noise_amp, seed); break;
         case SHARK_SETUP_DISK_POLAR: setup_disk(*s, noise_amp, seed); break;
+        case SHARK_SETUP_KH: setup_kh(*s); break;
+        case SHARK_SETUP_SEDOV: setup_sedov(*s); break;
         default: return SHARK_ERR_UNSUPPORTED;
     }
     s->time = 0.0;
@@ -2183,7 +2242,7 @@ int32_t oracle_set_threads(int32_t n) {
 // info.dat (formatted, the reference's labels and edit descriptors I11 / E23.15) and one
 // unformatted stream file per field, active cells in cell order, unit-scaled: x (position(:,1)
 // or radii_c for GEOM 2), rho (unit_d, or unit_dcol = unit_d unit_l for GEOM 2), v, y (2D:
-// position(:,2)), vy, vz (unit_v), P (unit_P = unit_v^2 of the five setups, times unit_l for
+// position(:,2)), vy, vz (unit_v), P (unit_P: unit_v^2, unit_d unit_v^2 in KH; times unit_l for
 // GEOM 2), and with dust rhod_tot, rhod, sd (unit_l), vd, vdy, vdz (species-major), with charging
 // eta_a, eta_o, eta_h, ni, ne, zd.  MHD, NDUSTPSCAL and the 1D-turbulence rms files are not part
 // of any configuration here (MHD = NDUSTPSCAL = TURB = 0).  ctoprim runs first (the final dump of
@@ -2230,7 +2289,8 @@ int32_t oracle_output(oracle_state* s, int32_t iout, double time, const char* pr
     ctoprim(*s);
     const auto& g = s->cfg;
     const double ul = unit_or_1(g.unit_l), ud = unit_or_1(g.unit_d), ut = unit_or_1(g.unit_t);
-    const double uv = ul / ut, uP = uv * uv, udcol = ud * ul;
+    // unit_P: unit_v**2 (disk_polar/units.f90, 1 in the unit-free setups), unit_d unit_v**2 in KH/units.f90
+    const double uv = ul / ut, uP = g.setup == SHARK_SETUP_KH ? ud * (uv * uv) : uv * uv, udcol = ud * ul;
     const bool polar = g.geom == 2;
     char nchar[8];
     std::snprintf(nchar, sizeof nchar, "%05d", iout);

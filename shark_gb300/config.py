@@ -4,6 +4,7 @@ The field order and types must match the C struct exactly; ``tests/test_capi_cpu
 size and the offsets of the default-filled fields against the compiled library.
 """
 import ctypes as C
+import struct
 
 ABI_VERSION = 1
 MAX_DUST = 64
@@ -27,6 +28,8 @@ SETUP_DUSTYWAVE = 2
 SETUP_SI = 3
 SETUP_DISK_POLAR = 4
 SETUP_DUSTYTURB = 5
+SETUP_KH = 6
+SETUP_SEDOV = 7
 
 FLAG_DRAG = 0x1
 FLAG_BACK_REACTION = 0x2
@@ -83,7 +86,10 @@ class SharkConfig(C.Structure):
         ("grw_alpha_turb", _D), ("grw_size_mono", _D), ("grw_slope_mono", _D), ("grw_Abr", _D),
         ("grw_gamma_grains", _D), ("grw_estar_grains", _D), ("grw_kernel", _I), ("grw_mode", _I),
         ("disk_alpha_visc", _D),
-        ("reserved", _D * 11),
+        ("kh_rho_dense", _D), ("kh_rho_diffuse", _D), ("kh_T_dense", _D), ("kh_mach", _D), ("kh_vy0", _D),
+        ("kh_kx", _D),
+        ("sedov_rho_ext", _D), ("sedov_P_ext", _D), ("sedov_P_cen", _D), ("sedov_r_expl", _D),
+        ("reserved", _D * 1),
         ("dx", _P), ("surf", _P), ("vol", _P), ("radii_c", _P), ("position", _P), ("cs", _P),
     ]
 
@@ -159,4 +165,9 @@ def default_config():
     c.grw_gamma_grains = 25.0
     c.grw_estar_grains = 2.8e11
     c.disk_alpha_visc = 1e-2                  # disk_polar/setup_commons.f90:21
+    c.kh_rho_dense, c.kh_rho_diffuse = 1.0, 0.8              # KH/setup_commons.f90:8-9
+    c.kh_T_dense, c.kh_mach, c.kh_vy0, c.kh_kx = 10.0, 0.5, 0.1, 10.0   # KH/setup_commons.f90:13-19
+    c.sedov_rho_ext, c.sedov_P_cen = 1.0, 1.0                # sedov/setup_commons.f90:9-10
+    c.sedov_P_ext = 1e-5                                     # sedov/setup_commons.f90:11
+    c.sedov_r_expl = struct.unpack("f", struct.pack("f", 0.1))[0]   # `r_expl=0.1`: a default-REAL literal
     return c

@@ -312,9 +312,25 @@ int32_t validate(const shark_gpu_config* c) {
     if (c->slope_type < 0 || c->slope_type > 3) return fail(SHARK_ERR_INVALID_ARG, "unknown slope limiter");
     if (c->precision != SHARK_PREC_FP64 && c->precision != SHARK_PREC_MIXED)
         return fail(SHARK_ERR_INVALID_ARG, "precision must be FP64 or MIXED");
-    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_DUSTYTURB)
+    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_SEDOV)
         return fail(SHARK_ERR_UNSUPPORTED, "setup %d has no device hooks in this build", c->setup);
     const int f = c->flags;
+    if (c->setup == SHARK_SETUP_KH || c->setup == SHARK_SETUP_SEDOV) {
+        // both are 2D Cartesian periodic boxes on the adiabatic equation of state
+        // (KH/setup.f90:17-33, sedov/setup.f90:15-33, */boundaries.f90, iso_cs = -1)
+        const char* nm = c->setup == SHARK_SETUP_KH ? "KH" : "sedov";
+        if (c->geom != 0 || c->ny < 4) return fail(SHARK_ERR_UNSUPPORTED, "%s is a 2D Cartesian box", nm);
+        if (c->iso_cs == 1) return fail(SHARK_ERR_UNSUPPORTED, "%s is adiabatic (iso_cs < 1)", nm);
+        if (f & SHARK_FLAG_FORCE_KICK)
+            return fail(SHARK_ERR_UNSUPPORTED, "%s: explicit forces (force_kick) are not built", nm);
+        if (c->setup == SHARK_SETUP_SEDOV && c->ndust > 0)
+            return fail(SHARK_ERR_UNSUPPORTED, "sedov is a gas-only setup");
+        if (c->setup == SHARK_SETUP_KH && (f & SHARK_FLAG_DRAG) && c->ndust > 0) {
+            if (!(c->rhograin > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "rhograin must be > 0");
+            for (int k = 0; k < c->ndust; ++k)
+                if (!(c->dust_size[k] > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "dust_size[%d] must be > 0", k);
+        }
+    }
     if ((f & SHARK_FLAG_VISCOSITY) && c->setup != SHARK_SETUP_DISK_POLAR)
         return fail(SHARK_ERR_UNSUPPORTED, "viscosity: only the polar disk defines eta_visc (disk_polar/setup.f90:67)");
     if (f & SHARK_FLAG_GROWTH) {
@@ -897,6 +913,16 @@ int32_t shark_gpu_config_defaults(shark_gpu_config* cfg) {
     cfg->grw_gamma_grains = 25.0;
     cfg->grw_estar_grains = 2.8e11;
     cfg->disk_alpha_visc = 1e-2;        // disk_polar/setup_commons.f90:21
+    cfg->kh_rho_dense = 1.0;            // KH/setup_commons.f90:8-19
+    cfg->kh_rho_diffuse = 0.8;
+    cfg->kh_T_dense = 10.0;
+    cfg->kh_mach = 0.5;
+    cfg->kh_vy0 = 0.1;
+    cfg->kh_kx = 10.0;
+    cfg->sedov_rho_ext = 1.0;           // sedov/setup_commons.f90:9-12
+    cfg->sedov_P_ext = 1e-5;
+    cfg->sedov_P_cen = 1.0;
+    cfg->sedov_r_expl = (double)0.1f;   // `r_expl=0.1` is a default-REAL literal
     return SHARK_OK;
 }
 
@@ -1341,7 +1367,9 @@ OutUnits out_units(const shark_gpu_config& c) {
     u.ud = unit1(c.unit_d);
     u.ut = unit1(c.unit_t);
     u.uv = u.ul / u.ut;
-    u.uP = u.uv * u.uv;                                   // unit_P = unit_v**2 (disk_polar/units.f90)
+    // unit_P = unit_v**2 (disk_polar/units.f90; 1 in SOD, DUSTYWAVE, SI, dustyTurb, sedov),
+    // unit_d unit_v**2 in KH/units.f90
+    u.uP = c.setup == SHARK_SETUP_KH ? u.ud * (u.uv * u.uv) : u.uv * u.uv;
     u.urho = c.geom == 2 ? u.ud * u.ul : u.ud;            // unit_dcol for GEOM 2
     u.uPe = c.geom == 2 ? u.uP * u.ul : u.uP;
     return u;

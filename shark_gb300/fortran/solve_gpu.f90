@@ -1,7 +1,8 @@
 ! solve_gpu.f90 -- drop-in replacement of src/solver/solve.f90 that runs each step on the GPU.
 !
 ! Build: put this file (and shark_gpu_mod.f90) before src/solver on VPATH instead of solve.f90,
-! add -DSHARK_GPU_SETUP=<1 SOD | 2 DUSTYWAVE | 3 SI> and -DSHARK_GPU_PREC=<0 FP64 | 1 mixed>
+! add -DSHARK_GPU_SETUP=<1 SOD | 2 DUSTYWAVE | 3 SI | 6 KH | 7 sedov> and
+! -DSHARK_GPU_PREC=<0 FP64 | 1 mixed>
 ! to DEFINES and link with -L<repo>/shark_gb300 -lshark_gpu.  The time loop (src/shark.f90),
 ! setups, namelists and output stay as they are.
 !
@@ -62,6 +63,21 @@ subroutine solve(verbose,outputing)
 #if SHARK_GPU_SETUP==3
     cfg%si_q_shear = q_shear; cfg%si_omega = Omega_shear; cfg%si_eta_stream = eta_stream
     cfg%si_rad0 = rad0; cfg%box_l = box_l; cfg%box_l_y = box_l_y
+#endif
+#if SHARK_GPU_SETUP==6
+    ! KH/setup.f90 works in KH/units.f90's code units; its compute_tstop uses rhograin/unit_d
+    cfg%unit_l = unit_l; cfg%unit_d = unit_d; cfg%unit_t = unit_t; cfg%mu_gas = mu_gas
+    cfg%box_l = box_l; cfg%box_l_y = box_l_y
+    cfg%kh_rho_dense = rho_dense; cfg%kh_rho_diffuse = rho_diffuse; cfg%kh_T_dense = T_dense
+    cfg%kh_mach = Mach; cfg%kh_vy0 = vy0; cfg%kh_kx = kx
+#if NDUST>0
+    cfg%rhograin = rhograin/unit_d
+#endif
+#endif
+#if SHARK_GPU_SETUP==7
+    cfg%box_l = box_l; cfg%box_l_y = box_l_y
+    cfg%sedov_rho_ext = rho_ext; cfg%sedov_P_ext = P_ext; cfg%sedov_P_cen = P_cen
+    cfg%sedov_r_expl = r_expl
 #endif
     rc = shark_gpu_init(cfg, gpu_ctx)
     if (rc /= SHARK_OK) stop 'shark_gpu_init failed'

@@ -15,7 +15,7 @@ import numpy as np
 import math
 
 from .config import (SharkConfig, default_config, SETUP_SOD, SETUP_DUSTYWAVE, SETUP_SI, SETUP_DISK_POLAR,
-                     SETUP_DUSTYTURB, FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO,
+                     SETUP_DUSTYTURB, SETUP_KH, SETUP_SEDOV, FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO,
                      FLAG_CHARGING, FLAG_GROWTH, GROWTH_TURB, GROWTH_BROWNIAN, GROWTH_DRIFT, PREC_FP64)
 
 GROWTH_DEFAULT = GROWTH_TURB | GROWTH_BROWNIAN | GROWTH_DRIFT
@@ -201,19 +201,19 @@ def dustywave(nx=2048, ndust=4, eps=None, tstop=None, K=None, cs0=1.0, rho_0=1.0
 # SI shearing box
 # ---------------------------------------------------------------------------------------------
 def mrn_bins(ndust, smin, smax, scutmin, scut, dust2gas, mrn=3.5, rhograin=1.0,
-             dust_ratio_min=1e-11):
+             dust_ratio_min=1e-11, unit_l=1.0, unit_m=1.0):
     """distribution_dust(.true.) + mrn_distri (src/dust/dust_init.f90:11-103,164-197).
 
-    Returns (sdust, eps) per species (ice mantle excluded)."""
+    Returns (sdust, eps) per species (ice mantle excluded), radii in code units (/unit_l)."""
     zeta = (smax / smin) ** (1.0 / ndust)
     eta = zeta ** 3.0
-    m_min = F43 * PI * rhograin * smin ** 3.0
-    aminus = np.array([smin * _powi(zeta, k) for k in range(ndust)])
-    aplus = np.array([smin * _powi(zeta, k + 1) for k in range(ndust)])
+    m_min = F43 * PI * rhograin * smin ** 3.0 / unit_m
+    aminus = np.array([smin * _powi(zeta, k) / unit_l for k in range(ndust)])
+    aplus = np.array([smin * _powi(zeta, k + 1) / unit_l for k in range(ndust)])
     sdust = np.sqrt(aminus * aplus)
     massmin = m_min
-    mono1 = F43 * PI * rhograin * scutmin ** 3.0
-    mono2 = F43 * PI * rhograin * scut ** 3.0
+    mono1 = F43 * PI * rhograin * scutmin ** 3.0 / unit_m
+    mono2 = F43 * PI * rhograin * scut ** 3.0 / unit_m
     icutmin = max(1, int(np.floor(np.log(mono1 / massmin) / np.log(eta) + 1)))
     icutmax = min(int(np.floor(np.log(mono2 / massmin) / np.log(eta) + 1)), ndust)
     eps = np.zeros(ndust)
@@ -552,7 +552,126 @@ def turb_ic(cfg, mach, seed, kmin, kmax):
     return u0
 
 
+# ---------------------------------------------------------------------------------------------
+# Kelvin-Helmholtz shear layer
+# ---------------------------------------------------------------------------------------------
+GRAV = 6.67e-8       # src/commons/phys_const.f90:10
+
+# test/KH/kh.nml of the reference: a 1 au box of 1e-18 g cm^-3 gas at 10 K, Mach 0.25 shear,
+# MRN grains from 5e-7 to 0.1 cm (initial 1e-7 .. 2.5e-5 cm) of density 2.3, MC limiter, CFL 0.1
+KH_NML = dict(box_pc=4.8481e-6, rho_dense=1.0e-18, rho_diffuse=1.0e-18, T_dense=10.0, mach=0.25, vy0=0.1,
+              kx=2.0, smin=5e-7, scutmin=1e-7, scut=250e-7, smax=0.10, rhograin=2.3, dust2gas=0.01,
+              mrn=3.5, gamma=1.666667, slope_type=3, cfl=0.1)
+
+
+def kh_units(mu_gas=2.31):
+    """(unit_l, unit_d, unit_t) of KH/units.f90: parsec, mu_gas mH, 1/sqrt(G unit_d)."""
+    unit_d = mu_gas * MH
+    return PC, unit_d, 1.0 / math.sqrt(GRAV * unit_d)
+
+
+def kh(n=256, ny=None, ndust=4, box_pc=1.0, rho_dense=1.0, rho_diffuse=0.8, T_dense=10.0, mach=0.5,
+       vy0=0.1, kx=10.0, smin=1e-7, smax=1e-2, scutmin=5e-7, scut=250e-7, mrn=3.5, rhograin=2.7,
+       dust2gas=0.01, gamma=1.66667, cfl=0.5, slope_type=1, solver=2, drag=True, precision=PREC_FP64):
+    """Kelvin-Helmholtz shear layer (src/setups/KH/setup.f90:1-51, setup_commons.f90, units.f90).
+
+    Inputs are cgs and Kelvin as in the reference's namelist (box in parsec); the run is in the
+    setup's code units (unit_l = pc, unit_d = mu_gas mH, unit_t = 1/sqrt(G unit_d)).  Periodic,
+    adiabatic; grains in ``ndust`` MRN bins (distribution_dust), or one species of radius
+    ``scut`` at dust-to-gas ratio 0.01 for ``ndust == 1``, at rest, with Epstein drag on the
+    adiabatic sound speed (KH/setup.f90:218-239) and back reaction.  Defaults are the reference's
+    (KH/setup_commons.f90, dust_commons.f90); ``KH_NML`` holds its test/KH/kh.nml values.
+    """
+    cfg = default_config()
+    cfg.nx = n
+    cfg.ny = n if ny is None else ny
+    cfg.ndust = ndust
+    cfg.gamma, cfg.cfl, cfg.slope_type, cfg.solver = gamma, cfl, slope_type, solver
+    cfg.precision = precision
+    cfg.setup = SETUP_KH
+    cfg.flags = (FLAG_DRAG | FLAG_BACK_REACTION) if (ndust > 0 and drag) else 0
+    cfg.mu_gas = 2.31
+    ul, ud, ut = kh_units(cfg.mu_gas)
+    cfg.unit_l, cfg.unit_d, cfg.unit_t = ul, ud, ut
+    cfg.box_l = cfg.box_l_y = box_pc
+    cfg.kh_rho_dense, cfg.kh_rho_diffuse, cfg.kh_T_dense = rho_dense, rho_diffuse, T_dense
+    cfg.kh_mach, cfg.kh_vy0, cfg.kh_kx = mach, vy0, kx
+    cfg.rhograin = rhograin / ud                    # (rhograin/unit_d) of compute_tstop
+    if ndust == 1:
+        cfg.dust_size[0] = scut / ul                # KH/setup.f90:41
+        cfg.dust_eps[0] = float(np.float32(0.01))   # `epsilondust = 0.01`: a default-REAL literal
+    elif ndust > 1:
+        sdust, eps = mrn_bins(ndust, smin, smax, scutmin, scut, dust2gas, mrn=mrn, rhograin=rhograin,
+                              dust_ratio_min=cfg.dust_ratio_min, unit_l=ul, unit_m=ul ** 3 * ud)
+        for k in range(ndust):
+            cfg.dust_size[k] = sdust[k]
+            cfg.dust_eps[k] = eps[k]
+    return cfg, kh_ic(cfg)
+
+
+def kh_ic(cfg):
+    """Initial conserved state of the shear layer (KH/setup.f90:17-51), over all cells and then
+    periodic ghosts."""
+    uv = cfg.unit_l / cfg.unit_t
+    uP = cfg.unit_d * (uv * uv)
+    cs = math.sqrt(cfg.gamma * KB * cfg.kh_T_dense / (cfg.mu_gas * MH))     # KH/eos.f90 cs_eos
+    pos = positions(cfg)
+    xx = pos[:, 0] - 0.5 * cfg.box_l
+    yy = pos[:, 1] - 0.5 * cfg.box_l_y
+    band = np.abs(yy / cfg.box_l_y) < 0.25
+    q = np.zeros((cfg.nvar, cfg.ncells))
+    q[0] = np.where(band, cfg.kh_rho_diffuse / cfg.unit_d, cfg.kh_rho_dense / cfg.unit_d)
+    q[1] = np.where(band, -(cs * cfg.kh_mach / uv / 2.0), cs * cfg.kh_mach / uv * 0.5)
+    # libm's cos per grid column (numpy's vectorised cos may differ in the last bit)
+    cosx = {v: math.cos(v * 2.0 * cfg.kh_kx * PI / cfg.box_l) for v in np.unique(xx).tolist()}
+    q[2] = (cfg.kh_vy0 * cs * cfg.kh_mach * np.array([cosx[v] for v in xx.tolist()])) / uv
+    q[4] = cfg.kh_rho_dense * (cs * cs) / uP
+    for k in range(cfg.ndust):
+        q[5 + k] = cfg.dust_eps[k] * q[0]
+    u0 = primtoc(cfg, q).reshape(-1)
+    periodic_boundaries(cfg, u0)
+    return u0
+
+
+# ---------------------------------------------------------------------------------------------
+# Sedov blast wave
+# ---------------------------------------------------------------------------------------------
+def sedov(n=256, box_l=1.0, rho_ext=1.0, P_ext=1e-5, P_cen=1.0, r_expl=None, gamma=1.66667, cfl=0.5,
+          slope_type=1, solver=2, precision=PREC_FP64):
+    """2D Sedov blast wave in a periodic square (src/setups/sedov/setup.f90:1-34,
+    setup_commons.f90): gas at rest of density ``rho_ext`` and pressure ``P_ext``, raised by
+    ``P_cen`` inside radius ``r_expl`` of the box centre.  Unit-free, gas only.  The default
+    radius is the reference's `r_expl=0.1`, a default-REAL literal (0.1 rounded to float)."""
+    cfg = default_config()
+    cfg.nx = cfg.ny = n
+    cfg.ndust = 0
+    cfg.gamma, cfg.cfl, cfg.slope_type, cfg.solver = gamma, cfl, slope_type, solver
+    cfg.precision = precision
+    cfg.setup = SETUP_SEDOV
+    cfg.flags = 0
+    cfg.box_l = cfg.box_l_y = box_l
+    cfg.sedov_rho_ext, cfg.sedov_P_ext, cfg.sedov_P_cen = rho_ext, P_ext, P_cen
+    if r_expl is not None:
+        cfg.sedov_r_expl = r_expl
+    return cfg, sedov_ic(cfg)
+
+
+def sedov_ic(cfg):
+    """Initial conserved state of the blast (sedov/setup.f90:15-33): active cells set, ghosts
+    from the periodic images."""
+    pos = positions(cfg)
+    xn = np.abs(pos[:, 0] - 0.5 * cfg.box_l)
+    yn = np.abs(pos[:, 1] - 0.5 * cfg.box_l_y)
+    q = np.zeros((cfg.nvar, cfg.ncells))
+    q[0] = cfg.sedov_rho_ext
+    q[4] = np.where(xn * xn + yn * yn < cfg.sedov_r_expl * cfg.sedov_r_expl,
+                    cfg.sedov_P_ext + cfg.sedov_P_cen, cfg.sedov_P_ext)
+    u0 = primtoc(cfg, q).reshape(-1)
+    periodic_boundaries(cfg, u0)
+    return u0
+
+
 def build(name, **kw):
-    """Dispatch by setup name ('sod', 'dustywave', 'si', 'disk_polar', 'dusty_turb')."""
+    """Dispatch by setup name ('sod', 'dustywave', 'si', 'disk_polar', 'dusty_turb', 'kh', 'sedov')."""
     return {"sod": sod, "dustywave": dustywave, "si": si, "disk_polar": disk_polar,
-            "dusty_turb": dusty_turb}[name](**kw)
+            "dusty_turb": dusty_turb, "kh": kh, "sedov": sedov}[name](**kw)

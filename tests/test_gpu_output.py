@@ -4,7 +4,7 @@ after the same steps, and the restart reader (the reference's read_output is a s
 Files: the same set, info.dat text identical, every field stream within the path's parity
 tolerance, as relative L1 with velocities scaled by the species' velocity magnitude (FP64: 1e-10,
 set by the last bit of exp() in the charging and the disk relaxation; mixed: 1e-5, and 2e-4 for
-the Mach-1 forced box, the stated mixed tolerance of its parity test).  Restart: the state read back
+the Mach-1 forced box and the KH shear layer, whose band edges amplify FP32 round-off).  Restart: the state read back
 equals the written one to rounding (unit scaling and ctoprim/primtoc round trip, 1e-13 relative),
 and the next step's dt agrees to 1e-12."""
 import os
@@ -25,6 +25,8 @@ def _case(make, precision=K.PREC_FP64):
         return setups.si(n=32, ndust=3, precision=precision)
     if make == "disk":
         return setups.disk_polar_au(nr=24, nphi=32, ndust=3, noise=1e-2, precision=precision)
+    if make == "kh":
+        return setups.kh(n=32, ndust=3, precision=precision, **setups.KH_NML)
     return setups.dusty_turb(n=64, ndust=4, charging=True, forcing=True, precision=precision)
 
 
@@ -32,7 +34,7 @@ def _files(d):
     return sorted(os.listdir(d))
 
 
-@pytest.mark.parametrize("make", ["si", "disk", "turb"])
+@pytest.mark.parametrize("make", ["si", "disk", "turb", "kh"])
 @pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED])
 def test_output_matches_oracle(tmp_path, make, prec):
     cfg, u0 = _case(make, prec)
@@ -52,7 +54,7 @@ def test_output_matches_oracle(tmp_path, make, prec):
     assert _files(dg) == _files(dc)
     assert open(dg / "info.dat").read() == open(dc / "info.dat").read()
     R = lambda d, n: np.fromfile(d / n, dtype="<f8")
-    tol = 1e-10 if prec == K.PREC_FP64 else (2e-4 if make == "turb" else 1e-5)
+    tol = 1e-10 if prec == K.PREC_FP64 else (2e-4 if make in ("turb", "kh") else 1e-5)
     for name in _files(dc):
         if name == "info.dat":
             continue
@@ -71,7 +73,7 @@ def test_output_matches_oracle(tmp_path, make, prec):
         assert err <= tol, (name, err)
 
 
-@pytest.mark.parametrize("make", ["si", "disk", "turb"])
+@pytest.mark.parametrize("make", ["si", "disk", "turb", "kh"])
 def test_restart_round_trip(tmp_path, make):
     cfg, u0 = _case(make)
     with Shark(cfg) as a, Shark(cfg) as b:

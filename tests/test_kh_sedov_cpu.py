@@ -1,0 +1,134 @@
+"""The KH shear layer and the Sedov blast (src/setups/KH, src/setups/sedov) on the CPU: the host
+builders against the oracle's restatement of the two setup routines, the configuration checks of
+the C ABI, and properties of a few oracle steps (periodic conservation, the blast's symmetry).
+
+Neither setup has golden data in the reference's test suite, so these tests pin the builders to
+the oracle and the oracle to the properties the problems have."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from shark_gb300 import build as gbuild, config as K, setups
+from shark_gb300.solver import load_library
+from oracle.oracle import Oracle
+
+
+@pytest.fixture(scope="module")
+def lib():
+    gbuild.build()
+    return load_library()
+
+
+def _oracle_ic(cfg):
+    """The oracle's setup, then the periodic fill every step begins with: the reference fills
+    the ghosts before primtoc, so right after setup they hold the formula's values (KH) or zeros
+    (sedov); the builders hand over the periodic images."""
+    o = Oracle(cfg)
+    o.setup_ic()
+    o.apply_boundaries()
+    return o, o.get_u()
+
+
+def _active(cfg, u):
+    g = u.reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)
+    ng = cfg.nghost
+    return g[:, ng:ng + cfg.ny, ng:ng + cfg.nx]
+
+
+@pytest.mark.parametrize("ndust", [0, 1, 4])
+def test_kh_builder_matches_oracle_setup(ndust):
+    kw = dict(setups.KH_NML)
+    cfg, u0 = setups.kh(n=32, ndust=ndust, **kw)
+    _, ref = _oracle_ic(cfg)
+    np.testing.assert_array_equal(u0, ref)
+
+
+def test_kh_default_builder_matches_oracle_setup():
+    cfg, u0 = setups.kh(n=24, ny=40, ndust=3)
+    _, ref = _oracle_ic(cfg)
+    np.testing.assert_array_equal(u0, ref)
+
+
+def test_kh_state_in_code_units():
+    """Pressure equilibrium across the band, shear of +-Mach cs/2, the MRN bins of the namelist."""
+    cfg, u0 = setups.kh(n=32, ndust=4, **setups.KH_NML)
+    a = _active(cfg, u0)
+    uv = cfg.unit_l / cfg.unit_t
+    cs = np.sqrt(cfg.gamma * setups.KB * 10.0 / (2.31 * setups.MH))
+    rho = a[0]
+    vx = a[1] / rho
+    assert np.allclose(np.unique(np.round(vx * uv / cs, 12)), [-0.125, 0.125])
+    assert np.allclose(rho * cfg.unit_d, 1e-18)
+    p = (cfg.gamma - 1.0) * (a[4] - 0.5 * (a[1] ** 2 + a[2] ** 2) / rho)
+    assert np.allclose(p * cfg.unit_d * uv ** 2, 1e-18 * cs ** 2, rtol=1e-12)
+    eps = a[5:9].sum(0) / rho
+    assert np.allclose(eps, 0.01, rtol=1e-9)
+    assert np.all(a[9:] == 0)                                   # grains start at rest
+    sizes = np.array(cfg.dust_size[:4]) * cfg.unit_l
+    assert np.all(np.diff(sizes) > 0) and 5e-7 < sizes[0] < sizes[-1] < 0.1
+
+
+def test_sedov_builder_matches_oracle_setup():
+    cfg, u0 = setups.sedov(n=40)
+    _, ref = _oracle_ic(cfg)
+    np.testing.assert_array_equal(u0, ref)
+    a = _active(cfg, u0)
+    hot = a[4] * (cfg.gamma - 1.0) > 0.5
+    # cells whose centre lies within r_expl = 0.1 (as a float) of the centre of the unit box
+    assert hot.sum() == 52         # 13 per quadrant of the 40^2 grid (centres at (i + 1/2)/40)
+
+
+def test_oracle_steps_conserve_in_the_periodic_boxes():
+    """Mass of the gas and of the grains above the floor, gas + dust momentum; total energy
+    where nothing heats the gas (the drag heating of a dusty adiabatic gas changes it)."""
+    runs = ((setups.kh(n=32, ndust=2, **setups.KH_NML), False), (setups.kh(n=32, ndust=0), True),
+            (setups.sedov(n=32), True))
+    for (cfg, u0), energy in runs:
+        o = Oracle(cfg)
+        o.set_u(u0)
+        t0 = _active(cfg, u0).reshape(cfg.nvar, -1).sum(1)
+        o.run(6)
+        t1 = _active(cfg, o.get_u()).reshape(cfg.nvar, -1).sum(1)
+        scale = np.abs(_active(cfg, u0)).reshape(cfg.nvar, -1).sum(1)
+        N = cfg.ndust
+        # species held at the dust_ratio_min floor gain mass from the floor
+        dust = [5 + k for k in range(N) if cfg.dust_eps[k] > 1e3 * cfg.dust_ratio_min]
+        cons = [0] + dust + ([4] if energy else [])
+        assert np.all(np.abs(t1[cons] - t0[cons]) <= 1e-12 * scale[cons]), (cfg.setup, t1 - t0)
+        for gv in (1, 2):
+            dv0 = 5 + gv * N
+            m0 = t0[gv] + t0[dv0:dv0 + N].sum()
+            m1 = t1[gv] + t1[dv0:dv0 + N].sum()
+            assert abs(m1 - m0) <= 1e-12 * (scale[gv] + scale[dv0:dv0 + N].sum() + scale[0])
+
+
+def test_sedov_blast_stays_symmetric():
+    cfg, u0 = setups.sedov(n=32)
+    o = Oracle(cfg)
+    o.set_u(u0)
+    o.run(20)
+    a = _active(cfg, o.get_u())
+    rho = a[0]
+    assert rho.max() > 1.05 * cfg.sedov_rho_ext                    # a shell has formed
+    np.testing.assert_allclose(rho, rho.T, rtol=1e-10, atol=0)      # x <-> y
+    np.testing.assert_allclose(rho, rho[::-1, :], rtol=1e-10, atol=0)
+    np.testing.assert_allclose(rho, rho[:, ::-1], rtol=1e-10, atol=0)
+
+
+def test_kh_and_sedov_configs_are_checked_before_touching_a_device(lib):
+    h = C.c_void_p()
+    kh, _ = setups.kh(n=16, ndust=2)
+    sd, _ = setups.sedov(n=16)
+    cases = []
+    bad = kh.copy(); bad.ny = 1; cases.append((bad, K.ERR_UNSUPPORTED, b"2D"))
+    bad = kh.copy(); bad.iso_cs = 1; cases.append((bad, K.ERR_UNSUPPORTED, b"adiabatic"))
+    bad = kh.copy(); bad.flags |= K.FLAG_FORCE_KICK; cases.append((bad, K.ERR_UNSUPPORTED, b"force_kick"))
+    bad = kh.copy(); bad.dust_size[1] = 0.0; cases.append((bad, K.ERR_INVALID_ARG, b"dust_size"))
+    bad = kh.copy(); bad.flags |= K.FLAG_GROWTH; cases.append((bad, K.ERR_UNSUPPORTED, b"growth"))
+    bad = sd.copy(); bad.ndust = 2; cases.append((bad, K.ERR_UNSUPPORTED, b"gas-only"))
+    bad = sd.copy(); bad.geom = 2; cases.append((bad, K.ERR_UNSUPPORTED, b"Cartesian"))
+    bad = sd.copy(); bad.setup = 8; cases.append((bad, K.ERR_UNSUPPORTED, b"setup 8"))
+    for cfg, code, msg in cases:
+        assert lib.shark_gpu_init(C.byref(cfg), C.byref(h)) == code, msg
+        assert msg in lib.shark_gpu_last_error(), (msg, lib.shark_gpu_last_error())

@@ -52,7 +52,7 @@ def test_e23_15_examples():
     assert fortran_e23_15(0.0) == "  0.000000000000000E+00"
 
 
-@pytest.mark.parametrize("make", ["si", "sod", "disk", "turb"])
+@pytest.mark.parametrize("make", ["si", "sod", "disk", "turb", "kh"])
 def test_oracle_output_layout(tmp_path, make):
     if make == "si":
         cfg, u0 = setups.si(n=16, ndust=3)
@@ -60,6 +60,8 @@ def test_oracle_output_layout(tmp_path, make):
         cfg, u0 = setups.sod(nx=64, ndust=2)
     elif make == "disk":
         cfg, u0 = setups.disk_polar_au(nr=12, nphi=16, ndust=2, noise=1e-2)
+    elif make == "kh":
+        cfg, u0 = setups.kh(n=12, ndust=2, **setups.KH_NML)
     else:
         cfg, u0 = setups.dusty_turb(n=8, ndust=3, charging=True)
     o = Oracle(cfg)
@@ -79,7 +81,8 @@ def test_oracle_output_layout(tmp_path, make):
     ud = cfg.unit_d or 1.0
     ut = cfg.unit_t or 1.0
     uv = ul / ut
-    assert info["unit_v"] == fortran_e23_15(uv) and info["unit_p"] == fortran_e23_15(uv * uv)
+    uP = ud * (uv * uv) if cfg.setup == K.SETUP_KH else uv * uv     # KH/units.f90: unit_d unit_v**2
+    assert info["unit_v"] == fortran_e23_15(uv) and info["unit_p"] == fortran_e23_15(uP)
     for line in open(os.path.join(d, "info.dat")):
         assert len(line.rstrip("\n").split("=")[1]) in (11, 23)
     q, _ = o.get_q()
@@ -91,7 +94,7 @@ def test_oracle_output_layout(tmp_path, make):
     np.testing.assert_array_equal(_read(d, "v"), qa[1] * uv)
     np.testing.assert_array_equal(_read(d, "vy"), qa[2] * uv)
     np.testing.assert_array_equal(_read(d, "vz"), qa[3] * uv)
-    np.testing.assert_array_equal(_read(d, "P"), qa[4] * (uv * uv) * ul if polar else qa[4] * (uv * uv))
+    np.testing.assert_array_equal(_read(d, "P"), qa[4] * uP * ul if polar else qa[4] * uP)
     grid = o.grid()
     xs = grid["radii_c"] if polar else grid["position"][0]
     np.testing.assert_array_equal(_read(d, "x"), _active(cfg, xs)[0])
