@@ -43,10 +43,11 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
     const bool col_upd = lane >= 2 && lane <= 29 && gx < p.ng + p.nx;                    // cell updated
     const bool col_active = gx >= p.ng && gx < p.ng + p.nx;
 
-    const R dt = R(*p.dt);
+    const R dt = step_dt(p);
     const R half = R(0.5);
-    const R gamma = R(p.gamma);
-    const R inv_g1 = R(1.0 / (p.gamma - 1.0));
+    const R gamma = prm<R>(p.gamma, p.f_gamma);
+    const R inv_g1 = prm<R>(1.0 / (p.gamma - 1.0), p.f_inv_g1);
+    const R smallP = prm<R>(p.smallp, p.f_smallp), smallR = prm<R>(p.smallr, p.f_smallr);
     const bool fk = (p.flags & SHARK_FLAG_FORCE_KICK) != 0;
     const bool polar = (p.geom == 2);
     const bool iso = (p.iso == 1);
@@ -90,13 +91,13 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
             if constexpr (FAST) {
                 const R ir = R(1) / rho;
                 vx = px * ir; vy = py * ir; vz = pz * ir;
-                P = fmax2((gamma - R(1)) * (us[4] - half * (px * vx + py * vy + pz * vz)), R(p.smallp));
+                P = fmax2((gamma - R(1)) * (us[4] - half * (px * vx + py * vy + pz * vz)), smallP);
             } else {
                 vx = px / rho; vy = py / rho; vz = pz / rho;
                 const R ekin = half * rho * sq(px / rho) + half * rho * sq(py / rho) + half * rho * sq(pz / rho);
-                P = fmax2((gamma - R(1)) * (us[4] - ekin - R(0)), R(p.smallp));
+                P = fmax2((gamma - R(1)) * (us[4] - ekin - R(0)), smallP);
             }
-            const R qrho = fmax2(rho, R(p.smallr));
+            const R qrho = fmax2(rho, smallR);
             if (!iso) c = sqrt(gamma * P / qrho);
             else { c = cs_col; P = rho * sq(c); }
             q[0] = qrho; q[1] = vx; q[2] = vy; q[3] = vz; q[4] = P;
@@ -185,7 +186,6 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 su0 = -u * dux - v * duy - dpx_r + over_r(sq(v));
                 sv0 = -u * dvx - v * dvy - dpy_r - over_r(u * v);
             }
-            const R smallP = R(p.smallp);
             if constexpr (FAST) {
                 const R b0 = r_rho + hdt * sr0, b1 = u + hdt * su0, b2 = v + hdt * sv0, b3 = w + hdt * sw0, b4 = pp + hdt * sp0;
                 qmx[0] = b0 + hdx * drx; qpx[0] = b0 - hdx * drx;

@@ -76,7 +76,7 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
     const bool upd_a = !halo && ga < p.ng + p.nx, upd_b = !halo && ga + 1 < p.ng + p.nx;
     const bool act_a = ga >= p.ng && ga < p.ng + p.nx, act_b = ga + 1 >= p.ng && ga + 1 < p.ng + p.nx;
 
-    const float dt = (float)*p.dt;
+    const float dt = *p.dtf;
     const float qdt = 0.25f * dt;
     // column tables: x-face factors of the faces left of a, between a and b, right of b
     const float sfa = p.sfx[ca], sfb = p.sfx[cb], sfc = p.sfx[cc];
@@ -89,9 +89,9 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
     const float2 hy = make_float2(0.25f * p.dx2[ca], 0.25f * p.dx2[cb]), nhy = make_float2(-hy.x, -hy.y);
     // SI force kick on the dust (setup_force, species s >= 1): f1 = 2 q om^2 xc - 2 om vz, f3 = 2 om vx
     const bool fk = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
-    const float om = (float)p.si_om, qs = (float)p.si_q;
-    const float2 f1c = make_float2(2.f * qs * (om * om) * (p.xpos[ca] - 0.5f * (float)p.box_l),
-                                   2.f * qs * (om * om) * (p.xpos[cb] - 0.5f * (float)p.box_l));
+    const float om = p.f_si_om, qs = p.f_si_q;
+    const float2 f1c = make_float2(2.f * qs * (om * om) * (p.xpos[ca] - p.f_half_box_l),
+                                   2.f * qs * (om * om) * (p.xpos[cb] - p.f_half_box_l));
     const float2 m2om = bc2(-2.f * om), p2om = bc2(2.f * om);
 
     float2 q0[4], q1[4], q2[4];      // primitive rows P-1, P, P+1

@@ -43,6 +43,13 @@ static KParams<R> make_params(const DeviceView& v) {
     p.dK = v.dK; p.dtstop = v.dtstop; p.dsize = v.dsize; p.dstokes = v.dstokes; p.dinvts = v.dinvts;
     p.turb_rho0 = c.turb_rho0;
     p.dt = nullptr; p.dt_next = nullptr; p.status = v.status; p.coef = v.coef;
+    p.dtf = v.coef + 2 * SHARK_MAX_DUST;
+    p.f_gamma = (float)c.gamma; p.f_gm1 = (float)(c.gamma - 1.0); p.f_inv_g1 = (float)(1.0 / (c.gamma - 1.0));
+    p.f_cfl = (float)c.cfl; p.f_smallr = (float)c.smallr; p.f_smallp = (float)c.smallp;
+    p.f_dust_ratio_min = (float)c.dust_ratio_min;
+    p.f_box_l = (float)c.box_l; p.f_half_box_l = 0.5f * (float)c.box_l;
+    p.f_si_q = (float)c.si_q_shear; p.f_si_om = (float)c.si_omega;
+    p.f_si_r0 = (float)c.si_rad0; p.f_si_eta = (float)c.si_eta_stream;
     p.u_cur = (const R*)v.u[v.cur];
     p.u_next = (R*)v.u[(v.cur + 1) % v.nbuf];
     return p;

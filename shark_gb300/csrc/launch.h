@@ -9,6 +9,10 @@
 
 namespace shark {
 
+// Floats of the per-step buffer `coef`: the drag coefficients 1/(1+a_k), a_k/(1+a_k) of the
+// species, then the step's dt as float.
+constexpr int SHARK_COEF_FLOATS = 2 * SHARK_MAX_DUST + 4;
+
 // Charging (K5) tables, outputs and constants; see charge.cuh.
 struct ChargeView {
     bool on;
@@ -50,7 +54,7 @@ struct DeviceView {
     const double* dinvts;       // 1/C_k with t_k = C_k / (cell factor) for the per-cell stopping times
     double* dt_slots;           // [2] dt of step n lives in slot n % 2
     unsigned int* status;       // OR of SHARK_STATUS_* bits
-    float* coef;                // [2*SHARK_MAX_DUST] per-step drag coefficients (mixed path)
+    float* coef;                // [SHARK_COEF_FLOATS] per-step drag coefficients (mixed path), float dt
     cudaStream_t stream;
     cudaStream_t stream2;       // side stream for the gas flux kernel (forked/joined per step)
     cudaEvent_t fork, join;

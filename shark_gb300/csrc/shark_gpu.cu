@@ -83,7 +83,7 @@ struct shark_gpu_ctx {
     double* species = nullptr;       // dK | dtstop | dsize | dstokes | dinvts (5 x SHARK_MAX_DUST)
     double* dt_slots = nullptr;      // [2]
     unsigned int* status = nullptr;
-    float* coef = nullptr;           // per-step drag coefficients
+    float* coef = nullptr;           // per-step drag coefficients, then the step's dt as float
     double* staging = nullptr;       // ncells*nvar FP64 (Fortran order) for uploads/downloads
     double* part = nullptr;          // totals partials
     double* tot_out = nullptr;
@@ -1048,8 +1048,8 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     INIT_TRY(cudaMalloc(&c->dt_slots, 2 * sizeof(double)));
     INIT_TRY(cudaMalloc(&c->status, sizeof(unsigned int)));
     INIT_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
-    INIT_TRY(cudaMalloc(&c->coef, 2 * SHARK_MAX_DUST * sizeof(float)));
-    INIT_TRY(cudaMemsetAsync(c->coef, 0, 2 * SHARK_MAX_DUST * sizeof(float), c->stream));
+    INIT_TRY(cudaMalloc(&c->coef, shark::SHARK_COEF_FLOATS * sizeof(float)));
+    INIT_TRY(cudaMemsetAsync(c->coef, 0, shark::SHARK_COEF_FLOATS * sizeof(float), c->stream));
     v.dt_slots = c->dt_slots;
     v.status = c->status;
     v.coef = c->coef;

@@ -58,9 +58,29 @@ struct KParams {
     unsigned long long* dt_next;      // bit image of the next dt (positive doubles order as u64)
     unsigned int* status;             // SHARK_STATUS_* bits
     float* coef;                      // [2*SHARK_MAX_DUST] per-step drag coefficients 1/(1+a_k), a_k/(1+a_k)
+    const float* dtf;                 // (float) dt of the current step, coef[2*SHARK_MAX_DUST]
+    // FP32 copies of the scalar parameters for the mixed kernels, converted once on the host: a
+    // double-to-float conversion issues on the FP64 pipe, which is narrow and variable-latency on
+    // this GPU, so per-thread conversions stall the warps that do them
+    float f_gamma, f_gm1, f_inv_g1, f_cfl, f_smallr, f_smallp, f_dust_ratio_min, f_box_l, f_half_box_l;
+    float f_si_q, f_si_om, f_si_r0, f_si_eta;
     const R* u_cur;                   // state at the start of the step (read only)
     R* u_next;                        // state after the step
 };
+
+// A scalar parameter in the kernel's precision: the double itself, or its float copy.
+template <typename R>
+__device__ __forceinline__ R prm(double d, float f) {
+    if constexpr (std::is_same<R, float>::value) return f;
+    else return d;
+}
+
+// dt of the current step in the kernel's precision (the float copy k_prepare_step wrote).
+template <typename R>
+__device__ __forceinline__ R step_dt(const KParams<R>& p) {
+    if constexpr (std::is_same<R, float>::value) return *p.dtf;
+    else return *p.dt;
+}
 
 template <typename R>
 __device__ __forceinline__ long long uidx(const KParams<R>& p, int v, int iy, int ix) {
@@ -203,7 +223,7 @@ __device__ __forceinline__ void fill_ghost_images(const KParams<R>& p, R* u, int
     if (tx < 0 && ty < 0) return;
     const bool shear = p.setup == SHARK_SETUP_SI;
     const R sgn = (tx >= 0 && tx > gx) ? R(1) : R(-1);   // right ghost: + rho q Omega L
-    const R qoL = R(p.si_q), om = R(p.si_om), L = R(p.box_l);
+    const R qoL = prm<R>(p.si_q, p.f_si_q), om = prm<R>(p.si_om, p.f_si_om), L = prm<R>(p.box_l, p.f_box_l);
     const int N = p.ndust;
     for (int v = 0; v < p.nvar; ++v) {
         R val = u[uidx(p, v, gy, gx)];
@@ -811,7 +831,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                 }
                 float rk[NMAX], wk[NMAX];
                 const float rho_old = ucur[(0) * pl];
-                const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
+                const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
                 const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
                 const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
                 float rhon = rho, pnx = px, pny = py, pnz = pz;
@@ -826,7 +846,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                 }
                 const float irhon = 1.0f / rhon;
                 const float vbx = pnx * irhon, vby = pny * irhon, vbz = pnz * irhon;
-                const float fl = rho * (float)p.dust_ratio_min;   // floor (dust_drag.f90:63-73)
+                const float fl = rho * p.f_dust_ratio_min;   // floor (dust_drag.f90:63-73)
 #pragma unroll
                 for (int k = 0; k < NS; ++k) {
                     const float wr = wk[k] * dr[k];
@@ -850,7 +870,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
             float rk[NMAX], wk[NMAX];
             float rhon = rho, pnx = px, pny = py, pnz = pz;
             const float rho_old = ucur[(0) * pl];
-            const double qrho_old = (double)fmaxf(rho_old, (float)p.smallr);
+            const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
             const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
             const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
             for (int k = 0; k < N; ++k) {
@@ -884,7 +904,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                 uc[(2) * pl] = py;
                 uc[(3) * pl] = pz;
             }
-            const float fl = rho * (float)p.dust_ratio_min;   // floor (dust_drag.f90:63-73)
+            const float fl = rho * p.f_dust_ratio_min;   // floor (dust_drag.f90:63-73)
             for (int k = 0; k < N; ++k) {
                 const long long ir = uidx(p, 5 + k, gy, gx);
                 if (fl > u[ir]) u[ir] = fl;
@@ -904,10 +924,10 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
             in_regs = false;
-            const float om = (float)p.si_om, qsh = (float)p.si_q;
+            const float om = p.f_si_om, qsh = p.f_si_q;
             const float Ohmdt = (float)(p.si_om * dt), O2 = Ohmdt * Ohmdt, inv = 1.0f / (1.0f + O2);
-            const float xc = p.xpos[gx] - 0.5f * (float)p.box_l;
-            float AA = 2.0f * qsh * om * xc - 2.0f * (float)p.si_r0 * (float)p.si_eta;
+            const float xc = p.xpos[gx] - p.f_half_box_l;
+            float AA = 2.0f * qsh * om * xc - 2.0f * p.f_si_r0 * p.f_si_eta;
             {
                 const float uz = pz / rho, vx = px / rho;
                 pz = rho * (uz * (1.f - O2) + 2.f * vx * Ohmdt + AA * O2) * inv;
@@ -932,7 +952,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
             pz = uc[(3) * pl];
         }
         // ---- courant on the final state (src/solver/courant.f90:11-124), FP32 ----------------------
-        const float cfl = (float)p.cfl;
+        const float cfl = p.f_cfl;
         const float irho = 1.0f / rho;
         const float vx = px * irho, vy = py * irho, vz = pz * irho;
         float cs;
@@ -940,8 +960,8 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         else {
             const float E = uc[(4) * pl];
             const float ekin = 0.5f * rho * (vx * vx) + 0.5f * rho * (vy * vy) + 0.5f * rho * (vz * vz);
-            const float P = fmaxf((float)(p.gamma - 1.0) * (E - ekin), (float)p.smallp);
-            cs = sqrtf((float)p.gamma * P / fmaxf(rho, (float)p.smallr));
+            const float P = fmaxf(p.f_gm1 * (E - ekin), p.f_smallp);
+            cs = sqrtf(p.f_gamma * P / fmaxf(rho, p.f_smallr));
             if (!(E == E)) st |= SHARK_STATUS_NAN;
         }
         float dxx;
@@ -953,11 +973,11 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         float fmx = 0.f;
         const bool fk_si = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
         const bool fk = fk_si || ((p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_DISK_POLAR);
-        const float om = (float)p.si_om, qsh = (float)p.si_q;
-        const float xc = p.xpos[gx] - 0.5f * (float)p.box_l;
+        const float om = p.f_si_om, qsh = p.f_si_q;
+        const float xc = p.xpos[gx] - p.f_half_box_l;
         float fmx2 = 0.f;                 // SI: the largest |f|^2, one square root after the loop
         if (fk_si) {
-            const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vz - 2.0f * (float)p.si_r0 * om * (float)p.si_eta;
+            const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vz - 2.0f * p.f_si_r0 * om * p.f_si_eta;
             const float f3 = 2.0f * om * vx;
             fmx2 = f1 * f1 + f3 * f3;
         } else if (fk) {
@@ -1044,7 +1064,10 @@ static __global__ void k_ou_update(double* ou, int nm, const double* dt, double 
 static __global__ void k_prepare_step(unsigned long long* dt_next, const double* dt, const double* dtstop, int ndust,
                                       int const_ts, float* coef) {
     const int k = threadIdx.x;
-    if (k == 0) *dt_next = (unsigned long long)__double_as_longlong(2e44);
+    if (k == 0) {
+        *dt_next = (unsigned long long)__double_as_longlong(2e44);
+        coef[2 * SHARK_MAX_DUST] = (float)*dt;
+    }
     if (const_ts && k < ndust) {
         float r, w;
         drag_coeffs(1.0 * (*dt) / dtstop[k], r, w);
