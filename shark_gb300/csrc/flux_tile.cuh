@@ -65,10 +65,10 @@ struct TileSmem {
 template <typename R>
 __device__ __forceinline__ void setup_force(const KParams<R>& p, int s, int ix, R vx, R vz, R& f1, R& f2, R& f3) {
     if (p.setup == SHARK_SETUP_SI) {
-        const R qs = R(p.si_q), om = R(p.si_om);
-        const R xc = p.xpos[ix] - R(0.5) * R(p.box_l);
+        const R qs = prm<R>(p.si_q, p.f_si_q), om = prm<R>(p.si_om, p.f_si_om);
+        const R xc = p.xpos[ix] - prm<R>(R(0.5) * R(p.box_l), p.f_half_box_l);
         if (s == 0)
-            f1 = R(2) * qs * sq(om) * xc - R(2) * om * vz - R(2) * R(p.si_r0) * om * R(p.si_eta);
+            f1 = R(2) * qs * sq(om) * xc - R(2) * om * vz - R(2) * prm<R>(p.si_r0, p.f_si_r0) * om * prm<R>(p.si_eta, p.f_si_eta);
         else
             f1 = R(2) * qs * sq(om) * xc - R(2) * om * vz;
         f2 = R(0);
@@ -198,10 +198,11 @@ __device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
     const int ax0 = blockIdx.x * T::TX + p.ng;                     // first active column of tile
     const int ay0 = (NDIM == 2) ? blockIdx.y * T::TY + p.ng : 0;   // first active row of tile
     const int hx0 = ax0 - T::OX, hy0 = ay0 - T::OY;                 // halo origin (global)
-    const R dt = R(*p.dt);
+    const R dt = step_dt(p);
     const R half = R(0.5);
-    const R gamma = R(p.gamma);
-    const R inv_g1 = R(1.0 / (p.gamma - 1.0));
+    const R gamma = prm<R>(p.gamma, p.f_gamma);
+    const R smallR = prm<R>(p.smallr, p.f_smallr);
+    const R inv_g1 = prm<R>(1.0 / (p.gamma - 1.0), p.f_inv_g1);
     const bool fk = (p.flags & SHARK_FLAG_FORCE_KICK) != 0;
     const bool polar = (p.geom == 2);
     const bool iso = (p.iso == 1);
@@ -233,13 +234,13 @@ __device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
                 const R ir = R(1) / rho;
                 vx = px * ir; vy = py * ir; vz = pz * ir;
                 const R ekin = half * (px * vx + py * vy + pz * vz);
-                P = fmax2((gamma - R(1)) * (us[4] - ekin), R(p.smallp));
+                P = fmax2((gamma - R(1)) * (us[4] - ekin), prm<R>(p.smallp, p.f_smallp));
             } else {
                 vx = px / rho; vy = py / rho; vz = pz / rho;
                 const R ekin = half * rho * sq(px / rho) + half * rho * sq(py / rho) + half * rho * sq(pz / rho);
-                P = fmax2((gamma - R(1)) * (us[4] - ekin - R(0)), R(p.smallp));
+                P = fmax2((gamma - R(1)) * (us[4] - ekin - R(0)), prm<R>(p.smallp, p.f_smallp));
             }
-            const R qrho = fmax2(rho, R(p.smallr));
+            const R qrho = fmax2(rho, smallR);
             R cs;
             if (!iso) cs = sqrt(gamma * P / qrho);
             else { cs = p.cs[gx]; P = rho * sq(cs); }
@@ -352,7 +353,7 @@ __device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
                 sv0 = -u * dvx - v * dvy - dpy_r - over_r(u * v);
                 sw0 = -u * dwx - v * dwy;
             }
-            const R smallP = R(p.smallp);
+            const R smallP = prm<R>(p.smallp, p.f_smallp);
             face[0][0] = r_rho + half * dt * sr0 + half * drx * dxl;
             face[1][0] = u + half * dt * su0 + half * dux * dxl;
             face[4][0] = fmax2(pp + half * dt * sp0 + half * dpx * dxl, smallP);

@@ -57,7 +57,15 @@ static KParams<R> make_params(const DeviceView& v) {
 
 template <typename R, int NS, int MODE, bool GROW = false>
 static void finalize_launch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
-    if constexpr (std::is_same<R, float>::value) k_finalize_mixed<NS, MODE, GROW><<<grid, 256, 0, st>>>(p);
+    if constexpr (std::is_same<R, float>::value) {
+        if constexpr (GROW) {
+            k_finalize_mixed<NS, MODE, GROW><<<grid, 256, 0, st>>>(p);
+        } else {
+            dim3 g = grid;
+            g.x = (p.nx + K2M_THREADS - 1) / K2M_THREADS;
+            k_finalize_mixed<NS, MODE, GROW><<<g, K2M_THREADS, 0, st>>>(p);
+        }
+    }
     else k_finalize<R, NS, MODE, GROW><<<grid, 256, 0, st>>>(p);
 }
 

@@ -788,8 +788,14 @@ __device__ __forceinline__ void drag_coeffs_mix(double a, float& r, float& w) {
     }
 }
 
+// Threads per block of the mixed K2 without growth: small blocks, so that the warps of a block
+// waiting at the dt reduction's barrier and the last wave hold fewer idle slots (the growth
+// variant keeps 256 threads: its block-cooperative phase is laid out for 8 warps).
+constexpr int K2M_THREADS = 128;
+
 template <int NS, int MODE, bool GROW = false>
-__global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KParams<float> p) {
+__global__ void __launch_bounds__(GROW ? 256 : K2M_THREADS, GROW ? ((NS >= 8) ? 2 : 3) : ((NS >= 8) ? 2 : 3) * (256 / K2M_THREADS))
+k_finalize_mixed(KParams<float> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;
     const bool drag = MODE == 0 && N > 0 && (p.flags & SHARK_FLAG_DRAG);
@@ -815,6 +821,15 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
     // in flight together) and the CFL loop reads it there unless a setup hook rewrote it
     float dr[NMAX], dmx[NMAX], dmy[NMAX], dmz[NMAX];
     bool in_regs = false;
+    // courant's dust terms taken in the drag update loop, right after each species' final values
+    // (the species' registers then die one by one instead of living until the CFL): allowed when
+    // no setup hook changes the dust between the drag and the CFL
+    const bool fk_si = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
+    const bool cfl_in_drag = NS > 0 && NS <= 8 && drag && p.ou_nm == 0 && p.setup != SHARK_SETUP_DISK_POLAR &&
+                             !(p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK));
+    bool cfl_done = false;
+    float vmax_d = 0.f, vv_last = 0.f, fmx2_d = 0.f;
+    const float xc = act ? p.xpos[gx] - p.f_half_box_l : 0.f;
     // part 1: drag, floor, drag heating; part 2: kick, setup_inloop, CFL.  With growth in between
     // (a block-wide phase) the two parts are separate; otherwise they form one block of code.
     auto part1 = [&]() {
@@ -847,6 +862,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                 const float irhon = 1.0f / rhon;
                 const float vbx = pnx * irhon, vby = pny * irhon, vbz = pnz * irhon;
                 const float fl = rho * p.f_dust_ratio_min;   // floor (dust_drag.f90:63-73)
+                const float om = p.f_si_om, qsh = p.f_si_q;
 #pragma unroll
                 for (int k = 0; k < NS; ++k) {
                     const float wr = wk[k] * dr[k];
@@ -857,7 +873,22 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
                     uc[(5 + 2 * N + k) * pl] = dmy[k];
                     uc[(5 + 3 * N + k) * pl] = dmz[k];
                     if (fl > dr[k]) { dr[k] = fl; uc[(5 + k) * pl] = fl; }
+                    if (cfl_in_drag) {   // the dust loop of courant, see part 2
+                        const float ird = 1.0f / dr[k];
+                        const float vdx = dmx[k] * ird, vdy = dmy[k] * ird, vdz = dmz[k] * ird;
+                        const float vv = fabsf(vdx) + fabsf(vdy) + fabsf(vdz);
+                        vmax_d = fmaxf(vmax_d, vv);
+                        vv_last = vv;
+                        if (fk_si) {
+                            const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vdz;
+                            const float f3 = 2.0f * om * vdx;
+                            fmx2_d = fmaxf(fmx2_d, f1 * f1 + f3 * f3);
+                        }
+                        if (!(dr[k] > 0.f)) st |= SHARK_STATUS_NEG_DENSITY;
+                        if (!isfinite(vv)) st |= SHARK_STATUS_NAN;
+                    }
                 }
+                cfl_done = cfl_in_drag;
                 if (p.flags & SHARK_FLAG_BACK_REACTION) {
                     px = vbx * rho; py = vby * rho; pz = vbz * rho;
                     uc[(1) * pl] = px;
@@ -971,10 +1002,8 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         float vv = fabsf(vx) + fabsf(vy) + fabsf(vz);
         float vmax = cs + vv;
         float fmx = 0.f;
-        const bool fk_si = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
         const bool fk = fk_si || ((p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_DISK_POLAR);
         const float om = p.f_si_om, qsh = p.f_si_q;
-        const float xc = p.xpos[gx] - p.f_half_box_l;
         float fmx2 = 0.f;                 // SI: the largest |f|^2, one square root after the loop
         if (fk_si) {
             const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vz - 2.0f * p.f_si_r0 * om * p.f_si_eta;
@@ -983,6 +1012,11 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
         } else if (fk) {
             fmx = fabsf(p.fgrav[gx]);   // polar disk: the point-mass force, the same on gas and dust
         }
+        if (cfl_done) {   // dust terms taken in the drag loop: the same maxima, the last species' vv
+            vmax = fmaxf(vmax, vmax_d);
+            fmx2 = fmaxf(fmx2, fmx2_d);
+            vv = vv_last;
+        } else {
 #pragma unroll
         for (int k = 0; k < N; ++k) {
             float rd, mx, my, mz;
@@ -1007,6 +1041,7 @@ __global__ void __launch_bounds__(256, (NS >= 8) ? 2 : 3) k_finalize_mixed(KPara
             }
             if (!(rd > 0.f)) st |= SHARK_STATUS_NEG_DENSITY;
             if (!isfinite(vv)) st |= SHARK_STATUS_NAN;
+        }
         }
         if (fk_si) fmx = sqrtf(fmx2);
         dtc = cfl * dxx / fabsf(vmax);
