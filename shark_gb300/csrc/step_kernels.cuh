@@ -441,12 +441,14 @@ constexpr int GROWTH_SMEM_ROWS = 80;        // gather rows staged in shared memo
 static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p, int gx_block, int gy, double dt) {
     __shared__ float sw[8][GROWTH_MAX_PAIRS];
     __shared__ int2 sg[GROWTH_SMEM_ROWS * 32];
+    __shared__ int spair[GROWTH_PAIR_SLOTS * 32];   // pair (k << 8 | j) of slot i, lane l at [32 i + l]
     const GrowthDev& g = p.gw;
     const int N = p.ndust, P = g.npair, L = g.gL;
     const bool staged = L <= GROWTH_SMEM_ROWS;
     if (staged)
         for (int e = threadIdx.x; e < L * 32; e += blockDim.x)
             sg[e] = make_int2(__ldg(g.gq + e), __float_as_int(__ldg(g.gc + e)));
+    for (int e = threadIdx.x; e < GROWTH_PAIR_SLOTS * 32; e += blockDim.x) spair[e] = e < P ? __ldg(g.pair + e) : 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float* w = sw[wid];
@@ -496,17 +498,14 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
         const GrowthCellF cc = growth_cell_consts_f(g, rf, g.t_per_col ? growth_row_f(g, gx) : row0, qrho_old, hs, eta_a);
         const float ihs = 1.f / hs;
         float kp[GROWTH_PAIR_SLOTS];
-        int kj[GROWTH_PAIR_SLOTS];
 #pragma unroll
         for (int i = 0; i < GROWTH_PAIR_SLOTS; ++i) {
             kp[i] = 0.f;
-            kj[i] = 0;
             if (32 * i >= P) continue;                      // uniform over the warp
             const int q = lane + 32 * i;
             const bool has = q < P;
-            const int pr = has ? __ldg(g.pair + q) : 0;
+            const int pr = spair[q];
             const int k = pr >> 8, j = pr & 255;
-            kj[i] = pr;
             const float tk = __shfl_sync(FULL, ts, k), tj = __shfl_sync(FULL, ts, j);
             const float dx = __shfl_sync(FULL, vx, k) - __shfl_sync(FULL, vx, j);
             const float dy = __shfl_sync(FULL, vy, k) - __shfl_sync(FULL, vy, j);
@@ -526,7 +525,8 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
             for (int i = 0; i < GROWTH_PAIR_SLOTS; ++i) {
                 if (32 * i >= P) continue;
                 const int q = lane + 32 * i;
-                const float rk = __shfl_sync(FULL, rd, kj[i] >> 8), rj = __shfl_sync(FULL, rd, kj[i] & 255);
+                const int pr = spair[q];
+                const float rk = __shfl_sync(FULL, rd, pr >> 8), rj = __shfl_sync(FULL, rd, pr & 255);
                 float pc = kp[i] * rk * rj;
                 if (thr_on && (rk < thr || rj < thr)) pc = 0.f;
                 if (q < P) w[q] = pc * stick;
@@ -534,11 +534,22 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
             __syncwarp();
             float d = 0.f;
             if (staged) {
-#pragma unroll 4
-                for (int t = 0; t < L; ++t) {
-                    const int2 e = sg[t * 32 + lane];
-                    d += __int_as_float(e.y) * w[e.x];
+                // four partial sums: the gather's products are independent, its FMA chain is not
+                float d1 = 0.f, d2 = 0.f, d3 = 0.f;
+                int t = 0;
+                for (; t + 4 <= L; t += 4) {
+                    const int2 e0 = sg[t * 32 + lane], e1 = sg[(t + 1) * 32 + lane];
+                    const int2 e2 = sg[(t + 2) * 32 + lane], e3 = sg[(t + 3) * 32 + lane];
+                    d = fmaf(__int_as_float(e0.y), w[e0.x], d);
+                    d1 = fmaf(__int_as_float(e1.y), w[e1.x], d1);
+                    d2 = fmaf(__int_as_float(e2.y), w[e2.x], d2);
+                    d3 = fmaf(__int_as_float(e3.y), w[e3.x], d3);
                 }
+                for (; t < L; ++t) {
+                    const int2 e = sg[t * 32 + lane];
+                    d = fmaf(__int_as_float(e.y), w[e.x], d);
+                }
+                d = (d + d1) + (d2 + d3);
             } else {
                 for (int t = 0; t < L; ++t) d += __ldg(g.gc + t * 32 + lane) * w[__ldg(g.gq + t * 32 + lane)];
             }
