@@ -138,9 +138,10 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
         R dqx[NV], dqy[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            const R ql = shfl_up1(q1[k]), qr = shfl_dn1(q1[k]);
             dqx[k] = R(0);
             dqy[k] = R(0);
+            if (IS_GAS && k == 4 && iso) continue;   // isothermal: the pressure slopes are rho's times cs^2
+            const R ql = shfl_up1(q1[k]), qr = shfl_dn1(q1[k]);
             if constexpr (ST > 0) {
                 if constexpr (FAST) {
                     dqx[k] = slope_limit_t<ST>((q1[k] - ql) * sfl, (qr - q1[k]) * sfr);

@@ -856,15 +856,21 @@ k_finalize_mixed(KParams<float> p) {
                     dmz[k] = uc[(5 + 3 * N + k) * pl];
                 }
                 float rk[NMAX], wk[NMAX];
-                const float rho_old = ucur[(0) * pl];
-                const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
-                const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
-                const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
+                if (const_ts) {          // the step's coefficients (no FP64 work per cell)
+#pragma unroll
+                    for (int k = 0; k < NS; ++k) { rk[k] = cr[k]; wk[k] = cw[k]; }
+                } else {
+                    const float rho_old = ucur[(0) * pl];
+                    const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
+                    const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
+                    const double Fc = direct ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
+#pragma unroll
+                    for (int k = 0; k < NS; ++k)
+                        drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], rk[k], wk[k]);
+                }
                 float rhon = rho, pnx = px, pny = py, pnz = pz;
 #pragma unroll
                 for (int k = 0; k < NS; ++k) {
-                    if (const_ts) { rk[k] = cr[k]; wk[k] = cw[k]; }
-                    else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], rk[k], wk[k]);
                     pnx += wk[k] * dmx[k];
                     pny += wk[k] * dmy[k];
                     pnz += wk[k] * dmz[k];
