@@ -95,7 +95,7 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
     const float2 m2om = bc2(-2.f * om), p2om = bc2(2.f * om);
 
     float2 q0[4], q1[4], q2[4];      // primitive rows P-1, P, P+1
-    float2 qmy_prev[4], g_prev[4], t_prev[4];
+    float2 qmy_prev[4], t_prev[4];   // t_prev: row P-1 after its kick, x fluxes and lower y flux
     int voff[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) voff[k] = svar(s, k, N) * (int)p.plane + ca;
@@ -193,12 +193,12 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
             hb2(qmy_prev[0], qmy_prev[2], qmy_prev[1], qmy_prev[3], qpy[0], qpy[2], qpy[1], qpy[3], f);
             gb[0] = f[0]; gb[2] = f[1]; gb[1] = f[2]; gb[3] = f[3];
         }
-        // ---- finish row P-1 with its y fluxes ------------------------------------------------
+        // ---- finish row P-1 with the flux above it -------------------------------------------
         if (row > ay0 && finish_upd) {
             const int ro = (P - 1) * pitch;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const float2 un = fma2(gb[k], ncy, fma2(g_prev[k], cy, t_prev[k]));
+                const float2 un = fma2(gb[k], ncy, t_prev[k]);
                 if (upd_b) *reinterpret_cast<float2*>(dst + (voff[k] + ro)) = un;
                 else dst[voff[k] + ro] = un.x;
             }
@@ -211,13 +211,12 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
                 uu[3] = fma2(rdt, f3, uu[3]);
             }
 #pragma unroll
-            for (int k = 0; k < 4; ++k) uu[k] = fma2(fxr[k], ncr, fma2(fxl[k], cl, uu[k]));
+            for (int k = 0; k < 4; ++k) uu[k] = fma2(gb[k], cy, fma2(fxr[k], ncr, fma2(fxl[k], cl, uu[k])));
         }
         // ---- slide the window -----------------------------------------------------------------
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             qmy_prev[k] = qmy[k];
-            g_prev[k] = gb[k];
             t_prev[k] = uu[k];
             q0[k] = q1[k];
             q1[k] = q2[k];
@@ -225,16 +224,22 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
     }
 }
 
-// Gas and dust of the mixed path's K1 in one launch: blocks 0 .. ng-1 take the gas strips (28
-// columns per warp, flux_strip.cuh), the rest the dust strips of every species (60 columns per
-// warp).  The gas blocks come first in the launch order, so the small gas grid runs beside the
-// dust instead of after it.
+}  // namespace shark
+
+#include "flux_strip_gas2.cuh"
+
+namespace shark {
+
+// Gas and dust of the mixed path's K1 in one launch: blocks 0 .. ng-1 take the gas strips, the
+// rest the dust strips of every species, both 60 columns per warp.  The gas blocks come first in
+// the launch order, so the gas grid runs beside the dust instead of after it.
 template <int ST, int GSOLV>
 __global__ void __launch_bounds__(32 * STRIP_WARPS, 4) k_flux_strip_mixed(KParams<float> p, int nbx_g, int nbx_d, int nby) {
     const int warp = threadIdx.x >> 5;
     const int id = blockIdx.x, ngas = nbx_g * nby;
     if (id < ngas) {
-        flux_strip<float, true, ST, GSOLV>(p, 0, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
+        if (p.iso == 1) flux_strip_gas2<ST, GSOLV, true>(p, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
+        else flux_strip_gas2<ST, GSOLV, false>(p, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
     } else {
         const int d = id - ngas, bx = d % nbx_d, rest = d / nbx_d;
         flux_strip_dust2<ST>(p, rest / nby + 1, bx, (rest % nby) * STRIP_WARPS + warp);

@@ -141,7 +141,7 @@ static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
     if constexpr (std::is_same<R, float>::value) {
         if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0) {
             // mixed path, Cartesian, Huang & Bai dust: gas and dust strips in one launch
-            const int nbx_g = (p.nx + STRIP_UX - 1) / STRIP_UX, nbx_d = (p.nx + STRIP2_UX - 1) / STRIP2_UX;
+            const int nbx_g = (p.nx + STRIP2_UX - 1) / STRIP2_UX, nbx_d = nbx_g;
             const int nby = (int)grid.y;
             const long long nblk = (long long)nbx_g * nby + (long long)nbx_d * nby * p.ndust;
             const dim3 g1((unsigned)nblk, 1, 1), b1(32 * STRIP_WARPS, 1, 1);
