@@ -96,9 +96,10 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
 
     float2 q0[4], q1[4], q2[4];      // primitive rows P-1, P, P+1
     float2 qmy_prev[4], t_prev[4];   // t_prev: row P-1 after its kick, x fluxes and lower y flux
-    int voff[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) voff[k] = svar(s, k, N) * (int)p.plane + ca;
+    // element offset of component k of this lane's first column, svar(s, k, N) * plane + ca,
+    // from a base and a stride (two registers instead of four offsets)
+    const int vbase = svar(s, 0, N) * (int)p.plane + ca, vstride = N * (int)p.plane;
+    auto voff = [&](int k) { return vbase + k * vstride; };
     const float* __restrict__ src = p.u_cur;
     float* __restrict__ dst = p.u_next;
     const int pitch = p.pitch;
@@ -107,7 +108,7 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
         const int ro = min(row, p.ny_max - 1) * pitch;
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-            us[k] = in ? __ldg(reinterpret_cast<const float2*>(src + (voff[k] + ro))) : make_float2(1.f, 1.f);
+            us[k] = in ? __ldg(reinterpret_cast<const float2*>(src + (voff(k) + ro))) : make_float2(1.f, 1.f);
     };
     auto to_prim = [&](const float2* us, float2* q) {
         const float2 ir = make_float2(1.f / us[0].x, 1.f / us[0].y);
@@ -134,7 +135,7 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
         float2 uu[4];
         if (start_upd) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k) uu[k] = __ldg(reinterpret_cast<const float2*>(src + (voff[k] + P * pitch)));
+            for (int k = 0; k < 4; ++k) uu[k] = __ldg(reinterpret_cast<const float2*>(src + (voff(k) + P * pitch)));
         }
         // ---- doubled limited slopes of row P -----------------------------------------------------
         float2 Dx[4], Dy[4];
@@ -199,8 +200,8 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const float2 un = fma2(gb[k], ncy, t_prev[k]);
-                if (upd_b) *reinterpret_cast<float2*>(dst + (voff[k] + ro)) = un;
-                else dst[voff[k] + ro] = un.x;
+                if (upd_b) *reinterpret_cast<float2*>(dst + (voff(k) + ro)) = un;
+                else dst[voff(k) + ro] = un.x;
             }
         }
         // ---- start row P: kick with the force of its old q, then the x fluxes ------------------

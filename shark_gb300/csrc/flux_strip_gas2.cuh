@@ -130,9 +130,10 @@ __device__ void flux_strip_gas2(const KParams<float>& p, int bx, int by) {
     constexpr int NV = 5;
     float2 q0[NV], q1[NV], q2[NV];      // primitive rows P-1, P, P+1 (rho, vx, vy, vz, P)
     float2 qmy_prev[NV], t_prev[NV];   // t_prev: row P-1 after its kick, x fluxes and lower y flux
-    int voff[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) voff[k] = k * (int)p.plane + ca;
+    // element offset of variable k of this lane's first column: ca + k * plane (computed per
+    // access from two registers instead of holding five offsets)
+    const int vpl = (int)p.plane;
+    auto voff = [&](int k) { return ca + k * vpl; };
     const float* __restrict__ src = p.u_cur;
     float* __restrict__ dst = p.u_next;
     const int pitch = p.pitch;
@@ -141,7 +142,7 @@ __device__ void flux_strip_gas2(const KParams<float>& p, int bx, int by) {
         const int ro = min(row, p.ny_max - 1) * pitch;
 #pragma unroll
         for (int k = 0; k < NV; ++k)
-            us[k] = in ? __ldg(reinterpret_cast<const float2*>(src + (voff[k] + ro))) : make_float2(1.f, 1.f);
+            us[k] = in ? __ldg(reinterpret_cast<const float2*>(src + (voff(k) + ro))) : make_float2(1.f, 1.f);
     };
     auto to_prim = [&](const float2* us, float2* q) {
         const float2 ir = rcp2(us[0]);
@@ -176,7 +177,7 @@ __device__ void flux_strip_gas2(const KParams<float>& p, int bx, int by) {
         float2 uu[NV];
         if (start_upd) {
 #pragma unroll
-            for (int k = 0; k < NV; ++k) uu[k] = __ldg(reinterpret_cast<const float2*>(src + (voff[k] + P * pitch)));
+            for (int k = 0; k < NV; ++k) uu[k] = __ldg(reinterpret_cast<const float2*>(src + (voff(k) + P * pitch)));
         }
         // ---- doubled limited slopes of row P (isothermal: the pressure's are rho's times cs^2) ------
         float2 Dx[NV], Dy[NV];
@@ -277,8 +278,8 @@ __device__ void flux_strip_gas2(const KParams<float>& p, int bx, int by) {
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
                 const float2 un = fma2(gb[k], ncy, t_prev[k]);
-                if (upd_b) *reinterpret_cast<float2*>(dst + (voff[k] + ro)) = un;
-                else dst[voff[k] + ro] = un.x;
+                if (upd_b) *reinterpret_cast<float2*>(dst + (voff(k) + ro)) = un;
+                else dst[voff(k) + ro] = un.x;
             }
         }
         // ---- start row P: kick with the force of its old q, then the x fluxes ------------------
