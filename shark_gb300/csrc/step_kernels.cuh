@@ -804,8 +804,10 @@ __device__ __forceinline__ void drag_coeffs_mix(double a, float& r, float& w) {
 // variant keeps 256 threads: its block-cooperative phase is laid out for 8 warps).
 constexpr int K2M_THREADS = 128;
 
+// Blocks per SM: 8 species at 5 blocks of 128 threads (96 registers), measured best of 4-6.
 template <int NS, int MODE, bool GROW = false>
-__global__ void __launch_bounds__(GROW ? 256 : K2M_THREADS, GROW ? ((NS >= 8) ? 2 : 3) : ((NS >= 8) ? 2 : 3) * (256 / K2M_THREADS))
+__global__ void __launch_bounds__(GROW ? 256 : K2M_THREADS,
+                                  GROW ? ((NS >= 8) ? 2 : 3) : (NS == 8 ? 5 : ((NS > 8) ? 2 : 3) * (256 / K2M_THREADS)))
 k_finalize_mixed(KParams<float> p) {
     constexpr int NMAX = NS > 0 ? NS : 1;
     const int N = NS >= 0 ? NS : p.ndust;

@@ -37,8 +37,11 @@ def test_kh_default_parameters_fp64():
     assert rel_l1(cfg, ug, uo).max() <= FP64_TOL
 
 
-def test_kh_mixed():
+@pytest.mark.parametrize("solver", [2, 1, 0])
+def test_kh_mixed(solver):
+    """The adiabatic two-column gas strips with each gas solver."""
     cfg, u0 = _kh(K.PREC_MIXED)
+    cfg.solver = solver
     dto, dtg, uo, ug, st = run_pair(cfg, u0, 30)
     assert st == 0
     np.testing.assert_allclose(dtg, dto, rtol=1e-5, atol=0)

@@ -119,8 +119,11 @@ def test_si_without_force_kick_uses_inloop_rotation():
     assert rel_l1(cfg, ug, uo).max() <= FP64_TOL
 
 
-def test_si_mixed_precision():
-    cfg, u0 = setups.si(n=128, ndust=8, precision=K.PREC_MIXED)
+@pytest.mark.parametrize("solver,slope_type", [(2, 3), (1, 3), (0, 3), (2, 1), (2, 2)])
+def test_si_mixed_precision(solver, slope_type):
+    """Every gas solver and limiter of the two-column strips on the isothermal box."""
+    cfg, u0 = setups.si(n=128, ndust=8, precision=K.PREC_MIXED, slope_type=slope_type)
+    cfg.solver = solver
     dto, dtg, uo, ug, st = run_pair(cfg, u0, 30)
     assert st == 0
     np.testing.assert_allclose(dtg, dto, rtol=1e-5, atol=0)
