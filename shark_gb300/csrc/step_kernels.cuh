@@ -923,11 +923,15 @@ k_finalize_mixed(KParams<float> p) {
             const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
             const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
             const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
+            // run-time species count: the cell's FP64-formed coefficients are kept (thread-local
+            // memory) for the update loop instead of being formed a second time
+            float2 rw_local[NS < 0 ? SHARK_MAX_DUST : 1];
             for (int k = 0; k < N; ++k) {
                 float r, w;
                 if (const_ts) { r = cr[k]; w = cw[k]; }
                 else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], r, w);
                 if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
+                else if (!const_ts) rw_local[k] = make_float2(r, w);
                 pnx += w * uc[(5 + N + k) * pl];
                 pny += w * uc[(5 + 2 * N + k) * pl];
                 pnz += w * uc[(5 + 3 * N + k) * pl];
@@ -939,7 +943,7 @@ k_finalize_mixed(KParams<float> p) {
                 float r, w;
                 if (NS > 0) { r = rk[k < NMAX ? k : 0]; w = wk[k < NMAX ? k : 0]; }
                 else if (const_ts) { r = cr[k]; w = cw[k]; }
-                else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], r, w);
+                else { r = rw_local[k].x; w = rw_local[k].y; }
                 const float rd = uc[(5 + k) * pl];
                 const long long ixx = uidx(p, 5 + N + k, gy, gx), iyy = uidx(p, 5 + 2 * N + k, gy, gx),
                                 izz = uidx(p, 5 + 3 * N + k, gy, gx);
