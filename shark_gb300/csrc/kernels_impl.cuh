@@ -44,6 +44,7 @@ static KParams<R> make_params(const DeviceView& v) {
     p.turb_rho0 = c.turb_rho0;
     p.dt = nullptr; p.dt_next = nullptr; p.status = v.status; p.coef = v.coef;
     p.dtf = v.coef + 2 * SHARK_MAX_DUST;
+    p.dinvts_f = v.coef + SHARK_COEF_INVTS;
     p.f_gamma = (float)c.gamma; p.f_gm1 = (float)(c.gamma - 1.0); p.f_inv_g1 = (float)(1.0 / (c.gamma - 1.0));
     p.f_cfl = (float)c.cfl; p.f_smallr = (float)c.smallr; p.f_smallp = (float)c.smallp;
     p.f_dust_ratio_min = (float)c.dust_ratio_min;

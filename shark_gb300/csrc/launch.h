@@ -9,9 +9,10 @@
 
 namespace shark {
 
-// Floats of the per-step buffer `coef`: the drag coefficients 1/(1+a_k), a_k/(1+a_k) of the
-// species, then the step's dt as float.
-constexpr int SHARK_COEF_FLOATS = 2 * SHARK_MAX_DUST + 4;
+// Floats of the buffer `coef`: the per-step drag coefficients 1/(1+a_k), a_k/(1+a_k) of the
+// species, the step's dt as float, then (from SHARK_COEF_INVTS, written once) 1/C_k as float.
+constexpr int SHARK_COEF_INVTS = 2 * SHARK_MAX_DUST + 4;
+constexpr int SHARK_COEF_FLOATS = SHARK_COEF_INVTS + SHARK_MAX_DUST;
 
 // Charging (K5) tables, outputs and constants; see charge.cuh.
 struct ChargeView {

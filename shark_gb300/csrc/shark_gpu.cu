@@ -1023,6 +1023,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         for (int a = 0; a < 9; ++a) v.md[a] = c->metrics_d + a * ncol;
     }
     INIT_TRY(cudaMalloc(&c->species, 5 * SHARK_MAX_DUST * sizeof(double)));
+    float invf[SHARK_MAX_DUST] = {0};   // FP32 copy of 1/C_k for the mixed path's coefficients
     {
         // 1/C_k of the stopping times t_k = C_k / F_cell that K2's mixed path multiplies out:
         // dustyTurb C_k = St_0,k L rho_0 (F = c_s rho), polar disk (Epstein on the midplane density)
@@ -1033,6 +1034,7 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
                                  ? cfg->dust_stokes[k] * cfg->box_l * cfg->turb_rho0
                                  : std::sqrt(kPi * cfg->gamma / 8.0) * cfg->rhograin * cfg->dust_size[k];
             inv[k] = C != 0.0 ? 1.0 / C : 0.0;
+            invf[k] = (float)inv[k];
         }
         INIT_TRY(cudaMemcpy(c->species + 4 * SHARK_MAX_DUST, inv, SHARK_MAX_DUST * sizeof(double), cudaMemcpyHostToDevice));
     }
@@ -1050,6 +1052,8 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     INIT_TRY(cudaMemsetAsync(c->status, 0, sizeof(unsigned int), c->stream));
     INIT_TRY(cudaMalloc(&c->coef, shark::SHARK_COEF_FLOATS * sizeof(float)));
     INIT_TRY(cudaMemsetAsync(c->coef, 0, shark::SHARK_COEF_FLOATS * sizeof(float), c->stream));
+    INIT_TRY(cudaMemcpyAsync(c->coef + shark::SHARK_COEF_INVTS, invf, SHARK_MAX_DUST * sizeof(float),
+                             cudaMemcpyHostToDevice, c->stream));
     v.dt_slots = c->dt_slots;
     v.status = c->status;
     v.coef = c->coef;

@@ -59,6 +59,7 @@ struct KParams {
     unsigned int* status;             // SHARK_STATUS_* bits
     float* coef;                      // [2*SHARK_MAX_DUST] per-step drag coefficients 1/(1+a_k), a_k/(1+a_k)
     const float* dtf;                 // (float) dt of the current step, coef[2*SHARK_MAX_DUST]
+    const float* dinvts_f;            // 1/C_k as float (mixed path)
     // FP32 copies of the scalar parameters for the mixed kernels, converted once on the host: a
     // double-to-float conversion issues on the FP64 pipe, which is narrow and variable-latency on
     // this GPU, so per-thread conversions stall the warps that do them
@@ -465,7 +466,7 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
     // stopping times for the pair velocities (FP32): t_k = C_k / F_cell with the tabulated 1/C_k
     // (dustyTurb F = c_s rho, polar disk F = rho/hs c_s); other setups through tstop_cell
     const bool ts_tab = p.setup == SHARK_SETUP_DUSTYTURB || p.setup == SHARK_SETUP_DISK_POLAR;
-    const float invc = (float)p.dinvts[b];
+    const float invc = p.dinvts_f[b];
     const GrowthRunF rf = growth_run_consts_f(g);
     const float4 row0 = growth_row_f(g, 0);        // the one temperature row (dustyTurb)
     unsigned st = 0;
@@ -788,6 +789,16 @@ __device__ __forceinline__ double drag_cell_factor(const KParams<float>& p, doub
     return dt * (qrho_old / p.hsd[gx] * p.csd[gx]);
 }
 
+// The same coefficients in FP32 from a = dt F_cell / C_k formed in FP32 (dt F_cell once per cell
+// in FP64, then per species one product): r = 1/(1+a) and w = a r are well conditioned for every
+// a >= 0 (no cancellation; a = dt/t_k >> 1 gives r ~ 1/a, w ~ 1 to FP32 rounding), so the state's
+// FP32 precision bounds them.  a is capped at 1e30 so that 1 + a stays finite.
+__device__ __forceinline__ void drag_coeffs_f(float a, float& r, float& w) {
+    a = fminf(a, 1e30f);
+    r = 1.0f / (1.0f + a);
+    w = a * r;
+}
+
 __device__ __forceinline__ void drag_coeffs_mix(double a, float& r, float& w) {
     const double d = 1.0 + a;
     if (d < 1e30) {
@@ -865,10 +876,12 @@ k_finalize_mixed(KParams<float> p) {
                     const float rho_old = ucur[(0) * pl];
                     const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
                     const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
-                    const double Fc = direct ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
+                    const float Fcf = direct ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx);
 #pragma unroll
-                    for (int k = 0; k < NS; ++k)
-                        drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], rk[k], wk[k]);
+                    for (int k = 0; k < NS; ++k) {
+                        if (direct) drag_coeffs_mix(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), rk[k], wk[k]);
+                        else drag_coeffs_f(Fcf * p.dinvts_f[k], rk[k], wk[k]);
+                    }
                 }
                 float rhon = rho, pnx = px, pny = py, pnz = pz;
 #pragma unroll
@@ -922,14 +935,15 @@ k_finalize_mixed(KParams<float> p) {
             const float rho_old = ucur[(0) * pl];
             const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
             const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
-            const double Fc = (const_ts || direct) ? 0.0 : drag_cell_factor(p, dt, qrho_old, gx);
-            // run-time species count: the cell's FP64-formed coefficients are kept (thread-local
-            // memory) for the update loop instead of being formed a second time
+            const float Fcf = (const_ts || direct) ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx);
+            // run-time species count: the cell's coefficients are kept (thread-local memory) for
+            // the update loop instead of being formed a second time
             float2 rw_local[NS < 0 ? SHARK_MAX_DUST : 1];
             for (int k = 0; k < N; ++k) {
                 float r, w;
                 if (const_ts) { r = cr[k]; w = cw[k]; }
-                else drag_coeffs_mix(direct ? 1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy) : Fc * p.dinvts[k], r, w);
+                else if (direct) drag_coeffs_mix(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), r, w);
+                else drag_coeffs_f(Fcf * p.dinvts_f[k], r, w);
                 if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
                 else if (!const_ts) rw_local[k] = make_float2(r, w);
                 pnx += w * uc[(5 + N + k) * pl];
