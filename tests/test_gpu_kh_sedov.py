@@ -65,3 +65,29 @@ def test_sedov_mixed():
     np.testing.assert_allclose(dtg, dto, rtol=1e-5, atol=0)
     err = rel_l1(cfg, ug, uo)
     assert err.max() <= MIXED_TOL * 10, err
+
+
+def test_sedov_blast_on_gpu_is_symmetric_and_matches_oracle():
+    """200 FP64 steps of the blast: the GPU state equals the oracle's and keeps the blast's
+    x <-> y and mirror symmetries (to rounding)."""
+    cfg, u0 = setups.sedov(n=64)
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 200)
+    assert st == 0
+    assert rel_l1(cfg, ug, uo).max() <= FP64_TOL
+    g = ug.reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)
+    ng = cfg.nghost
+    rho = g[0, ng:ng + cfg.ny, ng:ng + cfg.nx]
+    assert rho.max() > 1.2 * cfg.sedov_rho_ext                     # the shell has formed
+    np.testing.assert_allclose(rho, rho.T, rtol=1e-9, atol=0)
+    np.testing.assert_allclose(rho, rho[::-1, :], rtol=1e-9, atol=0)
+    np.testing.assert_allclose(rho, rho[:, ::-1], rtol=1e-9, atol=0)
+
+
+def test_kh_long_run_fp64():
+    """300 FP64 steps of the namelist's shear layer with dust: the band's edges roll up the same
+    way on the GPU as in the oracle."""
+    cfg, u0 = setups.kh(n=64, ndust=4, **setups.KH_NML)
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 300)
+    assert st == 0
+    np.testing.assert_allclose(dtg, dto, rtol=1e-12, atol=0)
+    assert rel_l1(cfg, ug, uo).max() <= FP64_TOL
