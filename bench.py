@@ -48,6 +48,21 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def max_over_ranks(x, world, device):
+    """The largest of a per-rank time over all ranks (the slowest replica sets the job's time)."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(units_per_step, steps, world, seconds):
+    """Whole-job rate of `world` independent replicas: the units all ranks processed over the
+    slowest rank's time (the path has no exchange step, so ranks only share the clock)."""
+    return units_per_step * steps * world / seconds
+
+
 def workload(args, precision, name=None):
     from shark_gb300 import setups
     name = name or args.workload
@@ -275,11 +290,8 @@ def run_gpu(args):
     with ClockSampler(local_rank) as clocks:
         ms = gm.timed_run(args.steps)
     barrier()
-    ms_all = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(ms_all, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(ms_all.item())
-    value = zs_step * args.steps * world / (ms_max * 1e-3)
+    ms_max = max_over_ranks(ms, world, "cuda")
+    value = replica_rate(zs_step, args.steps, world, ms_max * 1e-3)
     st = gm.sync()
 
     # per-kernel times (separate pass, events around every launch)
@@ -321,10 +333,7 @@ def run_gpu(args):
     gm.sync()
     el = time.perf_counter() - t0
     barrier()
-    el_all = torch.tensor([el], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.all_reduce(el_all, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = zs_step * e2e_steps * world / float(el_all.item())
+    e2e_value = replica_rate(zs_step, e2e_steps, world, max_over_ranks(el, world, "cuda"))
     # resident variant: what the Fortran driver does (solve + 8-byte dt readback per step)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
