@@ -34,7 +34,7 @@ def _rank(rank, world, port, times, out):
 def test_two_replicas_share_the_slowest_time():
     world = 2
     times = [0.25, 0.40]
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:   # no fork of a multi-threaded test process
         out = m.dict()
         mp.spawn(_rank, args=(world, _free_port(), times, out), nprocs=world, join=True)
         res = dict(out)
