@@ -52,6 +52,8 @@ extern "C" {
 #define SHARK_STATUS_DT_UNDERFLOW 0x4  /* CFL dt not positive/finite                           */
 #define SHARK_STATUS_NEWTON       0x8  /* a charging Newton solve hit its iteration cap        */
 #define SHARK_STATUS_GROWTH       0x10 /* growth sub-cycling hit its cap                        */
+#define SHARK_STATUS_COPY_WAIT    0x20 /* a kernel gave up waiting for a shared-memory copy (TMA)
+                                          and left its part of the step undone                  */
 
 /* ---- setups whose per-step hooks exist on the device (src/setups/<NAME>/) ----------------- */
 #define SHARK_SETUP_SOD         1   /* fixed left/right ghost states   SOD/boundaries.f90:49-77 */
@@ -108,7 +110,7 @@ typedef struct shark_gpu_config {
     int32_t geom;             /* -DGEOM: 0 Cartesian, 2 polar face-on                            */
     int32_t gridspace;        /* -DGRIDSPACE: 0 linear, 1 log-spaced radius (geom 2)             */
     int32_t solver;           /* -DSOLVER: 0 LLF, 1 HLL, 2 HLLC                                  */
-    int32_t solverdust;       /* -DSOLVERDUST: 0 Huang & Bai, 1 LLF, 2 HLL                       */
+    int32_t solverdust;       /* -DSOLVERDUST: 0 Huang & Bai, 1 LLF, 2 HLL, 3 HLLC (isothermal gas) */
     int32_t slope_type;       /* 1 minmod, 2 van Leer (harmonic), 3 MC(1.5)                      */
     int32_t iso_cs;           /* 1: isothermal (P = rho cs^2 with cs fixed by the setup)         */
     int32_t precision;        /* SHARK_PREC_*                                                    */
@@ -300,12 +302,17 @@ int32_t shark_gpu_kernel_times(shark_gpu_ctx* ctx, int64_t nsteps, float* avg_ms
  * application whose own allocator owns every device allocation, or a time loop that cannot take
  * cudaMalloc's implicit synchronisation or a change of its device footprint), which rules out
  * shark_gpu_totals because its context allocates.  It needs no context and allocates nothing:
- * its partial sums live in a fixed device array of about 1 MiB compiled into the library, held by
- * every GPU that loads it until the process exits.  Limit: ndust <= 64 (SHARK_ERR_INVALID_ARG
- * beyond).  The kernels are queued on `stream` (a cudaStream_t, NULL = default stream) and the call
- * returns without waiting.  The first call on a device looks up the array's device address with
- * that device current, so make it before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race and give wrong results; order them on one stream. */
+ * its partial sums live in a fixed device array of about 1 MiB compiled into the library.  The
+ * array becomes resident when the library's CUDA module is loaded on the device: under CUDA's
+ * default lazy module loading that happens in the first call on each device, which therefore
+ * allocates the module's memory and may synchronise -- make one warm-up call at start-up, before
+ * any stream capture (or run with CUDA_MODULE_LOADING=EAGER); afterwards the device holds it until
+ * the process exits.  Limit: ndust <= 64 (SHARK_ERR_INVALID_ARG beyond).  The kernels are queued on
+ * `stream` (a cudaStream_t, NULL = default stream) and the call returns without waiting.  Each call
+ * whose stream is not capturing looks the array's device address up with the device current (so a
+ * cudaDeviceReset between calls leaves no stale address); a call on a capturing stream reuses the
+ * address of the previous call on that device and fails if there was none.  All calls share the
+ * array: calls that overlap on the GPU race and give wrong results; order them on one stream. */
 int32_t shark_gpu_totals_noalloc(const double* u_dev, int32_t nx, int32_t ny, int32_t nghost, int32_t ndust,
                                  double* out_dev, void* stream);
 

@@ -1505,6 +1505,34 @@ DustFace solver_dust_hll(double rho_lft, double u_lft, double v_lft, double w_lf
     return f;
 }
 
+// solver_hllc_dust (solvers.f90:704-836), one species: the gas HLLC of the reference with zero
+// pressure, bounded by the gas sound speeds csl, csr of the face; the star "pressure" comes from
+// the Lagrangian speeds.  The energies the reference forms are not used by the flux and are left
+// out.
+DustFace solver_dust_hllc(double rho_lft, double u_lft, double v_lft, double w_lft, double rho_rgt, double u_rgt,
+                          double v_rgt, double w_rgt, double csl, double csr) {
+    const double P_rgt = 0.0, P_lft = 0.0;
+    double S_lft = fmin2(fmin2(u_lft, u_rgt) - fmax2(csl, csr), 0.0);
+    double S_rgt = fmax2(fmax2(u_lft, u_rgt) + fmax2(csl, csr), 0.0);
+    double hllc_l = rho_lft * (u_lft - S_lft);
+    double hllc_r = rho_rgt * (S_rgt - u_rgt);
+    double ustar = (hllc_r * u_rgt + hllc_l * u_lft + (P_lft - P_rgt)) / (hllc_r + hllc_l);
+    double Pstar = (hllc_r * P_lft + hllc_l * P_rgt + hllc_l * hllc_r * (u_lft - u_rgt)) / (hllc_r + hllc_l);
+    double rhostarleft = rho_lft * (S_lft - u_lft) / (S_lft - ustar);
+    double rhostarright = rho_rgt * (S_rgt - u_rgt) / (S_rgt - ustar);
+    double r_o, u_o, P_o;
+    if (S_lft > 0.0) { r_o = rho_lft; u_o = u_lft; P_o = P_lft; }
+    else if (ustar > 0.0) { r_o = rhostarleft; u_o = ustar; P_o = Pstar; }
+    else if (S_rgt > 0.0) { r_o = rhostarright; u_o = ustar; P_o = Pstar; }
+    else { r_o = rho_rgt; u_o = u_rgt; P_o = P_rgt; }
+    DustFace f;
+    f.rho = r_o * u_o;
+    f.mn = r_o * u_o * u_o + P_o;
+    if (ustar > 0.0) { f.mt = r_o * u_o * v_lft; f.mz = r_o * u_o * w_lft; }
+    else { f.mt = r_o * u_o * v_rgt; f.mz = r_o * u_o * w_rgt; }
+    return f;
+}
+
 // solve_wrapper (godunov.f90:768-833): gas solver then each dust species, flx in nvar order.
 void solve_wrapper(const oracle_state& s, const double* ql, const double* qr, double* flx, double csl,
                    double csr, int idim) {
@@ -1527,7 +1555,8 @@ void solve_wrapper(const oracle_state& s, const double* ql, const double* qr, do
         DustFace d;
         if (s.cfg.solverdust == 0) d = solver_dust_hb(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw]);
         else if (s.cfg.solverdust == 1) d = solver_dust_llf(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw]);
-        else d = solver_dust_hll(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw]);
+        else if (s.cfg.solverdust == 2) d = solver_dust_hll(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw]);
+        else d = solver_dust_hllc(ql[ir], ql[iu], ql[iv], ql[iw], qr[ir], qr[iu], qr[iv], qr[iw], csl, csr);
         flx[ir] = d.rho;
         flx[iu] = d.mn;
         flx[iv] = d.mt;

@@ -22,6 +22,7 @@ STATUS_NEG_DENSITY = 0x2
 STATUS_DT_UNDERFLOW = 0x4
 STATUS_NEWTON = 0x8
 STATUS_GROWTH = 0x10
+STATUS_COPY_WAIT = 0x20
 
 SETUP_SOD = 1
 SETUP_DUSTYWAVE = 2

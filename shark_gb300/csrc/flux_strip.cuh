@@ -281,7 +281,9 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                                               qpx[0], qpx[1], qpx[2], qpx[3], qpx[4], csl, csr);
                 fxl[0] = g.rho; fxl[1] = g.mn; fxl[2] = g.mt; fxl[3] = g.mz; fxl[4] = g.e;
             } else {
-                const DustFlux<R> d = dust_flux_t<SOLV>(ql[0], ql[1], ql[2], ql[3], qpx[0], qpx[1], qpx[2], qpx[3]);
+                // gas sound speeds of the face for the HLLC dust solver (isothermal: per column)
+                const DustFlux<R> d = dust_flux_t<SOLV>(ql[0], ql[1], ql[2], ql[3], qpx[0], qpx[1], qpx[2], qpx[3],
+                                                        shfl_up1(cs_col), cs_col);
                 fxl[0] = d.rho; fxl[1] = d.mn; fxl[2] = d.mt; fxl[3] = d.mz;
             }
         }
@@ -302,7 +304,7 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 gb[0] = g.rho; gb[2] = g.mn; gb[1] = g.mt; gb[3] = g.mz; gb[4] = g.e;
             } else {
                 const DustFlux<R> d = dust_flux_t<SOLV>(qmy_prev[0], qmy_prev[2], qmy_prev[1], qmy_prev[3],
-                                                qpy[0], qpy[2], qpy[1], qpy[3]);
+                                                qpy[0], qpy[2], qpy[1], qpy[3], cs_col, cs_col);
                 gb[0] = d.rho; gb[2] = d.mn; gb[1] = d.mt; gb[3] = d.mz;
             }
         }

@@ -15,6 +15,8 @@
 // limiters are the FP32 forms of physics.cuh on the doubled slopes.
 #pragma once
 
+#include "rows.cuh"
+
 namespace shark {
 
 constexpr int STRIP2_UX = 60;    // columns updated per warp
@@ -26,25 +28,35 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 // a - b
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 
-// Doubled limited slope 2 dq of the FP32 limiters (physics.cuh) for two columns.
+// min(|a|, |b|) carrying the sign sign(a) xor sign(b): >= 0 exactly when a and b have the same
+// sign (or one is zero).
+__device__ __forceinline__ float min_xorsign_abs(float a, float b) {
+    float d;
+    asm("min.xorsign.abs.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+
+// Doubled limited slope 2 dq of the FP32 limiters (physics.cuh) for two columns.  minmod and MC
+// start from m = max(min.xorsign.abs(l, r), 0), which is min(|l|, |r|) when l and r have the same
+// sign and 0 otherwise (the l r <= 0 case of the reference limiters).
 template <int ST>
 __device__ __forceinline__ float2 limit2(float2 l, float2 r) {
     if constexpr (ST == 0) {
         return make_float2(0.f, 0.f);
-    } else if constexpr (ST == 1) {   // minmod
-        const float2 pr = mul2(l, r);
-        const float mx = fabsf(r.x) < fabsf(l.x) ? r.x : l.x, my = fabsf(r.y) < fabsf(l.y) ? r.y : l.y;
-        const float2 m = make_float2(pr.x < 0.f ? 0.f : mx, pr.y < 0.f ? 0.f : my);
-        return add2(m, m);
+    } else if constexpr (ST == 1) {   // minmod: 2 sign(l) min(|l|, |r|)
+        const float2 m = make_float2(fmaxf(min_xorsign_abs(l.x, r.x), 0.f), fmaxf(min_xorsign_abs(l.y, r.y), 0.f));
+        const float2 m2 = add2(m, m);
+        return make_float2(copysignf(m2.x, l.x), copysignf(m2.y, l.y));
     } else if constexpr (ST == 2) {   // van Leer: 2 (2 l r / (l + r))
         const float2 pr = mul2(l, r), s = add2(l, r);
         const float2 q = mul2(pr, make_float2(4.f / s.x, 4.f / s.y));
         return make_float2(pr.x <= 0.f ? 0.f : q.x, pr.y <= 0.f ? 0.f : q.y);
     } else {                          // MC: 2 sign(s) min(1.5 min(|l|,|r|), |s|/2) = sign(s) min(3 min, |s|)
-        const float2 pr = mul2(l, r), s = add2(l, r);
-        const float2 t = mul2(make_float2(fminf(fabsf(l.x), fabsf(r.x)), fminf(fabsf(l.y), fabsf(r.y))), bc2(3.f));
-        const float mx = copysignf(fminf(t.x, fabsf(s.x)), s.x), my = copysignf(fminf(t.y, fabsf(s.y)), s.y);
-        return make_float2(pr.x <= 0.f ? 0.f : mx, pr.y <= 0.f ? 0.f : my);
+        const float2 s = add2(l, r);
+        const float2 a = mul2(make_float2(fmaxf(min_xorsign_abs(l.x, r.x), 0.f), fmaxf(min_xorsign_abs(l.y, r.y), 0.f)),
+                              bc2(3.f));
+        // sign(s) min(|s|, a) for a >= 0: s clamped to [-a, a]
+        return make_float2(fmaxf(fminf(s.x, a.x), -a.x), fmaxf(fminf(s.y, a.y), -a.y));
     }
 }
 
@@ -60,8 +72,64 @@ __device__ __forceinline__ void hb2(float2 rL, float2 uL, float2 vL, float2 wL, 
     f[3] = fma2(mr, wR, mul2(ml, wL));
 }
 
-template <int ST>
-__device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by) {
+// Arguments of a strip's row source: the tensor map of this launch's current state and the
+// warp's shared-memory ring.
+struct RingArgs {
+    const CUtensorMap* map;
+    float* ring;
+    uint64_t* bar;
+};
+
+// The row source of a strip (overloads chosen by the type of the null first argument).
+template <int NV, int R, int NST>
+__device__ __forceinline__ TmaRows<NV, R, NST> make_rows_impl(TmaRows<NV, R, NST>*, const KParams<float>&,
+                                                              const RingArgs& ra, int, int, bool, int x0, int r0,
+                                                              int sp, int nrows) {
+    TmaRows<NV, R, NST> t;
+    t.map = ra.map;
+    t.ring = ra.ring;
+    t.bar = ra.bar;
+    t.x0 = x0;
+    t.r0 = r0;
+    t.sp = sp;
+    t.lane = threadIdx.x & 31;
+    t.setup(nrows);
+    return t;
+}
+template <class Rows>
+__device__ __forceinline__ Rows make_rows(const KParams<float>& p, const RingArgs& ra, int vb, int vs, bool col_in,
+                                          int x0, int r0, int sp, int nrows) {
+    return make_rows_impl(static_cast<Rows*>(nullptr), p, ra, vb, vs, col_in, x0, r0, sp, nrows);
+}
+
+// Scalars of a uniform Cartesian grid (every column has the same dx1, dx2, surf1, surf2, vol, as
+// gridinit builds them, grid.f90:104-160): the limited slopes are formed from the raw differences
+// (the limiters are homogeneous of degree one, so limit(d_l/dx, d_r/dx) dx = limit(d_l, d_r)),
+// the half-step factors dt/(4 dx), dt/(4 dy) multiply the velocities once per row, and the
+// update factors surf dt/vol are the same for every cell.
+struct UniformGrid {
+    float cxq, cyq;   // dt / (4 dx1), dt / (4 dx2): doubled slopes -> half-step source
+    float cxf, cyf;   // surf1 dt / vol, surf2 dt / vol: face fluxes -> cell update
+};
+
+__device__ __forceinline__ UniformGrid uniform_grid(const KParams<float>& p, float dt) {
+    const int c = p.ng;
+    UniformGrid g;
+    g.cxq = 0.25f * dt * p.sfx[c];          // sfx = 1/dx1 on a uniform grid
+    g.cyq = 0.25f * dt * p.sfy[c];          // sfy = 1/dx2
+    g.cxf = p.surf1[c] * (dt * p.rvol[c]);
+    g.cyf = p.surf2[c] * (dt * p.rvol[c]);
+    return g;
+}
+
+// K1 of one dust species (4 variables) on a uniform Cartesian grid, two columns per lane.
+// Per row: the x differences of the row, the y difference to the next row (the y difference
+// below the row is the one the previous row computed), the limited doubled slopes, the
+// predictor, the four face states, the Huang & Bai fluxes of the x faces and of the y face below,
+// then the row below is finished and this row started.  The row loop is unrolled by two so that
+// the rows carried from one iteration to the next change registers without moves.
+template <int ST, class Rows>
+__device__ void flux_strip_dust2(const KParams<float>& p, const RingArgs& ra, int s, int bx, int by) {
     const unsigned FULL = 0xffffffffu;
     const int N = p.ndust;
     const int lane = threadIdx.x & 31;
@@ -71,45 +139,29 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
     if (ay0 >= p.ng + p.ny) return;            // uniform over the warp
     const int ylast = min(ay0 + STRIP_H, p.ng + p.ny) - 1;
     const bool col_in = ga < p.nx_max;         // ga + 1 is then inside the row's pitch padding
-    const int ca = min(ga, p.nx_max - 1), cb = min(ga + 1, p.nx_max - 1), cc = min(ga + 2, p.nx_max - 1);
+    const int ca = min(ga, p.nx_max - 1), cb = min(ga + 1, p.nx_max - 1);
     const bool halo = lane == 0 || lane == 31;
     const bool upd_a = !halo && ga < p.ng + p.nx, upd_b = !halo && ga + 1 < p.ng + p.nx;
     const bool act_a = ga >= p.ng && ga < p.ng + p.nx, act_b = ga + 1 >= p.ng && ga + 1 < p.ng + p.nx;
 
     const float dt = *p.dtf;
-    const float qdt = 0.25f * dt;
-    // column tables: x-face factors of the faces left of a, between a and b, right of b
-    const float sfa = p.sfx[ca], sfb = p.sfx[cb], sfc = p.sfx[cc];
-    const float2 sfy = make_float2(p.sfy[ca], p.sfy[cb]);
-    const float2 dtv = make_float2(dt * p.rvol[ca], dt * p.rvol[cb]);
-    const float2 cl = mul2(make_float2(p.surf1[ca], p.surf1[cb]), dtv);           // left x faces
-    const float2 ncr = mul2(make_float2(-p.surf1[cb], -p.surf1[cc]), dtv);        // right x faces, negated
-    const float2 cy = mul2(make_float2(p.surf2[ca], p.surf2[cb]), dtv), ncy = make_float2(-cy.x, -cy.y);
-    const float2 hx = make_float2(0.25f * p.dx1[ca], 0.25f * p.dx1[cb]), nhx = make_float2(-hx.x, -hx.y);
-    const float2 hy = make_float2(0.25f * p.dx2[ca], 0.25f * p.dx2[cb]), nhy = make_float2(-hy.x, -hy.y);
+    const UniformGrid G = uniform_grid(p, dt);
+    const float2 cxf = bc2(G.cxf), ncxf = bc2(-G.cxf), cyf = bc2(G.cyf), ncyf = bc2(-G.cyf);
+    const float2 q4 = bc2(0.25f), nq4 = bc2(-0.25f);
     // SI force kick on the dust (setup_force, species s >= 1): f1 = 2 q om^2 xc - 2 om vz, f3 = 2 om vx
     const bool fk = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
     const float om = p.f_si_om, qs = p.f_si_q;
     const float2 f1c = make_float2(2.f * qs * (om * om) * (p.xpos[ca] - p.f_half_box_l),
                                    2.f * qs * (om * om) * (p.xpos[cb] - p.f_half_box_l));
     const float2 m2om = bc2(-2.f * om), p2om = bc2(2.f * om);
+    const float2 fsel = make_float2(act_a ? 1.f : 0.f, act_b ? 1.f : 0.f);   // ghost columns: force 0
 
-    float2 q0[4], q1[4], q2[4];      // primitive rows P-1, P, P+1
-    float2 qmy_prev[4], t_prev[4];   // t_prev: row P-1 after its kick, x fluxes and lower y flux
-    // element offset of component k of this lane's first column, svar(s, k, N) * plane + ca,
-    // from a base and a stride (two registers instead of four offsets)
-    const int vbase = svar(s, 0, N) * (int)p.plane + ca, vstride = N * (int)p.plane;
-    auto voff = [&](int k) { return vbase + k * vstride; };
-    const float* __restrict__ src = p.u_cur;
+    // element offset of component k of this lane's first column: svar(s, k, N) * plane + ca
+    // = vb + k * vs (species planes from a base and a stride)
+    const int vb = svar(s, 0, N) * (int)p.plane + ca, vs = N * (int)p.plane;
     float* __restrict__ dst = p.u_next;
     const int pitch = p.pitch;
-    auto fetch_row = [&](int row, float2* us) {
-        const bool in = col_in && row < p.ny_max;
-        const int ro = min(row, p.ny_max - 1) * pitch;
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            us[k] = in ? __ldg(reinterpret_cast<const float2*>(src + (voff(k) + ro))) : make_float2(1.f, 1.f);
-    };
+    Rows rows = make_rows<Rows>(p, ra, vb, vs, col_in, ax0 - 2, ay0 - 2, s - 1, ylast - ay0 + 5);
     auto to_prim = [&](const float2* us, float2* q) {
         const float2 ir = make_float2(1.f / us[0].x, 1.f / us[0].y);
         q[0] = us[0];
@@ -118,33 +170,41 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
         q[3] = mul2(us[3], ir);
     };
 
-    float2 raw[4];
-    fetch_row(ay0 - 2, raw);
-    to_prim(raw, q0);
-    fetch_row(ay0 - 1, raw);
-    to_prim(raw, q1);
-    float2 nxt[4];
-    fetch_row(ay0, nxt);
-    const int rend = ylast + 2;
-    for (int row = ay0; row <= rend; ++row) {
-        to_prim(nxt, q2);
-        if (row < rend) fetch_row(row + 1, nxt);
-        const int P = row - 1;
-        const bool in_p = P >= ay0 && P <= ylast, in_pm = P - 1 >= ay0 && P - 1 <= ylast;
-        const bool start_upd = upd_a && in_p, finish_upd = upd_a && in_pm;
-        float2 uu[4];
-        if (start_upd) {
+    float2 q1[4];                    // primitive row P
+    float2 dyl[4];                   // y difference q(P) - q(P-1)
+    float2 qmy_prev[4], t_prev[4];   // t_prev: row P-1 after its kick, x fluxes and lower y flux
+    rows.begin();
+    {
+        float2 raw[4], q0[4];
+        rows.fetch(ay0 - 2, raw);
+        to_prim(raw, q0);
+        rows.fetch(ay0 - 1, raw);
+        to_prim(raw, q1);
 #pragma unroll
-            for (int k = 0; k < 4; ++k) uu[k] = __ldg(reinterpret_cast<const float2*>(src + (voff(k) + P * pitch)));
+        for (int k = 0; k < 4; ++k) dyl[k] = sub2(q1[k], q0[k]);
+    }
+    const int rend = ylast + 2;
+#pragma unroll 1
+    for (int row = ay0; row <= rend; ++row) {
+        float2 q2[4];                // primitive row P+1, straight from the staged row
+        {
+            float2 raw[4];
+            rows.fetch(row, raw);
+            if (!rows.ok()) break;
+            to_prim(raw, q2);
         }
-        // ---- doubled limited slopes of row P -----------------------------------------------------
-        float2 Dx[4], Dy[4];
+        const int P = row - 1;
+        const bool in_p = P >= ay0 && P <= ylast, in_pm = P - 1 >= ay0 && P - 1 <= ylast;   // warp-uniform
+        // ---- doubled limited slopes of row P (raw differences, uniform grid) ---------------------
+        float2 Lx[4], Ly[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const float qL = __shfl_up_sync(FULL, q1[k].y, 1), qR = __shfl_down_sync(FULL, q1[k].x, 1);
-            const float mid = (q1[k].y - q1[k].x) * sfb;
-            Dx[k] = limit2<ST>(make_float2((q1[k].x - qL) * sfa, mid), make_float2(mid, (qR - q1[k].y) * sfc));
-            Dy[k] = limit2<ST>(mul2(sub2(q1[k], q0[k]), sfy), mul2(sub2(q2[k], q1[k]), sfy));
+            const float mid = q1[k].y - q1[k].x;
+            Lx[k] = limit2<ST>(make_float2(q1[k].x - qL, mid), make_float2(mid, qR - q1[k].y));
+            const float2 dyr = sub2(q2[k], q1[k]);
+            Ly[k] = limit2<ST>(dyl[k], dyr);
+            dyl[k] = dyr;
         }
         // ---- predictor ------------------------------------------------------------------------
         const float2 r = q1[0];
@@ -153,75 +213,79 @@ __device__ void flux_strip_dust2(const KParams<float>& p, int s, int bx, int by)
         if (fk) {
             const bool in_rows = P >= p.ng && P < p.ng + p.ny;   // ghost cells keep force = 0
             const float2 g1 = fma2(w, m2om, f1c), g3 = mul2(u, p2om);
-            f1 = make_float2(in_rows && act_a ? g1.x : 0.f, in_rows && act_b ? g1.y : 0.f);
-            f3 = make_float2(in_rows && act_a ? g3.x : 0.f, in_rows && act_b ? g3.y : 0.f);
+            const float2 fs = in_rows ? fsel : bc2(0.f);
+            f1 = mul2(g1, fs);
+            f3 = mul2(g3, fs);
             const float2 hd = bc2(0.5f * dt);
             u = fma2(f1, hd, u);
             w = fma2(f3, hd, w);
         }
-        // doubled sources: s = -(u dq/dx + v dq/dy) (- rho (du/dx + dv/dy) for the density)
-        const float2 tr = fma2(add2(Dx[1], Dy[2]), r, fma2(v, Dy[0], mul2(u, Dx[0])));
-        const float2 tu = fma2(v, Dy[1], mul2(u, Dx[1]));
-        const float2 tv = fma2(v, Dy[2], mul2(u, Dx[2]));
-        const float2 tw = fma2(v, Dy[3], mul2(u, Dx[3]));
-        const float2 nq = bc2(-qdt);
+        // half-step sources: -(u dq/dx + v dq/dy) dt/2 (- rho (du/dx + dv/dy) dt/2 for the density)
+        const float2 ux = mul2(u, bc2(G.cxq)), vy = mul2(v, bc2(G.cyq));
+        const float2 div = fma2(Lx[1], bc2(G.cxq), mul2(Ly[2], bc2(G.cyq)));
         float2 b[4];
-        b[0] = fma2(tr, nq, r);
-        b[1] = fma2(tu, nq, u);
-        b[2] = fma2(tv, nq, v);
-        b[3] = fma2(tw, nq, w);
-        float2 qmx[4], qpx[4], qmy[4], qpy[4];
+        b[0] = sub2(r, fma2(div, r, fma2(vy, Ly[0], mul2(ux, Lx[0]))));
+        b[1] = sub2(u, fma2(vy, Ly[1], mul2(ux, Lx[1])));
+        b[2] = sub2(v, fma2(vy, Ly[2], mul2(ux, Lx[2])));
+        b[3] = sub2(w, fma2(vy, Ly[3], mul2(ux, Lx[3])));
+        // ---- y face below row P: (qm_y of row P-1, qp_y of row P); normal velocity vy ----------
+        float2 qpy[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            qmx[k] = fma2(Dx[k], hx, b[k]);
-            qpx[k] = fma2(Dx[k], nhx, b[k]);
-            qmy[k] = fma2(Dy[k], hy, b[k]);
-            qpy[k] = fma2(Dy[k], nhy, b[k]);
-        }
-        // ---- x faces left of a and b: (qm_x of the column to the left, qp_x of the column) -------
-        float2 ql[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) ql[k] = make_float2(__shfl_up_sync(FULL, qmx[k].y, 1), qmx[k].x);
-        float2 fxl[4];
-        hb2(ql[0], ql[1], ql[2], ql[3], qpx[0], qpx[1], qpx[2], qpx[3], fxl);
-        float2 fxr[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) fxr[k] = make_float2(fxl[k].y, __shfl_down_sync(FULL, fxl[k].x, 1));
-        // ---- y faces below row P: (qm_y of row P-1, qp_y of row P); normal velocity vy ----------
+        for (int k = 0; k < 4; ++k) qpy[k] = fma2(Ly[k], nq4, b[k]);
         float2 gb[4];
         if (row > ay0) {
             float2 f[4];
             hb2(qmy_prev[0], qmy_prev[2], qmy_prev[1], qmy_prev[3], qpy[0], qpy[2], qpy[1], qpy[3], f);
             gb[0] = f[0]; gb[2] = f[1]; gb[1] = f[2]; gb[3] = f[3];
         }
-        // ---- finish row P-1 with the flux above it -------------------------------------------
-        if (row > ay0 && finish_upd) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) qmy_prev[k] = fma2(Ly[k], q4, b[k]);   // qm_y of row P
+        // ---- x faces left of a and b: (qm_x of the column to the left, qp_x of the column) -------
+        float2 fxl[4];
+        {
+            float2 ql[4], qpx[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float2 qmx = fma2(Lx[k], q4, b[k]);
+                qpx[k] = fma2(Lx[k], nq4, b[k]);
+                ql[k] = make_float2(__shfl_up_sync(FULL, qmx.y, 1), qmx.x);
+            }
+            hb2(ql[0], ql[1], ql[2], ql[3], qpx[0], qpx[1], qpx[2], qpx[3], fxl);
+        }
+        float2 fxr[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) fxr[k] = make_float2(fxl[k].y, __shfl_down_sync(FULL, fxl[k].x, 1));
+        // ---- finish row P-1 with the flux above it (every lane computes, updated columns store) --
+        if (row > ay0 && in_pm) {
             const int ro = (P - 1) * pitch;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const float2 un = fma2(gb[k], ncy, t_prev[k]);
-                if (upd_b) *reinterpret_cast<float2*>(dst + (voff(k) + ro)) = un;
-                else dst[voff(k) + ro] = un.x;
+                const float2 un = fma2(gb[k], ncyf, t_prev[k]);
+                if (upd_b) *reinterpret_cast<float2*>(dst + (vb + k * vs + ro)) = un;
+                else if (upd_a) dst[vb + k * vs + ro] = un.x;
             }
         }
         // ---- start row P: kick with the force of its old q, then the x fluxes ------------------
-        if (start_upd) {
+        if (in_p) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) t_prev[k] = rows.get(P, k);
             if (fk) {
-                const float2 rdt = mul2(uu[0], bc2(dt));
-                uu[1] = fma2(rdt, f1, uu[1]);
-                uu[3] = fma2(rdt, f3, uu[3]);
+                const float2 rdt = mul2(t_prev[0], bc2(dt));
+                t_prev[1] = fma2(rdt, f1, t_prev[1]);
+                t_prev[3] = fma2(rdt, f3, t_prev[3]);
             }
 #pragma unroll
-            for (int k = 0; k < 4; ++k) uu[k] = fma2(gb[k], cy, fma2(fxr[k], ncr, fma2(fxl[k], cl, uu[k])));
+            for (int k = 0; k < 4; ++k)
+                t_prev[k] = fma2(gb[k], cyf, fma2(fxr[k], ncxf, fma2(fxl[k], cxf, t_prev[k])));
         }
         // ---- slide the window -----------------------------------------------------------------
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            qmy_prev[k] = qmy[k];
-            t_prev[k] = uu[k];
-            q0[k] = q1[k];
-            q1[k] = q2[k];
-        }
+        for (int k = 0; k < 4; ++k) q1[k] = q2[k];
+        rows.done(row);
+    }
+    if (!rows.ok()) {
+        if (lane == 0) atomicOr(p.status, SHARK_STATUS_COPY_WAIT);
+        rows.finish();
     }
 }
 
@@ -233,17 +297,40 @@ namespace shark {
 
 // Gas and dust of the mixed path's K1 in one launch: blocks 0 .. ng-1 take the gas strips, the
 // rest the dust strips of every species, both 60 columns per warp.  The gas blocks come first in
-// the launch order, so the gas grid runs beside the dust instead of after it.
+// the launch order, so the gas grid runs beside the dust instead of after it.  Rows reach the
+// strips through a per-warp ring of TMA stages in dynamic shared memory (K1_R rows per stage,
+// K1_NST stages; the maps of the gas and of the dust planes of this step's state).
+struct K1Maps {
+    CUtensorMap gas, dust;
+};
+
+constexpr int K1_R = K1_TMA_ROWS, K1_NST = K1_TMA_STAGES;
+using K1Ring = RingSize<K1_R, K1_NST, 5>;
+constexpr int K1_SMEM = STRIP_WARPS * (K1Ring::ring_bytes + K1Ring::bar_bytes);
+
+// blocks per SM the kernel is compiled for (4 blocks of 128 threads: 128 registers per thread)
+#ifndef SHARK_K1_MINBLOCKS
+#define SHARK_K1_MINBLOCKS 4
+#endif
+template <int NV> using K1Rows = TmaRows<NV, K1_R, K1_NST>;
 template <int ST, int GSOLV>
-__global__ void __launch_bounds__(32 * STRIP_WARPS, 4) k_flux_strip_mixed(KParams<float> p, int nbx_g, int nbx_d, int nby) {
+__global__ void __launch_bounds__(32 * STRIP_WARPS, SHARK_K1_MINBLOCKS)
+    k_flux_strip_mixed(const __grid_constant__ K1Maps maps, KParams<float> p, int nbx_g, int nbx_d, int nby) {
+    extern __shared__ __align__(128) unsigned char k1_smem[];
     const int warp = threadIdx.x >> 5;
     const int id = blockIdx.x, ngas = nbx_g * nby;
+    RingArgs ra;
+    ra.ring = reinterpret_cast<float*>(k1_smem + warp * K1Ring::ring_bytes);
+    ra.bar = reinterpret_cast<uint64_t*>(k1_smem + STRIP_WARPS * K1Ring::ring_bytes + warp * K1Ring::bar_bytes);
     if (id < ngas) {
-        if (p.iso == 1) flux_strip_gas2<ST, GSOLV, true>(p, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
-        else flux_strip_gas2<ST, GSOLV, false>(p, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
+        ra.map = &maps.gas;
+        using GR = K1Rows<5>;
+        if (p.iso == 1) flux_strip_gas2<ST, GSOLV, true, GR>(p, ra, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
+        else flux_strip_gas2<ST, GSOLV, false, GR>(p, ra, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
     } else {
+        ra.map = &maps.dust;
         const int d = id - ngas, bx = d % nbx_d, rest = d / nbx_d;
-        flux_strip_dust2<ST>(p, rest / nby + 1, bx, (rest % nby) * STRIP_WARPS + warp);
+        flux_strip_dust2<ST, K1Rows<4>>(p, ra, rest / nby + 1, bx, (rest % nby) * STRIP_WARPS + warp);
     }
 }
 

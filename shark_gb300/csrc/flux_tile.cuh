@@ -170,19 +170,23 @@ __device__ __forceinline__ GasFlux<R> gas_flux_t(R gamma, R inv_g1, R rl, R ul, 
     }
 }
 
+// csl, csr: the gas sound speeds of the face (used by the HLLC dust solver only).
 template <int SOLVERDUST, typename R>
-__device__ __forceinline__ DustFlux<R> dust_flux_t(R rl, R ul, R vl, R wl, R rr, R ur, R vr, R wr) {
+__device__ __forceinline__ DustFlux<R> dust_flux_t(R rl, R ul, R vl, R wl, R rr, R ur, R vr, R wr, R csl, R csr) {
     if constexpr (SOLVERDUST == 0 && std::is_same<R, float>::value) return dust_hb_f(rl, ul, vl, wl, rr, ur, vr, wr);
     else if constexpr (SOLVERDUST == 0) return dust_hb(rl, ul, vl, wl, rr, ur, vr, wr);
     else if constexpr (SOLVERDUST == 1) return dust_llf(rl, ul, vl, wl, rr, ur, vr, wr);
-    else return dust_hll(rl, ul, vl, wl, rr, ur, vr, wr);
+    else if constexpr (SOLVERDUST == 2) return dust_hll(rl, ul, vl, wl, rr, ur, vr, wr);
+    else return dust_hllc(rl, ul, vl, wl, rr, ur, vr, wr, csl, csr);
 }
 
 template <typename R>
-__device__ __forceinline__ DustFlux<R> dust_flux(int solverdust, R rl, R ul, R vl, R wl, R rr, R ur, R vr, R wr) {
+__device__ __forceinline__ DustFlux<R> dust_flux(int solverdust, R rl, R ul, R vl, R wl, R rr, R ur, R vr, R wr,
+                                                 R csl, R csr) {
     if (solverdust == 0) return dust_hb(rl, ul, vl, wl, rr, ur, vr, wr);
     if (solverdust == 1) return dust_llf(rl, ul, vl, wl, rr, ur, vr, wr);
-    return dust_hll(rl, ul, vl, wl, rr, ur, vr, wr);
+    if (solverdust == 2) return dust_hll(rl, ul, vl, wl, rr, ur, vr, wr);
+    return dust_hllc(rl, ul, vl, wl, rr, ur, vr, wr, csl, csr);
 }
 
 // One species of one tile.  IS_GAS selects the 5-variable gas (solver per p.solver) or a
@@ -448,7 +452,8 @@ __device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
         } else {
             const R rl0 = qmx[0 * S::ring + rl], ul = qmx[1 * S::ring + rl], vl = qmx[2 * S::ring + rl], wl = qmx[3 * S::ring + rl];
             const R rr0 = qpx[0 * S::ring + rr], ur = qpx[1 * S::ring + rr], vr = qpx[2 * S::ring + rr], wr = qpx[3 * S::ring + rr];
-            const DustFlux<R> d = dust_flux(p.solverdust, rl0, ul, vl, wl, rr0, ur, vr, wr);
+            // the HLLC dust solver's gas sound speeds (isothermal gas: per column, godunov.f90:675-677)
+            const DustFlux<R> d = dust_flux(p.solverdust, rl0, ul, vl, wl, rr0, ur, vr, wr, p.cs[gxl], p.cs[gxl + 1]);
             fl[0] = d.rho; fl[1] = d.mn; fl[2] = d.mt; fl[3] = d.mz;
         }
 #pragma unroll
@@ -481,7 +486,7 @@ __device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
             } else {
                 const R rl0 = qmy[0 * S::ring + rl], ul = qmy[2 * S::ring + rl], vl = qmy[1 * S::ring + rl], wl = qmy[3 * S::ring + rl];
                 const R rr0 = qpy[0 * S::ring + rr], ur = qpy[2 * S::ring + rr], vr = qpy[1 * S::ring + rr], wr = qpy[3 * S::ring + rr];
-                const DustFlux<R> d = dust_flux(p.solverdust, rl0, ul, vl, wl, rr0, ur, vr, wr);
+                const DustFlux<R> d = dust_flux(p.solverdust, rl0, ul, vl, wl, rr0, ur, vr, wr, p.cs[gx], p.cs[gx]);
                 fl[0] = d.rho; fl[2] = d.mn; fl[1] = d.mt; fl[3] = d.mz;
             }
 #pragma unroll

@@ -51,6 +51,7 @@ static KParams<R> make_params(const DeviceView& v) {
     p.f_box_l = (float)c.box_l; p.f_half_box_l = 0.5f * (float)c.box_l;
     p.f_si_q = (float)c.si_q_shear; p.f_si_om = (float)c.si_omega;
     p.f_si_r0 = (float)c.si_rad0; p.f_si_eta = (float)c.si_eta_stream;
+    p.f_rho_ref = (float)v.rho_ref;
     p.u_cur = (const R*)v.u[v.cur];
     p.u_next = (R*)v.u[(v.cur + 1) % v.nbuf];
     return p;
@@ -115,6 +116,12 @@ static void strip_kernel(const KParams<R>& p, dim3 grid, cudaStream_t st) {
 
 template <typename R, bool IS_GAS, int ST>
 static void strip_by_solver(const KParams<R>& p, dim3 grid, cudaStream_t st) {
+    if constexpr (!IS_GAS) {
+        if (p.solverdust == 3) {   // HLLC dust (solver_hllc_dust)
+            strip_kernel<R, false, ST, 3>(p, grid, st);
+            return;
+        }
+    }
     switch (IS_GAS ? p.solver : p.solverdust) {
         case 0: strip_kernel<R, IS_GAS, ST, 0>(p, grid, st); break;
         case 1: strip_kernel<R, IS_GAS, ST, 1>(p, grid, st); break;
@@ -140,21 +147,25 @@ static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
     const int nstrips = (p.ny + STRIP_H - 1) / STRIP_H;
     dim3 grid(nbx, (nstrips + STRIP_WARPS - 1) / STRIP_WARPS, 1);
     if constexpr (std::is_same<R, float>::value) {
-        if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0) {
-            // mixed path, Cartesian, Huang & Bai dust: gas and dust strips in one launch
+        if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0 && v.uniform) {
+            // mixed path, uniform Cartesian grid, Huang & Bai dust: gas and dust strips in one launch
             const int nbx_g = (p.nx + STRIP2_UX - 1) / STRIP2_UX, nbx_d = nbx_g;
             const int nby = (int)grid.y;
             const long long nblk = (long long)nbx_g * nby + (long long)nbx_d * nby * p.ndust;
             const dim3 g1((unsigned)nblk, 1, 1), b1(32 * STRIP_WARPS, 1, 1);
             const int gs = p.solver == 0 ? 0 : p.solver == 1 ? 1 : 2;
+            K1Maps maps;
+            maps.gas = v.k1_gas[v.cur];
+            maps.dust = v.k1_dust[v.cur];
             switch (p.slope_type * 3 + gs) {
-#define SHARK_K1M(ST, GS) \
-    case ST * 3 + GS: k_flux_strip_mixed<ST, GS><<<g1, b1, 0, v.stream>>>(p, nbx_g, nbx_d, nby); break;
+#define SHARK_K1M(ST, GS)                                                                                \
+    case ST * 3 + GS:                                                                                    \
+        k_flux_strip_mixed<ST, GS><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, nbx_g, nbx_d, nby); break;
                 SHARK_K1M(0, 0) SHARK_K1M(0, 1) SHARK_K1M(0, 2)
                 SHARK_K1M(1, 0) SHARK_K1M(1, 1) SHARK_K1M(1, 2)
                 SHARK_K1M(2, 0) SHARK_K1M(2, 1) SHARK_K1M(2, 2)
                 SHARK_K1M(3, 0) SHARK_K1M(3, 1)
-                default: k_flux_strip_mixed<3, 2><<<g1, b1, 0, v.stream>>>(p, nbx_g, nbx_d, nby); break;
+                default: k_flux_strip_mixed<3, 2><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, nbx_g, nbx_d, nby); break;
 #undef SHARK_K1M
             }
             return cudaGetLastError();

@@ -2,12 +2,25 @@
 // translation units (kernels_f64.cu compiled without FMA contraction, kernels_f32.cu with it).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "../../include/shark_gpu.h"
 #include "growth.cuh"
 
 namespace shark {
+
+// Rows per TMA stage and stages per warp of the mixed path's flux kernel (K1): each warp's ring
+// holds K1_TMA_STAGES boxes of 64 columns x K1_TMA_ROWS rows x the variables of one species
+// (4 x 2 measured best on the SI 1024^2 x 8 box; 2 x 3 and 2 x 4 within 4 %).
+#ifndef SHARK_K1_TMA_ROWS
+#define SHARK_K1_TMA_ROWS 4
+#endif
+#ifndef SHARK_K1_TMA_STAGES
+#define SHARK_K1_TMA_STAGES 2
+#endif
+constexpr int K1_TMA_ROWS = SHARK_K1_TMA_ROWS;
+constexpr int K1_TMA_STAGES = SHARK_K1_TMA_STAGES;
 
 // Floats of the buffer `coef`: the per-step drag coefficients 1/(1+a_k), a_k/(1+a_k) of the
 // species, the step's dt as float, then (from SHARK_COEF_INVTS, written once) 1/C_k as float.
@@ -70,6 +83,15 @@ struct DeviceView {
     double ou_sigma, ou_tcorr;
     unsigned long long ou_seed;
     long long step;             // 1-based number of the step being launched
+    // mixed path, 2D: tensor maps of each state buffer for K1's TMA row staging, the gas planes
+    // (x, y, variable 0..4) and the dust planes (x, y, species, component)
+    CUtensorMap k1_gas[3], k1_dust[3];
+    bool uniform;               // Cartesian grid with the same dx1, dx2, surf1, surf2, vol in every column
+    bool cs_uniform;            // the same isothermal sound speed in every column
+    // reference gas density of the mixed fused flux kernel: the mean active density of the first
+    // uploaded state on a uniform grid with an isothermal, uniform sound speed (0 otherwise); the
+    // kernel carries rho - rho_ref and c^2 (rho - rho_ref) (flux_strip_gas2.cuh)
+    double rho_ref;
 };
 
 // Record `msg` as this thread's shark_gpu_last_error text and return `code`.

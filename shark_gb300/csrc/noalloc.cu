@@ -10,10 +10,14 @@
 // library.
 //
 // Scratch: g_totals_scratch, a file-scope __device__ array of kScratchDoubles doubles
-// (256 blocks x 260 sums x 2 = 133,120 doubles = 1,064,960 bytes, about 1 MiB).  Every GPU that
-// loads this library holds it until the process exits.  Every call shares it: the first kernel
-// writes every slot the second kernel reads, so nothing needs clearing, but two calls that overlap
-// on the GPU (different streams, no ordering) race on it and give wrong results.
+// (256 blocks x 260 sums x 2 = 133,120 doubles = 1,064,960 bytes, about 1 MiB).  It becomes
+// resident on a device when the CUDA module that holds it is loaded there: with CUDA's default
+// lazy module loading that is the first call of this entry point on the device (which therefore
+// allocates the module's memory and may synchronise), with CUDA_MODULE_LOADING=EAGER it is the
+// creation of the device's context.  From then on the device holds it until the process exits or
+// its context is reset.  Every call shares it: the first kernel writes every slot the second
+// kernel reads, so nothing needs clearing, but two calls that overlap on the GPU (different
+// streams, no ordering) race on it and give wrong results.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -31,8 +35,11 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_totals_scratch[kScratchDoubles];
 
-// Per-device address of g_totals_scratch, looked up once with the device current.  The host-side
+// Per-device address of g_totals_scratch, looked up with the device current.  The host-side
 // symbol g_totals_scratch is only a stand-in for the runtime and must never reach a kernel.
+// The address is looked up again on every call whose stream is not capturing (cheap once the
+// module is loaded), so a cudaDeviceReset between calls, which unloads the module, cannot leave a
+// stale address behind; a call on a capturing stream uses the address of the previous call.
 std::mutex g_mutex;
 double* g_scratch_addr[kMaxDevices] = {nullptr};
 
@@ -94,24 +101,30 @@ extern "C" int32_t shark_gpu_totals_noalloc(const double* u_dev, int32_t nx, int
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(SHARK_ERR_NO_DEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return fail(SHARK_ERR_NO_DEVICE, "device ordinal beyond the supported 64");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     double* part = nullptr;
     {
-        // one-time set-up per device, with that device current: resolve the device address of the
-        // scratch array (the first call on a device should therefore come before any stream capture)
+        // set-up with the device current: resolve the device address of the scratch array.  The
+        // first call on a device must do this outside any capture (it may load the module), so it
+        // must come before any stream capture; later calls refresh it unless `stream` is capturing
         std::lock_guard<std::mutex> lock(g_mutex);
-        if (!g_scratch_addr[dev]) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        const bool capturing = cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone;
+        if (!capturing) {
             void* ptr = nullptr;
             e = cudaGetSymbolAddress(&ptr, g_totals_scratch);
             if (e != cudaSuccess)
                 return fail(SHARK_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             g_scratch_addr[dev] = static_cast<double*>(ptr);
+        } else if (!g_scratch_addr[dev]) {
+            return fail(SHARK_ERR_INVALID_ARG,
+                        "first call on this device made on a capturing stream: make one call before capture");
         }
         part = g_scratch_addr[dev];
     }
     const long long nact = (long long)nx * ny;
     const int nblocks = (int)((nact + 1023) / 1024 < kMaxBlocks ? (nact + 1023) / 1024 : kMaxBlocks);
     const long long per = (nact + nblocks - 1) / nblocks;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     k_noalloc_stage1<<<nblocks, 128, 0, st>>>(u_dev, nx, ny, nghost, ndust, per, part);
     k_noalloc_stage2<<<1, 128, 0, st>>>(part, nblocks, 4 * (ndust + 1), out_dev);
     e = cudaGetLastError();

@@ -253,4 +253,32 @@ __device__ __forceinline__ DustFlux<R> dust_hll(R rho_lft, R u_lft, R v_lft, R w
     return f;
 }
 
+// solver_hllc_dust (src/solver/solvers.f90:704-836): the gas HLLC with zero pressure on one
+// pressureless species, signal speeds bounded by the gas sound speeds csl, csr of the face (the
+// reference's operation order; the energies it forms do not enter the flux).
+template <typename R>
+__device__ __forceinline__ DustFlux<R> dust_hllc(R rho_lft, R u_lft, R v_lft, R w_lft, R rho_rgt, R u_rgt, R v_rgt,
+                                                 R w_rgt, R csl, R csr) {
+    const R P_rgt = R(0), P_lft = R(0);
+    const R cm = fmax2(csl, csr);
+    const R S_lft = fmin2(fmin2(u_lft, u_rgt) - cm, R(0));
+    const R S_rgt = fmax2(fmax2(u_lft, u_rgt) + cm, R(0));
+    const R hllc_l = rho_lft * (u_lft - S_lft);
+    const R hllc_r = rho_rgt * (S_rgt - u_rgt);
+    const R ustar = (hllc_r * u_rgt + hllc_l * u_lft + (P_lft - P_rgt)) / (hllc_r + hllc_l);
+    const R Pstar = (hllc_r * P_lft + hllc_l * P_rgt + hllc_l * hllc_r * (u_lft - u_rgt)) / (hllc_r + hllc_l);
+    R r_o, u_o, P_o;
+    if (S_lft > R(0)) { r_o = rho_lft; u_o = u_lft; P_o = P_lft; }
+    else if (ustar > R(0)) { r_o = rho_lft * (S_lft - u_lft) / (S_lft - ustar); u_o = ustar; P_o = Pstar; }
+    else if (S_rgt > R(0)) { r_o = rho_rgt * (S_rgt - u_rgt) / (S_rgt - ustar); u_o = ustar; P_o = Pstar; }
+    else { r_o = rho_rgt; u_o = u_rgt; P_o = P_rgt; }
+    DustFlux<R> f;
+    f.rho = r_o * u_o;
+    f.mn = r_o * u_o * u_o + P_o;
+    const bool lft = ustar > R(0);
+    f.mt = r_o * u_o * (lft ? v_lft : v_rgt);
+    f.mz = r_o * u_o * (lft ? w_lft : w_rgt);
+    return f;
+}
+
 }  // namespace shark

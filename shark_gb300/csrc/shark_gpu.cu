@@ -4,7 +4,9 @@
 // (src/solver/solve.f90:10-181).  The conserved state never leaves the GPU between steps; the
 // only per-step device->host traffic is the 8-byte dt (plus the 4-byte status word) that the
 // Fortran driver needs for `time = time + dt` (src/shark.f90:107).
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -125,6 +127,7 @@ struct shark_gpu_ctx {
     unsigned int* mlp_err = nullptr;
     long long nstep = 0;             // steps launched since upload
     bool uploaded = false;
+    bool rho_ref_set = false;        // the mixed flux kernel's reference density is fixed at the first upload
     bool pending_read[2] = {false, false};
     int totals_blocks = 0;
     unsigned int status_seen = 0;
@@ -153,6 +156,18 @@ void derive_tables(const shark_gpu_config& c, Columns& col) {
         col.irp[i] = 1.0 / rp;
         col.rvol[i] = col.vol[i] != 0.0 ? 1.0 / col.vol[i] : 0.0;
     }
+}
+
+// Every column has the same spacing, face areas and volume (to 1e-12 relative): the mixed
+// path's fused flux kernel then takes the grid factors as scalars.
+bool uniform_columns(const Columns& col) {
+    const std::vector<double>* t[] = {&col.dx1, &col.dx2, &col.surf1, &col.surf2, &col.vol};
+    for (const auto* a : t) {
+        const double ref = (*a)[a->size() / 2];
+        for (double x : *a)
+            if (!(std::fabs(x - ref) <= 1e-12 * std::fabs(ref))) return false;
+    }
+    return true;
 }
 
 // Positions written by the output routine (write_output.f90:46-96): position(:,1) (radii_c for
@@ -307,8 +322,13 @@ int32_t validate(const shark_gpu_config* c) {
     if (c->geom != 0 && c->geom != 2) return fail(SHARK_ERR_UNSUPPORTED, "geom %d not built (0, 2 only)", c->geom);
     if (c->geom == 2 && c->ny == 1) return fail(SHARK_ERR_UNSUPPORTED, "geom 2 needs ny > 1");
     if (c->solver < 0 || c->solver > 2) return fail(SHARK_ERR_INVALID_ARG, "solver must be 0..2");
-    if (c->solverdust < 0 || c->solverdust > 2)
-        return fail(SHARK_ERR_UNSUPPORTED, "solverdust %d not built (0 HB, 1 LLF, 2 HLL)", c->solverdust);
+    if (c->solverdust < 0 || c->solverdust > 3)
+        return fail(SHARK_ERR_UNSUPPORTED, "solverdust %d not built (0 HB, 1 LLF, 2 HLL, 3 HLLC)", c->solverdust);
+    // solver_hllc_dust bounds the dust signal speeds with the gas sound speeds of the face: with an
+    // isothermal gas those are the cells' (per column), with an adiabatic gas they come from the
+    // gas face states, which the per-species dust kernels do not form
+    if (c->solverdust == 3 && c->iso_cs != 1 && c->ndust > 0)
+        return fail(SHARK_ERR_UNSUPPORTED, "solverdust 3 (HLLC dust) needs an isothermal gas (iso_cs = 1)");
     if (c->slope_type < 0 || c->slope_type > 3) return fail(SHARK_ERR_INVALID_ARG, "unknown slope limiter");
     if (c->precision != SHARK_PREC_FP64 && c->precision != SHARK_PREC_MIXED)
         return fail(SHARK_ERR_INVALID_ARG, "precision must be FP64 or MIXED");
@@ -755,6 +775,58 @@ int32_t release(shark_gpu_ctx* c) {
 
 bool is_mixed(const shark_gpu_ctx* c) { return c->cfg.precision == SHARK_PREC_MIXED; }
 
+// cuTensorMapEncodeTiled from the driver (through the runtime's entry-point query, so the library
+// does not link libcuda itself).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    }
+    return fn;
+}
+
+// Tensor maps of K1's TMA row staging for every FP32 state buffer of a 2D context: the gas planes
+// as a 3D tensor (x over the row pitch, y over ny_max rows, the 5 gas variables) and the dust
+// planes as a 4D tensor (x, y, species, component: plane 5 + c N + s), boxes of 64 columns x
+// K1_TMA_ROWS rows x every variable of one species.  Out-of-range parts of a box read as zeros.
+int32_t encode_k1_maps(shark_gpu_ctx* c) {
+    shark::DeviceView& v = c->v;
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(SHARK_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t pitch = (cuuint64_t)v.pitch, rows = (cuuint64_t)v.ny_max, plane = (cuuint64_t)v.plane;
+    const cuuint32_t R = (cuuint32_t)shark::K1_TMA_ROWS;
+    for (int b = 0; b < v.nbuf; ++b) {
+        float* base = static_cast<float*>(v.u[b]);
+        {
+            const cuuint64_t dim[3] = {pitch, rows, 5};
+            const cuuint64_t stride[2] = {pitch * 4, plane * 4};
+            const cuuint32_t box[3] = {64, R, 5};
+            const cuuint32_t es[3] = {1, 1, 1};
+            CUresult r = enc(&v.k1_gas[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dim, stride, box, es,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(SHARK_ERR_CUDA, "cuTensorMapEncodeTiled (gas planes): error %d", (int)r);
+        }
+        if (v.ndust > 0) {
+            const cuuint64_t N = (cuuint64_t)v.ndust;
+            const cuuint64_t dim[4] = {pitch, rows, N, 4};
+            const cuuint64_t stride[3] = {pitch * 4, plane * 4, N * plane * 4};
+            const cuuint32_t box[4] = {64, R, 1, 4};
+            const cuuint32_t es[4] = {1, 1, 1, 1};
+            CUresult r = enc(&v.k1_dust[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base + 5 * plane, dim, stride, box, es,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) return fail(SHARK_ERR_CUDA, "cuTensorMapEncodeTiled (dust planes): error %d", (int)r);
+        }
+    }
+    return SHARK_OK;
+}
+
 cudaError_t do_step(shark_gpu_ctx* c, int slot) {
     return is_mixed(c) ? shark::launch_step<float>(c->v, slot) : shark::launch_step<double>(c->v, slot);
 }
@@ -968,6 +1040,9 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     if ((rc = build_columns(*cfg, v.nx_max, v.ny_max, col))) { release(c); return rc; }
     output_positions(*cfg, col, v.nx_max, v.ny_max, c->out_x, c->out_y);
     derive_tables(*cfg, col);
+    v.uniform = cfg->geom == 0 && v.ndim == 2 && uniform_columns(col);
+    v.cs_uniform = std::all_of(col.cs.begin(), col.cs.end(), [&](double x) { return x == col.cs[0]; });
+    v.rho_ref = 0.0;
 
 #define INIT_TRY(call)                                                                            \
     do {                                                                                          \
@@ -996,6 +1071,10 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
     }
     v.u[2] = c->ubuf[2];
     v.cur = 0;
+    if (is_mixed(c) && v.ndim == 2 && (rc = encode_k1_maps(c))) {
+        release(c);
+        return rc;
+    }
     if (cfg->setup == SHARK_SETUP_DISK_POLAR) {
         INIT_TRY(cudaMalloc(&c->uinit, c->state_bytes));
         INIT_TRY(cudaMemsetAsync(c->uinit, 0, c->state_bytes, c->stream));
@@ -1188,6 +1267,19 @@ int32_t shark_gpu_upload(shark_gpu_ctx* c, const double* u_prim, int64_t ncells,
         return fail(SHARK_ERR_INVALID_ARG, "state is %lld x %d, context expects %lld x %d", (long long)ncells, nvar,
                     (long long)v.nx_max * v.ny_max, v.nvar);
     CUDA_TRY(cudaSetDevice(c->cfg.device));
+    if (!c->rho_ref_set) {
+        // reference density of the mixed fused flux kernel: the mean gas density of the active
+        // cells of the first state (kept for the life of the context; any value is exact in
+        // theory, one near the typical density keeps the pressure variations at FP32 precision)
+        c->rho_ref_set = true;
+        if (is_mixed(c) && v.ndim == 2 && v.uniform && c->cfg.iso_cs == 1 && v.cs_uniform) {
+            double sum = 0.0;
+            for (int iy = v.ng; iy < v.ng + v.ny; ++iy)
+                for (int ix = v.ng; ix < v.ng + v.nx; ++ix) sum += u_prim[(long long)iy * v.nx_max + ix];
+            const double mean = sum / ((double)v.nx * (double)v.ny);
+            c->v.rho_ref = std::isfinite(mean) && mean > 0.0 ? mean : 0.0;
+        }
+    }
     // drain any readbacks still in flight: the new state starts a new dt sequence
     for (int s = 0; s < 2; ++s) if (c->pending_read[s]) { cudaEventSynchronize(c->ev_read[s]); c->pending_read[s] = false; }
     const size_t bytes = (size_t)ncells * nvar * sizeof(double);

@@ -65,6 +65,7 @@ struct KParams {
     // this GPU, so per-thread conversions stall the warps that do them
     float f_gamma, f_gm1, f_inv_g1, f_cfl, f_smallr, f_smallp, f_dust_ratio_min, f_box_l, f_half_box_l;
     float f_si_q, f_si_om, f_si_r0, f_si_eta;
+    float f_rho_ref;                  // reference gas density of the mixed flux kernel (0: none)
     const R* u_cur;                   // state at the start of the step (read only)
     R* u_next;                        // state after the step
 };

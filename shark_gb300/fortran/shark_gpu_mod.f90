@@ -19,6 +19,9 @@ module shark_gpu
   integer(c_int32_t), parameter :: SHARK_PREC_FP64 = 0, SHARK_PREC_MIXED = 1
   integer(c_int32_t), parameter :: SHARK_CHARGE_RESISTIVITIES = 1, SHARK_CHARGE_ANALYTICAL = 2
   integer(c_int32_t), parameter :: SHARK_CHARGE_MLP_SEED = 4
+  integer(c_int32_t), parameter :: SHARK_GROWTH_FRAGMENTATION = 1, SHARK_GROWTH_DRIFT = 2
+  integer(c_int32_t), parameter :: SHARK_GROWTH_TURB = 4, SHARK_GROWTH_BROWNIAN = 8
+  integer(c_int32_t), parameter :: SHARK_GROWTH_AMBIPOLAR = 16
 
   type, bind(C) :: shark_gpu_config
     integer(c_int32_t) :: abi_version, nx, ny, nghost, ndust, geom, gridspace, solver, solverdust
@@ -102,6 +105,13 @@ module shark_gpu
       type(c_ptr), value :: ctx
       character(kind=c_char), intent(in) :: dir(*)
       real(c_double), intent(out) :: time
+    end function
+    ! last charging outputs (Fortran order): zd(ncells,N), ni, ne, psi_old (ncells),
+    ! eta(ncells,3) = (eta_o, eta_H, eta_a), gamma_d(ncells,N), iterations; c_null_ptr skips one
+    integer(c_int32_t) function shark_gpu_download_charge(ctx, zd, ni, ne, psi, eta, gamma_d, iters) &
+        bind(C, name="shark_gpu_download_charge")
+      import :: c_int32_t, c_ptr
+      type(c_ptr), value :: ctx, zd, ni, ne, psi, eta, gamma_d, iters
     end function
     integer(c_int32_t) function shark_gpu_free(ctx) bind(C, name="shark_gpu_free")
       import :: c_int32_t, c_ptr

@@ -1,5 +1,5 @@
-"""Copies the reference's own golden data for this path into tests/golden/ (run once, in a
-checkout where the reference is mounted; the outputs are committed).
+"""Copies the reference's own golden data for this path into tests/golden/ (run once with the path
+of a reference checkout as its only argument; the outputs are committed).
 
 Sources (reference test suite):
   test/test-suite/Sod-tube/solution.dat           exact Sod solution, t=0.245, gamma=1.4, 1024 cells
@@ -14,7 +14,9 @@ Their namelists (sod.nml, wave{50,100,1000}.nml) fix the run parameters used by 
 import os
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python make_golden.py <path of the reference checkout>")
+REF = sys.argv[1]
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 FILES = {

@@ -82,6 +82,17 @@ def test_invalid_configs_are_rejected_before_touching_a_device(lib):
     assert lib.shark_gpu_free(None) == K.OK
 
 
+def test_hllc_dust_needs_an_isothermal_gas(lib):
+    h = C.c_void_p()
+    cfg, _ = setups.sod(nx=64, ndust=2)
+    assert cfg.iso_cs != 1
+    cfg.solverdust = 3
+    assert lib.shark_gpu_init(C.byref(cfg), C.byref(h)) == K.ERR_UNSUPPORTED
+    assert b"isothermal" in lib.shark_gpu_last_error()
+    cfg.solverdust = 4
+    assert lib.shark_gpu_init(C.byref(cfg), C.byref(h)) == K.ERR_UNSUPPORTED
+
+
 def test_disk_and_fargo_configs_are_checked_before_touching_a_device(lib):
     h = C.c_void_p()
     si, _ = setups.si(n=32, ndust=2)
@@ -113,3 +124,58 @@ def test_no_cpu_fallback_without_a_gpu(lib):
     with pytest.raises(solver.SharkError) as e:
         solver.Shark(cfg)
     assert e.value.code == K.ERR_NO_DEVICE
+
+
+# ---- the Fortran side of the boundary (shark_gb300/fortran/), checked without a Fortran compiler --
+FORTRAN = os.path.join(ROOT, "shark_gb300", "fortran")
+_FKIND = {"integer(c_int32_t)": (4, 4), "real(c_double)": (8, 8), "type(c_ptr)": (8, 8)}
+
+
+def _fortran_config_layout():
+    """Offsets of the bind(C) derived type shark_gpu_config of shark_gpu_mod.f90, laid out with the
+    C rules bind(C) promises (natural alignment of c_int32_t, c_double and c_ptr, arrays packed)."""
+    text = open(os.path.join(FORTRAN, "shark_gpu_mod.f90")).read()
+    body = re.search(r"type, bind\(C\) :: shark_gpu_config\n(.*?)\n\s*end type shark_gpu_config", text, re.S).group(1)
+    consts = {"SHARK_MAX_DUST": 64}
+    off, layout = 0, {}
+    for line in body.splitlines():
+        line = line.split("!")[0].strip()
+        if not line:
+            continue
+        kind, names = [x.strip() for x in line.split("::")]
+        size, align = _FKIND[kind]
+        for m in re.finditer(r"(\w+)(?:\((\w+)\))?", names):
+            n = 1 if m.group(2) is None else int(consts.get(m.group(2), m.group(2)))
+            off = (off + align - 1) // align * align
+            layout[m.group(1).lower()] = off
+            off += size * n
+    return layout, (off + 7) // 8 * 8
+
+
+def test_fortran_config_type_matches_the_c_struct():
+    layout, size = _fortran_config_layout()
+    c_fields = {f.lower(): getattr(SharkConfig, f).offset for f, _ in SharkConfig._fields_}
+    assert size == C.sizeof(SharkConfig)
+    assert set(layout) == set(c_fields), set(layout) ^ set(c_fields)
+    for f, off in layout.items():
+        assert off == c_fields[f], f
+
+
+def test_fortran_shim_writes_only_existing_fields_and_maps_every_setup():
+    layout, _ = _fortran_config_layout()
+    src = open(os.path.join(FORTRAN, "solve_gpu.f90")).read()
+    written = {m.lower() for m in re.findall(r"\bcfg%(\w+)", src)}
+    assert written <= set(layout), written - set(layout)
+    # the per-setup parameters of every setup id the library accepts
+    for sid in range(1, 8):
+        assert f"#if SHARK_GPU_SETUP=={sid}" in src, sid
+    for f in ("disk_mstar", "disk_hoverr", "disk_sigma0", "disk_r_relax", "disk_n_rel", "disk_temp_slope",
+              "turb_rho0", "t_cloud", "dust_stokes", "turb_mach", "turb_tcorr", "turb_kmin", "turb_kmax",
+              "chg_x", "chg_eps", "chg_nitermax", "chg_mode", "grw_smin", "grw_smax", "grw_cfl", "grw_mode"):
+        assert f in written, f
+    # before an output step the charging outputs come back with the state
+    assert "shark_gpu_download_charge" in src
+    mod = open(os.path.join(FORTRAN, "shark_gpu_mod.f90")).read()
+    assert 'bind(C, name="shark_gpu_download_charge")' in mod
+    bound = set(re.findall(r'bind\(C, name="(shark_gpu_\w+)"\)', mod))
+    assert bound <= set(solver.EXPORTS), bound - set(solver.EXPORTS)

@@ -4,8 +4,9 @@ GPU training on (state, converged psi) pairs from the charging solver, and the g
 fewer Newton iterations from a cold start at the same residual tolerance.
 
 Tolerances: the forward output within 2e-3 of the target scale and every gradient group within
-1e-2 relative L2 of the oracle (FP32 accumulation order of the tensor cores, tanhf vs numpy tanh
-moving a few BF16 roundings by one unit)."""
+1e-4 relative L2 of the oracle, which applies the same BF16 rounding points: what remains is the
+FP32 accumulation order of the tensor cores and tanhf against numpy's tanh, moving a few BF16
+roundings by one unit (measured: at most 9e-6 per group, forward 8e-4 of the target scale)."""
 import math
 
 import numpy as np
@@ -52,12 +53,12 @@ def test_gradient_matches_oracle():
         target = rng.standard_normal(1000).astype(np.float32)
         _, grad, loss = g.mlp_eval(feat, target)
     ref, ref_loss = M.gradient(blob, feat, target)
-    assert loss == pytest.approx(ref_loss, rel=1e-2)
+    assert loss == pytest.approx(ref_loss, rel=1e-4)
     groups = dict(W1=(M.OFF_W1, M.OFF_B1), b1=(M.OFF_B1, M.OFF_W2), W2=(M.OFF_W2, M.OFF_B2), b2=(M.OFF_B2, M.OFF_W3),
                   w3=(M.OFF_W3, M.OFF_B3), b3=(M.OFF_B3, M.NPARAM))
     for name, (a, b) in groups.items():
         err = np.linalg.norm(grad[a:b] - ref[a:b]) / max(np.linalg.norm(ref[a:b]), 1e-30)
-        assert err <= 1e-2, (name, err)
+        assert err <= 1e-4, (name, err)
 
 
 def test_features_match_numpy():

@@ -85,7 +85,7 @@ def test_sod_full_run_to_tend():
         assert rel_l1(cfg, g.download(), o.get_u()).max() <= FP64_TOL
 
 
-@pytest.mark.parametrize("solverdust", [0, 1, 2])
+@pytest.mark.parametrize("solverdust", [0, 1, 2, 3])
 def test_dustywave_fp64(solverdust):
     cfg, u0 = setups.dustywave(nx=2048, ndust=4)
     cfg.solverdust = solverdust
@@ -110,6 +110,18 @@ def _ragged_si(nx, ny, ndust, precision=K.PREC_FP64):
     cfg.nx, cfg.ny = nx, ny
     u0 = setups.si_ic(cfg, 1e-3 * cfg.cs0, 5)
     return cfg, u0
+
+
+@pytest.mark.parametrize("precision,tol", [(K.PREC_FP64, FP64_TOL), (K.PREC_MIXED, MIXED_TOL)])
+def test_si_hllc_dust(precision, tol):
+    """solver_hllc_dust (solvers.f90:704-836, SOLVERDUST=3) on the SI box: ragged tiles in FP64,
+    the generic FP32 strips in mixed precision."""
+    cfg, u0 = _ragged_si(70, 45, 4, precision=precision)
+    cfg.solverdust = 3
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 25)
+    assert st == 0
+    np.testing.assert_allclose(dtg, dto, rtol=1e-14 if precision == K.PREC_FP64 else 1e-5, atol=0)
+    assert rel_l1(cfg, ug, uo).max() <= tol
 
 
 def test_si_without_force_kick_uses_inloop_rotation():
