@@ -836,10 +836,11 @@ k_finalize_mixed(KParams<float> p) {
     unsigned int st = 0;
     const bool act = gx < p.ng + p.nx;
     float* u = p.u_next;
-    // this cell's element of plane 0; variable v sits v planes further (32-bit plane offsets: the
-    // context guarantees nvar * plane < 2^31)
-    float* const uc = u + ((long long)gy * p.pitch + gx);
-    const float* const ucur = p.u_cur + ((long long)gy * p.pitch + gx);
+    // this cell's element of plane 0, variable v v planes further, as 32-bit offsets from the
+    // state's (uniform) base pointer (the context guarantees nvar * plane < 2^31): an access is a
+    // 32-bit offset on a uniform base, not a 64-bit address formed per thread
+    const int cc = gy * p.pitch + gx;
+    const float* __restrict__ ucur = p.u_cur;
     const int pl = (int)p.plane;
     float rho = 0.f, px = 0.f, py = 0.f, pz = 0.f;
     // compile-time species count: the cell's dust state is loaded once into registers (all loads
@@ -858,23 +859,27 @@ k_finalize_mixed(KParams<float> p) {
     // part 1: drag, floor, drag heating; part 2: kick, setup_inloop, CFL.  With growth in between
     // (a block-wide phase) the two parts are separate; otherwise they form one block of code.
     auto part1 = [&]() {
-        rho = uc[(0) * pl];
-        px = uc[(1) * pl]; py = uc[(2) * pl]; pz = uc[(3) * pl];
+        // the loads take their offsets from an opaque copy of the cell offset, so that the
+        // compiler forms the stores' offsets anew instead of keeping every load offset live
+        int cl = cc;
+        asm volatile("" : "+r"(cl));
+        rho = u[cl + (0) * pl];
+        px = u[cl + (1) * pl]; py = u[cl + (2) * pl]; pz = u[cl + (3) * pl];
         if constexpr (NS > 0) {
             if (drag) {
 #pragma unroll
                 for (int k = 0; k < NS; ++k) {
-                    dr[k] = uc[(5 + k) * pl];
-                    dmx[k] = uc[(5 + N + k) * pl];
-                    dmy[k] = uc[(5 + 2 * N + k) * pl];
-                    dmz[k] = uc[(5 + 3 * N + k) * pl];
+                    dr[k] = u[cl + (5 + k) * pl];
+                    dmx[k] = u[cl + (5 + N + k) * pl];
+                    dmy[k] = u[cl + (5 + 2 * N + k) * pl];
+                    dmz[k] = u[cl + (5 + 3 * N + k) * pl];
                 }
                 float rk[NMAX], wk[NMAX];
                 if (const_ts) {          // the step's coefficients (no FP64 work per cell)
 #pragma unroll
                     for (int k = 0; k < NS; ++k) { rk[k] = cr[k]; wk[k] = cw[k]; }
                 } else {
-                    const float rho_old = ucur[(0) * pl];
+                    const float rho_old = ucur[cc + (0) * pl];
                     const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
                     const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
                     const float Fcf = direct ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx);
@@ -902,10 +907,10 @@ k_finalize_mixed(KParams<float> p) {
                     dmx[k] = dmx[k] * rk[k] + wr * vbx;
                     dmy[k] = dmy[k] * rk[k] + wr * vby;
                     dmz[k] = dmz[k] * rk[k] + wr * vbz;
-                    uc[(5 + N + k) * pl] = dmx[k];
-                    uc[(5 + 2 * N + k) * pl] = dmy[k];
-                    uc[(5 + 3 * N + k) * pl] = dmz[k];
-                    if (fl > dr[k]) { dr[k] = fl; uc[(5 + k) * pl] = fl; }
+                    u[cc + (5 + N + k) * pl] = dmx[k];
+                    u[cc + (5 + 2 * N + k) * pl] = dmy[k];
+                    u[cc + (5 + 3 * N + k) * pl] = dmz[k];
+                    if (fl > dr[k]) { dr[k] = fl; u[cc + (5 + k) * pl] = fl; }
                     if (cfl_in_drag) {   // the dust loop of courant, see part 2
                         const float ird = 1.0f / dr[k];
                         const float vdx = dmx[k] * ird, vdy = dmy[k] * ird, vdz = dmz[k] * ird;
@@ -924,16 +929,16 @@ k_finalize_mixed(KParams<float> p) {
                 cfl_done = cfl_in_drag;
                 if (p.flags & SHARK_FLAG_BACK_REACTION) {
                     px = vbx * rho; py = vby * rho; pz = vbz * rho;
-                    uc[(1) * pl] = px;
-                    uc[(2) * pl] = py;
-                    uc[(3) * pl] = pz;
+                    u[cc + (1) * pl] = px;
+                    u[cc + (2) * pl] = py;
+                    u[cc + (3) * pl] = pz;
                 }
                 in_regs = true;
             }
         } else if (drag) {
             float rk[NMAX], wk[NMAX];
             float rhon = rho, pnx = px, pny = py, pnz = pz;
-            const float rho_old = ucur[(0) * pl];
+            const float rho_old = ucur[cc + (0) * pl];
             const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
             const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
             const float Fcf = (const_ts || direct) ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx);
@@ -947,10 +952,10 @@ k_finalize_mixed(KParams<float> p) {
                 else drag_coeffs_f(Fcf * p.dinvts_f[k], r, w);
                 if (NS > 0) { rk[k < NMAX ? k : 0] = r; wk[k < NMAX ? k : 0] = w; }
                 else if (!const_ts) rw_local[k] = make_float2(r, w);
-                pnx += w * uc[(5 + N + k) * pl];
-                pny += w * uc[(5 + 2 * N + k) * pl];
-                pnz += w * uc[(5 + 3 * N + k) * pl];
-                rhon += w * uc[(5 + k) * pl];
+                pnx += w * u[cc + (5 + N + k) * pl];
+                pny += w * u[cc + (5 + 2 * N + k) * pl];
+                pnz += w * u[cc + (5 + 3 * N + k) * pl];
+                rhon += w * u[cc + (5 + k) * pl];
             }
             const float irhon = 1.0f / rhon;
             const float vbx = pnx * irhon, vby = pny * irhon, vbz = pnz * irhon;
@@ -959,7 +964,7 @@ k_finalize_mixed(KParams<float> p) {
                 if (NS > 0) { r = rk[k < NMAX ? k : 0]; w = wk[k < NMAX ? k : 0]; }
                 else if (const_ts) { r = cr[k]; w = cw[k]; }
                 else { r = rw_local[k].x; w = rw_local[k].y; }
-                const float rd = uc[(5 + k) * pl];
+                const float rd = u[cc + (5 + k) * pl];
                 const long long ixx = uidx(p, 5 + N + k, gy, gx), iyy = uidx(p, 5 + 2 * N + k, gy, gx),
                                 izz = uidx(p, 5 + 3 * N + k, gy, gx);
                 const float wr = w * rd;
@@ -969,9 +974,9 @@ k_finalize_mixed(KParams<float> p) {
             }
             if (p.flags & SHARK_FLAG_BACK_REACTION) {
                 px = vbx * rho; py = vby * rho; pz = vbz * rho;
-                uc[(1) * pl] = px;
-                uc[(2) * pl] = py;
-                uc[(3) * pl] = pz;
+                u[cc + (1) * pl] = px;
+                u[cc + (2) * pl] = py;
+                u[cc + (3) * pl] = pz;
             }
             const float fl = rho * p.f_dust_ratio_min;   // floor (dust_drag.f90:63-73)
             for (int k = 0; k < N; ++k) {
@@ -987,8 +992,8 @@ k_finalize_mixed(KParams<float> p) {
     auto part2 = [&]() {
         if (MODE == 0 && p.ou_nm > 0) {                                    // turbulence kick (solve.f90:129-146)
             turb_kick_cell<float>(p, u, gx, gy, dt);
-            px = uc[(1) * pl];
-            py = uc[(2) * pl];
+            px = u[cc + (1) * pl];
+            py = u[cc + (2) * pl];
         }
         if (MODE == 0 && p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK)) {
             // setup_inloop: Crank-Nicolson rotation (SI/setup.f90:299-332)
@@ -1001,13 +1006,13 @@ k_finalize_mixed(KParams<float> p) {
                 const float uz = pz / rho, vx = px / rho;
                 pz = rho * (uz * (1.f - O2) + 2.f * vx * Ohmdt + AA * O2) * inv;
                 px = rho * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
-                uc[(3) * pl] = pz;
-                uc[(1) * pl] = px;
+                u[cc + (3) * pl] = pz;
+                u[cc + (1) * pl] = px;
             }
             AA = 2.0f * qsh * om * xc;
             for (int k = 0; k < N; ++k) {
                 const long long iz = uidx(p, 5 + 3 * N + k, gy, gx), ixx = uidx(p, 5 + N + k, gy, gx);
-                const float d = uc[(5 + k) * pl];
+                const float d = u[cc + (5 + k) * pl];
                 const float uz = u[iz] / d, vx = u[ixx] / d;
                 u[iz] = d * (uz * (1.f - O2) + 2.f * vx * Ohmdt + AA * O2) * inv;
                 u[ixx] = d * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
@@ -1015,10 +1020,10 @@ k_finalize_mixed(KParams<float> p) {
         }
         if (MODE == 0 && p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<float, float>(p, u, gx, gy, dt)) {
             in_regs = false;
-            rho = uc[(0) * pl];
-            px = uc[(1) * pl];
-            py = uc[(2) * pl];
-            pz = uc[(3) * pl];
+            rho = u[cc + (0) * pl];
+            px = u[cc + (1) * pl];
+            py = u[cc + (2) * pl];
+            pz = u[cc + (3) * pl];
         }
         // ---- courant on the final state (src/solver/courant.f90:11-124), FP32 ----------------------
         const float cfl = p.f_cfl;
@@ -1027,7 +1032,7 @@ k_finalize_mixed(KParams<float> p) {
         float cs;
         if (p.iso == 1) cs = p.cs[gx];
         else {
-            const float E = uc[(4) * pl];
+            const float E = u[cc + (4) * pl];
             const float ekin = 0.5f * rho * (vx * vx) + 0.5f * rho * (vy * vy) + 0.5f * rho * (vz * vz);
             const float P = fmaxf(p.f_gm1 * (E - ekin), p.f_smallp);
             cs = sqrtf(p.f_gamma * P / fmaxf(rho, p.f_smallr));
@@ -1061,10 +1066,10 @@ k_finalize_mixed(KParams<float> p) {
             if (NS > 0 && in_regs) {
                 rd = dr[k < NMAX ? k : 0]; mx = dmx[k < NMAX ? k : 0]; my = dmy[k < NMAX ? k : 0]; mz = dmz[k < NMAX ? k : 0];
             } else {
-                rd = uc[(5 + k) * pl];
-                mx = uc[(5 + N + k) * pl];
-                my = uc[(5 + 2 * N + k) * pl];
-                mz = uc[(5 + 3 * N + k) * pl];
+                rd = u[cc + (5 + k) * pl];
+                mx = u[cc + (5 + N + k) * pl];
+                my = u[cc + (5 + 2 * N + k) * pl];
+                mz = u[cc + (5 + 3 * N + k) * pl];
             }
             const float ird = 1.0f / rd;
             const float vdx = mx * ird;
