@@ -472,10 +472,39 @@ def config_leg(args, name, device, mixed_steps=5, fp64_steps=2):
     out["l1_mixed_vs_fp64"] = rel_l1_max(cm, gm.download(), gd.download())
     out["l1_note"] = f"max relative L1 over the {cm.nvar} conserved fields after {nm} steps from the same state"
     out["mixed_over_fp64"] = out["mixed"]["value"] / out["fp64"]["value"]
+    if name == "turb" and cm.ndust == 32:
+        out["mixed"]["alu_roofline"] = alu_roofline_turb(cm, out["mixed"]["kernel_ms"])
     out["workload"] = describe(argparse.Namespace(workload=name), cm)
     gm.close()
     gd.close()
     return out
+
+
+def alu_roofline_turb(cfg, kernel_ms):
+    """Arithmetic roofline of the driven box's two compute-bound kernels: the per-cell FLOP counts
+    of an ncu capture of the same kernels (profiles/alu_roofline_turb.txt, 512^2 cells) times this
+    run's cells, over this run's event-timed milliseconds.  The growth sub-step and Newton
+    iteration counts depend on the state, so the rates are estimates at the captured counts."""
+    path = os.path.join(ROOT, "profiles", "alu_roofline_turb.txt")
+    if not os.path.exists(path):
+        return None
+    vals = {}
+    with open(path) as f:
+        for line in f:
+            if ":" in line and not line.startswith("#"):
+                k, v = line.split(":", 1)
+                vals[k.strip()] = float(v)
+    cells = cfg.nx * cfg.ny
+    growth_s = kernel_ms["drag_growth_dt"] * 1e-3
+    charge_s = kernel_ms["charge_forcing"] * 1e-3
+    fp32_peak, fp64_peak = vals["fp32_peak_tflops_at_2070mhz"], vals["fp64_peak_tflops_at_2070mhz"]
+    g32 = vals["k_finalize_mixed_growth_fp32_flop_per_cell"] * cells / growth_s / 1e12
+    c64 = vals["k_charge_fp64_flop_per_cell"] * cells / charge_s / 1e12
+    return {"growth": {"kernel": "k_finalize_mixed (drag + growth + CFL)", "bound": "fp32 issue latency",
+                       "achieved": g32, "peak": fp32_peak, "unit": "TFLOP/s", "frac": g32 / fp32_peak},
+            "charging": {"kernel": "k_charge (+ OU forcing update)", "bound": "fp64 pipe",
+                         "achieved": c64, "peak": fp64_peak, "unit": "TFLOP/s", "frac": c64 / fp64_peak},
+            "source": "per-cell FLOPs from profiles/alu_roofline_turb.txt (ncu, 512^2), nominal peaks at 2070 MHz"}
 
 
 def noisy_box(cfg, u, seed, amp=0.5):
