@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define SHARK_GPU_ABI_VERSION 1
+#define SHARK_GPU_ABI_VERSION 2
 #define SHARK_MAX_DUST 64
 
 /* ---- return codes ------------------------------------------------------------------------ */
@@ -63,6 +63,7 @@ extern "C" {
 #define SHARK_SETUP_DUSTYTURB   5   /* periodic driven turbulence       dustyTurb/                  */
 #define SHARK_SETUP_KH          6   /* periodic shear layer, Epstein    KH/setup.f90, KH/units.f90  */
 #define SHARK_SETUP_SEDOV       7   /* periodic blast wave, gas only    sedov/setup.f90             */
+#define SHARK_SETUP_DISK_CART   8   /* Cartesian disk, softened star    disk/setup.f90, disk/boundaries.f90 */
 
 /* ---- run-time switches (the reference's namelist logicals) -------------------------------- */
 #define SHARK_FLAG_DRAG           0x1   /* drag               src/dust/dust_commons.f90:5        */
@@ -189,7 +190,12 @@ typedef struct shark_gpu_config {
     double kh_rho_dense, kh_rho_diffuse, kh_T_dense, kh_mach, kh_vy0, kh_kx;
     /* sedov (sedov/setup_commons.f90): ambient density and pressure, blast overpressure, radius */
     double sedov_rho_ext, sedov_P_ext, sedov_P_cen, sedov_r_expl;
-    double reserved[1];
+    /* Cartesian disk (src/setups/disk/setup_commons.f90), in the disk units (AU, Msun, G = 1):
+     * the star (disk_mstar) at the box centre with softening length cdisk_smooth_r, H/R =
+     * disk_hoverr, Sigma = disk_sigma0 disk_r0 / r inside frac_R_disk box_l (1/100 of its edge
+     * value outside), viscosity eta = disk_alpha_visc H cs; setup_inloop resets the cells with
+     * r < buffer_in box_l or r > buffer_out box_l (r softened) every step.  No planet. */
+    double cdisk_smooth_r, cdisk_frac_r_disk, cdisk_buffer_in, cdisk_buffer_out;
 
     /* Optional grid metrics from the caller (Fortran dx(ncells,ndim), surf(ncells,ndim),
      * vol(ncells), radii_c(ncells), position(ncells,ndim), cs(ncells)).  NULL: the library

@@ -384,14 +384,59 @@ void disk_boundaries(oracle_state& s) {
         }
 }
 
+// Cartesian disk apply_boundaries = zero_gradients (disk/boundaries.f90, boundary_types.f90:48-100)
+// as written: in 2D the source of every ghost is u_prim(first_active_y), u_prim(last_active_y),
+// u_prim(first_active) or u_prim(last_active) -- cell indices of the first (ghost) row, since the
+// row numbers are used as cell numbers -- so the ghosts take the values of cells of that row,
+// in the order of the loops: y ghosts of the active columns first (column by column, bottom
+// before top), then the x ghosts of every row.
+void disk_cart_boundaries(oracle_state& s) {
+    const int ng = s.nghost;
+    // Fortran cell numbers first_active_y, last_active_y, first_active, last_active (1-based)
+    // as 0-based linear indices
+    const int64_t sy_l = s.first_active_y, sy_r = s.last_active_y, sx_l = s.first_active, sx_r = s.last_active;
+    for (int ix = s.first_active; ix <= s.last_active; ++ix)
+        for (int g = 0; g < ng; ++g) {
+            int64_t bl = s.icell(ix, g), br = s.icell(ix, s.ny_max - 1 - g);
+            for (int v = 0; v < s.nvar; ++v) {
+                s.U(bl, v) = s.U(sy_l, v);
+                s.U(br, v) = s.U(sy_r, v);
+            }
+        }
+    for (int g = 0; g < ng; ++g)
+        for (int iy = 0; iy < s.ny_max; ++iy) {
+            int64_t bl = s.icell(g, iy), br = s.icell(s.nx_max - 1 - g, iy);
+            for (int v = 0; v < s.nvar; ++v) {
+                s.U(bl, v) = s.U(sx_l, v);
+                s.U(br, v) = s.U(sx_r, v);
+            }
+        }
+}
+
 void apply_boundaries(oracle_state& s) {
     switch (s.cfg.setup) {
         case SHARK_SETUP_SOD: sod_boundaries(s); break;
         case SHARK_SETUP_SI: si_boundaries(s); break;
         case SHARK_SETUP_DISK_POLAR: disk_boundaries(s); break;
+        case SHARK_SETUP_DISK_CART: disk_cart_boundaries(s); break;
         default: periodic_boundaries(s); break;   // DUSTYWAVE, dustyTurb, KH, sedov (*/boundaries.f90)
     }
 }
+
+// Cartesian disk geometry of cell i (disk/setup.f90): offsets from the box centre, softened
+// radius rr = sqrt(xx^2 + yy^2 + smooth_r^2), H = HoverR rr
+struct CdiskCell {
+    double xx, yy, rr, r_cyl;
+};
+CdiskCell cdisk_cell(const oracle_state& s, int64_t i) {
+    CdiskCell c;
+    c.xx = s.position[i] - half * s.box_l;
+    c.yy = s.position[(size_t)s.ncells + i] - half * s.box_l_y;
+    c.r_cyl = std::sqrt(sq(c.xx) + sq(c.yy));
+    c.rr = std::sqrt(sq(c.xx) + sq(c.yy) + sq(s.cfg.cdisk_smooth_r));
+    return c;
+}
+double cdisk_H(const oracle_state& s, int64_t i) { return s.cfg.disk_hoverr * cdisk_cell(s, i).rr; }
 
 // ---------------------------------------------------------------------------------------------
 // compute_tstop per setup
@@ -412,6 +457,11 @@ void compute_tstop(oracle_state& s) {
                 case SHARK_SETUP_DUSTYTURB:   // dustyTurb/setup.f90:456
                     ts = s.cfg.dust_stokes[k] * s.box_l * s.cfg.turb_rho0 / s.cs[i] / s.Q(i, s.irho);
                     break;
+                case SHARK_SETUP_DISK_CART: {    // disk/setup.f90 compute_tstop: Epstein with Sigma/sqrt(2 pi H)
+                    ts = std::sqrt(pi * s.cfg.gamma / 8.0) * (s.cfg.rhograin) * s.SDUST(i, k) /
+                         (s.Q(i, s.irho) / (std::sqrt(2.0 * pi * cdisk_H(s, i))) * s.cs[i]);
+                    break;
+                }
                 case SHARK_SETUP_DISK_POLAR: {   // disk_polar/setup.f90:425-451, Epstein with Sigma/(sqrt(2 pi) H)
                     const double H = disk_h(s.cfg, s.radii_c[i]) * s.radii_c[i];
                     ts = std::sqrt(pi * s.cfg.gamma / 8.0) * (s.cfg.rhograin) * s.SDUST(i, k) /
@@ -1042,9 +1092,23 @@ void disk_force(oracle_state& s) {
     }
 }
 
+// update_force_setup of the Cartesian disk (disk/setup.f90) without a planet: the star's
+// softened gravity -Mstar (xx, yy)/rr^3 on gas and dust (active cells; the ghosts keep 0).
+void disk_cart_force(oracle_state& s) {
+    const double M = s.cfg.disk_mstar;
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        const CdiskCell c = cdisk_cell(s, i);
+        const double fx = -M * c.xx / powi(c.rr, 3), fy = -M * c.yy / powi(c.rr, 3);
+        s.FORCE(i, 0) = fx; s.FORCE(i, 1) = fy; s.FORCE(i, 2) = 0.0;
+        for (int k = 0; k < s.ndust; ++k) { s.FDUST(i, 0, k) = fx; s.FDUST(i, 1, k) = fy; s.FDUST(i, 2, k) = 0.0; }
+    }
+}
+
 // update_force_setup (SI/setup.f90:335-368); SOD and DUSTYWAVE leave force at zero.
 void update_force_setup(oracle_state& s) {
     if (s.cfg.setup == SHARK_SETUP_DISK_POLAR) { disk_force(s); return; }
+    if (s.cfg.setup == SHARK_SETUP_DISK_CART) { disk_cart_force(s); return; }
     if (s.cfg.setup != SHARK_SETUP_SI) return;
     const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, r0 = s.cfg.si_rad0, eta = s.cfg.si_eta_stream;
     const bool drag = s.flag(SHARK_FLAG_DRAG);
@@ -1103,9 +1167,47 @@ void disk_inloop(oracle_state& s) {
             for (int v = 0; v < s.nvar; ++v) s.U(s.icell(ix, iy), v) = UI(s.icell(s.first_active, iy), v);
 }
 
+// setup_inloop of the Cartesian disk (disk/setup.f90) as written, with its relaxation rate 0:
+// the cells with rr < buffer_in box_l or rr > buffer_out box_l are reset to rho_ana =
+// Sigma_0 R_0/rr (1/100 of the edge value beyond R_out = frac_R_disk box_l), the momenta
+// (-y_soft, x_soft) v_ana with v_ana = -Omega rho_ana, the energy slot rho_ana cs0^2, and every
+// dust species to dust2gas times that with (-yy, xx) in place of the softened offsets.  (With
+// v_ana = -Omega rho_ana the buffers turn the other way round from the initial rotation; the
+// vz momenta are not touched.)  dust_to is the first species' initial dust-to-gas ratio.
+void disk_cart_inloop(oracle_state& s) {
+    const double M = s.cfg.disk_mstar, hr = s.cfg.disk_hoverr;
+    const double R_out = s.cfg.cdisk_frac_r_disk * s.box_l;
+    const double bin = s.cfg.cdisk_buffer_in * s.box_l, bout = s.cfg.cdisk_buffer_out * s.box_l;
+    const double rate = 0.0;
+    for (int64_t i = 0; i < s.ncells; ++i) {
+        if (!s.active[i]) continue;
+        const CdiskCell c = cdisk_cell(s, i);
+        const double rr = c.rr;
+        if (!(rr < bin || rr > bout)) continue;
+        const double x_soft = c.xx * rr / c.r_cyl, y_soft = c.yy * rr / c.r_cyl;
+        const double H = hr * rr;
+        const double Omega = std::sqrt(M / powi(rr, 3));
+        const double cs0 = H * Omega;
+        double rho_ana = s.cfg.disk_sigma0 * (s.cfg.disk_r0 / rr);
+        if (rr > R_out) rho_ana = s.cfg.disk_sigma0 * (s.cfg.disk_r0 / R_out) / 100.0;
+        const double v_ana = -Omega * rho_ana;
+        s.U(i, s.irho) = rho_ana + (s.U(i, s.irho) - rho_ana) * rate;
+        s.U(i, s.ivx) = -y_soft * v_ana + (s.U(i, s.ivx) + c.yy * v_ana) * rate;
+        s.U(i, s.ivy) = x_soft * v_ana + (s.U(i, s.ivy) - c.xx * v_ana) * rate;
+        s.U(i, s.iP) = (rho_ana + (s.U(i, s.irho) - rho_ana) * rate) * sq(cs0);
+        for (int k = 0; k < s.ndust; ++k) {
+            const double dust_to = s.cfg.dust_eps[0];
+            s.U(i, s.irhod[k]) = dust_to * rho_ana + (s.U(i, s.irhod[k]) - rho_ana * dust_to) * rate;
+            s.U(i, s.ivdx[k]) = -c.yy * v_ana * dust_to + (s.U(i, s.ivdx[k]) + dust_to * c.yy * v_ana) * rate;
+            s.U(i, s.ivdy[k]) = c.xx * v_ana * dust_to + (s.U(i, s.ivdy[k]) - dust_to * c.xx * v_ana) * rate;
+        }
+    }
+}
+
 // setup_inloop (SI/setup.f90:299-332): Crank-Nicolson rotation, only without force_kick.
 void setup_inloop(oracle_state& s) {
     if (s.cfg.setup == SHARK_SETUP_DISK_POLAR) { disk_inloop(s); return; }
+    if (s.cfg.setup == SHARK_SETUP_DISK_CART) { disk_cart_inloop(s); return; }
     if (s.cfg.setup != SHARK_SETUP_SI) return;
     if (s.flag(SHARK_FLAG_FORCE_KICK)) return;
     const double qs = s.cfg.si_q_shear, om = s.cfg.si_omega, r0 = s.cfg.si_rad0, eta = s.cfg.si_eta_stream;
@@ -2055,6 +2157,13 @@ oracle_state* oracle_create(const shark_gpu_config* cfg) {
         for (size_t i = 0; i < nc; ++i) s->cs[i] = cfg->cs0;
     if (cfg->setup == SHARK_SETUP_DUSTYTURB && cfg->turb_mach > 0.0) turb_init(*s);
     s->eta_visc.assign(nc, 0.0);
+    if (cfg->setup == SHARK_SETUP_DISK_CART) {   // disk/setup.f90: cs0 = HoverR sqrt(Mstar/rr), eta = alpha H cs
+        for (size_t i = 0; i < nc; ++i) {
+            const double rr = cdisk_cell(*s, (int64_t)i).rr;
+            s->cs[i] = cfg->disk_hoverr * std::sqrt(cfg->disk_mstar / rr);
+            s->eta_visc[i] = cfg->disk_alpha_visc * (cfg->disk_hoverr * rr) * s->cs[i];
+        }
+    }
     if (cfg->setup == SHARK_SETUP_DISK_POLAR) {
         for (size_t i = 0; i < nc; ++i) {
             const double rr = s->radii_c[i];

@@ -6,7 +6,7 @@ size and the offsets of the default-filled fields against the compiled library.
 import ctypes as C
 import struct
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_DUST = 64
 
 OK = 0
@@ -31,6 +31,7 @@ SETUP_DISK_POLAR = 4
 SETUP_DUSTYTURB = 5
 SETUP_KH = 6
 SETUP_SEDOV = 7
+SETUP_DISK_CART = 8
 
 FLAG_DRAG = 0x1
 FLAG_BACK_REACTION = 0x2
@@ -90,7 +91,7 @@ class SharkConfig(C.Structure):
         ("kh_rho_dense", _D), ("kh_rho_diffuse", _D), ("kh_T_dense", _D), ("kh_mach", _D), ("kh_vy0", _D),
         ("kh_kx", _D),
         ("sedov_rho_ext", _D), ("sedov_P_ext", _D), ("sedov_P_cen", _D), ("sedov_r_expl", _D),
-        ("reserved", _D * 1),
+        ("cdisk_smooth_r", _D), ("cdisk_frac_r_disk", _D), ("cdisk_buffer_in", _D), ("cdisk_buffer_out", _D),
         ("dx", _P), ("surf", _P), ("vol", _P), ("radii_c", _P), ("position", _P), ("cs", _P),
     ]
 

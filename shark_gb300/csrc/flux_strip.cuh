@@ -68,6 +68,7 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
     R g_prev[NV];                   // y flux at the bottom face of the previous predicted row
     R t_prev[NV];                   // previous row after kick + x-flux part of the update
     R c_prev = R(0);                // cs of the previous predicted row (isothermal y faces)
+    R vxm2 = R(0), vym2 = R(0);     // old vx, vy of row P-2 (Cartesian viscosity, y neighbour)
 
     // per-lane 32-bit element offsets of the species' planes (the context guarantees
     // nvar * plane < 2^31); row offsets are added per access
@@ -84,7 +85,9 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) us[k] = in ? __ldg(src + (voff[k] + ro)) : R(1);
     };
-    auto to_prim = [&](const R* us, R* q, R& c) {
+    // isothermal sound speed of (row, column): per column, or per cell on the Cartesian disk
+    auto cs_at = [&](int row) -> R { return p.ccs ? p.ccs[min(row, p.ny_max - 1) * pitch + gxc] : cs_col; };
+    auto to_prim = [&](const R* us, R* q, R& c, int row) {
         if (IS_GAS) {
             const R rho = us[0], px = us[1], py = us[2], pz = us[3];
             R P, vx, vy, vz;
@@ -99,7 +102,7 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
             }
             const R qrho = fmax2(rho, smallR);
             if (!iso) c = sqrt(gamma * P / qrho);
-            else { c = cs_col; P = rho * sq(c); }
+            else { c = cs_at(row); P = rho * sq(c); }
             q[0] = qrho; q[1] = vx; q[2] = vy; q[3] = vz; q[4] = P;
         } else {
             q[0] = us[0];
@@ -115,14 +118,14 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
     // rows ay0-2 and ay0-1 prime the window; row ay0 is in flight
     R raw[NV];
     fetch_row(ay0 - 2, raw);
-    to_prim(raw, q0, c0);
+    to_prim(raw, q0, c0, ay0 - 2);
     fetch_row(ay0 - 1, raw);
-    to_prim(raw, q1, c1);
+    to_prim(raw, q1, c1, ay0 - 1);
     R nxt[NV];
     fetch_row(ay0, nxt);
     const int rend = ylast + 2;   // last row loaded
     for (int row = ay0; row <= rend; ++row) {
-        to_prim(nxt, q2, c2);
+        to_prim(nxt, q2, c2, row);
         if (row < rend) fetch_row(row + 1, nxt);   // prefetch the next row (uniform branch)
         const int P = row - 1;    // predicted row, ay0-1 .. ylast+1
         // the update of row P starts in this iteration (kick + x fluxes) and ends in the next one
@@ -159,7 +162,7 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
         R f1 = R(0), f2 = R(0), f3 = R(0);   // force of row P; the kick of row P below reuses it
         if (fk) {
             const bool active = col_active && P >= p.ng && P < p.ng + p.ny;
-            if (active) setup_force(p, s, gxc, u, w, f1, f2, f3);   // ghost cells keep force = 0 (SI/setup.f90:339)
+            if (active) setup_force(p, s, gxc, (long long)P * pitch + gxc, u, w, f1, f2, f3);   // ghost cells keep force = 0 (SI/setup.f90:339)
             u = u + f1 * half * dt;
             v = v + f2 * half * dt;
             w = w + f3 * half * dt;
@@ -346,6 +349,21 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 }
                 un[1] = un[1] + S1;
                 un[2] = un[2] + S2;
+            } else if (IS_GAS && p.visc) {
+                // Cartesian viscosity (source_terms.f90:99-109) on the old velocities of row P-1,
+                // its x neighbours and rows P-2 and P, accumulated in S_U before the update
+                const R qr = q0[0], qvx = q0[1], qvy = q0[2];
+                const R eta = p.ceta[(P - 1) * pitch + gxc];
+                const R dy = p.dx2[gxc];
+                const R lap_x_u = (vxr + vxl - R(2) * qvx) / (dx1 * dx1);
+                R S1 = qr * dt * eta * lap_x_u;
+                const R lap_y_u = (q1[1] + vxm2 - R(2) * qvx) / (dy * dy);
+                S1 = S1 + qr * dt * eta * lap_y_u;
+                const R lap_x_v = (vyr + vyl - R(2) * qvy) / (dx1 * dx1);
+                const R lap_y_v = (q1[2] + vym2 - R(2) * qvy) / (dy * dy);
+                const R S2 = qr * dt * eta * (lap_x_v + lap_y_v);
+                un[1] = un[1] + S1;
+                un[2] = un[2] + S2;
             } else if (polar) {   // Source_terms GEOM==2 (source_terms.f90:37-47)
                 const R qr = q0[0], qvx = q0[1], qvy = q0[2];
                 if constexpr (FAST) {
@@ -395,7 +413,9 @@ __device__ void flux_strip(const KParams<R>& p, int s, int bx, int by) {
                 else uu[k] = uu[k] + (fxl[k] * s1l - fxr[k] * s1r) / vol * dt;
             }
         }
-        // ---- slide the window ---------------------------------------------------------------
+            // ---- slide the window ---------------------------------------------------------------
+        vxm2 = q0[1];
+        vym2 = q0[2];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
             qmy_prev[k] = qmy[k];

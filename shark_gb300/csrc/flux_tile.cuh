@@ -63,7 +63,8 @@ struct TileSmem {
 // self-gravity).  SOD and DUSTYWAVE have no force.  `drag` is on for every configuration that
 // uses the force (the !drag extra terms are rejected at init).
 template <typename R>
-__device__ __forceinline__ void setup_force(const KParams<R>& p, int s, int ix, R vx, R vz, R& f1, R& f2, R& f3) {
+__device__ __forceinline__ void setup_force(const KParams<R>& p, int s, int ix, long long cell, R vx, R vz, R& f1,
+                                            R& f2, R& f3) {
     if (p.setup == SHARK_SETUP_SI) {
         const R qs = prm<R>(p.si_q, p.f_si_q), om = prm<R>(p.si_om, p.f_si_om);
         const R xc = p.xpos[ix] - prm<R>(R(0.5) * R(p.box_l), p.f_half_box_l);
@@ -76,6 +77,10 @@ __device__ __forceinline__ void setup_force(const KParams<R>& p, int s, int ix, 
     } else if (p.setup == SHARK_SETUP_DISK_POLAR) {
         f1 = p.fgrav[ix];
         f2 = f3 = R(0);
+    } else if (p.setup == SHARK_SETUP_DISK_CART) {   // the star's softened gravity (disk/setup.f90)
+        f1 = p.cfx[cell];
+        f2 = p.cfy[cell];
+        f3 = R(0);
     } else {
         f1 = f2 = f3 = R(0);
     }
@@ -320,7 +325,7 @@ __device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
             R f1, f2, f3;
             const int gy = hy0 + hy;
             const bool active = gx >= p.ng && gx < p.ng + p.nx && (NDIM == 1 || (gy >= p.ng && gy < p.ng + p.ny));
-            if (active) setup_force(p, s, gx, u, w, f1, f2, f3);
+            if (active) setup_force(p, s, gx, gx, u, w, f1, f2, f3);
             else f1 = f2 = f3 = R(0);
             u = u + f1 * half * dt;
             v = v + f2 * half * dt;
@@ -506,7 +511,7 @@ __device__ void flux_tile(const KParams<R>& p, int s, R* sm) {
         for (int c = 0; c < NV; ++c) uu[c] = p.u_cur[uidx(p, svar(s, c, N), gy, gx)];
         if (fk) {   // kick(1.0) (src/solver/force_kicks.f90:2-41) before the flux update
             R f1, f2, f3;
-            setup_force(p, s, gx, qs[1 * S::halo + hc], qs[3 * S::halo + hc], f1, f2, f3);
+            setup_force(p, s, gx, gx, qs[1 * S::halo + hc], qs[3 * S::halo + hc], f1, f2, f3);
             const R rho = uu[0];
             if (IS_GAS) {
                 R eo, en;

@@ -52,6 +52,19 @@ static KParams<R> make_params(const DeviceView& v) {
     p.f_si_q = (float)c.si_q_shear; p.f_si_om = (float)c.si_omega;
     p.f_si_r0 = (float)c.si_rad0; p.f_si_eta = (float)c.si_eta_stream;
     p.f_rho_ref = (float)v.rho_ref;
+    p.ccs = p.cfx = p.cfy = p.ceta = nullptr;
+    p.ccsd = p.chsd = p.ctgt = nullptr;
+    p.cgs = nullptr;
+    if (v.cdisk.on) {
+        p.ccs = (const R*)v.cdisk.r;
+        p.cfx = p.ccs + v.plane;
+        p.cfy = p.ccs + 2 * v.plane;
+        p.ceta = p.ccs + 3 * v.plane;
+        p.ccsd = v.cdisk.csd;
+        p.chsd = v.cdisk.hsd;
+        p.ctgt = v.cdisk.tgt;
+        p.cgs = (R*)v.cdisk.gs;
+    }
     p.u_cur = (const R*)v.u[v.cur];
     p.u_next = (R*)v.u[(v.cur + 1) % v.nbuf];
     return p;
@@ -88,11 +101,47 @@ static void finalize_dispatch(const KParams<R>& p, dim3 grid, cudaStream_t st) {
     }
 }
 
+// The Cartesian disk's zero_gradients (boundary_types.f90:48-100) as written, first call, on an
+// uploaded state: its sources are the cells numbered first_active_y, last_active_y,
+// first_active and last_active, i.e. cells (2, 0), (ny + 1, 0), (2, 0) and (nx + 1, 0) of the
+// first ghost row (0-based; ny <= nx is validated).  The loops fill the y ghosts of the active
+// columns column by column (bottom from cell (2, 0), top from cell (ny + 1, 0)), then the x
+// ghosts of every row from cells (2, 0) and (nx + 1, 0).  Cell (ny + 1, 0) is itself the bottom
+// ghost of column ny + 1 and takes cell (2, 0)'s state when the loop reaches that column, so the
+// top ghosts of the active columns left of column ny + 1 keep its uploaded state and every other
+// ghost takes cell (2, 0)'s.  From the second call on every ghost takes cell (2, 0)'s state, which
+// no step changes: k_finalize writes it (fill_ghost_images).
+template <typename R>
+__global__ void k_cdisk_snapshot(KParams<R> p, const R* u) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= p.nvar) return;
+    p.cgs[v] = u[uidx(p, v, 0, 2)];
+    p.cgs[p.nvar + v] = u[uidx(p, v, 0, p.ny + 1)];
+}
+
+template <typename R>
+__global__ void k_cdisk_ghosts(KParams<R> p, R* u) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)p.nx_max * p.ny_max) return;
+    const int ix = (int)(t % p.nx_max), iy = (int)(t / p.nx_max);
+    const bool ax = ix >= p.ng && ix < p.ng + p.nx, ay = iy >= p.ng && iy < p.ng + p.ny;
+    if (ax && ay) return;
+    const int src = (ax && iy >= p.ng + p.ny && ix < p.ny + 1) ? p.nvar : 0;
+    for (int v = 0; v < p.nvar; ++v) u[uidx(p, v, iy, ix)] = p.cgs[src + v];
+}
+
 // Full ghost fill of the current state (used after an upload; the steps themselves refill the
 // ghosts in k_finalize).
 template <typename R>
 cudaError_t launch_boundaries(const DeviceView& v) {
     KParams<R> p = make_params<R>(v);
+    if (v.cdisk.on) {
+        R* u = (R*)v.u[v.cur];
+        k_cdisk_snapshot<R><<<(v.nvar + 127) / 128, 128, 0, v.stream>>>(p, u);
+        const long long n = (long long)v.nx_max * v.ny_max;
+        k_cdisk_ghosts<R><<<(unsigned)((n + 255) / 256), 256, 0, v.stream>>>(p, u);
+        return cudaGetLastError();
+    }
     const long long n = (v.ndim == 2 ? 2LL * v.ng * v.nx_max : 0) + 2LL * v.ng * (v.ndim == 2 ? v.ny : 1);
     k_boundaries<R><<<(unsigned)((n + 255) / 256), 256, 0, v.stream>>>(p, (R*)v.u[v.cur]);
     return cudaGetLastError();
@@ -147,7 +196,7 @@ static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
     const int nstrips = (p.ny + STRIP_H - 1) / STRIP_H;
     dim3 grid(nbx, (nstrips + STRIP_WARPS - 1) / STRIP_WARPS, 1);
     if constexpr (std::is_same<R, float>::value) {
-        if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0 && v.uniform) {
+        if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0 && v.uniform && !v.cdisk.on) {
             // mixed path, uniform Cartesian grid, Huang & Bai dust: gas and dust strips in one launch
             const int nbx_g = (p.nx + STRIP2_UX - 1) / STRIP2_UX, nbx_d = nbx_g;
             const int nby = (int)grid.y;

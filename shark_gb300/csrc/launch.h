@@ -92,6 +92,18 @@ struct DeviceView {
     // uploaded state on a uniform grid with an isothermal, uniform sound speed (0 otherwise); the
     // kernel carries rho - rho_ref and c^2 (rho - rho_ref) (flux_strip_gas2.cuh)
     double rho_ref;
+    // Cartesian disk per-cell tables (on = false for every other setup): FP64 cs and
+    // sqrt(2 pi H); in state precision r = cs | force x | force y | viscosity (4 planes); the
+    // setup_inloop targets (7 FP64 planes, rho_ana = 0 outside the buffers); the ghost state
+    // gs[2 nvar] (state precision) that zero_gradients copies into the ghost cells
+    struct {
+        bool on = false;
+        const double* csd = nullptr;
+        const double* hsd = nullptr;
+        const double* tgt = nullptr;
+        const void* r = nullptr;
+        void* gs = nullptr;
+    } cdisk;
 };
 
 // Record `msg` as this thread's shark_gpu_last_error text and return `code`.

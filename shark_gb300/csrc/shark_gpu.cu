@@ -109,6 +109,12 @@ struct shark_gpu_ctx {
     std::vector<double> out_x, out_y;   // output positions of the active cells (x / radius, y)
     int32_t* grw_i = nullptr;        // dust growth target bins | net-transfer bins
     float* grw_f = nullptr;          // dust growth net-transfer coefficients (mixed path)
+    // Cartesian disk per-cell tables (plane layout): cs, sqrt(2 pi H) in FP64; cs, force x, force y,
+    // viscosity in state precision; setup_inloop targets (7 FP64 planes); ghost state (2 nvar)
+    double* cdisk_d = nullptr;
+    void* cdisk_r = nullptr;
+    double* cdisk_tgt = nullptr;
+    void* cdisk_gs = nullptr;
     bool chg_cold = true;            // psi_old is zero everywhere (no charging call since reset)
     // charging network
     float* mlp_blob = nullptr;       // SHARK_MLP_NBLOB FP32
@@ -311,6 +317,58 @@ int32_t build_columns(const shark_gpu_config& c, int nx_max, int ny_max, Columns
     return SHARK_OK;
 }
 
+// Cartesian disk (disk/setup.f90) per-cell tables over every cell of the plane layout, with the
+// operations of the setup loop, update_force_setup and setup_inloop: sound speed HoverR
+// sqrt(Mstar/rr), sqrt(2 pi H) (H = HoverR rr), viscosity alpha H cs, the star's softened force on
+// the active cells (ghosts 0), and for the active cells of the buffers (rr < buffer_in box_l or
+// rr > buffer_out box_l) the state setup_inloop resets them to with its rate 0 (rho_ana, m_x, m_y,
+// the energy slot rho_ana cs0^2, and per dust species dust_to rho_ana, dust_to v_ana (-yy, xx)),
+// rho_ana = 0 elsewhere.  rr = sqrt(xx^2 + yy^2 + smooth_r^2) from the cell centres of gridinit.
+struct CdiskTables {
+    std::vector<double> cs, hs, fx, fy, eta, tgt;   // tgt: 7 planes
+};
+void build_cdisk_tables(const shark_gpu_config& c, int nx_max, int ny_max, int pitch, long long plane, CdiskTables& t) {
+    const int ng = c.nghost, nx = c.nx, ny = c.ny;
+    const double M = c.disk_mstar, hr = c.disk_hoverr, sm = c.cdisk_smooth_r;
+    const double R_out = c.cdisk_frac_r_disk * c.box_l;
+    const double bin = c.cdisk_buffer_in * c.box_l, bout = c.cdisk_buffer_out * c.box_l;
+    const double dust_to = c.dust_eps[0], rate = 0.0;
+    const size_t pl = (size_t)plane;
+    t.cs.assign(pl, 0.0); t.hs.assign(pl, 0.0); t.fx.assign(pl, 0.0); t.fy.assign(pl, 0.0); t.eta.assign(pl, 0.0);
+    t.tgt.assign(7 * pl, 0.0);
+    for (int iy = 0; iy < ny_max; ++iy)
+        for (int ix = 0; ix < nx_max; ++ix) {
+            const size_t e = (size_t)iy * pitch + ix;
+            const double px = ((double)(float)(ix - ng) + 0.5) * c.box_l / (double)(float)nx;
+            const double py = ((double)(float)(iy - ng) + 0.5) * c.box_l_y / (double)(float)ny;
+            const double xx = px - 0.5 * c.box_l, yy = py - 0.5 * c.box_l_y;
+            const double r_cyl = std::sqrt(xx * xx + yy * yy);
+            const double rr = std::sqrt(xx * xx + yy * yy + sm * sm);
+            const double H = hr * rr;
+            t.cs[e] = hr * std::sqrt(M / rr);
+            t.hs[e] = std::sqrt(2.0 * kPi * H);
+            t.eta[e] = c.disk_alpha_visc * H * t.cs[e];
+            const bool act = ix >= ng && ix < ng + nx && iy >= ng && iy < ng + ny;
+            if (!act) continue;
+            t.fx[e] = -M * xx / powi(rr, 3);
+            t.fy[e] = -M * yy / powi(rr, 3);
+            if (!(rr < bin || rr > bout)) continue;
+            const double x_soft = xx * rr / r_cyl, y_soft = yy * rr / r_cyl;
+            const double Omega = std::sqrt(M / powi(rr, 3));
+            const double cs0 = H * Omega;
+            double rho_ana = c.disk_sigma0 * (c.disk_r0 / rr);
+            if (rr > R_out) rho_ana = c.disk_sigma0 * (c.disk_r0 / R_out) / 100.0;
+            const double v_ana = -Omega * rho_ana;
+            t.tgt[0 * pl + e] = rho_ana;
+            t.tgt[1 * pl + e] = -y_soft * v_ana;
+            t.tgt[2 * pl + e] = x_soft * v_ana;
+            t.tgt[3 * pl + e] = (rho_ana + (rho_ana - rho_ana) * rate) * (cs0 * cs0);
+            t.tgt[4 * pl + e] = dust_to * rho_ana;
+            t.tgt[5 * pl + e] = -yy * v_ana * dust_to;
+            t.tgt[6 * pl + e] = xx * v_ana * dust_to;
+        }
+}
+
 int32_t validate(const shark_gpu_config* c) {
     if (!c) return fail(SHARK_ERR_INVALID_ARG, "config is NULL");
     if (c->abi_version != SHARK_GPU_ABI_VERSION)
@@ -332,7 +390,7 @@ int32_t validate(const shark_gpu_config* c) {
     if (c->slope_type < 0 || c->slope_type > 3) return fail(SHARK_ERR_INVALID_ARG, "unknown slope limiter");
     if (c->precision != SHARK_PREC_FP64 && c->precision != SHARK_PREC_MIXED)
         return fail(SHARK_ERR_INVALID_ARG, "precision must be FP64 or MIXED");
-    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_SEDOV)
+    if (c->setup < SHARK_SETUP_SOD || c->setup > SHARK_SETUP_DISK_CART)
         return fail(SHARK_ERR_UNSUPPORTED, "setup %d has no device hooks in this build", c->setup);
     const int f = c->flags;
     if (c->setup == SHARK_SETUP_KH || c->setup == SHARK_SETUP_SEDOV) {
@@ -351,8 +409,29 @@ int32_t validate(const shark_gpu_config* c) {
                 if (!(c->dust_size[k] > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "dust_size[%d] must be > 0", k);
         }
     }
-    if ((f & SHARK_FLAG_VISCOSITY) && c->setup != SHARK_SETUP_DISK_POLAR)
-        return fail(SHARK_ERR_UNSUPPORTED, "viscosity: only the polar disk defines eta_visc (disk_polar/setup.f90:67)");
+    if ((f & SHARK_FLAG_VISCOSITY) && c->setup != SHARK_SETUP_DISK_POLAR && c->setup != SHARK_SETUP_DISK_CART)
+        return fail(SHARK_ERR_UNSUPPORTED, "viscosity: only the disks define eta_visc (disk_polar/setup.f90:67, disk/setup.f90)");
+    if (c->setup == SHARK_SETUP_DISK_CART) {
+        // disk/setup.f90: a 2D Cartesian isothermal box; the star's softened gravity, per-cell
+        // sound speed and viscosity come from the config (no caller grid arrays)
+        if (c->geom != 0 || c->ny < 4) return fail(SHARK_ERR_UNSUPPORTED, "the Cartesian disk is a 2D Cartesian box");
+        if (c->iso_cs != 1) return fail(SHARK_ERR_UNSUPPORTED, "the Cartesian disk is isothermal (iso_cs 1)");
+        // zero_gradients takes its sources from cells of the first row: cell ny + 2 must lie in it
+        if (c->ny > c->nx) return fail(SHARK_ERR_UNSUPPORTED, "the Cartesian disk needs ny <= nx");
+        if (c->dx || c->surf || c->vol || c->radii_c || c->position || c->cs)
+            return fail(SHARK_ERR_UNSUPPORTED, "the Cartesian disk builds its own grid and sound speed");
+        if (c->solverdust == 3) return fail(SHARK_ERR_UNSUPPORTED, "the Cartesian disk: HLLC dust is not built for a per-cell sound speed");
+        if (f & (SHARK_FLAG_FARGO | SHARK_FLAG_GROWTH | SHARK_FLAG_CHARGING))
+            return fail(SHARK_ERR_UNSUPPORTED, "the Cartesian disk: FARGO, growth and charging are not built");
+        if (!(c->disk_mstar > 0.0) || !(c->disk_hoverr > 0.0) || !(c->cdisk_smooth_r > 0.0) || !(c->disk_r0 > 0.0) ||
+            !(c->cdisk_frac_r_disk > 0.0))
+            return fail(SHARK_ERR_INVALID_ARG, "disk_mstar, disk_hoverr, disk_r0, cdisk_smooth_r, cdisk_frac_r_disk must be > 0");
+        if ((f & SHARK_FLAG_DRAG) && c->ndust > 0) {
+            if (!(c->rhograin > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "rhograin must be > 0");
+            for (int k = 0; k < c->ndust; ++k)
+                if (!(c->dust_size[k] > 0.0)) return fail(SHARK_ERR_INVALID_ARG, "dust_size[%d] must be > 0", k);
+        }
+    }
     if (f & SHARK_FLAG_GROWTH) {
         if (c->ndust < 1) return fail(SHARK_ERR_INVALID_ARG, "growth needs dust species");
         if (c->ndust > 32) return fail(SHARK_ERR_UNSUPPORTED, "growth is built for at most 32 dust species");
@@ -764,6 +843,7 @@ int32_t release(shark_gpu_ctx* c) {
     if (c->ou_d) cudaFree(c->ou_d);
     if (c->grw_i) cudaFree(c->grw_i);
     if (c->grw_f) cudaFree(c->grw_f);
+    for (void* p : {(void*)c->cdisk_d, c->cdisk_r, (void*)c->cdisk_tgt, c->cdisk_gs}) if (p) cudaFree(p);
     for (void* p : {(void*)c->mlp_blob, (void*)c->mlp_packed, (void*)c->mlp_grad, (void*)c->mlp_adam,
                     (void*)c->mlp_feat, (void*)c->mlp_train, (void*)c->mlp_count, (void*)c->mlp_perm,
                     (void*)c->mlp_scratch, (void*)c->mlp_err})
@@ -1233,6 +1313,36 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
             v.gw.pBf = c->grw_f + P;
             v.gw.gc = c->grw_f + 2 * P;
         }
+    }
+    if (cfg->setup == SHARK_SETUP_DISK_CART) {
+        CdiskTables t;
+        build_cdisk_tables(*cfg, v.nx_max, v.ny_max, v.pitch, v.plane, t);
+        const size_t pl = (size_t)v.plane;
+        std::vector<double> hd(2 * pl);
+        std::memcpy(hd.data(), t.cs.data(), pl * sizeof(double));
+        std::memcpy(hd.data() + pl, t.hs.data(), pl * sizeof(double));
+        INIT_TRY(cudaMalloc(&c->cdisk_d, hd.size() * sizeof(double)));
+        INIT_TRY(cudaMemcpy(c->cdisk_d, hd.data(), hd.size() * sizeof(double), cudaMemcpyHostToDevice));
+        INIT_TRY(cudaMalloc(&c->cdisk_tgt, t.tgt.size() * sizeof(double)));
+        INIT_TRY(cudaMemcpy(c->cdisk_tgt, t.tgt.data(), t.tgt.size() * sizeof(double), cudaMemcpyHostToDevice));
+        std::vector<double> hr(4 * pl);
+        const std::vector<double>* src[4] = {&t.cs, &t.fx, &t.fy, &t.eta};
+        for (int a = 0; a < 4; ++a) std::memcpy(hr.data() + a * pl, src[a]->data(), pl * sizeof(double));
+        INIT_TRY(cudaMalloc(&c->cdisk_r, 4 * pl * c->elem));
+        if (is_mixed(c)) {
+            std::vector<float> hf(hr.begin(), hr.end());
+            INIT_TRY(cudaMemcpy(c->cdisk_r, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice));
+        } else {
+            INIT_TRY(cudaMemcpy(c->cdisk_r, hr.data(), hr.size() * sizeof(double), cudaMemcpyHostToDevice));
+        }
+        INIT_TRY(cudaMalloc(&c->cdisk_gs, 2 * (size_t)v.nvar * c->elem));
+        INIT_TRY(cudaMemsetAsync(c->cdisk_gs, 0, 2 * (size_t)v.nvar * c->elem, c->stream));
+        v.cdisk.csd = c->cdisk_d;
+        v.cdisk.hsd = c->cdisk_d + pl;
+        v.cdisk.tgt = c->cdisk_tgt;
+        v.cdisk.r = c->cdisk_r;
+        v.cdisk.gs = c->cdisk_gs;
+        v.cdisk.on = true;
     }
     INIT_TRY(cudaHostAlloc(&c->host_ring, 4 * sizeof(double), cudaHostAllocDefault));
     std::memset(c->host_ring, 0, 4 * sizeof(double));

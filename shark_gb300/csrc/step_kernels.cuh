@@ -66,6 +66,13 @@ struct KParams {
     float f_gamma, f_gm1, f_inv_g1, f_cfl, f_smallr, f_smallp, f_dust_ratio_min, f_box_l, f_half_box_l;
     float f_si_q, f_si_om, f_si_r0, f_si_eta;
     float f_rho_ref;                  // reference gas density of the mixed flux kernel (0: none)
+    // Cartesian disk per-cell tables (null for the other setups), plane layout: sound speed,
+    // force x, force y and viscosity in the kernel's precision; FP64 sound speed and sqrt(2 pi H);
+    // the setup_inloop targets (7 FP64 planes, rho_ana = 0 outside the buffers); the ghost state
+    // (2 nvar: the value every ghost takes, then the top ghosts' source of the first fill)
+    const R *ccs, *cfx, *cfy, *ceta;
+    const double *ccsd, *chsd, *ctgt;
+    R* cgs;
     const R* u_cur;                   // state at the start of the step (read only)
     R* u_next;                        // state after the step
 };
@@ -187,6 +194,29 @@ namespace shark {
 template <typename R>
 __device__ __forceinline__ void fill_ghost_images(const KParams<R>& p, R* u, int gx, int gy) {
     const int ng = p.ng, nx = p.nx, ny = p.ny;
+    if (p.setup == SHARK_SETUP_DISK_CART) {
+        // zero_gradients as written (boundary_types.f90:48-100) from the second call on: every
+        // ghost takes the state of cell (first_active, 1), which no step changes (k_cdisk_ghosts
+        // does the first call).  The active cells on the edge write the ghosts next to them.
+        const bool l = gx == ng, r = gx == ng + nx - 1, b = gy == ng, t = gy == ng + ny - 1;
+        if (!(l || r || b || t)) return;
+        for (int v = 0; v < p.nvar; ++v) {
+            const R val = p.cgs[v];
+            for (int g = 0; g < ng; ++g) {
+                if (b) u[uidx(p, v, g, gx)] = val;
+                if (t) u[uidx(p, v, ng + ny + g, gx)] = val;
+                if (l) u[uidx(p, v, gy, g)] = val;
+                if (r) u[uidx(p, v, gy, ng + nx + g)] = val;
+                for (int h = 0; h < ng; ++h) {   // corners, by the corner cells
+                    if (l && b) u[uidx(p, v, g, h)] = val;
+                    if (r && b) u[uidx(p, v, g, ng + nx + h)] = val;
+                    if (l && t) u[uidx(p, v, ng + ny + g, h)] = val;
+                    if (r && t) u[uidx(p, v, ng + ny + g, ng + nx + h)] = val;
+                }
+            }
+        }
+        return;
+    }
     if (p.setup == SHARK_SETUP_DISK_POLAR) {
         // disk_polar/boundaries.f90:1-70 by the producer: phi images of the rows next to the
         // periodic seam; the first/last active column also writes its radial ghosts (and their
@@ -311,7 +341,7 @@ __device__ __forceinline__ void block_reduce_dt_f(float dtc, unsigned int st, un
 // sqrt(gamma P / max(rho, smallr)) of the adiabatic state (solve.f90:205-233).
 template <typename R>
 __device__ __forceinline__ double cs_start(const KParams<R>& p, int gx, int gy) {
-    if (p.iso == 1) return p.csd[gx];
+    if (p.iso == 1) return p.ccsd ? p.ccsd[(long long)gy * p.pitch + gx] : p.csd[gx];
     const double rho = (double)p.u_cur[uidx(p, 0, gy, gx)];
     const double vx = (double)p.u_cur[uidx(p, 1, gy, gx)] / rho, vy = (double)p.u_cur[uidx(p, 2, gy, gx)] / rho;
     const double vz = (double)p.u_cur[uidx(p, 3, gy, gx)] / rho;
@@ -336,6 +366,10 @@ __device__ __forceinline__ double tstop_cell(const KParams<R>& p, int k, double 
         return p.dstokes[k] * p.box_l * p.turb_rho0 / p.csd[gx] / qrho_old;
     if (p.setup == SHARK_SETUP_DISK_POLAR)   // Epstein on the midplane density Sigma/(sqrt(2 pi) H)
         return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old / p.hsd[gx] * p.csd[gx]);
+    if (p.setup == SHARK_SETUP_DISK_CART) {  // disk/setup.f90 compute_tstop: Sigma/sqrt(2 pi H)
+        const long long e = (long long)gy * p.pitch + gx;
+        return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old / p.chsd[e] * p.ccsd[e]);
+    }
     // Epstein (SOD/setup.f90:179-185) with the cell's sound speed
     return sqrt(pi * p.gamma / 8.0) * (p.rhograin) * p.dsize[k] / (qrho_old * cs_start(p, gx, gy));
 }
@@ -389,6 +423,28 @@ __device__ __forceinline__ bool disk_inloop_cell(const KParams<R>& p, R* u, int 
         u[uidx(p, ir, gy, gx)] = R(rho_new);
         u[uidx(p, ivx, gy, gx)] = R(rho_new * vx_new);
         u[uidx(p, ivy, gy, gx)] = R(rho_new * vy_new);
+    }
+    return true;
+}
+
+// setup_inloop of the Cartesian disk (disk/setup.f90) for one active cell: a buffer cell takes
+// the state the host tabulated with the routine's operations (its relaxation rate is 0).
+// Returns true when it changed the cell.
+template <typename R>
+__device__ __forceinline__ bool cdisk_inloop_cell(const KParams<R>& p, R* u, int gx, int gy) {
+    const long long e = (long long)gy * p.pitch + gx, pl = p.plane;
+    const double rho_ana = p.ctgt[e];
+    if (!(rho_ana > 0.0)) return false;
+    const int N = p.ndust;
+    u[uidx(p, 0, gy, gx)] = R(rho_ana);
+    u[uidx(p, 1, gy, gx)] = R(p.ctgt[pl + e]);
+    u[uidx(p, 2, gy, gx)] = R(p.ctgt[2 * pl + e]);
+    u[uidx(p, 4, gy, gx)] = R(p.ctgt[3 * pl + e]);
+    const R rd = R(p.ctgt[4 * pl + e]), mx = R(p.ctgt[5 * pl + e]), my = R(p.ctgt[6 * pl + e]);
+    for (int k = 0; k < N; ++k) {
+        u[uidx(p, 5 + k, gy, gx)] = rd;
+        u[uidx(p, 5 + N + k, gy, gx)] = mx;
+        u[uidx(p, 5 + 2 * N + k, gy, gx)] = my;
     }
     return true;
 }
@@ -697,7 +753,8 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
                 u[ixx] = R(d * (vx * (1. - Ohmdt * Ohmdt) - 2. * uz * Ohmdt + AA * Ohmdt) / (1. + Ohmdt * Ohmdt));
             }
         }
-        if (MODE == 0 && p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<R, double>(p, u, gx, gy, dt)) {
+        if (MODE == 0 && ((p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<R, double>(p, u, gx, gy, dt)) ||
+                          (p.setup == SHARK_SETUP_DISK_CART && cdisk_inloop_cell<R>(p, u, gx, gy)))) {
             rho = (double)u[uidx(p, 0, gy, gx)];
             px = (double)u[uidx(p, 1, gy, gx)];
             py = (double)u[uidx(p, 2, gy, gx)];
@@ -708,7 +765,7 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
         const double qrho = rho > p.smallr ? rho : p.smallr;
         const double vx = px / rho, vy = py / rho, vz = pz / rho;
         double cs;
-        if (p.iso == 1) cs = p.csd[gx];
+        if (p.iso == 1) cs = p.ccsd ? p.ccsd[(long long)gy * p.pitch + gx] : p.csd[gx];
         else {
             const double E = (double)u[uidx(p, 4, gy, gx)];
             const double ekin = 0.5 * rho * (vx * vx) + 0.5 * rho * (vy * vy) + 0.5 * rho * (vz * vz);
@@ -734,6 +791,10 @@ __global__ void __launch_bounds__(256) k_finalize(KParams<R> p) {
             // the same point-mass force acts on gas and every dust species
             const double g = p.fgravd[gx];
             fmax_d = sqrt(g * g + 0.0 * 0.0 + 0.0 * 0.0);
+        } else if (fk && p.setup == SHARK_SETUP_DISK_CART) {   // the star's softened force, gas and dust
+            const long long e = (long long)gy * p.pitch + gx;
+            const double fx = (double)p.cfx[e], fy = (double)p.cfy[e];
+            fmax_d = sqrt(fx * fx + fy * fy + 0.0 * 0.0);
         }
         for (int k = 0; k < N; ++k) {
             const double rd = (double)u[uidx(p, 5 + k, gy, gx)];
@@ -782,11 +843,15 @@ __device__ __forceinline__ void drag_coeffs(double a, float& r, float& w) {
 }
 
 // a_k = dt/t_k of the mixed path where the per-cell stopping time factors as t_k = C_k / F_cell
-// (dustyTurb C_k = St_0,k L rho_0, F = c_s rho; polar disk Epstein F = rho/hs c_s): dt F_cell times
+// (dustyTurb C_k = St_0,k L rho_0, F = c_s rho; the disks' Epstein F = rho/hs c_s): dt F_cell times
 // the tabulated 1/C_k, and the coefficients with a refined reciprocal (FP64 throughout; the
 // divisions cost most of K2's FP64 work at 32 species).  Other setups divide directly.
-__device__ __forceinline__ double drag_cell_factor(const KParams<float>& p, double dt, double qrho_old, int gx) {
+__device__ __forceinline__ double drag_cell_factor(const KParams<float>& p, double dt, double qrho_old, int gx, int gy) {
     if (p.setup == SHARK_SETUP_DUSTYTURB) return dt * (p.csd[gx] * qrho_old);
+    if (p.setup == SHARK_SETUP_DISK_CART) {
+        const long long e = (long long)gy * p.pitch + gx;
+        return dt * (qrho_old / p.chsd[e] * p.ccsd[e]);
+    }
     return dt * (qrho_old / p.hsd[gx] * p.csd[gx]);
 }
 
@@ -852,6 +917,7 @@ k_finalize_mixed(KParams<float> p) {
     // no setup hook changes the dust between the drag and the CFL
     const bool fk_si = (p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_SI;
     const bool cfl_in_drag = NS > 0 && NS <= 8 && drag && p.ou_nm == 0 && p.setup != SHARK_SETUP_DISK_POLAR &&
+                             p.setup != SHARK_SETUP_DISK_CART &&
                              !(p.setup == SHARK_SETUP_SI && !(p.flags & SHARK_FLAG_FORCE_KICK));
     bool cfl_done = false;
     float vmax_d = 0.f, vv_last = 0.f, fmx2_d = 0.f;
@@ -881,8 +947,9 @@ k_finalize_mixed(KParams<float> p) {
                 } else {
                     const float rho_old = ucur[cc + (0) * pl];
                     const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
-                    const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
-                    const float Fcf = direct ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx);
+                    const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR &&
+                                          p.setup != SHARK_SETUP_DISK_CART;
+                    const float Fcf = direct ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx, gy);
 #pragma unroll
                     for (int k = 0; k < NS; ++k) {
                         if (direct) drag_coeffs_mix(1.0 * dt / tstop_cell(p, k, qrho_old, gx, gy), rk[k], wk[k]);
@@ -940,8 +1007,9 @@ k_finalize_mixed(KParams<float> p) {
             float rhon = rho, pnx = px, pny = py, pnz = pz;
             const float rho_old = ucur[cc + (0) * pl];
             const double qrho_old = (double)fmaxf(rho_old, p.f_smallr);
-            const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR;
-            const float Fcf = (const_ts || direct) ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx);
+            const bool direct = p.setup != SHARK_SETUP_DUSTYTURB && p.setup != SHARK_SETUP_DISK_POLAR &&
+                                          p.setup != SHARK_SETUP_DISK_CART;
+            const float Fcf = (const_ts || direct) ? 0.f : (float)drag_cell_factor(p, dt, qrho_old, gx, gy);
             // run-time species count: the cell's coefficients are kept (thread-local memory) for
             // the update loop instead of being formed a second time
             float2 rw_local[NS < 0 ? SHARK_MAX_DUST : 1];
@@ -1018,7 +1086,8 @@ k_finalize_mixed(KParams<float> p) {
                 u[ixx] = d * (vx * (1.f - O2) - 2.f * uz * Ohmdt + AA * Ohmdt) * inv;
             }
         }
-        if (MODE == 0 && p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<float, float>(p, u, gx, gy, dt)) {
+        if (MODE == 0 && ((p.setup == SHARK_SETUP_DISK_POLAR && disk_inloop_cell<float, float>(p, u, gx, gy, dt)) ||
+                          (p.setup == SHARK_SETUP_DISK_CART && cdisk_inloop_cell<float>(p, u, gx, gy)))) {
             in_regs = false;
             rho = u[cc + (0) * pl];
             px = u[cc + (1) * pl];
@@ -1030,7 +1099,7 @@ k_finalize_mixed(KParams<float> p) {
         const float irho = 1.0f / rho;
         const float vx = px * irho, vy = py * irho, vz = pz * irho;
         float cs;
-        if (p.iso == 1) cs = p.cs[gx];
+        if (p.iso == 1) cs = p.ccs ? p.ccs[cc] : p.cs[gx];
         else {
             const float E = u[cc + (4) * pl];
             const float ekin = 0.5f * rho * (vx * vx) + 0.5f * rho * (vy * vy) + 0.5f * rho * (vz * vz);
@@ -1045,13 +1114,16 @@ k_finalize_mixed(KParams<float> p) {
         float vv = fabsf(vx) + fabsf(vy) + fabsf(vz);
         float vmax = cs + vv;
         float fmx = 0.f;
-        const bool fk = fk_si || ((p.flags & SHARK_FLAG_FORCE_KICK) != 0 && p.setup == SHARK_SETUP_DISK_POLAR);
+        const bool fk = fk_si || ((p.flags & SHARK_FLAG_FORCE_KICK) != 0 &&
+                                  (p.setup == SHARK_SETUP_DISK_POLAR || p.setup == SHARK_SETUP_DISK_CART));
         const float om = p.f_si_om, qsh = p.f_si_q;
         float fmx2 = 0.f;                 // SI: the largest |f|^2, one square root after the loop
         if (fk_si) {
             const float f1 = 2.0f * qsh * (om * om) * xc - 2.0f * om * vz - 2.0f * p.f_si_r0 * om * p.f_si_eta;
             const float f3 = 2.0f * om * vx;
             fmx2 = f1 * f1 + f3 * f3;
+        } else if (fk && p.setup == SHARK_SETUP_DISK_CART) {   // the star's softened force, gas and dust
+            fmx = sqrtf(p.cfx[cc] * p.cfx[cc] + p.cfy[cc] * p.cfy[cc]);
         } else if (fk) {
             fmx = fabsf(p.fgrav[gx]);   // polar disk: the point-mass force, the same on gas and dust
         }

@@ -6,12 +6,13 @@ module shark_gpu
   use iso_c_binding
   implicit none
 
-  integer(c_int32_t), parameter :: SHARK_GPU_ABI_VERSION = 1
+  integer(c_int32_t), parameter :: SHARK_GPU_ABI_VERSION = 2
   integer, parameter :: SHARK_MAX_DUST = 64
   integer(c_int32_t), parameter :: SHARK_OK = 0
   integer(c_int32_t), parameter :: SHARK_SETUP_SOD = 1, SHARK_SETUP_DUSTYWAVE = 2, SHARK_SETUP_SI = 3
   integer(c_int32_t), parameter :: SHARK_SETUP_DISK_POLAR = 4, SHARK_SETUP_DUSTYTURB = 5
   integer(c_int32_t), parameter :: SHARK_SETUP_KH = 6, SHARK_SETUP_SEDOV = 7
+  integer(c_int32_t), parameter :: SHARK_SETUP_DISK_CART = 8
   integer(c_int32_t), parameter :: SHARK_FLAG_DRAG = 1, SHARK_FLAG_BACK_REACTION = 2
   integer(c_int32_t), parameter :: SHARK_FLAG_FORCE_KICK = 4, SHARK_FLAG_FARGO = 8
   integer(c_int32_t), parameter :: SHARK_FLAG_GROWTH = 16, SHARK_FLAG_CHARGING = 32
@@ -48,7 +49,7 @@ module shark_gpu
     real(c_double) :: disk_alpha_visc
     real(c_double) :: kh_rho_dense, kh_rho_diffuse, kh_T_dense, kh_mach, kh_vy0, kh_kx
     real(c_double) :: sedov_rho_ext, sedov_P_ext, sedov_P_cen, sedov_r_expl
-    real(c_double) :: reserved(1)
+    real(c_double) :: cdisk_smooth_r, cdisk_frac_r_disk, cdisk_buffer_in, cdisk_buffer_out
     type(c_ptr) :: dx, surf, vol, radii_c, position, cs
   end type shark_gpu_config
 

@@ -15,7 +15,7 @@ import numpy as np
 import math
 
 from .config import (SharkConfig, default_config, SETUP_SOD, SETUP_DUSTYWAVE, SETUP_SI, SETUP_DISK_POLAR,
-                     SETUP_DUSTYTURB, SETUP_KH, SETUP_SEDOV, FLAG_DRAG, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO,
+                     SETUP_DUSTYTURB, SETUP_KH, SETUP_SEDOV, SETUP_DISK_CART, FLAG_DRAG, FLAG_VISCOSITY, FLAG_BACK_REACTION, FLAG_FORCE_KICK, FLAG_FARGO,
                      FLAG_CHARGING, FLAG_GROWTH, GROWTH_TURB, GROWTH_BROWNIAN, GROWTH_DRIFT, PREC_FP64)
 
 GROWTH_DEFAULT = GROWTH_TURB | GROWTH_BROWNIAN | GROWTH_DRIFT
@@ -450,6 +450,97 @@ def disk_ic(cfg, noise_amp, seed):
 
 
 # ---------------------------------------------------------------------------------------------
+# Cartesian disk
+# ---------------------------------------------------------------------------------------------
+ICE_MANTLE_CM = 8.7e-7   # src/dust/dust_commons.f90:47
+# test/CARTESIAN_disk/disk.nml (SETUP_PARAMS and GRID_PARAMS)
+CARTESIAN_DISK_NML = dict(box_l=320.0, buffer_in=0.0, buffer_out=0.375, alpha_visc=1e-2, frac_r_disk=0.125,
+                          smooth_r=0.1, sigma_r0=300.0, cfl=0.8, gamma=1.666667, slope_type=3)
+
+
+def disk_cart(n=256, ndust=4, box_l=320.0, sigma_r0=300.0, r0_disk=1.0, mstar=1.0, hoverr=0.05, smooth_r=0.1,
+              alpha_visc=1e-2, frac_r_disk=0.125, buffer_in=0.0, buffer_out=0.375, dust2gas=0.01,
+              smin_cm=1e-7, smax_cm=1e-2, rhograin_cgs=2.7, cfl=0.8, gamma=1.666667, slope_type=3,
+              viscosity=True, force_kick=True, precision=PREC_FP64):
+    """The Cartesian disk (src/setups/disk/setup.f90, units.f90) on an n x n box of box_l AU: a
+    star of mstar Msun at the centre with softening smooth_r, Sigma = sigma_r0 (g cm^-2)
+    r0_disk/rr (1/100 of the value at R_out = frac_r_disk box_l beyond it), isothermal
+    cs = hoverr sqrt(Mstar/rr), Keplerian rotation Omega = sqrt(Mstar/rr^3) on the softened
+    offsets, viscosity alpha_visc H cs, every dust species at dust2gas with the gas velocity,
+    grains in MRN bins between smin_cm and smax_cm (the dust_commons defaults) plus the ice mantle.
+    The defaults are those of test/CARTESIAN_disk/disk.nml.  Every cell, ghosts included, gets
+    the profile at its own position, as the setup loop does; the boundaries are applied by the
+    step."""
+    unit_l = AU
+    unit_d = MSUN / AU ** 3
+    unit_t = 1.0 / math.sqrt(GRAV * unit_d)
+    unit_dcol = MSUN / AU ** 2
+    cfg = default_config()
+    cfg.nx, cfg.ny, cfg.ndust = n, n, ndust
+    cfg.geom = 0
+    cfg.gamma, cfg.cfl, cfg.slope_type = gamma, cfl, slope_type
+    cfg.iso_cs = 1
+    cfg.precision = precision
+    cfg.setup = SETUP_DISK_CART
+    cfg.flags = (FLAG_DRAG | FLAG_BACK_REACTION | (FLAG_FORCE_KICK if force_kick else 0)
+                 | (FLAG_VISCOSITY if viscosity else 0))
+    cfg.box_l = cfg.box_l_y = box_l * AU / unit_l
+    cfg.disk_mstar = mstar * MSUN / MSUN
+    cfg.disk_hoverr = hoverr
+    cfg.disk_sigma0 = sigma_r0 / unit_dcol
+    cfg.disk_r0 = r0_disk * AU / unit_l
+    cfg.disk_alpha_visc = alpha_visc
+    cfg.cdisk_smooth_r = smooth_r * AU / unit_l
+    cfg.cdisk_frac_r_disk, cfg.cdisk_buffer_in, cfg.cdisk_buffer_out = frac_r_disk, buffer_in, buffer_out
+    cfg.unit_l, cfg.unit_d, cfg.unit_t = unit_l, unit_d, unit_t
+    cfg.rhograin = rhograin_cgs / unit_d
+    if ndust > 0:
+        sdust, _ = mrn_bins(ndust, smin_cm, smax_cm, smin_cm, smax_cm, dust2gas, rhograin=rhograin_cgs,
+                            unit_l=unit_l, unit_m=MSUN)
+        for k in range(ndust):
+            cfg.dust_size[k] = sdust[k] + ICE_MANTLE_CM / unit_l
+            cfg.dust_eps[k] = dust2gas
+    cfg.cs0 = hoverr * math.sqrt(cfg.disk_mstar / cfg.disk_r0)
+    return cfg, disk_cart_ic(cfg)
+
+
+def disk_cart_geometry(cfg):
+    """Per cell (all cells): offsets xx, yy from the box centre, r_cyl, the softened radius rr and
+    the softened offsets x_soft, y_soft of disk/setup.f90."""
+    pos = positions(cfg)
+    xx = pos[:, 0] - 0.5 * cfg.box_l
+    yy = pos[:, 1] - 0.5 * cfg.box_l_y
+    r_cyl = np.sqrt(xx * xx + yy * yy)
+    rr = np.sqrt(xx * xx + yy * yy + cfg.cdisk_smooth_r * cfg.cdisk_smooth_r)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        x_soft = xx * rr / r_cyl
+        y_soft = yy * rr / r_cyl
+    return xx, yy, r_cyl, rr, x_soft, y_soft
+
+
+def disk_cart_ic(cfg):
+    """Initial conserved state of the Cartesian disk (disk/setup.f90 setup loop, then primtoc)."""
+    N = cfg.ndust
+    xx, yy, r_cyl, rr, x_soft, y_soft = disk_cart_geometry(cfg)
+    M = cfg.disk_mstar
+    cs0 = cfg.disk_hoverr * np.sqrt(M / rr)
+    omega = np.sqrt(M / (rr * (rr * rr)))
+    r_out = cfg.cdisk_frac_r_disk * cfg.box_l
+    rho = cfg.disk_sigma0 * (cfg.disk_r0 / rr)
+    rho = np.where(rr > r_out, cfg.disk_sigma0 * (cfg.disk_r0 / r_out) / 100.0, rho)
+    q = np.zeros((cfg.nvar, cfg.ncells))
+    q[0] = rho
+    q[1] = -omega * y_soft
+    q[2] = omega * x_soft
+    q[4] = rho * (cs0 * cs0)
+    for k in range(N):
+        q[5 + k] = cfg.dust_eps[k] * rho
+        q[5 + N + k] = -omega * y_soft
+        q[5 + 2 * N + k] = omega * x_soft
+    return primtoc(cfg, q).reshape(-1)
+
+
+# ---------------------------------------------------------------------------------------------
 # Dusty turbulence
 # ---------------------------------------------------------------------------------------------
 def dusty_turb(n=256, ndust=32, smin=1e-6, smax=0.1, dust2gas=0.01, nH=1e9, T=10.0, box_pc=0.1,
@@ -672,6 +763,7 @@ def sedov_ic(cfg):
 
 
 def build(name, **kw):
-    """Dispatch by setup name ('sod', 'dustywave', 'si', 'disk_polar', 'dusty_turb', 'kh', 'sedov')."""
-    return {"sod": sod, "dustywave": dustywave, "si": si, "disk_polar": disk_polar,
+    """Dispatch by setup name ('sod', 'dustywave', 'si', 'disk_polar', 'disk_cart', 'dusty_turb',
+    'kh', 'sedov')."""
+    return {"sod": sod, "dustywave": dustywave, "si": si, "disk_polar": disk_polar, "disk_cart": disk_cart,
             "dusty_turb": dusty_turb, "kh": kh, "sedov": sedov}[name](**kw)

@@ -1,0 +1,79 @@
+"""The Cartesian disk (src/setups/disk) through the C ABI against the oracle: per-cell isothermal
+sound speed in the flux strips, the star's softened force in the kicks and in courant, the
+Cartesian viscosity, Epstein stopping times on Sigma/sqrt(2 pi H), the setup_inloop buffers and
+zero_gradients as written (the ghosts, compared cell for cell).
+
+FP64 within 1e-10 relative L1 per conserved field (and the ghosts equal); mixed precision on the
+same boxes within MIXED_DISK_TOL: the softened point mass makes the inner disk a strong flow
+(the central cells' velocities sqrt(Mstar/smooth_r) are 30x the outer sound speed), where FP32
+rounding in the limiter branches grows fastest."""
+import numpy as np
+import pytest
+
+from shark_gb300 import config as K, setups
+from shark_gb300.solver import Shark
+from tests.test_gpu_parity import FP64_TOL, rel_l1, run_pair
+
+pytestmark = pytest.mark.gpu
+
+MIXED_DISK_TOL = 1e-4
+
+
+def _disk(nx, ny, ndust, precision=K.PREC_FP64, **kw):
+    cfg, _ = setups.disk_cart(n=nx, ndust=ndust, precision=precision, **kw)
+    cfg.ny = ny
+    return cfg, setups.disk_cart_ic(cfg)
+
+
+@pytest.mark.parametrize("nx,ny,ndust,visc", [(64, 64, 4, True), (96, 64, 2, True), (64, 64, 8, False),
+                                              (70, 46, 0, True)])
+def test_cartesian_disk_fp64(nx, ny, ndust, visc):
+    cfg, u0 = _disk(nx, ny, ndust, viscosity=visc)
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 12)
+    assert st == 0
+    np.testing.assert_allclose(dtg, dto, rtol=1e-13, atol=0)
+    assert rel_l1(cfg, ug, uo).max() <= FP64_TOL
+    np.testing.assert_allclose(ug, uo, rtol=1e-12, atol=0)   # ghosts included
+
+
+def test_cartesian_disk_without_force_kick_fp64():
+    cfg, u0 = _disk(64, 64, 4, force_kick=False)
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 8)
+    assert st == 0
+    np.testing.assert_allclose(dtg, dto, rtol=1e-13, atol=0)
+    assert rel_l1(cfg, ug, uo).max() <= FP64_TOL
+
+
+@pytest.mark.parametrize("nx,ny,ndust", [(64, 64, 4), (96, 64, 8)])
+def test_cartesian_disk_mixed(nx, ny, ndust):
+    cfg, u0 = _disk(nx, ny, ndust, precision=K.PREC_MIXED)
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 8)
+    assert st == 0
+    np.testing.assert_allclose(dtg, dto, rtol=1e-4, atol=0)
+    err = rel_l1(cfg, ug, uo)
+    assert err.max() <= MIXED_DISK_TOL, err
+
+
+def test_cartesian_disk_ghosts_after_upload_and_steps():
+    """The device's first zero_gradients (after the upload) and the later ones equal the oracle's
+    cell for cell, in both precisions."""
+    for prec, tol in ((K.PREC_FP64, 0.0), (K.PREC_MIXED, 1e-6)):
+        cfg, u0 = _disk(40, 24, 2, precision=prec)
+        ng = cfg.nghost
+        ghost = np.ones((cfg.ny_max, cfg.nx_max), bool)
+        ghost[ng:ng + cfg.ny, ng:ng + cfg.nx] = False
+        with Shark(cfg) as g:
+            g.upload(u0)
+            first = g.download().reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)[:, ghost]
+            g.solve()
+            g.solve()
+            later = g.download().reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)[:, ghost]
+            assert g.sync() == 0
+        g0 = u0.reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)
+        s3, sT = g0[:, 0, 2], g0[:, 0, cfg.ny + 1]
+        iy, ix = np.nonzero(ghost)
+        top = (iy >= ng + cfg.ny) & (ix >= ng) & (ix < ng + cfg.nx) & (ix < cfg.ny + 1)
+        expect = np.repeat(s3[:, None], ghost.sum(), axis=1)
+        expect[:, top] = sT[:, None]
+        np.testing.assert_allclose(first, expect, rtol=tol, atol=0)
+        np.testing.assert_allclose(later, np.repeat(s3[:, None], ghost.sum(), axis=1), rtol=tol, atol=0)

@@ -128,7 +128,7 @@ def test_kh_and_sedov_configs_are_checked_before_touching_a_device(lib):
     bad = kh.copy(); bad.flags |= K.FLAG_GROWTH; cases.append((bad, K.ERR_UNSUPPORTED, b"growth"))
     bad = sd.copy(); bad.ndust = 2; cases.append((bad, K.ERR_UNSUPPORTED, b"gas-only"))
     bad = sd.copy(); bad.geom = 2; cases.append((bad, K.ERR_UNSUPPORTED, b"Cartesian"))
-    bad = sd.copy(); bad.setup = 8; cases.append((bad, K.ERR_UNSUPPORTED, b"setup 8"))
+    bad = sd.copy(); bad.setup = 9; cases.append((bad, K.ERR_UNSUPPORTED, b"setup 9"))
     for cfg, code, msg in cases:
         assert lib.shark_gpu_init(C.byref(cfg), C.byref(h)) == code, msg
         assert msg in lib.shark_gpu_last_error(), (msg, lib.shark_gpu_last_error())
