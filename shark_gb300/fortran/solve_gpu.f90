@@ -1,7 +1,8 @@
 ! solve_gpu.f90 -- drop-in replacement of src/solver/solve.f90 that runs each step on the GPU.
 !
 ! Build: put this file (and shark_gpu_mod.f90) before src/solver on VPATH instead of solve.f90,
-! add -DSHARK_GPU_SETUP=<1 SOD | 2 DUSTYWAVE | 3 SI | 4 disk_polar | 5 dustyTurb | 6 KH | 7 sedov>
+! add -DSHARK_GPU_SETUP=<1 SOD | 2 DUSTYWAVE | 3 SI | 4 disk_polar | 5 dustyTurb | 6 KH | 7 sedov |
+! 8 disk (Cartesian)>
 ! and -DSHARK_GPU_PREC=<0 FP64 | 1 mixed>
 ! to DEFINES and link with -L<repo>/shark_gb300 -lshark_gpu.  The time loop (src/shark.f90),
 ! setups, namelists and output stay as they are.
@@ -135,6 +136,24 @@ subroutine solve(verbose,outputing)
     cfg%kh_mach = Mach; cfg%kh_vy0 = vy0; cfg%kh_kx = kx
 #if NDUST>0
     cfg%rhograin = rhograin/unit_d
+#endif
+#endif
+#if SHARK_GPU_SETUP==8
+    ! disk/setup_commons.f90, units.f90; setup.f90 has already put sigma_R0, R0_disk, smooth_r,
+    ! Mstar and box_l in code units.  The library builds the Cartesian grid and the per-cell sound
+    ! speed HoverR sqrt(Mstar/rr) itself from these (the same numbers as the setup's arrays).
+    ! Every dust species starts at dust2gas, the inloop buffers' dust-to-gas ratio.
+    cfg%dx = c_null_ptr; cfg%surf = c_null_ptr; cfg%vol = c_null_ptr
+    cfg%radii_c = c_null_ptr; cfg%position = c_null_ptr; cfg%cs = c_null_ptr
+    cfg%box_l = box_l; cfg%box_l_y = box_l_y
+    cfg%disk_mstar = Mstar; cfg%disk_hoverr = HoverR; cfg%disk_sigma0 = sigma_R0; cfg%disk_r0 = R0_disk
+    cfg%disk_alpha_visc = alpha_visc
+    cfg%cdisk_smooth_r = smooth_r; cfg%cdisk_frac_r_disk = frac_R_disk
+    cfg%cdisk_buffer_in = buffer_in; cfg%cdisk_buffer_out = buffer_out
+    cfg%unit_l = unit_l; cfg%unit_d = unit_d; cfg%unit_t = unit_t; cfg%mu_gas = mu_gas
+#if NDUST>0
+    cfg%rhograin = rhograin/unit_d   ! compute_tstop uses rhograin/unit_d
+    cfg%dust_eps(1:NDUST) = dust2gas
 #endif
 #endif
 #if SHARK_GPU_SETUP==7

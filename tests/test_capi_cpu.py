@@ -167,11 +167,12 @@ def test_fortran_shim_writes_only_existing_fields_and_maps_every_setup():
     written = {m.lower() for m in re.findall(r"\bcfg%(\w+)", src)}
     assert written <= set(layout), written - set(layout)
     # the per-setup parameters of every setup id the library accepts
-    for sid in range(1, 8):
+    for sid in range(1, 9):
         assert f"#if SHARK_GPU_SETUP=={sid}" in src, sid
     for f in ("disk_mstar", "disk_hoverr", "disk_sigma0", "disk_r_relax", "disk_n_rel", "disk_temp_slope",
               "turb_rho0", "t_cloud", "dust_stokes", "turb_mach", "turb_tcorr", "turb_kmin", "turb_kmax",
-              "chg_x", "chg_eps", "chg_nitermax", "chg_mode", "grw_smin", "grw_smax", "grw_cfl", "grw_mode"):
+              "chg_x", "chg_eps", "chg_nitermax", "chg_mode", "grw_smin", "grw_smax", "grw_cfl", "grw_mode",
+              "cdisk_smooth_r", "cdisk_frac_r_disk", "cdisk_buffer_in", "cdisk_buffer_out", "dust_eps"):
         assert f in written, f
     # before an output step the charging outputs come back with the state
     assert "shark_gpu_download_charge" in src

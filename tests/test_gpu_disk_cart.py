@@ -5,8 +5,8 @@ zero_gradients as written (the ghosts, compared cell for cell).
 
 FP64 within 1e-10 relative L1 per conserved field (and the ghosts equal); mixed precision on the
 same boxes within MIXED_DISK_TOL: the softened point mass makes the inner disk a strong flow
-(the central cells' velocities sqrt(Mstar/smooth_r) are 30x the outer sound speed), where FP32
-rounding in the limiter branches grows fastest."""
+(orbital velocities sqrt(Mstar/rr) near the centre about a hundred times the sound speed at the
+box edge), where FP32 rounding in the limiter branches grows fastest."""
 import numpy as np
 import pytest
 
