@@ -26,8 +26,11 @@ Config 2 in mixed precision: the wave's perturbation is 1e-4 of an O(1) backgrou
 state resolves rho ~ 1 only to 6e-8, i.e. 6e-4 of the perturbation.  After the 5,121 steps the
 densities and the energy (whose L1 scale is the background) stay within 5e-5 (measured: gas
 9e-8, energy 2.9e-6, dust up to 2.8e-5 for the least coupled species); the momenta, whose L1
-scale is the perturbation itself, within 5e-3 (measured 2.2e-3 for the gas); every mode of the
-run is within 1e-2 of the linear solution."""
+scale is the perturbation itself, within 5e-3 (measured 2.2e-3 for the gas).  Against the linear
+solution the gas modes and every velocity mode are within 1e-2 (measured 3.8e-3), the dust
+density modes within 6e-2 (measured up to 4.4e-2): their amplitude is 2.5e-5 on a background of
+0.25, and the FP32 state's rounding noise after 5,121 steps, ~sqrt(5121) ulp(0.25)/2 = 1e-6, is a
+few per cent of it."""
 import numpy as np
 import pytest
 
@@ -148,6 +151,9 @@ def test_driven_box_16_species_growth_fp64():
 # ---- config 2: the 4-species dusty wave to t = 2 ---------------------------------------------
 DW_TEND = 2.0
 DW_LINEAR_TOL = 1e-2         # the oracle's own distance to the linear solution: 6.4e-3 at 2048 cells
+# mixed: the dust density modes carry the FP32 state's rounding noise, ~sqrt(5121) x ulp(0.25)/2
+# = 1e-6 after the run, i.e. a few per cent of their 2.5e-5 amplitude (measured up to 4.4e-2)
+DW_MIXED_DUST_DENSITY_LINEAR_TOL = 6e-2
 DW_MIXED_MOMENTUM_TOL = 5e-3  # FP32 resolves the 1e-4 perturbation of rho ~ 1 to 6e-4 of itself
 DW_MIXED_DENSITY_TOL = 5e-5   # 5,121 FP32 steps on the perturbed densities
 
@@ -186,7 +192,14 @@ def test_dusty_wave_4_species_to_t2(precision):
     # mode damping and phase of every species against the linear solution at the time reached
     ua = active(cfg, ug)[:, 0, :]
     err = DW.mode_errors(cfg, ua, x, t_g)
-    assert err.max() <= DW_LINEAR_TOL, err
+    if precision == K.PREC_FP64:
+        assert err.max() <= DW_LINEAR_TOL, err
+    else:   # modes: gas density, gas velocity, N dust densities, N dust velocities
+        N = cfg.ndust
+        rd = list(range(2, 2 + N))
+        rest = [i for i in range(err.size) if i not in rd]
+        assert err[rest].max() <= DW_LINEAR_TOL, err
+        assert err[rd].max() <= DW_MIXED_DUST_DENSITY_LINEAR_TOL, err
     ref = DW.mode_errors(cfg, active(cfg, uo)[:, 0, :], x, t_o)
     if precision == K.PREC_FP64:   # the FP64 run is as close to the linear solution as the oracle's
         assert err.max() <= ref.max() * (1.0 + 1e-6), (err.max(), ref.max())

@@ -3,8 +3,12 @@ wavelength (tau_s = 0.1, eps = 3, K = 30, c_s = 2 eta v_K) seeded with the faste
 
 * FP64, 64 cells per wavelength: the mode's amplitude equals the oracle's on the same input, and
   its growth rate from t = 1 to 5 / Omega is within 2 % of the theory (measured -1.4 %).
-* Mixed precision, 64 cells: within 2 % of the theory and within 5e-3 of the FP64 rate.
-* FP64, 128 cells: within 1 % (the error falls with resolution)."""
+* Mixed precision, 64 cells: within 2 % of the theory and within 5e-3 of the FP64 rate (measured
+  -1.12 % and 1e-4), seeded at |drho_d| = 1e-3 rho_d: the mode's gas density perturbation is 1e-3
+  of the dust's, so at the FP64 tests' 1e-4 it is 3e-7 of rho_g ~ 1, two FP32 units in the last
+  place, and the FP32 state does not carry it (the mixed growth then falls 22 % short at 128
+  cells); at 1e-3 the mode is still linear over the run (growth x5).
+* FP64, 128 cells: within 1 % (the error falls with resolution: -1.4 %, -0.4 %)."""
 import math
 
 import numpy as np
@@ -48,8 +52,8 @@ def test_fp64_growth_matches_theory_and_oracle():
 
 
 def test_mixed_growth_matches_theory_and_fp64():
-    m = _growth(64, K.PREC_MIXED)
-    d = _growth(64, K.PREC_FP64)
+    m = _growth(64, K.PREC_MIXED, amp=1e-3)
+    d = _growth(64, K.PREC_FP64, amp=1e-3)
     assert abs(m["gpu_rate"] / m["theory"] - 1.0) <= 0.02, (m["gpu_rate"], m["theory"])
     assert abs(m["gpu_rate"] / d["gpu_rate"] - 1.0) <= 5e-3, (m["gpu_rate"], d["gpu_rate"])
 
