@@ -82,7 +82,7 @@ def describe(args, cfg):
     if args.workload == "turb":
         return (f"driven dusty turbulence {cfg.nx}x{cfg.ny}, {cfg.ndust} dust species 0.01 um-1 mm, OU forcing, "
                 f"charging and growth every step, mixed precision")
-    return f"SI shearing box {cfg.nx}x{cfg.ny} active cells, {cfg.ndust} dust species, mixed precision"
+    return f"SI shearing box {cfg.nx}x{cfg.ny} active cells, {cfg.ndust} dust species"
 
 
 def launches_per_step(cfg):
@@ -248,7 +248,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic",
-        "config": {"workload": f"SI shearing box {args.n}x{args.n}, {args.ndust} dust species",
+        "config": {"workload": f"SI shearing box {args.n}x{args.n} active cells, {args.ndust} dust species",
+                   "zone_species_per_step": args.n * args.n * (args.ndust + 1),
                    "sample_grid": f"{n}x{n}", "parallelism": "OpenMP host threads"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": samp},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
