@@ -55,8 +55,8 @@ __device__ __forceinline__ float2 limit2(float2 l, float2 r) {
         const float2 s = add2(l, r);
         const float2 a = mul2(make_float2(fmaxf(min_xorsign_abs(l.x, r.x), 0.f), fmaxf(min_xorsign_abs(l.y, r.y), 0.f)),
                               bc2(3.f));
-        // sign(s) min(|s|, a) for a >= 0: s clamped to [-a, a]
-        return make_float2(fmaxf(fminf(s.x, a.x), -a.x), fmaxf(fminf(s.y, a.y), -a.y));
+        // sign(s) min(|s|, a) for a >= +0 is min.xorsign.abs(a, s): one instruction per column
+        return make_float2(min_xorsign_abs(a.x, s.x), min_xorsign_abs(a.y, s.y));
     }
 }
 
