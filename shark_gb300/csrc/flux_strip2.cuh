@@ -28,23 +28,16 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 // a - b
 __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
 
-// min(|a|, |b|) carrying the sign sign(a) xor sign(b): >= 0 exactly when a and b have the same
-// sign (or one is zero).
-__device__ __forceinline__ float min_xorsign_abs(float a, float b) {
-    float d;
-    asm("min.xorsign.abs.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
-    return d;
-}
-
 // Doubled limited slope 2 dq of the FP32 limiters (physics.cuh) for two columns.  minmod and MC
-// start from m = max(min.xorsign.abs(l, r), 0), which is min(|l|, |r|) when l and r have the same
-// sign and 0 otherwise (the l r <= 0 case of the reference limiters).
+// start from m = max(min.xorsign.abs(l, r), 0) (min_xorsign_abs_f, physics.cuh), which is
+// min(|l|, |r|) when l and r have the same sign and 0 otherwise (the l r <= 0 case of the
+// reference limiters).
 template <int ST>
 __device__ __forceinline__ float2 limit2(float2 l, float2 r) {
     if constexpr (ST == 0) {
         return make_float2(0.f, 0.f);
     } else if constexpr (ST == 1) {   // minmod: 2 sign(l) min(|l|, |r|)
-        const float2 m = make_float2(fmaxf(min_xorsign_abs(l.x, r.x), 0.f), fmaxf(min_xorsign_abs(l.y, r.y), 0.f));
+        const float2 m = make_float2(fmaxf(min_xorsign_abs_f(l.x, r.x), 0.f), fmaxf(min_xorsign_abs_f(l.y, r.y), 0.f));
         const float2 m2 = add2(m, m);
         return make_float2(copysignf(m2.x, l.x), copysignf(m2.y, l.y));
     } else if constexpr (ST == 2) {   // van Leer: 2 (2 l r / (l + r))
@@ -53,10 +46,10 @@ __device__ __forceinline__ float2 limit2(float2 l, float2 r) {
         return make_float2(pr.x <= 0.f ? 0.f : q.x, pr.y <= 0.f ? 0.f : q.y);
     } else {                          // MC: 2 sign(s) min(1.5 min(|l|,|r|), |s|/2) = sign(s) min(3 min, |s|)
         const float2 s = add2(l, r);
-        const float2 a = mul2(make_float2(fmaxf(min_xorsign_abs(l.x, r.x), 0.f), fmaxf(min_xorsign_abs(l.y, r.y), 0.f)),
+        const float2 a = mul2(make_float2(fmaxf(min_xorsign_abs_f(l.x, r.x), 0.f), fmaxf(min_xorsign_abs_f(l.y, r.y), 0.f)),
                               bc2(3.f));
         // sign(s) min(|s|, a) for a >= +0 is min.xorsign.abs(a, s): one instruction per column
-        return make_float2(min_xorsign_abs(a.x, s.x), min_xorsign_abs(a.y, s.y));
+        return make_float2(min_xorsign_abs_f(a.x, s.x), min_xorsign_abs_f(a.y, s.y));
     }
 }
 

@@ -62,10 +62,18 @@ __device__ __forceinline__ float limit_vl_f(float l, float r) {
     const float p = l * r;
     return p <= 0.f ? 0.f : 2.f * p / (l + r);
 }
+// min(|a|, |b|) carrying the sign sign(a) xor sign(b): >= 0 exactly when a and b have the same
+// sign (or one is zero)
+__device__ __forceinline__ float min_xorsign_abs_f(float a, float b) {
+    float d;
+    asm("min.xorsign.abs.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+// MC: sign(s) min(1.5 min(|l|, |r|), |s|/2) when l r > 0, else 0; with m = max(min.xorsign.abs(l, r), 0)
+// (0 unless l and r have the same sign) it is min.xorsign.abs(1.5 m, s/2)
 __device__ __forceinline__ float limit_mc_f(float l, float r) {
-    const float s = l + r;
-    const float m = fminf(1.5f * fminf(fabsf(l), fabsf(r)), 0.5f * fabsf(s));
-    return l * r <= 0.f ? 0.f : copysignf(m, s);
+    const float m = fmaxf(min_xorsign_abs_f(l, r), 0.f);
+    return min_xorsign_abs_f(1.5f * m, 0.5f * (l + r));
 }
 
 // Compile-time limiter choice (0 = first order) for kernels specialised per configuration.
