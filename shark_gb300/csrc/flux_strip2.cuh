@@ -15,6 +15,8 @@
 // limiters are the FP32 forms of physics.cuh on the doubled slopes.
 #pragma once
 
+#include <algorithm>
+
 #include "rows.cuh"
 
 namespace shark {
@@ -65,12 +67,17 @@ __device__ __forceinline__ void hb2(float2 rL, float2 uL, float2 vL, float2 wL, 
     f[3] = fma2(mr, wR, mul2(ml, wL));
 }
 
-// Arguments of a strip's row source: the tensor map of this launch's current state and the
-// warp's shared-memory ring.
+// Arguments of a strip's row source: the tensor map of this launch's current state, the warp's
+// shared-memory ring, and the ring's barrier state carried from one strip of the warp to the
+// next (TmaRows: phase bits, whether the barriers are initialised, whether every wait so far
+// completed).
 struct RingArgs {
     const CUtensorMap* map;
     float* ring;
     uint64_t* bar;
+    uint32_t phase = 0;
+    bool fresh = true;
+    bool good = true;
 };
 
 // The row source of a strip (overloads chosen by the type of the null first argument).
@@ -86,8 +93,17 @@ __device__ __forceinline__ TmaRows<NV, R, NST> make_rows_impl(TmaRows<NV, R, NST
     t.r0 = r0;
     t.sp = sp;
     t.lane = threadIdx.x & 31;
+    t.phase = ra.phase;
+    t.fresh = ra.fresh;
     t.setup(nrows);
     return t;
+}
+// The ring's state after a strip, for the warp's next strip.
+template <int NV, int R, int NST>
+__device__ __forceinline__ void keep_ring(const TmaRows<NV, R, NST>& t, RingArgs& ra) {
+    ra.phase = t.phase;
+    ra.fresh = false;
+    ra.good = t.good;
 }
 template <class Rows>
 __device__ __forceinline__ Rows make_rows(const KParams<float>& p, const RingArgs& ra, int vb, int vs, bool col_in,
@@ -115,22 +131,20 @@ __device__ __forceinline__ UniformGrid uniform_grid(const KParams<float>& p, flo
     return g;
 }
 
-// K1 of one dust species (4 variables) on a uniform Cartesian grid, two columns per lane.
-// Per row: the x differences of the row, the y difference to the next row (the y difference
-// below the row is the one the previous row computed), the limited doubled slopes, the
-// predictor, the four face states, the Huang & Bai fluxes of the x faces and of the y face below,
-// then the row below is finished and this row started.  The row loop is unrolled by two so that
-// the rows carried from one iteration to the next change registers without moves.
+// K1 of one dust species (4 variables) on a uniform Cartesian grid, two columns per lane, rows
+// ay0 .. ylast (active rows, warp-uniform).  Per row: the x differences of the row, the y
+// difference to the next row (the y difference below the row is the one the previous row
+// computed), the limited doubled slopes, the predictor, the four face states, the Huang & Bai
+// fluxes of the x faces and of the y face below, then the row below is finished and this row
+// started.
 template <int ST, class Rows>
-__device__ void flux_strip_dust2(const KParams<float>& p, const RingArgs& ra, int s, int bx, int by) {
+__device__ __forceinline__ void flux_strip_dust2(const KParams<float>& p, RingArgs& ra, int s, int bx, int ay0,
+                                                 int ylast) {
     const unsigned FULL = 0xffffffffu;
     const int N = p.ndust;
     const int lane = threadIdx.x & 31;
     const int ax0 = p.ng + bx * STRIP2_UX;     // first active column updated by this warp
     const int ga = ax0 - 2 + 2 * lane;         // this lane's columns ga, ga + 1 (ga even)
-    const int ay0 = p.ng + by * STRIP_H;
-    if (ay0 >= p.ng + p.ny) return;            // uniform over the warp
-    const int ylast = min(ay0 + STRIP_H, p.ng + p.ny) - 1;
     const bool col_in = ga < p.nx_max;         // ga + 1 is then inside the row's pitch padding
     const int ca = min(ga, p.nx_max - 1), cb = min(ga + 1, p.nx_max - 1);
     const bool halo = lane == 0 || lane == 31;
@@ -280,6 +294,7 @@ __device__ void flux_strip_dust2(const KParams<float>& p, const RingArgs& ra, in
         if (lane == 0) atomicOr(p.status, SHARK_STATUS_COPY_WAIT);
         rows.finish();
     }
+    keep_ring(rows, ra);
 }
 
 }  // namespace shark
@@ -288,42 +303,90 @@ __device__ void flux_strip_dust2(const KParams<float>& p, const RingArgs& ra, in
 
 namespace shark {
 
-// Gas and dust of the mixed path's K1 in one launch: blocks 0 .. ng-1 take the gas strips, the
-// rest the dust strips of every species, both 60 columns per warp.  The gas blocks come first in
-// the launch order, so the gas grid runs beside the dust instead of after it.  Rows reach the
-// strips through a per-warp ring of TMA stages in dynamic shared memory (K1_R rows per stage,
-// K1_NST stages; the maps of the gas and of the dust planes of this step's state).
+// Gas and dust of the mixed path's K1 in one persistent launch of one wave of blocks.  The
+// launch's warps are split between the gas and the dust in proportion to their work (rows times
+// the strips' instructions per row: gas 711, dust 405 on the isothermal SI box with the MC
+// limiter, weights 7 : 4).  Within each class the column blocks (60 columns, ny active rows;
+// gas: nbx blocks; dust: ndust x nbx blocks, species-major) are laid end to end as one list of
+// rows, and warp i of the class's n warps marches rows [i R / n, (i + 1) R / n) of its R rows: one
+// piece per column block the range touches (a piece is a strip of flux_strip_gas2 /
+// flux_strip_dust2 with its own two halo rows above and below).  So every warp has about the
+// same work and the launch has no tail of partly filled waves.  A warp gets at least
+// K1_MIN_ROWS rows: small grids launch fewer warps rather than pieces of a row or two.  Rows
+// reach the strips through a per-warp ring of TMA stages in dynamic shared memory (K1_R rows per
+// stage, K1_NST stages; the maps of the gas and of the dust planes of this step's state), kept
+// from piece to piece.
 struct K1Maps {
     CUtensorMap gas, dust;
 };
 
+struct K1Work {
+    int nbx;        // column blocks per species
+    int ngw, ndw;   // gas warps, dust warps
+};
+#ifndef SHARK_K1_GAS_WEIGHT
+#define SHARK_K1_GAS_WEIGHT 7
+#endif
+constexpr int K1_WG = SHARK_K1_GAS_WEIGHT, K1_WD = 4, K1_MIN_ROWS = 16;
+
+inline K1Work k1_work(int nx, int ny, int ndust, int warps) {
+    K1Work w;
+    w.nbx = (nx + STRIP2_UX - 1) / STRIP2_UX;
+    const long long rg = (long long)w.nbx * ny, rd = rg * ndust;
+    const long long cg = std::max(1LL, rg / K1_MIN_ROWS), cd = std::max(1LL, rd / K1_MIN_ROWS);
+    const double share = (double)(rg * K1_WG) / (double)(rg * K1_WG + rd * K1_WD);
+    const int wtot = std::max(warps, 2);
+    w.ngw = (int)std::min<long long>(cg, std::max(1LL, std::llround(wtot * share)));
+    w.ndw = (int)std::min<long long>(cd, std::max(1, wtot - w.ngw));
+    return w;
+}
+
 constexpr int K1_R = K1_TMA_ROWS, K1_NST = K1_TMA_STAGES;
 using K1Ring = RingSize<K1_R, K1_NST, 5>;
 constexpr int K1_SMEM = STRIP_WARPS * (K1Ring::ring_bytes + K1Ring::bar_bytes);
+
+// Rows [i R / n, (i + 1) R / n) of a class's R = nblk ny rows as pieces (column block, first row,
+// last row), active-row numbering from 0; calls strip(block, r0, r1) for each until it fails.
+template <class Strip>
+__device__ __forceinline__ void k1_pieces(int ny, int nblk, int i, int n, RingArgs& ra, Strip&& strip) {
+    const long long R = (long long)nblk * ny;
+    const long long lo = (long long)i * R / n, hi = (long long)(i + 1) * R / n;
+    int t = (int)(lo / ny), r0 = (int)(lo - (long long)t * ny);
+    const int te = (int)((hi - 1) / ny), re = (int)(hi - 1 - (long long)te * ny);   // last row, inclusive
+#pragma unroll 1
+    for (; t <= te && ra.good; ++t, r0 = 0) strip(t, r0, t == te ? re : ny - 1);
+}
 
 // blocks per SM the kernel is compiled for (4 blocks of 128 threads: 128 registers per thread)
 #ifndef SHARK_K1_MINBLOCKS
 #define SHARK_K1_MINBLOCKS 4
 #endif
 template <int NV> using K1Rows = TmaRows<NV, K1_R, K1_NST>;
-template <int ST, int GSOLV>
+// ISO: the gas is isothermal (p.iso == 1); compiled apart so that each instance inlines one gas
+// strip (both in one kernel spill registers).
+template <int ST, int GSOLV, bool ISO>
 __global__ void __launch_bounds__(32 * STRIP_WARPS, SHARK_K1_MINBLOCKS)
-    k_flux_strip_mixed(const __grid_constant__ K1Maps maps, KParams<float> p, int nbx_g, int nbx_d, int nby) {
+    k_flux_strip_mixed(const __grid_constant__ K1Maps maps, const __grid_constant__ KParams<float> p, K1Work wk) {
     extern __shared__ __align__(128) unsigned char k1_smem[];
     const int warp = threadIdx.x >> 5;
-    const int id = blockIdx.x, ngas = nbx_g * nby;
+    const int w = blockIdx.x * STRIP_WARPS + warp;
+    if (w >= wk.ngw + wk.ndw) return;   // whole warps; the kernel has no block-wide barrier
     RingArgs ra;
     ra.ring = reinterpret_cast<float*>(k1_smem + warp * K1Ring::ring_bytes);
     ra.bar = reinterpret_cast<uint64_t*>(k1_smem + STRIP_WARPS * K1Ring::ring_bytes + warp * K1Ring::bar_bytes);
-    if (id < ngas) {
+    const int ng = p.ng;
+    if (w < wk.ngw) {
         ra.map = &maps.gas;
         using GR = K1Rows<5>;
-        if (p.iso == 1) flux_strip_gas2<ST, GSOLV, true, GR>(p, ra, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
-        else flux_strip_gas2<ST, GSOLV, false, GR>(p, ra, id % nbx_g, (id / nbx_g) * STRIP_WARPS + warp);
+        k1_pieces(p.ny, wk.nbx, w, wk.ngw, ra, [&](int t, int r0, int r1) {
+            flux_strip_gas2<ST, GSOLV, ISO, GR>(p, ra, t, ng + r0, ng + r1);
+        });
     } else {
         ra.map = &maps.dust;
-        const int d = id - ngas, bx = d % nbx_d, rest = d / nbx_d;
-        flux_strip_dust2<ST, K1Rows<4>>(p, ra, rest / nby + 1, bx, (rest % nby) * STRIP_WARPS + warp);
+        const int nbx = wk.nbx;
+        k1_pieces(p.ny, nbx * p.ndust, w - wk.ngw, wk.ndw, ra, [&](int t, int r0, int r1) {
+            flux_strip_dust2<ST, K1Rows<4>>(p, ra, t / nbx + 1, t % nbx, ng + r0, ng + r1);
+        });
     }
 }
 

@@ -97,18 +97,15 @@ __device__ __forceinline__ void gas_flux2(float gamma, float inv_g1, const float
 }
 
 // K1 of the gas on a uniform Cartesian grid (UniformGrid, flux_strip2.cuh), two columns per lane,
-// rows from `Rows` (rows.cuh).  ISO: isothermal (the pressure is rho cs^2 everywhere, so it is not
-// carried in the row window).  Same row structure as flux_strip_dust2: x differences of the row,
-// the y difference to the next row carried to the next iteration, row loop unrolled by two.
+// rows ay0 .. ylast from `Rows` (rows.cuh).  ISO: isothermal (the pressure is rho cs^2
+// everywhere, so it is not carried in the row window).  Same row structure as flux_strip_dust2:
+// x differences of the row, the y difference to the next row carried to the next iteration.
 template <int ST, int GSOLV, bool ISO, class Rows>
-__device__ void flux_strip_gas2(const KParams<float>& p, const RingArgs& ra, int bx, int by) {
+__device__ __forceinline__ void flux_strip_gas2(const KParams<float>& p, RingArgs& ra, int bx, int ay0, int ylast) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int ax0 = p.ng + bx * STRIP2_UX;
     const int ga = ax0 - 2 + 2 * lane;         // this lane's columns ga, ga + 1 (ga even)
-    const int ay0 = p.ng + by * STRIP_H;
-    if (ay0 >= p.ng + p.ny) return;            // uniform over the warp
-    const int ylast = min(ay0 + STRIP_H, p.ng + p.ny) - 1;
     const bool col_in = ga < p.nx_max;         // ga + 1 is then inside the row's pitch padding
     const int ca = min(ga, p.nx_max - 1), cb = min(ga + 1, p.nx_max - 1);
     const bool halo = lane == 0 || lane == 31;
@@ -326,6 +323,7 @@ __device__ void flux_strip_gas2(const KParams<float>& p, const RingArgs& ra, int
         if (lane == 0) atomicOr(p.status, SHARK_STATUS_COPY_WAIT);
         rows.finish();
     }
+    keep_ring(rows, ra);
 }
 
 }  // namespace shark

@@ -197,24 +197,26 @@ static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
     dim3 grid(nbx, (nstrips + STRIP_WARPS - 1) / STRIP_WARPS, 1);
     if constexpr (std::is_same<R, float>::value) {
         if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0 && v.uniform && !v.cdisk.on) {
-            // mixed path, uniform Cartesian grid, Huang & Bai dust: gas and dust strips in one launch
-            const int nbx_g = (p.nx + STRIP2_UX - 1) / STRIP2_UX, nbx_d = nbx_g;
-            const int nby = (int)grid.y;
-            const long long nblk = (long long)nbx_g * nby + (long long)nbx_d * nby * p.ndust;
-            const dim3 g1((unsigned)nblk, 1, 1), b1(32 * STRIP_WARPS, 1, 1);
+            // mixed path, uniform Cartesian grid, Huang & Bai dust: gas and dust strips in one
+            // persistent launch of one wave of blocks (K1Work)
+            const K1Work wk = k1_work(p.nx, p.ny, p.ndust, v.k1_warps);
+            const dim3 g1((unsigned)((wk.ngw + wk.ndw + STRIP_WARPS - 1) / STRIP_WARPS), 1, 1), b1(32 * STRIP_WARPS, 1, 1);
             const int gs = p.solver == 0 ? 0 : p.solver == 1 ? 1 : 2;
             K1Maps maps;
             maps.gas = v.k1_gas[v.cur];
             maps.dust = v.k1_dust[v.cur];
-            switch (p.slope_type * 3 + gs) {
+            switch ((p.slope_type * 3 + gs) * 2 + (p.iso == 1 ? 1 : 0)) {
 #define SHARK_K1M(ST, GS)                                                                                \
-    case ST * 3 + GS:                                                                                    \
-        k_flux_strip_mixed<ST, GS><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, nbx_g, nbx_d, nby); break;
+    case (ST * 3 + GS) * 2:                                                                              \
+        k_flux_strip_mixed<ST, GS, false><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, wk); break;            \
+    case (ST * 3 + GS) * 2 + 1:                                                                          \
+        k_flux_strip_mixed<ST, GS, true><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, wk); break;
                 SHARK_K1M(0, 0) SHARK_K1M(0, 1) SHARK_K1M(0, 2)
                 SHARK_K1M(1, 0) SHARK_K1M(1, 1) SHARK_K1M(1, 2)
                 SHARK_K1M(2, 0) SHARK_K1M(2, 1) SHARK_K1M(2, 2)
                 SHARK_K1M(3, 0) SHARK_K1M(3, 1)
-                default: k_flux_strip_mixed<3, 2><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, nbx_g, nbx_d, nby); break;
+                case (3 * 3 + 2) * 2: k_flux_strip_mixed<3, 2, false><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, wk); break;
+                default: k_flux_strip_mixed<3, 2, true><<<g1, b1, K1_SMEM, v.stream>>>(maps, p, wk); break;
 #undef SHARK_K1M
             }
             return cudaGetLastError();
@@ -442,7 +444,24 @@ cudaError_t launch_planes_to_fortran(const DeviceView& v, const void* src, int c
     return cudaGetLastError();
 }
 
+template <typename R>
+int k1_resident_warps(int nsm) {
+    if constexpr (std::is_same<R, float>::value) {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_flux_strip_mixed<3, 2, true>, 32 * STRIP_WARPS, K1_SMEM) !=
+                cudaSuccess ||
+            nb < 1) {
+            cudaGetLastError();
+            nb = 1;
+        }
+        return nsm * nb * STRIP_WARPS;
+    } else {
+        return 0;
+    }
+}
+
 #define SHARK_INSTANTIATE(R)                                                                       \
+    template int k1_resident_warps<R>(int);                                                        \
     template cudaError_t launch_step<R>(const DeviceView&, int);                                   \
     template cudaError_t launch_courant<R>(const DeviceView&, int);                                \
     template cudaError_t launch_boundaries<R>(const DeviceView&);                                  \

@@ -14,6 +14,11 @@
 // Interface used by the strips: begin(), fetch(row, us) (rows in increasing order), get(row, k)
 // (the row before the last fetched one), done(row) at the end of the iteration that fetched
 // row + 1 and re-read row - 1, ok() (false once a wait gave up), finish().
+//
+// One warp may march several strips in turn through the same ring (a persistent launch): every
+// strip starts its stages at slot 0, the barriers are initialised once, before the warp's first
+// strip, and the phase each barrier is waited on is carried from strip to strip as one bit per
+// slot (flipped after every completed wait on that slot).
 #pragma once
 
 #include <cuda.h>
@@ -80,7 +85,9 @@ struct TmaRows {
     float* ring;          // this warp's ring, 128-byte aligned
     uint64_t* bar;        // NST barriers
     int x0, r0, sp, lane, nstages;
-    int issued, waited;   // stages issued / waited for
+    int issued, waited;   // stages of this strip issued / waited for
+    uint32_t phase;       // bit i: the phase parity the next wait on barrier i waits for
+    bool fresh;           // the barriers are not initialised yet (the warp's first strip)
     bool good;
 
     __device__ __forceinline__ void issue(int k) {
@@ -100,10 +107,16 @@ struct TmaRows {
         good = true;
     }
     __device__ __forceinline__ void begin() {
-        if (lane == 0) {
+        if (fresh) {
+            if (lane == 0) {
 #pragma unroll
-            for (int i = 0; i < NST; ++i) umma::mbar_init(bar + i, 1);
-            umma::fence_proxy_async();
+                for (int i = 0; i < NST; ++i) umma::mbar_init(bar + i, 1);
+                umma::fence_proxy_async();
+            }
+        } else {
+            // the previous strip's generic reads of the ring come before the copies into it
+            __syncwarp();
+            if (lane == 0) umma::fence_proxy_async();
         }
         __syncwarp();
         const int n0 = nstages < NST ? nstages : NST;
@@ -116,11 +129,14 @@ struct TmaRows {
     __device__ __forceinline__ void fetch(int row, float2* us) {
         const int j = row - r0;
         if (j % R == 0) {   // first row of stage j / R: wait for its copy
-            const int k = j / R;
+            const int slot = (j / R) % NST;
             const bool w = __all_sync(0xffffffffu,
-                                      umma::mbar_wait(bar + (k % NST), (uint32_t)((k / NST) & 1), tma::WAIT_POLLS));
+                                      umma::mbar_wait(bar + slot, (phase >> slot) & 1u, tma::WAIT_POLLS));
             good = good && w;
-            if (w) ++waited;
+            if (w) {
+                ++waited;
+                phase ^= 1u << slot;
+            }
         }
         const float* pr = row_ptr(row);
 #pragma unroll
@@ -146,8 +162,11 @@ struct TmaRows {
     __device__ __forceinline__ bool ok() const { return good; }
     // on an early exit: wait (bounded) for the copies still in flight into this warp's ring
     __device__ __forceinline__ void finish() {
-        for (int k = waited; k < issued; ++k)
-            (void)umma::mbar_wait(bar + (k % NST), (uint32_t)((k / NST) & 1), tma::WAIT_POLLS);
+        for (int k = waited; k < issued; ++k) {
+            const int slot = k % NST;
+            (void)umma::mbar_wait(bar + slot, (phase >> slot) & 1u, tma::WAIT_POLLS);
+            phase ^= 1u << slot;
+        }
         waited = issued;
     }
 };

@@ -1155,6 +1155,11 @@ int32_t shark_gpu_init(const shark_gpu_config* cfg, shark_gpu_ctx** out) {
         release(c);
         return rc;
     }
+    if (is_mixed(c) && v.ndim == 2) {
+        int nsm = 0;
+        INIT_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, cfg->device));
+        v.k1_warps = shark::k1_resident_warps<float>(nsm);
+    }
     if (cfg->setup == SHARK_SETUP_DISK_POLAR) {
         INIT_TRY(cudaMalloc(&c->uinit, c->state_bytes));
         INIT_TRY(cudaMemsetAsync(c->uinit, 0, c->state_bytes, c->stream));
