@@ -86,7 +86,7 @@ struct DeviceView {
     // mixed path, 2D: tensor maps of each state buffer for K1's TMA row staging, the gas planes
     // (x, y, variable 0..4) and the dust planes (x, y, species, component)
     CUtensorMap k1_gas[3], k1_dust[3];
-    int k1_warps;               // warps of the persistent mixed K1: SMs x resident blocks x warps per block
+    int k1_warps;               // warps of one wave of the mixed 2D K1: SMs x resident blocks x warps per block
     bool uniform;               // Cartesian grid with the same dx1, dx2, surf1, surf2, vol in every column
     bool cs_uniform;            // the same isothermal sound speed in every column
     // reference gas density of the mixed fused flux kernel: the mean active density of the first
@@ -117,7 +117,7 @@ inline int next_cur(const DeviceView& v) { return v.nbuf == 3 ? (v.cur + 2) % 3 
 // one full step on view.u[view.cur] -> view.u[next_cur(view)]; dt read from slot `slot`, next dt
 // written to slot 1-slot.  Returns a cudaError_t.
 template <typename R> cudaError_t launch_step(const DeviceView& v, int slot);
-// warps of the persistent mixed-precision 2D flux kernel on `nsm` SMs (resident blocks x warps per
+// warps of one wave of the mixed-precision 2D flux kernel on `nsm` SMs (resident blocks x warps per
 // block x nsm; 0 for the FP64 instantiation, which has no such kernel)
 template <typename R> int k1_resident_warps(int nsm);
 // courant only on the current state into dt slot `slot`

@@ -121,6 +121,21 @@ def test_driven_box_32_species_forcing_charging_no_growth_fp64():
     assert rel_l1(cfg, ug, uo).max() <= FP64_TOL
 
 
+@pytest.mark.parametrize("n", [1024, 1088])
+def test_driven_box_32_species_mixed_flux_schedules(n):
+    """The mixed K1 at the driven box's species count on the two schedules of its launch (for a
+    GPU of 152 SMs): 1024^2 is one persistent wave of warps with the dust swept in two phases of
+    128-row pieces; 1088^2 fills more than eight waves of 32-row pieces and runs one piece per
+    warp.  Pieces of either schedule recompute their halo rows, so the result does not depend on
+    the schedule and the mixed tolerance of the driven box holds against the oracle."""
+    cfg, u0 = setups.dusty_turb(n=n, ndust=32, precision=K.PREC_MIXED)
+    dto, dtg, uo, ug, st = run_pair(cfg, u0, 3)
+    assert st == 0
+    np.testing.assert_allclose(dtg, dto, rtol=1e-5)
+    err = rel_l1(cfg, ug, uo)
+    assert err.max() <= 2e-4, err
+
+
 def test_driven_box_32_species_forcing_growth_charging_mixed():
     cfg, u0 = setups.dusty_turb(n=128, ndust=32, forcing=True, charging=True, growth=True,
                                 precision=K.PREC_MIXED)
