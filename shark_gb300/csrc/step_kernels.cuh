@@ -489,23 +489,30 @@ __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int
 // shuffles).  Every sub-step each lane writes the collision rate w_q = rate_q rho_k rho_j (times
 // the sticking efficiency) of its pairs to shared memory, and lane b gathers
 // drho_b/dt = sum_t gc[t][b] w[gq[t][b]] from the host-built table of net transfers (staged in
-// shared memory); the sub-step is the warp minimum of CFL_growth rho_b/|drho_b/dt|, and the part
-// of dt still to integrate is kept as an FP32 fraction (the last sub-step takes all of it).  The
-// lanes of a warp take the same sub-steps, so a warp costs the sub-steps of its own cell rather
-// than those of the slowest of 32 cells.  Called by every thread of the block.
+// shared memory, two rows per 128-bit entry, the four partial sums of rows t mod 4 as two packed
+// FMAs); the sub-step is the warp minimum of CFL_growth rho_b/|drho_b/dt| (one redux.sync on the
+// candidates' bit patterns), and the part of dt still to integrate is kept as an FP32 fraction
+// (the last sub-step takes all of it).  The lanes of a warp take the same sub-steps, so a warp
+// costs the sub-steps of its own cell rather than those of the slowest of 32 cells.  Called by
+// every thread of the block.  The sub-step is bound by the shared-memory and shuffle pipe: per
+// sub-step a warp moves about 270 shared-memory wavefronts, half of them the gather table's.
 constexpr int GROWTH_PAIR_SLOTS = (GROWTH_MAX_PAIRS + 31) / 32;
 constexpr int GROWTH_SMEM_ROWS = 80;        // gather rows staged in shared memory (64 at 32 species)
 
 static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p, int gx_block, int gy, double dt) {
     __shared__ float sw[8][GROWTH_MAX_PAIRS];
-    __shared__ int2 sg[GROWTH_SMEM_ROWS * 32];
+    __shared__ int4 sg[GROWTH_SMEM_ROWS / 2 * 32];   // rows 2 r, 2 r + 1 of lane l at [32 r + l]
     __shared__ int spair[GROWTH_PAIR_SLOTS * 32];   // pair (k << 8 | j) of slot i, lane l at [32 i + l]
     const GrowthDev& g = p.gw;
     const int N = p.ndust, P = g.npair, L = g.gL;
     const bool staged = L <= GROWTH_SMEM_ROWS;
     if (staged)
-        for (int e = threadIdx.x; e < L * 32; e += blockDim.x)
-            sg[e] = make_int2(__ldg(g.gq + e), __float_as_int(__ldg(g.gc + e)));
+        for (int e = threadIdx.x; e < (L + 1) / 2 * 32; e += blockDim.x) {
+            const int r = e >> 5, l = e & 31, t0 = 2 * r * 32 + l, t1 = t0 + 32;
+            const bool has1 = 2 * r + 1 < L;   // an odd last row pairs with a zero row
+            sg[e] = make_int4(__ldg(g.gq + t0), __float_as_int(__ldg(g.gc + t0)), has1 ? __ldg(g.gq + t1) : 0,
+                              has1 ? __float_as_int(__ldg(g.gc + t1)) : 0);
+        }
     for (int e = threadIdx.x; e < GROWTH_PAIR_SLOTS * 32; e += blockDim.x) spair[e] = e < P ? __ldg(g.pair + e) : 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -593,27 +600,26 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
             float d = 0.f;
             if (staged) {
                 // four partial sums: the gather's products are independent, its FMA chain is not
-                float d1 = 0.f, d2 = 0.f, d3 = 0.f;
+                float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
                 int t = 0;
                 for (; t + 4 <= L; t += 4) {
-                    const int2 e0 = sg[t * 32 + lane], e1 = sg[(t + 1) * 32 + lane];
-                    const int2 e2 = sg[(t + 2) * 32 + lane], e3 = sg[(t + 3) * 32 + lane];
-                    d = fmaf(__int_as_float(e0.y), w[e0.x], d);
-                    d1 = fmaf(__int_as_float(e1.y), w[e1.x], d1);
-                    d2 = fmaf(__int_as_float(e2.y), w[e2.x], d2);
-                    d3 = fmaf(__int_as_float(e3.y), w[e3.x], d3);
+                    const int4 e0 = sg[(t >> 1) * 32 + lane], e1 = sg[((t >> 1) + 1) * 32 + lane];
+                    a0 = __ffma2_rn(make_float2(__int_as_float(e0.y), __int_as_float(e0.w)), make_float2(w[e0.x], w[e0.z]), a0);
+                    a1 = __ffma2_rn(make_float2(__int_as_float(e1.y), __int_as_float(e1.w)), make_float2(w[e1.x], w[e1.z]), a1);
                 }
+                d = a0.x;
                 for (; t < L; ++t) {
-                    const int2 e = sg[t * 32 + lane];
-                    d = fmaf(__int_as_float(e.y), w[e.x], d);
+                    const int4 e = sg[(t >> 1) * 32 + lane];
+                    d = (t & 1) ? fmaf(__int_as_float(e.w), w[e.z], d) : fmaf(__int_as_float(e.y), w[e.x], d);
                 }
-                d = (d + d1) + (d2 + d3);
+                d = (d + a0.y) + (a1.x + a1.y);
             } else {
                 for (int t = 0; t < L; ++t) d += __ldg(g.gc + t * 32 + lane) * w[__ldg(g.gq + t * 32 + lane)];
             }
             __syncwarp();
-            float cand = (on && d != 0.f) ? rd / fabsf(d) * cflg : 1e30f;
-            for (int o = 16; o > 0; o >>= 1) cand = fminf(cand, __shfl_xor_sync(FULL, cand, o));
+            // non-negative floats order like their bit patterns read as unsigned integers
+            const float c0 = (on && d != 0.f) ? fmaxf(rd / fabsf(d) * cflg, 0.f) : 1e30f;
+            const float cand = __uint_as_float(__reduce_min_sync(FULL, __float_as_uint(c0)));
             const float dtg0 = fctl > 0.f ? dtctl : cand;
             const float frac = fctl > 0.f ? fctl : cand * idtf;
             float dtg;
