@@ -270,7 +270,7 @@ cudaError_t launch_step(const DeviceView& v, int slot) {
     if (v.time_kernels) cudaEventRecord(v.ev[0], v.stream);
     k_prepare_step<<<1, SHARK_MAX_DUST, 0, v.stream>>>(p.dt_next, p.dt, p.dtstop, p.ndust,
                                                       (p.setup == SHARK_SETUP_SI && std::is_same<R, float>::value) ? 1 : 0,
-                                                      p.coef);
+                                                      p.coef, v.dt_log);
     if (v.chg.on && (e = launch_charge<R>(v)) != cudaSuccess) return e;   // charge: solve.f90:36-42
     if (v.ou_nm > 0)   // this step's forcing coefficients, from the dt on the device
         k_ou_update<<<1, 2 * v.ou_nm, 0, v.stream>>>(v.ou, v.ou_nm, p.dt, v.ou_sigma, v.ou_tcorr, v.ou_seed, v.step);
@@ -297,7 +297,7 @@ cudaError_t launch_courant(const DeviceView& v, int slot) {
     p.u_cur = (const R*)v.u[v.cur];
     p.dt = v.dt_slots + slot;   // unused in MODE 1 except by the drag (disabled)
     p.dt_next = reinterpret_cast<unsigned long long*>(v.dt_slots + slot);
-    k_prepare_step<<<1, 1, 0, v.stream>>>(p.dt_next, p.dt, p.dtstop, 0, 0, p.coef);
+    k_prepare_step<<<1, 1, 0, v.stream>>>(p.dt_next, p.dt, p.dtstop, 0, 0, p.coef, nullptr);
     dim3 g2((v.nx + 255) / 256, v.ndim == 2 ? v.ny : 1, 1);
     finalize_dispatch<R, 1>(p, g2, v.stream);
     return cudaGetLastError();

@@ -67,6 +67,8 @@ struct DeviceView {
     const double* dstokes;
     const double* dinvts;       // 1/C_k with t_k = C_k / (cell factor) for the per-cell stopping times
     double* dt_slots;           // [2] dt of step n lives in slot n % 2
+    double* dt_log = nullptr;   // when set, the step's preparation kernel stores the step's dt there
+                                // (pinned host memory of a timed run: no copy per step)
     unsigned int* status;       // OR of SHARK_STATUS_* bits
     float* coef;                // [SHARK_COEF_FLOATS] per-step drag coefficients (mixed path), float dt
     cudaStream_t stream;

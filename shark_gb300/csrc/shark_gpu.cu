@@ -1787,11 +1787,17 @@ int32_t shark_gpu_timed_run(shark_gpu_ctx* c, int64_t nsteps, double* time_io, f
     if (!c->uploaded) return fail(SHARK_ERR_STATE, "timed run before upload");
     if (nsteps < 0) return fail(SHARK_ERR_INVALID_ARG, "nsteps < 0");
     // The steps are queued back to back with no host wait between them (the dt of every step
-    // lives on the device; a copy of it per step lands in pinned memory and is summed
-    // afterwards), so host-side stalls cannot leave the GPU idle inside the timed region.
+    // lives on the device; the step's preparation kernel stores it into pinned host memory, read
+    // through its unified address, and the host sums them afterwards), so host-side stalls cannot
+    // leave the GPU idle inside the timed region and no copy-engine transfer sits between steps.
     const bool is_static = (c->cfg.flags & SHARK_FLAG_STATIC) != 0;
     double* dts = nullptr;
-    CUDA_TRY(cudaHostAlloc(&dts, (size_t)(nsteps > 0 ? nsteps : 1) * sizeof(double), cudaHostAllocDefault));
+    CUDA_TRY(cudaHostAlloc(&dts, (size_t)(nsteps > 0 ? nsteps : 1) * sizeof(double), cudaHostAllocMapped));
+    double* dts_dev = nullptr;   // the same memory as the kernels address it
+    if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&dts_dev), dts, 0) != cudaSuccess) {
+        cudaFreeHost(dts);
+        return fail(SHARK_ERR_CUDA, "timed run: no device address for the dt log");
+    }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     int32_t rc = SHARK_OK;
     cudaError_t e = cudaEventCreate(&e0);
@@ -1815,11 +1821,14 @@ int32_t shark_gpu_timed_run(shark_gpu_ctx* c, int64_t nsteps, double* time_io, f
         const int slot = (int)(c->nstep & 1);
         if (!is_static) {
             c->v.step = c->nstep + 1;
-            if ((e = do_step(c, slot)) != cudaSuccess) { rc = fail(SHARK_ERR_CUDA, "step launch: %s", cudaGetErrorString(e)); break; }
+            c->v.dt_log = dts_dev + n;
+            e = do_step(c, slot);
+            c->v.dt_log = nullptr;
+            if (e != cudaSuccess) { rc = fail(SHARK_ERR_CUDA, "step launch: %s", cudaGetErrorString(e)); break; }
             c->chg_cold = false;
             c->v.cur = shark::next_cur(c->v);
-        }
-        if ((e = cudaMemcpyAsync(dts + n, c->dt_slots + slot, sizeof(double), cudaMemcpyDeviceToHost, c->stream)) != cudaSuccess) {
+        } else if ((e = cudaMemcpyAsync(dts + n, c->dt_slots + slot, sizeof(double), cudaMemcpyDeviceToHost,
+                                        c->stream)) != cudaSuccess) {
             rc = fail(SHARK_ERR_CUDA, "timed run: %s", cudaGetErrorString(e));
             break;
         }

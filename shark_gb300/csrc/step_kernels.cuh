@@ -1218,11 +1218,12 @@ static __global__ void k_ou_update(double* ou, int nm, const double* dt, double 
 }
 
 static __global__ void k_prepare_step(unsigned long long* dt_next, const double* dt, const double* dtstop, int ndust,
-                                      int const_ts, float* coef) {
+                                      int const_ts, float* coef, double* dt_log) {
     const int k = threadIdx.x;
     if (k == 0) {
         *dt_next = (unsigned long long)__double_as_longlong(2e44);
         coef[2 * SHARK_MAX_DUST] = (float)*dt;
+        if (dt_log) *dt_log = *dt;
     }
     if (const_ts && k < ndust) {
         float r, w;
