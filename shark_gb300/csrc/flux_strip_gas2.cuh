@@ -110,6 +110,7 @@ __device__ __forceinline__ void flux_strip_gas2(const KParams<float>& p, RingArg
     const int ca = min(ga, p.nx_max - 1), cb = min(ga + 1, p.nx_max - 1);
     const bool halo = lane == 0 || lane == 31;
     const bool upd_a = !halo && ga < p.ng + p.nx, upd_b = !halo && ga + 1 < p.ng + p.nx;
+    const bool upd_1 = upd_a && !upd_b;        // only the first of the pair is updated
     const bool act_a = ga >= p.ng && ga < p.ng + p.nx, act_b = ga + 1 >= p.ng && ga + 1 < p.ng + p.nx;
 
     const float dt = *p.dtf;
@@ -291,9 +292,7 @@ __device__ __forceinline__ void flux_strip_gas2(const KParams<float>& p, RingArg
             const int ro = (P - 1) * pitch;
 #pragma unroll
             for (int k = 0; k < NV; ++k) {
-                const float2 un = fma2(gb[k], ncyf, t_prev[k]);
-                if (upd_b) *reinterpret_cast<float2*>(dst + (voff(k) + ro)) = un;
-                else if (upd_a) dst[voff(k) + ro] = un.x;
+                store_cols(dst + (voff(k) + ro), fma2(gb[k], ncyf, t_prev[k]), upd_b, upd_1);
             }
         }
         // ---- start row P: kick with the force of its old q, then the x fluxes ------------------
