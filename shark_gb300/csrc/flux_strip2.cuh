@@ -334,7 +334,8 @@ namespace shark {
 //   scheduler balances the load and the last wave is a small part of the launch.
 // * few pieces: one wave of blocks (SMs x resident blocks), persistent warps.  The warps are split
 //   between the classes and P, Q and m chosen so that every warp has about the same work: cost =
-//   phases x (rows per piece + K1_PIECE_ROWS) x the class's weight per row (gas 6, dust 4),
+//   phases x (rows per piece + K1_PIECE_ROWS) x the class's weight per row (gas 6 isothermal or
+//   8 adiabatic, dust 4),
 //   K1_PIECE_ROWS standing for a piece's halo rows and its ring refill, pieces of at most
 //   K1_MAX_ROWS rows unless that needs more phases and of at least K1_MIN_ROWS rows.  On the SI box
 //   (1024^2, 8 species: 32-row strips are 2.13 waves) this is 14 dust pieces of 73 rows and 23 gas
@@ -353,14 +354,15 @@ struct K1Work {
     int nbx;             // column blocks per species
     K1Class g, d;        // gas, dust
 };
-#ifndef SHARK_K1_GAS_WEIGHT
-#define SHARK_K1_GAS_WEIGHT 6
-#endif
-constexpr int K1_WG = SHARK_K1_GAS_WEIGHT, K1_WD = 4, K1_PIECE_ROWS = 4, K1_MIN_ROWS = 16, K1_MAX_ROWS = 128,
+// weights per row: isothermal gas, adiabatic gas (it carries the pressure and the energy), dust
+// species (measured best of 5-9 on the SI box, of 6 and 8 on the adiabatic dusty KH box)
+constexpr int K1_WG_ISO = 6, K1_WG_ADI = 8, K1_WD = 4, K1_PIECE_ROWS = 4, K1_MIN_ROWS = 16, K1_MAX_ROWS = 128,
               K1_WAVES = 8;
 
-// `warps`: the warps of one wave (SMs x resident blocks x warps per block)
-inline K1Work k1_work(int nx, int ny, int ndust, int warps) {
+// `warps`: the warps of one wave (SMs x resident blocks x warps per block); `iso`: the gas is
+// isothermal
+inline K1Work k1_work(int nx, int ny, int ndust, int warps, bool iso) {
+    const int K1_WG = iso ? K1_WG_ISO : K1_WG_ADI;
     K1Work w;
     w.nbx = (nx + STRIP2_UX - 1) / STRIP2_UX;
     const int Bg = w.nbx, Bd = w.nbx * ndust;

@@ -199,7 +199,7 @@ static cudaError_t strip_launch(const DeviceView& v, const KParams<R>& p) {
         if (p.ndust > 0 && p.geom != 2 && p.solverdust == 0 && p.ng % 2 == 0 && v.uniform && !v.cdisk.on) {
             // mixed path, uniform Cartesian grid, Huang & Bai dust: gas and dust strips in one
             // launch (K1Work: one persistent wave, or one piece per warp when the pieces fill many waves)
-            const K1Work wk = k1_work(p.nx, p.ny, p.ndust, v.k1_warps);
+            const K1Work wk = k1_work(p.nx, p.ny, p.ndust, v.k1_warps, p.iso == 1);
             const dim3 g1((unsigned)((wk.g.n + wk.d.n + STRIP_WARPS - 1) / STRIP_WARPS), 1, 1), b1(32 * STRIP_WARPS, 1, 1);
             const int gs = p.solver == 0 ? 0 : p.solver == 1 ? 1 : 2;
             K1Maps maps;
