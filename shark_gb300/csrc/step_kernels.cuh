@@ -489,30 +489,38 @@ __device__ __noinline__ unsigned grow_in_finalize(const KParams<R>& p, R* u, int
 // shuffles).  Every sub-step each lane writes the collision rate w_q = rate_q rho_k rho_j (times
 // the sticking efficiency) of its pairs to shared memory, and lane b gathers
 // drho_b/dt = sum_t gc[t][b] w[gq[t][b]] from the host-built table of net transfers (staged in
-// shared memory, two rows per 128-bit entry, the four partial sums of rows t mod 4 as two packed
-// FMAs); the sub-step is the warp minimum of CFL_growth rho_b/|drho_b/dt| (one redux.sync on the
+// shared memory as four rows' coefficients per 128-bit entry and two rows' pair indices, 16 bits
+// each, per 32-bit word, the four partial sums of rows t mod 4 as two packed FMAs); the sub-step is the warp minimum of CFL_growth rho_b/|drho_b/dt| (one redux.sync on the
 // candidates' bit patterns), and the part of dt still to integrate is kept as an FP32 fraction
 // (the last sub-step takes all of it).  The lanes of a warp take the same sub-steps, so a warp
 // costs the sub-steps of its own cell rather than those of the slowest of 32 cells.  Called by
-// every thread of the block.  The sub-step is bound by the shared-memory and shuffle pipe: per
-// sub-step a warp moves about 270 shared-memory wavefronts, half of them the gather table's.
+// every thread of the block.
 constexpr int GROWTH_PAIR_SLOTS = (GROWTH_MAX_PAIRS + 31) / 32;
 constexpr int GROWTH_SMEM_ROWS = 80;        // gather rows staged in shared memory (64 at 32 species)
 
 static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p, int gx_block, int gy, double dt) {
     __shared__ float sw[8][GROWTH_MAX_PAIRS];
-    __shared__ int4 sg[GROWTH_SMEM_ROWS / 2 * 32];   // rows 2 r, 2 r + 1 of lane l at [32 r + l]
+    // gather table: coefficient of row t, lane l at sgc[128 (t >> 2) + 4 l + (t & 3)]; pair
+    // indices of rows 4 u + 2 h, 4 u + 2 h + 1 (low, high 16 bits) at sgi[64 u + 2 l + h]
+    __shared__ __align__(16) float sgc[GROWTH_SMEM_ROWS * 32];
+    __shared__ __align__(8) unsigned sgi[GROWTH_SMEM_ROWS / 2 * 32];
     __shared__ int spair[GROWTH_PAIR_SLOTS * 32];   // pair (k << 8 | j) of slot i, lane l at [32 i + l]
     const GrowthDev& g = p.gw;
     const int N = p.ndust, P = g.npair, L = g.gL;
     const bool staged = L <= GROWTH_SMEM_ROWS;
-    if (staged)
-        for (int e = threadIdx.x; e < (L + 1) / 2 * 32; e += blockDim.x) {
-            const int r = e >> 5, l = e & 31, t0 = 2 * r * 32 + l, t1 = t0 + 32;
-            const bool has1 = 2 * r + 1 < L;   // an odd last row pairs with a zero row
-            sg[e] = make_int4(__ldg(g.gq + t0), __float_as_int(__ldg(g.gc + t0)), has1 ? __ldg(g.gq + t1) : 0,
-                              has1 ? __float_as_int(__ldg(g.gc + t1)) : 0);
+    if (staged) {   // rows past L are zero (coefficient 0, pair 0)
+        const int L4 = (L + 3) & ~3;
+        for (int e = threadIdx.x; e < L4 * 32; e += blockDim.x) {
+            const int t = e >> 5, l = e & 31;
+            sgc[128 * (t >> 2) + 4 * l + (t & 3)] = t < L ? __ldg(g.gc + e) : 0.f;
         }
+        for (int e = threadIdx.x; e < L4 / 2 * 32; e += blockDim.x) {
+            const int r = e >> 5, l = e & 31, t0 = 2 * r;   // rows t0, t0 + 1 of lane l
+            const unsigned i0 = t0 < L ? (unsigned)__ldg(g.gq + t0 * 32 + l) : 0u;
+            const unsigned i1 = t0 + 1 < L ? (unsigned)__ldg(g.gq + (t0 + 1) * 32 + l) : 0u;
+            sgi[64 * (t0 >> 2) + 2 * l + ((t0 >> 1) & 1)] = i0 | (i1 << 16);
+        }
+    }
     for (int e = threadIdx.x; e < GROWTH_PAIR_SLOTS * 32; e += blockDim.x) spair[e] = e < P ? __ldg(g.pair + e) : 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -603,14 +611,16 @@ static __device__ __noinline__ unsigned grow_block_warps(const KParams<float>& p
                 float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
                 int t = 0;
                 for (; t + 4 <= L; t += 4) {
-                    const int4 e0 = sg[(t >> 1) * 32 + lane], e1 = sg[((t >> 1) + 1) * 32 + lane];
-                    a0 = __ffma2_rn(make_float2(__int_as_float(e0.y), __int_as_float(e0.w)), make_float2(w[e0.x], w[e0.z]), a0);
-                    a1 = __ffma2_rn(make_float2(__int_as_float(e1.y), __int_as_float(e1.w)), make_float2(w[e1.x], w[e1.z]), a1);
+                    const float4 c = *reinterpret_cast<const float4*>(sgc + 32 * t + 4 * lane);
+                    const uint2 ix = *reinterpret_cast<const uint2*>(sgi + 16 * t + 2 * lane);
+                    a0 = __ffma2_rn(make_float2(c.x, c.y), make_float2(w[ix.x & 0xffffu], w[ix.x >> 16]), a0);
+                    a1 = __ffma2_rn(make_float2(c.z, c.w), make_float2(w[ix.y & 0xffffu], w[ix.y >> 16]), a1);
                 }
                 d = a0.x;
                 for (; t < L; ++t) {
-                    const int4 e = sg[(t >> 1) * 32 + lane];
-                    d = (t & 1) ? fmaf(__int_as_float(e.w), w[e.z], d) : fmaf(__int_as_float(e.y), w[e.x], d);
+                    const float c = sgc[128 * (t >> 2) + 4 * lane + (t & 3)];
+                    const unsigned iw = sgi[64 * (t >> 2) + 2 * lane + ((t >> 1) & 1)];
+                    d = fmaf(c, w[(t & 1) ? (iw >> 16) : (iw & 0xffffu)], d);
                 }
                 d = (d + a0.y) + (a1.x + a1.y);
             } else {
