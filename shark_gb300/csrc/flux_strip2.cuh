@@ -33,14 +33,16 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b
 // Doubled limited slope 2 dq of the FP32 limiters (physics.cuh) for two columns.  minmod and MC
 // start from m = max(min.xorsign.abs(l, r), 0) (min_xorsign_abs_f, physics.cuh), which is
 // min(|l|, |r|) when l and r have the same sign and 0 otherwise (the l r <= 0 case of the
-// reference limiters).
+// reference limiters); the max is taken as (mx + |mx|) / 2, folded into the factor that follows.
 template <int ST>
 __device__ __forceinline__ float2 limit2(float2 l, float2 r) {
     if constexpr (ST == 0) {
         return make_float2(0.f, 0.f);
     } else if constexpr (ST == 1) {   // minmod: 2 sign(l) min(|l|, |r|)
-        const float2 m = make_float2(fmaxf(min_xorsign_abs_f(l.x, r.x), 0.f), fmaxf(min_xorsign_abs_f(l.y, r.y), 0.f));
-        const float2 m2 = add2(m, m);
+        const float2 mx = make_float2(min_xorsign_abs_f(l.x, r.x), min_xorsign_abs_f(l.y, r.y));
+        // 2 max(mx, 0) = mx + |mx| exactly: a packed add (the |.| an operand modifier) instead of two
+        // scalar max on the ALU pipe
+        const float2 m2 = add2(mx, make_float2(fabsf(mx.x), fabsf(mx.y)));
         return make_float2(copysignf(m2.x, l.x), copysignf(m2.y, l.y));
     } else if constexpr (ST == 2) {   // van Leer: 2 (2 l r / (l + r))
         const float2 pr = mul2(l, r), s = add2(l, r);
@@ -48,8 +50,10 @@ __device__ __forceinline__ float2 limit2(float2 l, float2 r) {
         return make_float2(pr.x <= 0.f ? 0.f : q.x, pr.y <= 0.f ? 0.f : q.y);
     } else {                          // MC: 2 sign(s) min(1.5 min(|l|,|r|), |s|/2) = sign(s) min(3 min, |s|)
         const float2 s = add2(l, r);
-        const float2 a = mul2(make_float2(fmaxf(min_xorsign_abs_f(l.x, r.x), 0.f), fmaxf(min_xorsign_abs_f(l.y, r.y), 0.f)),
-                              bc2(3.f));
+        const float2 mx = make_float2(min_xorsign_abs_f(l.x, r.x), min_xorsign_abs_f(l.y, r.y));
+        // 3 max(mx, 0) = 1.5 (mx + |mx|) exactly (the same single rounding of 3 mx, or 0), packed on
+        // the FMA pipe instead of two scalar max on the ALU pipe (FMNMX 8.6 -> 5.9 M per launch)
+        const float2 a = mul2(add2(mx, make_float2(fabsf(mx.x), fabsf(mx.y))), bc2(1.5f));
         // sign(s) min(|s|, a) for a >= +0 is min.xorsign.abs(a, s): one instruction per column
         return make_float2(min_xorsign_abs_f(a.x, s.x), min_xorsign_abs_f(a.y, s.y));
     }

@@ -72,8 +72,10 @@ __device__ __forceinline__ float min_xorsign_abs_f(float a, float b) {
 // MC: sign(s) min(1.5 min(|l|, |r|), |s|/2) when l r > 0, else 0; with m = max(min.xorsign.abs(l, r), 0)
 // (0 unless l and r have the same sign) it is min.xorsign.abs(1.5 m, s/2)
 __device__ __forceinline__ float limit_mc_f(float l, float r) {
-    const float m = fmaxf(min_xorsign_abs_f(l, r), 0.f);
-    return min_xorsign_abs_f(1.5f * m, 0.5f * (l + r));
+    // 1.5 max(mx, 0) = 0.75 (mx + |mx|) exactly (one rounding of 1.5 mx, or 0): an add with an
+    // operand modifier in place of a max
+    const float mx = min_xorsign_abs_f(l, r);
+    return min_xorsign_abs_f(0.75f * (mx + fabsf(mx)), 0.5f * (l + r));
 }
 
 // Compile-time limiter choice (0 = first order) for kernels specialised per configuration.
