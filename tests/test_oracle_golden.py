@@ -67,7 +67,7 @@ def test_dustywave_golden(K):
         assert l1 < (0.03 if name.startswith("v") else 0.1), (name, l1)
 
 
-def test_sod_baseline_config_vs_exact_riemann():
+def test_sod_1000_cells_minmod_hllc_vs_exact_riemann():
     """1000 cells, minmod, HLLC, CFL 0.5, to t = 0.2, against the exact solution at the final
     time actually reached (the last step overshoots tend)."""
     cfg, u0 = setups.sod(nx=1000, gamma=1.4, cfl=0.5, slope_type=1)
