@@ -116,6 +116,54 @@ def test_sedov_blast_stays_symmetric():
     np.testing.assert_allclose(rho, rho[:, ::-1], rtol=1e-10, atol=0)
 
 
+def _shock_radius(cfg, o):
+    """Radius of the blast's shock: the outer half-way point between the peak of the
+    azimuthally averaged density and the ambient density, interpolated between rings of one cell."""
+    ng = cfg.nghost
+    d = o.get_u().reshape(cfg.nvar, cfg.ny_max, cfg.nx_max)[0, ng:ng + cfg.ny, ng:ng + cfg.nx].ravel()
+    pos = setups.positions(cfg)
+    x = pos[:, 0].reshape(cfg.ny_max, cfg.nx_max)[ng:ng + cfg.ny, ng:ng + cfg.nx] - 0.5 * cfg.box_l
+    y = pos[:, 1].reshape(cfg.ny_max, cfg.nx_max)[ng:ng + cfg.ny, ng:ng + cfg.nx] - 0.5 * cfg.box_l_y
+    r = np.hypot(x, y).ravel()
+    dr = cfg.box_l / cfg.nx
+    nb = int(0.5 * cfg.box_l / dr)
+    idx = np.minimum((r / dr).astype(int), nb)
+    prof = np.bincount(idx, d, nb + 1)[:nb] / np.maximum(np.bincount(idx, None, nb + 1)[:nb], 1)
+    k = int(np.argmax(prof))
+    half = 0.5 * (prof[k] + cfg.sedov_rho_ext)
+    j = k
+    while j + 1 < nb and prof[j + 1] > half:
+        j += 1
+    return (j + 0.5) * dr + (prof[j] - half) / (prof[j] - prof[j + 1]) * dr, prof[k]
+
+
+def test_sedov_blast_follows_the_sedov_taylor_law():
+    """The reference's blast (energy P_cen/(gamma-1) pi r_expl^2 in a gas at rest, 2D) on the
+    oracle against the self-similar Sedov-Taylor solution: the shock radius grows as
+    (E t^2/rho)^(1/4), i.e. R ~ t^(1/2), measured between t = 0.2 and 0.5 (R from 2.3 to 3.8
+    r_expl, before the shock nears the periodic images at R = 0.5) as d ln R / d ln t within
+    0.45 - 0.55 (measured 0.52 at 128^2, 0.53 at 256^2 and 512^2: the finite initial bubble still
+    shows); the post-shock density stays below the strong-shock limit (gamma+1)/(gamma-1) = 4 and
+    approaches it as the resolution doubles (3.1, 3.4, 3.7 at 128^2, 256^2, 512^2)."""
+    peaks = []
+    for n in (128, 256):
+        cfg, u0 = setups.sedov(n=n)
+        o = Oracle(cfg)
+        o.set_u(u0)
+        ts, rs = [], []
+        for tend in (0.2, 0.3, 0.4, 0.5):
+            o.run(10 ** 7, tend)
+            R, pk = _shock_radius(cfg, o)
+            ts.append(o.time)
+            rs.append(R)
+        slope = np.polyfit(np.log(ts), np.log(rs), 1)[0]
+        assert 0.45 <= slope <= 0.55, (n, slope)
+        lim = (cfg.gamma + 1.0) / (cfg.gamma - 1.0)
+        assert pk < lim, (n, pk)
+        peaks.append(pk)
+    assert peaks[1] > peaks[0]
+
+
 def test_kh_and_sedov_configs_are_checked_before_touching_a_device(lib):
     h = C.c_void_p()
     kh, _ = setups.kh(n=16, ndust=2)
